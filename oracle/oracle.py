@@ -1,0 +1,159 @@
+"""ctypes binding of the CPU oracle (oracle/build/libsecir_oracle.so).
+
+TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg. The product (memilio_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from memilio_gb300.layout import (GraphArrays, MgpuGraph, MgpuIntegratorOpts, integrator_opts,
+                                  NUM_COMPARTMENTS, NUM_FLOWS)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "build", "libsecir_oracle.so")
+_lib = None
+
+
+class OrcStats(ctypes.Structure):
+    _fields_ = [
+        ("accepted_steps", ctypes.c_int64),
+        ("rejected_steps", ctypes.c_int64),
+        ("rhs_evals", ctypes.c_int64),
+        ("underflow_fixes", ctypes.c_int64),
+        ("failed_steps", ctypes.c_int64),
+    ]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (g++, no other dependency)."""
+    src = os.path.join(_HERE, "secir_oracle.cpp")
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        P = ctypes.POINTER
+        d = ctypes.c_double
+        L.orc_eval_rhs.argtypes = [P(MgpuGraph), ctypes.c_int, P(d), P(d), d, P(d)]
+        L.orc_eval_flows.argtypes = [P(MgpuGraph), ctypes.c_int, P(d), P(d), d, P(d)]
+        L.orc_simulate.argtypes = [P(MgpuGraph), ctypes.c_int, d, d, d, P(MgpuIntegratorOpts), ctypes.c_int,
+                                   P(d), P(d), P(ctypes.c_int), P(OrcStats)]
+        L.orc_graph_run.argtypes = [P(MgpuGraph), d, d, d, d, P(MgpuIntegratorOpts), P(d), P(d), P(OrcStats)]
+        L.orc_ensemble_run.argtypes = [P(MgpuGraph), ctypes.c_int, d, d, d, d, P(MgpuIntegratorOpts), ctypes.c_int,
+                                       P(d), P(d), P(OrcStats)]
+        L.orc_damping_cache.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P(d), P(ctypes.c_int32),
+                                        P(ctypes.c_int32), P(d), ctypes.c_int, P(d), P(d)]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def eval_rhs(g: GraphArrays, node: int, pop, y, t: float) -> np.ndarray:
+    pop = np.ascontiguousarray(pop, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    out = np.zeros(g.n)
+    cg = g.as_ctypes()
+    assert lib().orc_eval_rhs(ctypes.byref(cg), node, _p(pop), _p(y), t, _p(out)) == 0
+    return out
+
+
+def eval_flows(g: GraphArrays, node: int, pop, y, t: float) -> np.ndarray:
+    pop = np.ascontiguousarray(pop, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    out = np.zeros(g.num_groups * NUM_FLOWS)
+    cg = g.as_ctypes()
+    assert lib().orc_eval_flows(ctypes.byref(cg), node, _p(pop), _p(y), t, _p(out)) == 0
+    return out
+
+
+def simulate(g: GraphArrays, node: int, t0: float, tmax: float, dt: float, opts=None, max_points: int = 200000):
+    """Single-node simulate(): returns (times [P], values [P, 10G], stats)."""
+    opts = opts or integrator_opts()
+    out_t = np.zeros(max_points)
+    out_y = np.zeros((max_points, g.n))
+    npts = ctypes.c_int(0)
+    st = OrcStats()
+    cg = g.as_ctypes()
+    rc = lib().orc_simulate(ctypes.byref(cg), node, t0, tmax, dt, ctypes.byref(opts), max_points, _p(out_t),
+                            _p(out_y), ctypes.byref(npts), ctypes.byref(st))
+    if rc != 0:
+        raise RuntimeError("orc_simulate failed (max_points too small?)")
+    return out_t[:npts.value].copy(), out_y[:npts.value].copy(), st.as_dict()
+
+
+def num_boundaries(t0: float, tmax: float, dt_exchange: float) -> int:
+    t, nb = t0, 0
+    while t < tmax:
+        dt = dt_exchange if t + dt_exchange <= tmax else tmax - t
+        t += dt
+        nb += 1
+    return nb
+
+
+def graph_run(g: GraphArrays, t0: float, tmax: float, dt_exchange: float = 0.5, dt0: float = 0.1, opts=None,
+              record: bool = True):
+    """make_mobility_sim(t0, dt_exchange, graph).advance(tmax).
+
+    Returns (boundary_states [B, N, 10G] or None, final [N, 10G], stats)."""
+    opts = opts or integrator_opts()
+    nb = num_boundaries(t0, tmax, dt_exchange)
+    rec = np.zeros((nb, g.num_nodes, g.n)) if record else None
+    fin = np.zeros((g.num_nodes, g.n))
+    st = OrcStats()
+    cg = g.as_ctypes()
+    rc = lib().orc_graph_run(ctypes.byref(cg), t0, tmax, dt_exchange, dt0, ctypes.byref(opts),
+                             _p(rec) if record else ctypes.POINTER(ctypes.c_double)(), _p(fin), ctypes.byref(st))
+    assert rc == 0
+    return rec, fin, st.as_dict()
+
+
+def ensemble_run(graphs, t0: float, tmax: float, dt_exchange: float = 0.5, dt0: float = 0.1, opts=None,
+                 num_threads: int = 0):
+    """Independent runs of many graphs over `num_threads` host threads.
+
+    Returns (list of final [N_b, 10G], elapsed seconds, stats)."""
+    opts = opts or integrator_opts()
+    arr = (MgpuGraph * len(graphs))(*[g.as_ctypes() for g in graphs])
+    sizes = [g.num_nodes * g.n for g in graphs]
+    out = np.zeros(sum(sizes))
+    el = ctypes.c_double(0)
+    st = OrcStats()
+    rc = lib().orc_ensemble_run(arr, len(graphs), t0, tmax, dt_exchange, dt0, ctypes.byref(opts), num_threads,
+                                _p(out), ctypes.byref(el), ctypes.byref(st))
+    assert rc == 0
+    res, off = [], 0
+    for g, s in zip(graphs, sizes):
+        res.append(out[off:off + s].reshape(g.num_nodes, g.n))
+        off += s
+    return res, el.value, st.as_dict()
+
+
+def damping_cache(rows, cols, times, levels, types, matrices, cap=64):
+    times = np.ascontiguousarray(times, np.float64)
+    levels = np.ascontiguousarray(levels, np.int32)
+    types = np.ascontiguousarray(types, np.int32)
+    matrices = np.ascontiguousarray(matrices, np.float64)
+    out_t = np.zeros(cap)
+    out_m = np.zeros((cap, rows, cols))
+    k = lib().orc_damping_cache(rows, cols, len(times), _p(times),
+                                levels.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                types.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _p(matrices), cap,
+                                _p(out_t), _p(out_m))
+    assert k > 0
+    return out_t[:k].copy(), out_m[:k].copy()

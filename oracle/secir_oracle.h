@@ -1,0 +1,80 @@
+/*
+ * secir_oracle.h — TEST INFRASTRUCTURE, not product code.
+ *
+ * An FP64 CPU restatement of MEmilio's graph-ODE SECIR path, used only as
+ * the checker of the GPU library (tests/, __graft_entry__.smoke()) and as
+ * the timed CPU baseline in bench.py. Nothing in memilio_gb300/ links,
+ * loads or calls it.
+ *
+ * It follows, function by function (see secir_oracle.cpp for line cites):
+ *   models/ode_secir/model.h          get_flows, get_mobility_factors, test_commuters
+ *   memilio/compartments/flow_model.h get_derivatives
+ *   memilio/epidemiology/damping.h, contact_matrix.h, math/smoother.h
+ *   memilio/math/integrator.h         SystemIntegrator::advance
+ *   memilio/math/stepper_wrapper.h    ControlledStepperWrapper<cash_karp54>
+ *   memilio/math/adapt_rk.h           RKIntegratorCore (RKF45)
+ *   memilio/math/euler.h              EulerIntegratorCore
+ *   memilio/mobility/metapopulation_mobility_instant.h, graph_simulation.h
+ *   memilio/compartments/parameter_studies.h (run distribution)
+ *
+ * Parity pins: the reference's golden CSVs (tests/golden/), see tests/test_oracle_golden.py.
+ */
+#ifndef SECIR_ORACLE_H
+#define SECIR_ORACLE_H
+
+#include "../include/miogpu_layout.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_stats {
+    int64_t accepted_steps;   /* accepted integrator steps, all nodes */
+    int64_t rejected_steps;   /* rejected attempts (error or dt_max), all nodes */
+    int64_t rhs_evals;        /* right-hand-side evaluations incl. mobility returns */
+    int64_t underflow_fixes;  /* negative compartments fixed on mobility return */
+    int64_t failed_steps;     /* steps forced at dt_min */
+} orc_stats;
+
+/* Right-hand side of node `node` of graph g: dydt = f(pop, y, t)
+ * (FlowModel::get_derivatives(pop, y, t, dydt)). */
+int orc_eval_rhs(const mgpu_graph* g, int node, const double* pop, const double* y, double t, double* dydt);
+
+/* Flows of node `node` (Model::get_flows), 15G values. */
+int orc_eval_flows(const mgpu_graph* g, int node, const double* pop, const double* y, double t, double* flows);
+
+/* Single-node simulate(t0, tmax, dt, model, core) (compartments/simulation.h:99-110):
+ * records every accepted step. out_t [max_points], out_y [max_points][10G].
+ * Returns 0, or -1 when max_points is too small. */
+int orc_simulate(const mgpu_graph* g, int node, double t0, double tmax, double dt,
+                 const mgpu_integrator_opts* opts, int max_points, double* out_t, double* out_y,
+                 int* num_points, orc_stats* stats);
+
+/* make_mobility_sim(t0, dt_exchange, graph).advance(tmax). Writes the node
+ * states after every exchange boundary into out_states
+ * [num_boundaries][N][10G] when out_states != NULL (num_boundaries =
+ * ceil((tmax-t0)/dt_exchange)), and the final states into final_state [N][10G]. */
+int orc_graph_run(const mgpu_graph* g, double t0, double tmax, double dt_exchange, double dt0,
+                  const mgpu_integrator_opts* opts, double* out_states, double* final_state,
+                  orc_stats* stats);
+
+/* ParameterStudy-style ensemble: graphs[0..num_graphs) each run independently,
+ * one graph per thread, num_threads std::threads (0 = all hardware threads).
+ * final_states is the concatenation of each graph's [N_b][10G] block.
+ * elapsed_s receives the wall time of the runs alone (no setup). */
+int orc_ensemble_run(const mgpu_graph* graphs, int num_graphs, double t0, double tmax,
+                     double dt_exchange, double dt0, const mgpu_integrator_opts* opts,
+                     int num_threads, double* final_states, double* elapsed_s, orc_stats* stats);
+
+/* Cache builder for Dampings (damping.h:570-600). Dampings given sorted as
+ * Dampings::add_ keeps them (by time, type, level). Writes K points (times,
+ * G x G matrices, rows*cols values each). Returns K, or -1 if cap too small. */
+int orc_damping_cache(int rows, int cols, int num_dampings, const double* times, const int32_t* levels,
+                      const int32_t* types, const double* matrices, int cap, double* out_times,
+                      double* out_matrices);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
