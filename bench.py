@@ -1,0 +1,309 @@
+"""Benchmark: node-days/s of the batched ParameterStudy ensemble of graph-ODE
+SECIR simulations (1024 samples x 400 nodes, ~30 out-edges per node, 6 age
+groups, 90 days, mobility exchange every 0.5 days).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--precision mixed|fp64|plain] [--samples S] [--nodes N] [--days D]
+
+One step = one full solve of the ensemble (all samples, all 90 days).
+`value`: inputs resident in HBM (mgpu_batch_reset, then mgpu_batch_advance),
+device time from CUDA events on the library's stream. `e2e`: the public C ABI
+from host buffers per step: mgpu_batch_create (H2D of every input),
+mgpu_batch_advance, mgpu_batch_get_state (D2H of every node state).
+--impl reference: the FP64 CPU restatement of the reference path (the
+checker), all host threads, one graph per thread, on a bounded sample.
+Under torchrun every rank solves its own S samples (weak scaling, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "node-days/s, 1024x400-node SECIR ensemble vs plain GPU FP64; p50/p99 latency"
+UNIT = "node-days/s"
+
+
+def flops_per_attempt(G: int) -> float:
+    """Algorithmic FLOPs of one Cash-Karp attempt: 6 RHS of 6G^2 + 90G + 10 flops
+    (contact evaluation and G x G contraction, per-group prep, 14 linear flows,
+    derivative scatter) plus 55 n for stage combinations, 5th-order sum, error
+    combination and norm (n = 10 G)."""
+    return 6.0 * (6 * G * G + 90 * G + 10) + 55.0 * 10 * G
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_baseline_run(graphs, days, threads, repeats=1):
+    """Oracle ensemble on host threads: node-days/s on the given sample."""
+    from oracle import oracle as O
+    best = None
+    for _ in range(repeats):
+        _, el, st = O.ensemble_run(graphs, 0.0, days, num_threads=threads)
+        nd = sum(g.num_nodes for g in graphs) * days
+        v = nd / el
+        best = v if best is None else max(best, v)
+    return best, st
+
+
+def run_reference(args, graphs_builder):
+    """--impl reference: the CPU restatement of the reference path, all host threads."""
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    sample = max(cores, min(2 * cores, args.samples))
+    graphs = graphs_builder(sample)
+    for _ in range(args.warmup if args.warmup <= 1 else 1):
+        cpu_baseline_run(graphs[:cores], min(args.days, 5.0), cores)
+    times = []
+    for _ in range(args.steps):
+        from oracle import oracle as O
+        _, el, _ = O.ensemble_run(graphs, 0.0, args.days, num_threads=cores)
+        times.append(el)
+    nd = sum(g.num_nodes for g in graphs) * args.days
+    v = nd / float(np.median(times))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": float(np.median(times)) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{sample} of {args.samples} samples x {args.nodes} nodes x {args.days:g} days per "
+                                   f"step, one graph per thread"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args):
+    return {"workload": f"ParameterStudy ensemble: {args.samples} samples x {args.nodes}-node mobility graph, "
+                        f"6 age groups, ~30 out-edges/node, {args.days:g} days, exchange every 0.5 d",
+            "samples": args.samples, "nodes": args.nodes, "age_groups": 6, "days": args.days,
+            "integrator": "Cash-Karp 5(4), abs 1e-10, rel 1e-5, dt0 0.1",
+            "precision": args.precision,
+            "l2": "inputs larger than L2 (node parameters and states of the ensemble exceed 129 MB)"}
+
+
+def graph_bytes(g) -> int:
+    arrs = [g.params, g.contact_baseline, g.contact_minimum, g.damping_times, g.damping_values, g.init_state,
+            g.edge_src, g.edge_dst, g.edge_coeff_baseline, g.edge_damping_times, g.edge_damping_values]
+    if g.edge_coeff_minimum is not None:
+        arrs.append(g.edge_coeff_minimum)
+    return int(sum(a.nbytes for a in arrs))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "plain"])
+    ap.add_argument("--samples", type=int, default=1024)
+    ap.add_argument("--nodes", type=int, default=400)
+    ap.add_argument("--days", type=float, default=90.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    from memilio_gb300 import workloads as W
+
+    base = W.mobility_graph(seed=1, N=args.nodes)
+
+    def graphs_builder(count):
+        return W.ensemble(num_samples=count, base=base)
+
+    if args.impl == "reference":
+        run_reference(args, graphs_builder)
+        return
+
+    rank, world, local = dist_info()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    from memilio_gb300 import _native as N
+    from memilio_gb300 import build as B
+    B.build()
+    prec = {"mixed": N.PRECISION_MIXED, "fp64": N.PRECISION_FP64, "plain": N.PRECISION_FP64_PLAIN}[args.precision]
+    graphs = graphs_builder(args.samples)
+    nd_step = sum(g.num_nodes for g in graphs) * args.days
+    ctx = N.Context(local)
+    batch = N.Batch(ctx, graphs, 0.0, N.solver_opts(precision=prec))
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        batch.reset(0.0)
+        batch.advance(args.days)
+    st0 = batch.stats()
+    dev_ms = []
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_wall = time.perf_counter()
+        for _ in range(args.steps):
+            batch.reset(0.0)
+            batch.advance(args.days)
+            dev_ms.append(batch.timing()["advance_ms"])
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    barrier()
+    st1 = batch.stats()
+    launches = (st1["kernel_launches"] - st0["kernel_launches"])
+    ms_step = float(np.sum(dev_ms)) / args.steps
+    ms_max = ms_step
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_max = float(tt.item())
+    value = world * nd_step / (ms_max / 1e3)
+    final = batch.state_flat()
+    attempts_step = (st1["accepted_steps"] + st1["rejected_steps"] - st0["accepted_steps"] - st0["rejected_steps"]) \
+        / args.steps
+
+    # per-kernel device times (profile mode: events around the node-solve kernels)
+    prof = N.Batch(ctx, graphs, 0.0, N.solver_opts(precision=prec, profile=True))
+    prof.advance(args.days)
+    tm = prof.timing()
+    prof.close()
+    ode_ms_launch = tm["ode_ms"] / max(tm["ode_launches"], 1)
+    flops_launch = tm["attempts"] * flops_per_attempt(6) / max(tm["ode_launches"], 1)
+    clocks = clk.summary()
+    f_sm = clocks["sm_mhz"] or 1965.0
+    fp32_peak = 152 * 128 * 2 * f_sm * 1e6 / 1e12  # TFLOP/s at the sampled clock
+    achieved = flops_launch / (ode_ms_launch / 1e3) / 1e12
+    roofline = {"bound": "fp32" if prec == N.PRECISION_MIXED else "fp64",
+                "kernel": "k_ode_batched<6,float>" if prec == N.PRECISION_MIXED else (
+                    "k_ode_batched<6,double>" if prec == N.PRECISION_FP64 else "k_ode_plain"),
+                "achieved": achieved, "unit": "TFLOP/s",
+                "peak": fp32_peak if prec == N.PRECISION_MIXED else 1.25,
+                "peak_source": ("nominal FP32 FMA rate (152 SMs x 128 lanes x 2) at the sampled median SM clock; "
+                                "MEASURED_PEAKS.json holds no FP32 figure") if prec == N.PRECISION_MIXED else
+                               "nominal GB300 FP64 rate",
+                "frac": None, "traffic": None,
+                "ode_share_of_step": tm["ode_ms"] / max(tm["advance_ms"], 1e-9),
+                "exchange_ms_per_step": tm["exchange_ms"], "ode_ms_per_step": tm["ode_ms"],
+                "algorithmic_flops_per_launch": flops_launch, "avg_launch_ms": ode_ms_launch}
+    roofline["frac"] = roofline["achieved"] / roofline["peak"]
+
+    # end to end through the C ABI from host buffers
+    e2e = None
+    if not args.no_e2e:
+        h2d = sum(graph_bytes(g) for g in graphs)
+        d2h = batch.total * 8
+        e2e_t = []
+        for k in range(2):
+            t0 = time.perf_counter()
+            b2 = N.Batch(ctx, graphs, 0.0, N.solver_opts(precision=prec))
+            b2.advance(args.days)
+            out = b2.state_flat()
+            b2.close()
+            e2e_t.append(time.perf_counter() - t0)
+        e2e = {"value": world * nd_step / min(e2e_t), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h}
+        assert np.array_equal(out, final)
+    batch.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        sample = graphs[:cores]
+        v, _ = cpu_baseline_run(sample, args.days, cores)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{len(sample)} samples x {args.nodes} nodes x {args.days:g} days, one graph per thread"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": {"mixed": "f32+f64", "fp64": "f64", "plain": "f64"}[args.precision],
+            "data": "synthetic (seeded)", "config": workload_config(args), "clocks": clocks,
+            "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+            "attempts_per_node_day": attempts_step / nd_step, "wall_s_timed": t_wall,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

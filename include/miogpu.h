@@ -1,0 +1,159 @@
+/*
+ * miogpu.h — C ABI of libmiogpu, the GB300 (sm_103a) implementation of
+ * MEmilio's graph-ODE SECIR hot path.
+ *
+ * Plain C: opaque handles, flat arrays, int status codes, no exceptions and
+ * no CUDA or C++ types in the signatures. The data format of a graph is in
+ * miogpu_layout.h. Each entry point names the reference interface it
+ * replaces (paths inside the MEmilio source tree).
+ *
+ * Threading: one context per host thread; calls on one context are not
+ * reentrant. Every context owns one CUDA stream; all device memory belongs
+ * to the context and its batches, and no device pointer is returned.
+ */
+#ifndef MIOGPU_H
+#define MIOGPU_H
+
+#include "miogpu_layout.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. 0..7 mirror mio::StatusCode (cpp/memilio/io/io.h:49-59). */
+enum mgpu_status {
+    MGPU_OK                  = 0,
+    MGPU_UNKNOWN_ERROR       = 1,
+    MGPU_OUT_OF_RANGE        = 2,
+    MGPU_INVALID_VALUE       = 3,
+    MGPU_INVALID_FILE_FORMAT = 4,
+    MGPU_KEY_NOT_FOUND       = 5,
+    MGPU_INVALID_TYPE        = 6,
+    MGPU_FILE_NOT_FOUND      = 7,
+    MGPU_CUDA_ERROR          = 100, /* a CUDA call failed; see mgpu_last_error */
+    MGPU_OOM                 = 101, /* device memory budget exceeded */
+    MGPU_TIMEOUT             = 102, /* a bounded device wait gave up */
+    MGPU_STEP_FAILED         = 103, /* an instance hit the step cap or produced NaN/Inf */
+    MGPU_UNSUPPORTED         = 104  /* valid input this library does not implement */
+};
+
+/* Arithmetic of the node ODE solves. */
+enum mgpu_precision {
+    MGPU_PRECISION_FP64_PLAIN = 0, /* one thread per node, FP64, stage vectors in HBM (the plain drop-in) */
+    MGPU_PRECISION_FP64       = 1, /* batched lane-per-age-group solver, FP64 throughout */
+    MGPU_PRECISION_MIXED      = 2  /* batched: FP32 flows and stages, FP64 state, error norm, controller */
+};
+
+typedef struct mgpu_context mgpu_context;
+typedef struct mgpu_batch mgpu_batch;
+
+typedef struct mgpu_solver_opts {
+    mgpu_integrator_opts integrator; /* tolerances and dt bounds of every node's core */
+    double dt0;                      /* initial integrator step, Simulation(model, t0, dt) (default 0.1) */
+    double dt_exchange;              /* mobility interval, make_mobility_sim(t0, dt, graph) (0.5) */
+    int32_t precision;               /* enum mgpu_precision */
+    int32_t instances_per_block;     /* batched solver: node instances per CTA; 0 = autotuned */
+    int32_t max_steps_per_interval;  /* per node and exchange interval; 0 = 100000 */
+    int32_t use_cuda_graph;          /* capture the fixed exchange schedule as a CUDA graph */
+    int32_t profile;                 /* time node solves and exchanges separately with CUDA events
+                                        (launches stream by stream; no CUDA graph) */
+} mgpu_solver_opts;
+
+/* Device times of the last mgpu_batch_advance, from CUDA events on the context's stream. */
+typedef struct mgpu_timing {
+    double advance_ms;      /* whole advance */
+    double ode_ms;          /* node solves (profile mode only) */
+    double exchange_ms;     /* exchanges incl. interval bookkeeping (profile mode only) */
+    int64_t ode_launches;   /* node-solve kernel launches timed in ode_ms */
+    int64_t attempts;       /* integrator attempts (accepted + rejected) during the advance */
+} mgpu_timing;
+
+typedef struct mgpu_stats {
+    int64_t accepted_steps;   /* accepted integrator steps over all node instances */
+    int64_t rejected_steps;   /* rejected attempts */
+    int64_t failed_steps;     /* steps forced at dt_min (adaptive step sizing failed) */
+    int64_t underflow_fixes;  /* negative compartments fixed on mobility returns */
+    int64_t sequential_exchanges; /* graph exchanges that took the exact sequential path */
+    int64_t phases;           /* exchange intervals simulated */
+    int64_t kernel_launches;  /* kernels launched by this batch */
+} mgpu_stats;
+
+/* Default solver options: Cash-Karp 5(4) with the default core's tolerances
+ * (cpp/memilio/math/stepper_wrapper.h:83-91), dt0 0.1, exchange every 0.5 days. */
+void mgpu_default_solver_opts(mgpu_solver_opts* opts);
+
+/* Create / destroy a context on CUDA device `device`. */
+int mgpu_create(int device, mgpu_context** out);
+void mgpu_destroy(mgpu_context* ctx);
+/* Message of the last failed call on this context (never NULL). */
+const char* mgpu_last_error(const mgpu_context* ctx);
+/* Caps the device memory this context may allocate (bytes; 0 = free HBM). */
+int mgpu_set_memory_budget(mgpu_context* ctx, int64_t bytes);
+
+/*
+ * Right-hand side of node models: for k < count,
+ *   dydt[k] = f_{nodes[k]}(pop[k], y[k], t[k])
+ * Replaces FlowModel::get_derivatives(pop, y, t, dydt)
+ * (cpp/memilio/compartments/flow_model.h:138-144) with osecir::Model::get_flows
+ * (cpp/models/ode_secir/model.h:82-214). pop, y, dydt: [count][10G] host arrays.
+ */
+int mgpu_eval_rhs(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, const int32_t* nodes,
+                  const double* pop, const double* y, const double* t, double* dydt);
+
+/*
+ * Single-node simulations: for k < count, integrate node nodes[k] of `graph`
+ * (edges ignored) from t0 to tmax, initial step dt0, recording every accepted
+ * step. Replaces mio::simulate / osecir::simulate (cpp/memilio/compartments/simulation.h:99-110,
+ * cpp/models/ode_secir/model.h:385-390) and Simulation::advance with its
+ * TimeSeries result. out_t [count][max_points], out_y [count][max_points][10G],
+ * num_points [count]. Returns MGPU_OUT_OF_RANGE if a trajectory needs more than
+ * max_points (num_points then holds max_points). FP64, one thread per node.
+ */
+int mgpu_simulate(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, const int32_t* nodes, double t0,
+                  double tmax, double dt0, const mgpu_integrator_opts* opts, int32_t max_points, double* out_t,
+                  double* out_y, int32_t* num_points);
+
+/*
+ * Upload graphs and create their simulations: for every graph b,
+ *   make_mobility_sim(t0, opts->dt_exchange, graph_b)
+ * (cpp/memilio/mobility/metapopulation_mobility_instant.h:656-678) with each
+ * node's Simulation(model, t0, opts->dt0) (cpp/models/ode_secir/model.h:277-280).
+ * A batch of several graphs is ParameterStudy's set of runs
+ * (cpp/memilio/compartments/parameter_studies.h:288-345); graphs are independent.
+ */
+int mgpu_batch_create(mgpu_context* ctx, const mgpu_graph* graphs, int32_t num_graphs, double t0,
+                      const mgpu_solver_opts* opts, mgpu_batch** out);
+
+/*
+ * GraphSimulation::advance(tmax) (cpp/memilio/mobility/graph_simulation.h:101-120)
+ * for every graph: node solves, then MobilityEdge::apply_mobility
+ * (metapopulation_mobility_instant.h:544-623) every dt_exchange. tmax_per_graph
+ * [num_graphs] gives each graph its own horizon; NULL uses `tmax` for all.
+ */
+int mgpu_batch_advance(mgpu_batch* batch, double tmax, const double* tmax_per_graph);
+
+/* Restart every graph at time t0 from the initial states given at creation,
+ * with the inputs still resident on the device: the equivalent of building
+ * a fresh make_mobility_sim(t0, dt, graph) from the same graph
+ * (cpp/memilio/mobility/metapopulation_mobility_instant.h:656-678). */
+int mgpu_batch_reset(mgpu_batch* batch, double t0);
+
+/* Node states (result last values) of all graphs, concatenated [sum_b N_b][10 G_b]. */
+int mgpu_batch_get_state(mgpu_batch* batch, double* out);
+/* Graph times GraphSimulation::get_t() [num_graphs]. */
+int mgpu_batch_get_time(mgpu_batch* batch, double* out);
+/* Replace the node states (e.g. after a host-side intervention) [sum_b N_b][10 G_b]. */
+int mgpu_batch_set_state(mgpu_batch* batch, const double* state);
+int mgpu_batch_get_stats(mgpu_batch* batch, mgpu_stats* out);
+/* Event-measured device times of the last advance (no reference counterpart:
+ * replaces the reference's wall-clock timers, cpp/memilio/timer/auto_timer.h). */
+int mgpu_batch_get_timing(mgpu_batch* batch, mgpu_timing* out);
+/* Device bytes held by the batch. */
+int64_t mgpu_batch_device_bytes(const mgpu_batch* batch);
+void mgpu_batch_destroy(mgpu_batch* batch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MIOGPU_H */

@@ -1,0 +1,276 @@
+"""ctypes binding of libmiogpu (include/miogpu.h).
+
+The library must be built (memilio_gb300.build.build()); loading fails
+loudly otherwise — there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from .layout import GraphArrays, MgpuGraph, MgpuIntegratorOpts, integrator_opts
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libmiogpu.so")
+
+OK = 0
+STATUS_NAMES = {0: "OK", 1: "UnknownError", 2: "OutOfRange", 3: "InvalidValue", 4: "InvalidFileFormat",
+                5: "KeyNotFound", 6: "InvalidType", 7: "FileNotFound", 100: "CudaError", 101: "OutOfMemory",
+                102: "Timeout", 103: "StepFailed", 104: "Unsupported"}
+
+PRECISION_FP64_PLAIN = 0
+PRECISION_FP64 = 1
+PRECISION_MIXED = 2
+
+# every entry point declared in include/miogpu.h
+EXPORTED = ["mgpu_default_solver_opts", "mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_set_memory_budget",
+            "mgpu_eval_rhs", "mgpu_simulate", "mgpu_batch_create", "mgpu_batch_advance", "mgpu_batch_get_state",
+            "mgpu_batch_get_time", "mgpu_batch_set_state", "mgpu_batch_get_stats", "mgpu_batch_get_timing",
+            "mgpu_batch_device_bytes", "mgpu_batch_reset", "mgpu_batch_destroy"]
+
+
+class MgpuSolverOpts(ctypes.Structure):
+    _fields_ = [
+        ("integrator", MgpuIntegratorOpts),
+        ("dt0", ctypes.c_double),
+        ("dt_exchange", ctypes.c_double),
+        ("precision", ctypes.c_int32),
+        ("instances_per_block", ctypes.c_int32),
+        ("max_steps_per_interval", ctypes.c_int32),
+        ("use_cuda_graph", ctypes.c_int32),
+        ("profile", ctypes.c_int32),
+    ]
+
+
+class MgpuTiming(ctypes.Structure):
+    _fields_ = [
+        ("advance_ms", ctypes.c_double),
+        ("ode_ms", ctypes.c_double),
+        ("exchange_ms", ctypes.c_double),
+        ("ode_launches", ctypes.c_int64),
+        ("attempts", ctypes.c_int64),
+    ]
+
+    def as_dict(self):
+        return {k: (float(getattr(self, k)) if k.endswith("ms") else int(getattr(self, k))) for k, _ in self._fields_}
+
+
+class MgpuStats(ctypes.Structure):
+    _fields_ = [
+        ("accepted_steps", ctypes.c_int64),
+        ("rejected_steps", ctypes.c_int64),
+        ("failed_steps", ctypes.c_int64),
+        ("underflow_fixes", ctypes.c_int64),
+        ("sequential_exchanges", ctypes.c_int64),
+        ("phases", ctypes.c_int64),
+        ("kernel_launches", ctypes.c_int64),
+    ]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+class MgpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)} ({code}): {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """Load libmiogpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} not built: run memilio_gb300.build.build() (needs nvcc)")
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.POINTER
+    d = ctypes.c_double
+    vp = ctypes.c_void_p
+    L.mgpu_default_solver_opts.argtypes = [P(MgpuSolverOpts)]
+    L.mgpu_default_solver_opts.restype = None
+    L.mgpu_create.argtypes = [ctypes.c_int, P(vp)]
+    L.mgpu_destroy.argtypes = [vp]
+    L.mgpu_destroy.restype = None
+    L.mgpu_last_error.argtypes = [vp]
+    L.mgpu_last_error.restype = ctypes.c_char_p
+    L.mgpu_set_memory_budget.argtypes = [vp, ctypes.c_int64]
+    L.mgpu_eval_rhs.argtypes = [vp, P(MgpuGraph), ctypes.c_int32, P(ctypes.c_int32), P(d), P(d), P(d), P(d)]
+    L.mgpu_simulate.argtypes = [vp, P(MgpuGraph), ctypes.c_int32, P(ctypes.c_int32), d, d, d,
+                                P(MgpuIntegratorOpts), ctypes.c_int32, P(d), P(d), P(ctypes.c_int32)]
+    L.mgpu_batch_create.argtypes = [vp, P(MgpuGraph), ctypes.c_int32, d, P(MgpuSolverOpts), P(vp)]
+    L.mgpu_batch_advance.argtypes = [vp, d, P(d)]
+    L.mgpu_batch_get_state.argtypes = [vp, P(d)]
+    L.mgpu_batch_get_time.argtypes = [vp, P(d)]
+    L.mgpu_batch_set_state.argtypes = [vp, P(d)]
+    L.mgpu_batch_get_stats.argtypes = [vp, P(MgpuStats)]
+    L.mgpu_batch_get_timing.argtypes = [vp, P(MgpuTiming)]
+    L.mgpu_batch_reset.argtypes = [vp, d]
+    L.mgpu_batch_device_bytes.argtypes = [vp]
+    L.mgpu_batch_device_bytes.restype = ctypes.c_int64
+    L.mgpu_batch_destroy.argtypes = [vp]
+    L.mgpu_batch_destroy.restype = None
+    _lib = L
+    return L
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+def solver_opts(precision=PRECISION_MIXED, dt0=0.1, dt_exchange=0.5, integrator: Optional[MgpuIntegratorOpts] = None,
+                instances_per_block=0, max_steps_per_interval=0, use_cuda_graph=True,
+                profile=False) -> MgpuSolverOpts:
+    o = MgpuSolverOpts()
+    lib().mgpu_default_solver_opts(ctypes.byref(o))
+    if integrator is not None:
+        o.integrator = integrator
+    o.dt0 = dt0
+    o.dt_exchange = dt_exchange
+    o.precision = precision
+    o.instances_per_block = instances_per_block
+    o.max_steps_per_interval = max_steps_per_interval
+    o.use_cuda_graph = 1 if use_cuda_graph else 0
+    o.profile = 1 if profile else 0
+    return o
+
+
+class Context:
+    """One mgpu_context (one CUDA stream on one device)."""
+
+    def __init__(self, device: int = 0):
+        self._h = ctypes.c_void_p()
+        rc = lib().mgpu_create(device, ctypes.byref(self._h))
+        if rc != OK:
+            raise MgpuError(rc, "mgpu_create failed")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def check(self, rc: int):
+        if rc != OK:
+            raise MgpuError(rc, lib().mgpu_last_error(self._h).decode())
+
+    def close(self):
+        if self._h:
+            lib().mgpu_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_memory_budget(self, nbytes: int):
+        self.check(lib().mgpu_set_memory_budget(self._h, int(nbytes)))
+
+    def eval_rhs(self, g: GraphArrays, nodes, pop, y, t) -> np.ndarray:
+        nodes = np.ascontiguousarray(nodes, np.int32)
+        cnt = nodes.shape[0]
+        pop = np.ascontiguousarray(pop, np.float64).reshape(cnt, g.n)
+        y = np.ascontiguousarray(y, np.float64).reshape(cnt, g.n)
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(t, np.float64), (cnt,)))
+        out = np.zeros((cnt, g.n))
+        cg = g.as_ctypes()
+        self.check(lib().mgpu_eval_rhs(self._h, ctypes.byref(cg), cnt, _ip(nodes), _dp(pop), _dp(y), _dp(t),
+                                       _dp(out)))
+        return out
+
+    def simulate(self, g: GraphArrays, nodes, t0: float, tmax: float, dt0: float, opts=None, max_points=4096):
+        """Per node: (times [P], values [P, 10G]) of every accepted step."""
+        opts = opts or integrator_opts()
+        nodes = np.ascontiguousarray(nodes, np.int32)
+        cnt = nodes.shape[0]
+        out_t = np.zeros((cnt, max_points))
+        out_y = np.zeros((cnt, max_points, g.n))
+        npts = np.zeros(cnt, np.int32)
+        cg = g.as_ctypes()
+        self.check(lib().mgpu_simulate(self._h, ctypes.byref(cg), cnt, _ip(nodes), t0, tmax, dt0, ctypes.byref(opts),
+                                       max_points, _dp(out_t), _dp(out_y), _ip(npts)))
+        return [(out_t[k, :npts[k]].copy(), out_y[k, :npts[k]].copy()) for k in range(cnt)]
+
+
+class Batch:
+    """mgpu_batch: graphs simulated together (GraphSimulation per graph)."""
+
+    def __init__(self, ctx: Context, graphs: Sequence[GraphArrays], t0: float = 0.0, opts: MgpuSolverOpts = None):
+        self.ctx = ctx
+        self.graphs = list(graphs)
+        self._arr = (MgpuGraph * len(self.graphs))(*[g.as_ctypes() for g in self.graphs])
+        self._h = ctypes.c_void_p()
+        opts = opts or solver_opts()
+        ctx.check(lib().mgpu_batch_create(ctx.handle, self._arr, len(self.graphs), t0, ctypes.byref(opts),
+                                          ctypes.byref(self._h)))
+        self.sizes = [g.num_nodes * g.n for g in self.graphs]
+        self.total = int(sum(self.sizes))
+
+    def advance(self, tmax: float, tmax_per_graph=None):
+        if tmax_per_graph is not None:
+            tpg = np.ascontiguousarray(tmax_per_graph, np.float64)
+            assert tpg.shape[0] == len(self.graphs)
+            self.ctx.check(lib().mgpu_batch_advance(self._h, float(tmax), _dp(tpg)))
+        else:
+            self.ctx.check(lib().mgpu_batch_advance(self._h, float(tmax), ctypes.POINTER(ctypes.c_double)()))
+
+    def state_flat(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.total)
+        self.ctx.check(lib().mgpu_batch_get_state(self._h, _dp(out)))
+        return out
+
+    def states(self):
+        flat = self.state_flat()
+        res, off = [], 0
+        for g, s in zip(self.graphs, self.sizes):
+            res.append(flat[off:off + s].reshape(g.num_nodes, g.n))
+            off += s
+        return res
+
+    def set_state(self, flat: np.ndarray):
+        flat = np.ascontiguousarray(flat, np.float64)
+        assert flat.size == self.total
+        self.ctx.check(lib().mgpu_batch_set_state(self._h, _dp(flat)))
+
+    def times(self) -> np.ndarray:
+        out = np.zeros(len(self.graphs))
+        self.ctx.check(lib().mgpu_batch_get_time(self._h, _dp(out)))
+        return out
+
+    def stats(self) -> dict:
+        s = MgpuStats()
+        self.ctx.check(lib().mgpu_batch_get_stats(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def reset(self, t0: float = 0.0):
+        self.ctx.check(lib().mgpu_batch_reset(self._h, float(t0)))
+
+    def timing(self) -> dict:
+        t = MgpuTiming()
+        self.ctx.check(lib().mgpu_batch_get_timing(self._h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def device_bytes(self) -> int:
+        return int(lib().mgpu_batch_device_bytes(self._h))
+
+    def close(self):
+        if self._h:
+            lib().mgpu_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

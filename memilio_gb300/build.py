@@ -1,0 +1,82 @@
+"""Builds libmiogpu.so (the sm_103a kernels and the C ABI) in-tree with nvcc.
+
+Translation units are compiled in parallel, then linked into
+memilio_gb300/lib/libmiogpu.so. The C++ facade examples under
+memilio_gb300/cpp/ are built by build_facade().
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import hashlib
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
+LIB_DIR = os.path.join(HERE, "lib")
+LIB = os.path.join(LIB_DIR, "libmiogpu.so")
+
+SOURCES = ["capi.cu", "ode_plain.cu", "ode_batched.cu", "exchange.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+              "--expt-relaxed-constexpr"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _deps_hash(src: str) -> str:
+    h = hashlib.sha1()
+    for f in sorted(os.listdir(CSRC)) + ["../../include/miogpu.h", "../../include/miogpu_layout.h"]:
+        p = os.path.normpath(os.path.join(CSRC, f))
+        if p.endswith((".cu", ".cuh", ".h")) and os.path.exists(p):
+            with open(p, "rb") as fh:
+                h.update(fh.read())
+    h.update(" ".join(ARCH + NVCC_FLAGS).encode())
+    h.update(src.encode())
+    return h.hexdigest()[:16]
+
+
+def _compile(src: str, verbose: bool) -> str:
+    obj = os.path.join(OBJ, src.replace(".cu", f".{_deps_hash(src)}.o"))
+    if os.path.exists(obj):
+        return obj
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj + ".tmp"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
+    os.replace(obj + ".tmp", obj)
+    return obj
+
+
+def build(verbose: bool = False) -> str:
+    """Compile and link libmiogpu.so; returns its path. Up-to-date objects are reused."""
+    os.makedirs(OBJ, exist_ok=True)
+    os.makedirs(LIB_DIR, exist_ok=True)
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
+    stamp = hashlib.sha1("".join(objs).encode()).hexdigest()[:16]
+    stamp_file = LIB + ".stamp"
+    if os.path.exists(LIB) and os.path.exists(stamp_file) and open(stamp_file).read() == stamp:
+        return LIB
+    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB + ".tmp", *objs]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(LIB + ".tmp", LIB)
+    with open(stamp_file, "w") as fh:
+        fh.write(stamp)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

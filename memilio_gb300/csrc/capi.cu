@@ -1,0 +1,1052 @@
+// capi.cu — the extern "C" entry points of libmiogpu (include/miogpu.h):
+// contexts, device upload of graph batches, and the exchange-interval
+// schedule of GraphSimulation::advance.
+#include "mgpu_internal.cuh"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+using namespace mgpu;
+
+struct mgpu_context {
+    int device           = 0;
+    cudaStream_t stream  = nullptr;
+    std::string error    = "";
+    int64_t budget       = 0; // 0 = free HBM
+    int64_t allocated    = 0;
+};
+
+namespace
+{
+
+struct Fail {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string& msg)
+{
+    throw Fail{code, msg};
+}
+
+void ck(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) {
+        const int code = (e == cudaErrorMemoryAllocation) ? MGPU_OOM : MGPU_CUDA_ERROR;
+        fail(code, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+// Device allocations owned by a batch or a call.
+struct DevPool {
+    mgpu_context* ctx = nullptr;
+    std::vector<std::pair<void*, int64_t>> blocks;
+    int64_t bytes = 0;
+
+    template <class T>
+    T* alloc(int64_t count)
+    {
+        const int64_t nb = std::max<int64_t>(count, 1) * (int64_t)sizeof(T);
+        if (ctx->budget > 0 && ctx->allocated + nb > ctx->budget) {
+            fail(MGPU_OOM, "device memory budget exceeded (" + std::to_string(ctx->allocated + nb) + " > " +
+                               std::to_string(ctx->budget) + " bytes)");
+        }
+        void* p = nullptr;
+        ck(cudaMalloc(&p, nb), "cudaMalloc");
+        blocks.emplace_back(p, nb);
+        bytes += nb;
+        ctx->allocated += nb;
+        return static_cast<T*>(p);
+    }
+    template <class T>
+    T* upload(const std::vector<T>& v)
+    {
+        T* d = alloc<T>((int64_t)v.size());
+        if (!v.empty()) {
+            ck(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream), "upload");
+        }
+        return d;
+    }
+    void release()
+    {
+        for (auto& b : blocks) {
+            cudaFree(b.first);
+            ctx->allocated -= b.second;
+        }
+        blocks.clear();
+        bytes = 0;
+    }
+};
+
+void validate_graph(const mgpu_graph& g, bool need_edges_sorted = true)
+{
+    if (g.num_nodes < 0 || g.num_edges < 0) {
+        fail(MGPU_INVALID_VALUE, "negative node or edge count");
+    }
+    if (g.num_groups < 1) {
+        fail(MGPU_INVALID_VALUE, "num_groups must be >= 1");
+    }
+    if (g.num_groups > MGPU_MAX_GROUPS) {
+        fail(MGPU_UNSUPPORTED, "num_groups > MGPU_MAX_GROUPS (" + std::to_string(MGPU_MAX_GROUPS) + ")");
+    }
+    if (g.num_contact_matrices < 1 || g.num_contact_matrices > MGPU_MAX_CONTACT_MATRICES) {
+        fail(MGPU_UNSUPPORTED, "num_contact_matrices must be in [1, MGPU_MAX_CONTACT_MATRICES]");
+    }
+    if (g.num_damping_points < 0 || g.num_damping_points == 1 || g.num_edge_damping_points < 0 ||
+        g.num_edge_damping_points == 1) {
+        fail(MGPU_INVALID_VALUE, "a damping cache has 0 or >= 2 points");
+    }
+    if (g.num_nodes > 0 && (!g.params || !g.contact_baseline || !g.init_state)) {
+        fail(MGPU_INVALID_VALUE, "params, contact_baseline and init_state are required");
+    }
+    if (g.num_damping_points > 0 && (!g.damping_times || !g.damping_values)) {
+        fail(MGPU_INVALID_VALUE, "damping_times/values required when num_damping_points > 0");
+    }
+    if (g.num_edges > 0 && (!g.edge_src || !g.edge_dst || !g.edge_coeff_baseline)) {
+        fail(MGPU_INVALID_VALUE, "edge_src, edge_dst and edge_coeff_baseline are required");
+    }
+    if (g.num_edge_damping_points > 0 && (!g.edge_damping_times || !g.edge_damping_values)) {
+        fail(MGPU_INVALID_VALUE, "edge damping times/values required when num_edge_damping_points > 0");
+    }
+    for (int e = 0; e < g.num_edges; ++e) {
+        const int s = g.edge_src[e], d = g.edge_dst[e];
+        if (s < 0 || s >= g.num_nodes || d < 0 || d >= g.num_nodes) {
+            fail(MGPU_OUT_OF_RANGE, "edge node index out of range");
+        }
+        if (s == d) {
+            fail(MGPU_INVALID_VALUE, "self-loop edges are not supported");
+        }
+        if (need_edges_sorted && e > 0) {
+            const int ps = g.edge_src[e - 1], pd = g.edge_dst[e - 1];
+            if (ps > s || (ps == s && pd >= d)) {
+                fail(MGPU_INVALID_VALUE, "edges must be sorted by (src, dst) without duplicates (graph.h:231-241)");
+            }
+        }
+    }
+    const int K = g.num_damping_points;
+    if (K > 0) {
+        const long GG = (long)g.num_groups * g.num_groups;
+        for (long v = 0; v < (long)g.num_nodes * g.num_contact_matrices; ++v) {
+            const double* T = g.damping_times + v * K;
+            for (int k = 1; k < K; ++k) {
+                if (!(T[k] >= T[k - 1])) {
+                    fail(MGPU_INVALID_VALUE, "damping cache times must be non-decreasing");
+                }
+            }
+            (void)GG;
+        }
+    }
+}
+
+} // namespace
+
+struct mgpu_batch {
+    mgpu_context* ctx = nullptr;
+    mgpu_solver_opts opts{};
+    DevPool pool;
+    BatchDev dev{};
+    int32_t num_graphs = 0;
+    int64_t n_max      = 0;
+    std::vector<int32_t> N, G, n;
+    std::vector<int64_t> node0, edge0, state_off;
+    int64_t state_total = 0;
+    double* init_state  = nullptr; // initial states (for reset)
+    double dt0          = 0.1;
+    std::vector<double> t_host;  // mirror of rt.t
+    std::vector<double> tmax_host;
+    double* d_tmax = nullptr;
+    // batched solver work lists per age-group count
+    std::map<int, std::pair<int32_t*, int64_t>> inst_by_G;
+    int instances_per_block = 0;
+    int64_t launches        = 0;
+    int64_t phases          = 0;
+    int64_t seq_exchanges   = 0;
+    // CUDA graph of one batched interval
+    cudaGraphExec_t graph_exec = nullptr;
+    bool graph_failed          = false;
+    // timing
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    std::vector<cudaEvent_t> ev_phase;
+    mgpu_timing timing{};
+
+    ~mgpu_batch()
+    {
+        if (graph_exec) {
+            cudaGraphExecDestroy(graph_exec);
+        }
+        for (auto e : ev_phase) {
+            cudaEventDestroy(e);
+        }
+        if (ev_start) {
+            cudaEventDestroy(ev_start);
+        }
+        if (ev_stop) {
+            cudaEventDestroy(ev_stop);
+        }
+        pool.release();
+    }
+
+    cudaEvent_t phase_event(size_t i)
+    {
+        while (ev_phase.size() <= i) {
+            cudaEvent_t e;
+            ck(cudaEventCreate(&e), "cudaEventCreate");
+            ev_phase.push_back(e);
+        }
+        return ev_phase[i];
+    }
+};
+
+namespace
+{
+
+__global__ void k_set_tmax(GraphRt* rt, const double* tmax, int num_graphs)
+{
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gi < num_graphs) {
+        rt[gi].tmax = tmax[gi];
+    }
+}
+
+// Restart: graph clocks and flags, node clocks, states, pending travelers.
+__global__ void k_reset(BatchDev B, const double* init_state, int64_t state_total, double t0, double dt0)
+{
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid < state_total) {
+        B.state[tid] = init_state[tid];
+    }
+    if (tid < B.num_nodes) {
+        B.node_t[tid]  = t0;
+        B.node_dt[tid] = dt0;
+    }
+    if (tid < B.num_edges) {
+        B.edge_pending[tid] = 0;
+    }
+    if (tid < B.num_graphs) {
+        GraphRt r;
+        memset(&r, 0, sizeof(r));
+        r.t         = t0;
+        r.tmax      = t0;
+        B.rt[tid]   = r;
+    }
+}
+
+// Upload graphs into one set of pools. `with_edges` false: edges ignored.
+void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, double t0, double dt0,
+                 bool with_edges, int64_t scratch_slots)
+{
+    mgpu_context* ctx = b->ctx;
+    b->pool.ctx       = ctx;
+    b->num_graphs     = num_graphs;
+    std::vector<DevGraph> dg(num_graphs);
+    int64_t nodes = 0, edges = 0, par = 0, con = 0, dtt = 0, dtv = 0, st = 0, ec = 0, edt = 0, edv = 0, tr = 0;
+    b->N.resize(num_graphs);
+    b->G.resize(num_graphs);
+    b->n.resize(num_graphs);
+    b->node0.resize(num_graphs);
+    b->edge0.resize(num_graphs);
+    b->state_off.resize(num_graphs);
+    b->n_max = 0;
+    for (int i = 0; i < num_graphs; ++i) {
+        const mgpu_graph& g = graphs[i];
+        validate_graph(g);
+        DevGraph& d   = dg[i];
+        const int G   = g.num_groups;
+        const int n   = G * kC;
+        const int E   = with_edges ? g.num_edges : 0;
+        const long GG = (long)G * G;
+        d.N           = g.num_nodes;
+        d.G           = G;
+        d.E           = E;
+        d.M           = g.num_contact_matrices;
+        d.K           = g.num_damping_points;
+        d.Ke          = with_edges ? g.num_edge_damping_points : 0;
+        d.n           = n;
+        d.method      = b->opts.integrator.method;
+        d.node0       = nodes;
+        d.edge0       = edges;
+        d.param_off   = par;
+        d.contact_off = con;
+        d.dtime_off   = dtt;
+        d.dval_off    = dtv;
+        d.state_off   = st;
+        d.ecoef_off   = ec;
+        d.edt_off     = edt;
+        d.edv_off     = edv;
+        nodes += g.num_nodes;
+        edges += E;
+        par += (int64_t)g.num_nodes * param_stride(G);
+        con += (int64_t)g.num_nodes * d.M * 2 * GG;
+        dtt += (int64_t)g.num_nodes * d.M * d.K;
+        dtv += (int64_t)g.num_nodes * d.M * d.K * GG;
+        st += (int64_t)g.num_nodes * n;
+        ec += (int64_t)E * 2 * n;
+        edt += (int64_t)E * d.Ke;
+        edv += (int64_t)E * d.Ke * n;
+        tr += (int64_t)E * n;
+        b->N[i]         = g.num_nodes;
+        b->G[i]         = G;
+        b->n[i]         = n;
+        b->node0[i]     = d.node0;
+        b->edge0[i]     = d.edge0;
+        b->state_off[i] = d.state_off;
+        b->n_max        = std::max<int64_t>(b->n_max, n);
+    }
+    b->state_total = st;
+    // host staging
+    std::vector<double> h_par(par), h_con(con), h_dtt(dtt), h_dtv(dtv), h_state(st), h_ec(ec), h_edt(edt),
+        h_edv(edv);
+    std::vector<int32_t> h_node_graph(nodes), h_edge_graph(edges), h_src(edges), h_dst(edges);
+    std::vector<uint8_t> h_any(edges);
+    std::vector<int64_t> h_trav_off(edges), h_out_ptr(nodes + 1, 0), h_in_ptr(nodes + 1, 0), h_in_edges(edges);
+    int64_t trav_pos = 0;
+    for (int i = 0; i < num_graphs; ++i) {
+        const mgpu_graph& g = graphs[i];
+        const DevGraph& d   = dg[i];
+        const int G = d.G, n = d.n;
+        const long GG = (long)G * G;
+        std::memcpy(h_par.data() + d.param_off, g.params, sizeof(double) * (size_t)g.num_nodes * param_stride(G));
+        for (long v = 0; v < g.num_nodes; ++v) {
+            for (int m = 0; m < d.M; ++m) {
+                double* dst      = h_con.data() + d.contact_off + (v * d.M + m) * 2 * GG;
+                const double* Bs = g.contact_baseline + (v * d.M + m) * GG;
+                std::memcpy(dst, Bs, sizeof(double) * GG);
+                if (g.contact_minimum) {
+                    std::memcpy(dst + GG, g.contact_minimum + (v * d.M + m) * GG, sizeof(double) * GG);
+                }
+                else {
+                    std::fill(dst + GG, dst + 2 * GG, 0.0);
+                }
+            }
+        }
+        if (d.K) {
+            std::memcpy(h_dtt.data() + d.dtime_off, g.damping_times, sizeof(double) * (size_t)g.num_nodes * d.M * d.K);
+            std::memcpy(h_dtv.data() + d.dval_off, g.damping_values,
+                        sizeof(double) * (size_t)g.num_nodes * d.M * d.K * GG);
+        }
+        std::memcpy(h_state.data() + d.state_off, g.init_state, sizeof(double) * (size_t)g.num_nodes * n);
+        for (long v = 0; v < g.num_nodes; ++v) {
+            h_node_graph[d.node0 + v] = i;
+        }
+        // edges: CSR by source (already sorted), CSC by destination (sorted by source within)
+        std::vector<int64_t> indeg(g.num_nodes + 1, 0);
+        for (int e = 0; e < d.E; ++e) {
+            const int64_t ge = d.edge0 + e;
+            h_edge_graph[ge] = i;
+            h_src[ge]        = (int32_t)(d.node0 + g.edge_src[e]);
+            h_dst[ge]        = (int32_t)(d.node0 + g.edge_dst[e]);
+            h_out_ptr[d.node0 + g.edge_src[e] + 1]++;
+            indeg[g.edge_dst[e] + 1]++;
+            double* dc = h_ec.data() + d.ecoef_off + (int64_t)e * 2 * n;
+            std::memcpy(dc, g.edge_coeff_baseline + (int64_t)e * n, sizeof(double) * n);
+            if (g.edge_coeff_minimum) {
+                std::memcpy(dc + n, g.edge_coeff_minimum + (int64_t)e * n, sizeof(double) * n);
+            }
+            else {
+                std::fill(dc + n, dc + 2 * n, 0.0);
+            }
+            bool any = false;
+            for (int j = 0; j < n; ++j) {
+                any = any || (dc[j] > 0.0);
+            }
+            h_any[ge] = any ? 1 : 0;
+            if (d.Ke) {
+                std::memcpy(h_edt.data() + d.edt_off + (int64_t)e * d.Ke, g.edge_damping_times + (int64_t)e * d.Ke,
+                            sizeof(double) * d.Ke);
+                std::memcpy(h_edv.data() + d.edv_off + (int64_t)e * d.Ke * n,
+                            g.edge_damping_values + (int64_t)e * d.Ke * n, sizeof(double) * d.Ke * n);
+            }
+            h_trav_off[ge] = trav_pos;
+            trav_pos += n;
+        }
+        for (int v = 0; v < g.num_nodes; ++v) {
+            indeg[v + 1] += indeg[v];
+        }
+        std::vector<int64_t> fillp(indeg.begin(), indeg.end() - 1);
+        for (int e = 0; e < d.E; ++e) { // edges visited in (src, dst) order -> CSC sorted by src
+            const int v                                       = g.edge_dst[e];
+            h_in_edges[d.edge0 + indeg[0] + fillp[v]++ - 0]   = d.edge0 + e;
+        }
+        for (int v = 0; v <= g.num_nodes; ++v) {
+            h_in_ptr[d.node0 + v] = d.edge0 + indeg[v];
+        }
+    }
+    for (int64_t v = 0; v < nodes; ++v) {
+        h_out_ptr[v + 1] += h_out_ptr[v];
+    }
+    // the prefix over all nodes of all graphs is global because graphs are concatenated in order
+    BatchDev& B      = b->dev;
+    B.num_graphs     = num_graphs;
+    B.num_nodes      = nodes;
+    B.num_edges      = edges;
+    B.graphs         = b->pool.upload(dg);
+    std::vector<GraphRt> h_rt(num_graphs);
+    for (auto& r : h_rt) {
+        std::memset(&r, 0, sizeof(r));
+        r.t    = t0;
+        r.tmax = t0;
+    }
+    B.rt         = b->pool.upload(h_rt);
+    B.node_graph = b->pool.upload(h_node_graph);
+    B.edge_graph = b->pool.upload(h_edge_graph);
+    B.params     = b->pool.upload(h_par);
+    B.contact    = b->pool.upload(h_con);
+    B.dtimes     = b->pool.upload(h_dtt);
+    B.dvals      = b->pool.upload(h_dtv);
+    B.state      = b->pool.upload(h_state);
+    b->init_state = b->pool.upload(h_state);
+    b->dt0        = dt0;
+    B.v0         = b->pool.alloc<double>(st);
+    B.ypre       = b->pool.alloc<double>(st);
+    B.ynew       = b->pool.alloc<double>(std::max<int64_t>(st, scratch_slots * b->n_max));
+    std::vector<double> h_t(nodes, t0), h_dt(nodes, dt0);
+    B.node_t          = b->pool.upload(h_t);
+    B.node_dt         = b->pool.upload(h_dt);
+    B.edge_src        = b->pool.upload(h_src);
+    B.edge_dst        = b->pool.upload(h_dst);
+    B.ecoef           = b->pool.upload(h_ec);
+    B.edt             = b->pool.upload(h_edt);
+    B.edv             = b->pool.upload(h_edv);
+    B.edge_static_any = b->pool.upload(h_any);
+    B.edge_pending    = b->pool.alloc<uint8_t>(edges);
+    ck(cudaMemsetAsync(B.edge_pending, 0, std::max<int64_t>(edges, 1), ctx->stream), "memset");
+    B.trav     = b->pool.alloc<double>(tr);
+    B.trav_off = b->pool.upload(h_trav_off);
+    B.out_ptr  = b->pool.upload(h_out_ptr);
+    B.in_ptr   = b->pool.upload(h_in_ptr);
+    B.in_edges = b->pool.upload(h_in_edges);
+    B.scratch_stride = std::max<int64_t>(scratch_slots, 1);
+    B.scratch_nmax   = (int32_t)b->n_max;
+    B.scratch        = scratch_slots > 0 ? b->pool.alloc<double>(8 * b->n_max * B.scratch_stride) : nullptr;
+    B.opts.abs_tol   = b->opts.integrator.abs_tol;
+    B.opts.rel_tol   = b->opts.integrator.rel_tol;
+    B.opts.dt_min    = b->opts.integrator.dt_min;
+    B.opts.dt_max    = b->opts.integrator.dt_max;
+    B.opts.max_steps = b->opts.max_steps_per_interval > 0 ? b->opts.max_steps_per_interval : 100000;
+    B.opts.method    = b->opts.integrator.method;
+    B.err            = b->pool.alloc<int32_t>(1);
+    B.counters       = b->pool.alloc<unsigned long long>(CNT_NUM);
+    ck(cudaMemsetAsync(B.err, 0, sizeof(int32_t), ctx->stream), "memset");
+    ck(cudaMemsetAsync(B.counters, 0, sizeof(unsigned long long) * CNT_NUM, ctx->stream), "memset");
+    b->d_tmax = b->pool.alloc<double>(num_graphs);
+    b->t_host.assign(num_graphs, t0);
+    b->tmax_host.assign(num_graphs, t0);
+    // instance lists per G for the batched solver
+    std::map<int, std::vector<int32_t>> lists;
+    for (int i = 0; i < num_graphs; ++i) {
+        auto& l = lists[b->G[i]];
+        for (int v = 0; v < b->N[i]; ++v) {
+            l.push_back((int32_t)(b->node0[i] + v));
+        }
+    }
+    for (auto& kv : lists) {
+        b->inst_by_G[kv.first] = {b->pool.upload(kv.second), (int64_t)kv.second.size()};
+    }
+    ck(cudaStreamSynchronize(ctx->stream), "upload sync");
+}
+
+int check_device_error(mgpu_batch* b)
+{
+    int32_t err = 0;
+    ck(cudaMemcpyAsync(&err, b->dev.err, sizeof(err), cudaMemcpyDeviceToHost, b->ctx->stream), "read error word");
+    ck(cudaStreamSynchronize(b->ctx->stream), "sync");
+    if (err & (ERR_STEP_CAP | ERR_NONFINITE)) {
+        fail(MGPU_STEP_FAILED, std::string("node solve failed:") + ((err & ERR_STEP_CAP) ? " step cap reached" : "") +
+                                   ((err & ERR_NONFINITE) ? " non-finite state" : ""));
+    }
+    if (err) {
+        fail(MGPU_UNKNOWN_ERROR, "device error word " + std::to_string(err));
+    }
+    return MGPU_OK;
+}
+
+// One batched interval: interval bookkeeping, node solves per G, exchange.
+// With events (profile mode): ev[0] before the node solves, ev[1] after them,
+// ev[2] after the exchange.
+void enqueue_batched_phase(mgpu_batch* b, cudaStream_t s, cudaEvent_t* ev = nullptr)
+{
+    const BatchDev& B = b->dev;
+    launch_phase_begin(B, b->opts.dt_exchange, s);
+    if (ev) {
+        ck(cudaEventRecord(ev[0], s), "cudaEventRecord");
+    }
+    for (auto& kv : b->inst_by_G) {
+        launch_ode_batched(B, kv.first, b->opts.precision, kv.second.first, kv.second.second,
+                           b->instances_per_block, 0, s);
+    }
+    if (ev) {
+        ck(cudaEventRecord(ev[1], s), "cudaEventRecord");
+    }
+    int64_t l = 0;
+    launch_exchange(B, b->n_max, s, &l);
+    launch_phase_end(B, s);
+    if (ev) {
+        ck(cudaEventRecord(ev[2], s), "cudaEventRecord");
+    }
+}
+
+int64_t phases_needed(const mgpu_batch* b, std::vector<double>& t)
+{
+    // mirrors k_phase_begin/k_phase_end arithmetic
+    int64_t P = 0;
+    for (int i = 0; i < b->num_graphs; ++i) {
+        int64_t p = 0;
+        double tt = t[i];
+        while (tt < b->tmax_host[i]) {
+            double dt = b->opts.dt_exchange;
+            if (tt + dt > b->tmax_host[i]) {
+                dt = b->tmax_host[i] - tt;
+            }
+            tt += dt;
+            ++p;
+        }
+        t[i] = tt;
+        P    = std::max(P, p);
+    }
+    return P;
+}
+
+template <class F>
+int guarded(mgpu_context* ctx, F&& f)
+{
+    if (!ctx) {
+        return MGPU_INVALID_VALUE;
+    }
+    try {
+        const int rc = f();
+        if (rc == MGPU_OK) {
+            ctx->error.clear();
+        }
+        return rc;
+    }
+    catch (const Fail& e) {
+        ctx->error = e.msg;
+        return e.code;
+    }
+    catch (const std::bad_alloc&) {
+        ctx->error = "host allocation failed";
+        return MGPU_OOM;
+    }
+    catch (const std::exception& e) {
+        ctx->error = e.what();
+        return MGPU_UNKNOWN_ERROR;
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+void mgpu_default_solver_opts(mgpu_solver_opts* o)
+{
+    if (!o) {
+        return;
+    }
+    std::memset(o, 0, sizeof(*o));
+    o->integrator.method  = MGPU_METHOD_CASH_KARP54;
+    o->integrator.abs_tol = 1e-10;
+    o->integrator.rel_tol = 1e-5;
+    o->integrator.dt_min  = DBL_MIN;
+    o->integrator.dt_max  = DBL_MAX;
+    o->dt0                = 0.1;
+    o->dt_exchange        = 0.5;
+    o->precision          = MGPU_PRECISION_MIXED;
+    o->use_cuda_graph     = 1;
+}
+
+int mgpu_create(int device, mgpu_context** out)
+{
+    if (!out) {
+        return MGPU_INVALID_VALUE;
+    }
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        return MGPU_CUDA_ERROR;
+    }
+    if (device < 0 || device >= count) {
+        return MGPU_OUT_OF_RANGE;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) {
+        return MGPU_CUDA_ERROR;
+    }
+    auto* ctx   = new (std::nothrow) mgpu_context();
+    if (!ctx) {
+        return MGPU_OOM;
+    }
+    ctx->device = device;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return MGPU_CUDA_ERROR;
+    }
+    *out = ctx;
+    return MGPU_OK;
+}
+
+void mgpu_destroy(mgpu_context* ctx)
+{
+    if (!ctx) {
+        return;
+    }
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* mgpu_last_error(const mgpu_context* ctx)
+{
+    return ctx ? ctx->error.c_str() : "no context";
+}
+
+int mgpu_set_memory_budget(mgpu_context* ctx, int64_t bytes)
+{
+    return guarded(ctx, [&]() -> int {
+        if (bytes < 0) {
+            fail(MGPU_INVALID_VALUE, "negative budget");
+        }
+        ctx->budget = bytes;
+        return MGPU_OK;
+    });
+}
+
+int mgpu_eval_rhs(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, const int32_t* nodes,
+                  const double* pop, const double* y, const double* t, double* dydt)
+{
+    return guarded(ctx, [&]() -> int {
+        if (!graph || count < 0 || (count > 0 && (!nodes || !pop || !y || !t || !dydt))) {
+            fail(MGPU_INVALID_VALUE, "null argument");
+        }
+        if (count == 0) {
+            return MGPU_OK;
+        }
+        ck(cudaSetDevice(ctx->device), "cudaSetDevice");
+        mgpu_graph g = *graph;
+        g.num_edges  = 0;
+        for (int k = 0; k < count; ++k) {
+            if (nodes[k] < 0 || nodes[k] >= g.num_nodes) {
+                fail(MGPU_OUT_OF_RANGE, "node index out of range");
+            }
+        }
+        mgpu_batch b;
+        b.ctx = ctx;
+        mgpu_default_solver_opts(&b.opts);
+        build_batch(&b, &g, 1, 0.0, 0.1, false, 0);
+        const int n = g.num_groups * kC;
+        DevPool io;
+        io.ctx = ctx;
+        try {
+            int32_t* d_nodes = io.alloc<int32_t>(count);
+            double* d_pop    = io.alloc<double>((int64_t)count * n);
+            double* d_y      = io.alloc<double>((int64_t)count * n);
+            double* d_t      = io.alloc<double>(count);
+            double* d_out    = io.alloc<double>((int64_t)count * n);
+            cudaStream_t s   = ctx->stream;
+            ck(cudaMemcpyAsync(d_nodes, nodes, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s), "h2d");
+            ck(cudaMemcpyAsync(d_pop, pop, sizeof(double) * count * n, cudaMemcpyHostToDevice, s), "h2d");
+            ck(cudaMemcpyAsync(d_y, y, sizeof(double) * count * n, cudaMemcpyHostToDevice, s), "h2d");
+            ck(cudaMemcpyAsync(d_t, t, sizeof(double) * count, cudaMemcpyHostToDevice, s), "h2d");
+            launch_eval_rhs(b.dev, d_nodes, count, d_pop, d_y, d_t, d_out, s);
+            ck(cudaGetLastError(), "k_eval_rhs");
+            ck(cudaMemcpyAsync(dydt, d_out, sizeof(double) * count * n, cudaMemcpyDeviceToHost, s), "d2h");
+            ck(cudaStreamSynchronize(s), "sync");
+        }
+        catch (...) {
+            io.release();
+            throw;
+        }
+        io.release();
+        return MGPU_OK;
+    });
+}
+
+int mgpu_simulate(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, const int32_t* nodes, double t0,
+                  double tmax, double dt0, const mgpu_integrator_opts* opts, int32_t max_points, double* out_t,
+                  double* out_y, int32_t* num_points)
+{
+    return guarded(ctx, [&]() -> int {
+        if (!graph || !opts || count < 0 || max_points < 1 ||
+            (count > 0 && (!nodes || !out_t || !out_y || !num_points))) {
+            fail(MGPU_INVALID_VALUE, "null argument");
+        }
+        if (!(dt0 > 0)) {
+            fail(MGPU_INVALID_VALUE, "dt0 must be > 0");
+        }
+        if (count == 0) {
+            return MGPU_OK;
+        }
+        ck(cudaSetDevice(ctx->device), "cudaSetDevice");
+        mgpu_graph g = *graph;
+        g.num_edges  = 0;
+        for (int k = 0; k < count; ++k) {
+            if (nodes[k] < 0 || nodes[k] >= g.num_nodes) {
+                fail(MGPU_OUT_OF_RANGE, "node index out of range");
+            }
+        }
+        mgpu_batch b;
+        b.ctx = ctx;
+        mgpu_default_solver_opts(&b.opts);
+        b.opts.integrator = *opts;
+        build_batch(&b, &g, 1, t0, dt0, false, count);
+        const int n = g.num_groups * kC;
+        DevPool io;
+        io.ctx = ctx;
+        int rc = MGPU_OK;
+        try {
+            int32_t* d_nodes = io.alloc<int32_t>(count);
+            double* d_t      = io.alloc<double>((int64_t)count * max_points);
+            double* d_y      = io.alloc<double>((int64_t)count * max_points * n);
+            int32_t* d_np    = io.alloc<int32_t>(count);
+            cudaStream_t s   = ctx->stream;
+            ck(cudaMemcpyAsync(d_nodes, nodes, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s), "h2d");
+            launch_simulate(b.dev, d_nodes, count, t0, tmax, dt0, max_points, d_t, d_y, d_np, s);
+            ck(cudaGetLastError(), "k_simulate");
+            ck(cudaMemcpyAsync(num_points, d_np, sizeof(int32_t) * count, cudaMemcpyDeviceToHost, s), "d2h");
+            ck(cudaMemcpyAsync(out_t, d_t, sizeof(double) * count * max_points, cudaMemcpyDeviceToHost, s), "d2h");
+            ck(cudaMemcpyAsync(out_y, d_y, sizeof(double) * count * max_points * n, cudaMemcpyDeviceToHost, s),
+               "d2h");
+            ck(cudaStreamSynchronize(s), "sync");
+            for (int k = 0; k < count; ++k) {
+                if (num_points[k] < 0) {
+                    num_points[k] = max_points;
+                    rc            = MGPU_OUT_OF_RANGE;
+                }
+            }
+            check_device_error(&b);
+        }
+        catch (...) {
+            io.release();
+            throw;
+        }
+        io.release();
+        if (rc != MGPU_OK) {
+            ctx->error = "trajectory longer than max_points";
+        }
+        return rc;
+    });
+}
+
+int mgpu_batch_create(mgpu_context* ctx, const mgpu_graph* graphs, int32_t num_graphs, double t0,
+                      const mgpu_solver_opts* opts, mgpu_batch** out)
+{
+    return guarded(ctx, [&]() -> int {
+        if (!graphs || num_graphs < 1 || !out) {
+            fail(MGPU_INVALID_VALUE, "null argument or no graphs");
+        }
+        *out = nullptr;
+        mgpu_solver_opts o;
+        if (opts) {
+            o = *opts;
+        }
+        else {
+            mgpu_default_solver_opts(&o);
+        }
+        if (!(o.dt_exchange > 0) || !(o.dt0 > 0)) {
+            fail(MGPU_INVALID_VALUE, "dt0 and dt_exchange must be > 0");
+        }
+        if (o.precision < MGPU_PRECISION_FP64_PLAIN || o.precision > MGPU_PRECISION_MIXED) {
+            fail(MGPU_INVALID_VALUE, "unknown precision");
+        }
+        if (o.precision != MGPU_PRECISION_FP64_PLAIN && o.integrator.method != MGPU_METHOD_CASH_KARP54) {
+            fail(MGPU_UNSUPPORTED, "the batched solvers implement Cash-Karp 5(4) only; use MGPU_PRECISION_FP64_PLAIN");
+        }
+        ck(cudaSetDevice(ctx->device), "cudaSetDevice");
+        auto* b = new mgpu_batch();
+        b->ctx  = ctx;
+        b->opts = o;
+        try {
+            int64_t max_nodes = 0;
+            for (int i = 0; i < num_graphs; ++i) {
+                max_nodes = std::max<int64_t>(max_nodes, graphs[i].num_nodes);
+            }
+            const int64_t slots = (o.precision == MGPU_PRECISION_FP64_PLAIN) ? max_nodes : 0;
+            build_batch(b, graphs, num_graphs, t0, o.dt0, true, slots);
+            b->instances_per_block = o.instances_per_block;
+        }
+        catch (...) {
+            delete b;
+            throw;
+        }
+        *out = b;
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        cudaStream_t s = b->ctx->stream;
+        for (int i = 0; i < b->num_graphs; ++i) {
+            b->tmax_host[i] = tmax_per_graph ? tmax_per_graph[i] : tmax;
+        }
+        ck(cudaMemcpyAsync(b->d_tmax, b->tmax_host.data(), sizeof(double) * b->num_graphs, cudaMemcpyHostToDevice,
+                           s),
+           "h2d tmax");
+        if (!b->ev_start) {
+            ck(cudaEventCreate(&b->ev_start), "cudaEventCreate");
+            ck(cudaEventCreate(&b->ev_stop), "cudaEventCreate");
+        }
+        unsigned long long c0[CNT_NUM];
+        ck(cudaMemcpyAsync(c0, b->dev.counters, sizeof(c0), cudaMemcpyDeviceToHost, s), "d2h counters");
+        ck(cudaStreamSynchronize(s), "sync");
+        const int64_t attempts0 = (int64_t)(c0[CNT_ACCEPTED] + c0[CNT_REJECTED]);
+        std::vector<size_t> ev_base;
+        size_t nev           = 0;
+        int64_t ode_launches = 0;
+        ck(cudaEventRecord(b->ev_start, s), "cudaEventRecord");
+        k_set_tmax<<<(b->num_graphs + 127) / 128, 128, 0, s>>>(b->dev.rt, b->d_tmax, b->num_graphs);
+        ++b->launches;
+        std::vector<double> t_end = b->t_host;
+        const int64_t P           = phases_needed(b, t_end);
+        const BatchDev& B         = b->dev;
+        if (b->opts.precision == MGPU_PRECISION_FP64_PLAIN) {
+            // the plain drop-in: graphs one after another, as ParameterStudy runs them
+            for (int i = 0; i < b->num_graphs; ++i) {
+                BatchDev Bi   = B;
+                std::vector<double> ti(1, b->t_host[i]);
+                int64_t Pi    = 0;
+                {
+                    double tt = b->t_host[i];
+                    while (tt < b->tmax_host[i]) {
+                        double dt = b->opts.dt_exchange;
+                        if (tt + dt > b->tmax_host[i]) {
+                            dt = b->tmax_host[i] - tt;
+                        }
+                        tt += dt;
+                        ++Pi;
+                    }
+                }
+                // restrict every kernel to graph i
+                Bi.graphs     = B.graphs + i;
+                Bi.rt         = B.rt + i;
+                Bi.num_graphs = 1;
+                for (int64_t p = 0; p < Pi; ++p) {
+                    cudaEvent_t* ev = nullptr;
+                    if (b->opts.profile) {
+                        ev_base.push_back(nev);
+                        b->phase_event(nev + 2);
+                        ev = &b->ev_phase[nev];
+                        nev += 3;
+                    }
+                    launch_phase_begin(Bi, b->opts.dt_exchange, s);
+                    if (ev) {
+                        ck(cudaEventRecord(ev[0], s), "cudaEventRecord");
+                    }
+                    launch_ode_plain(B, b->node0[i], b->node0[i] + b->N[i], s);
+                    if (ev) {
+                        ck(cudaEventRecord(ev[1], s), "cudaEventRecord");
+                    }
+                    int64_t l = 0;
+                    launch_exchange_range(B, i, 1, b->node0[i], b->N[i], b->edge0[i],
+                                          (i + 1 < b->num_graphs ? b->edge0[i + 1] : B.num_edges) - b->edge0[i],
+                                          b->n[i], s, &l);
+                    launch_phase_end(Bi, s);
+                    if (ev) {
+                        ck(cudaEventRecord(ev[2], s), "cudaEventRecord");
+                    }
+                    b->launches += 3 + l;
+                    ++ode_launches;
+                }
+                b->phases += Pi;
+            }
+        }
+        else if (b->opts.profile) {
+            for (int64_t p = 0; p < P; ++p) {
+                b->phase_event(nev + 2);
+                ev_base.push_back(nev);
+                enqueue_batched_phase(b, s, &b->ev_phase[nev]);
+                nev += 3;
+                ode_launches += (int64_t)b->inst_by_G.size();
+            }
+            b->launches += P * (3 + (int64_t)b->inst_by_G.size() + (B.num_edges > 0 ? 7 : 1));
+            b->phases += P;
+        }
+        else {
+            const bool use_graph = b->opts.use_cuda_graph && !b->graph_failed;
+            if (use_graph && !b->graph_exec && P > 0) {
+                cudaGraph_t graph = nullptr;
+                ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+                enqueue_batched_phase(b, s);
+                cudaError_t e = cudaStreamEndCapture(s, &graph);
+                if (e == cudaSuccess) {
+                    e = cudaGraphInstantiate(&b->graph_exec, graph, 0);
+                    cudaGraphDestroy(graph);
+                }
+                if (e != cudaSuccess) {
+                    cudaGetLastError();
+                    b->graph_failed = true;
+                    b->graph_exec   = nullptr;
+                }
+            }
+            const int64_t per_phase = 3 + (int64_t)b->inst_by_G.size() + (B.num_edges > 0 ? 7 : 1);
+            for (int64_t p = 0; p < P; ++p) {
+                if (b->graph_exec) {
+                    ck(cudaGraphLaunch(b->graph_exec, s), "cudaGraphLaunch");
+                }
+                else {
+                    enqueue_batched_phase(b, s);
+                }
+            }
+            b->launches += P * per_phase;
+            b->phases += P;
+        }
+        ck(cudaGetLastError(), "advance launch");
+        ck(cudaEventRecord(b->ev_stop, s), "cudaEventRecord");
+        b->t_host = t_end;
+        const int rc = check_device_error(b);
+        float ms = 0.0f;
+        ck(cudaEventElapsedTime(&ms, b->ev_start, b->ev_stop), "cudaEventElapsedTime");
+        b->timing.advance_ms = ms;
+        double ode = 0.0, exch = 0.0;
+        for (size_t k : ev_base) {
+            float a = 0.0f, c = 0.0f;
+            ck(cudaEventElapsedTime(&a, b->ev_phase[k], b->ev_phase[k + 1]), "cudaEventElapsedTime");
+            ck(cudaEventElapsedTime(&c, b->ev_phase[k + 1], b->ev_phase[k + 2]), "cudaEventElapsedTime");
+            ode += a;
+            exch += c;
+        }
+        b->timing.ode_ms       = ode;
+        b->timing.exchange_ms  = exch;
+        b->timing.ode_launches = ode_launches;
+        unsigned long long c1[CNT_NUM];
+        ck(cudaMemcpy(c1, b->dev.counters, sizeof(c1), cudaMemcpyDeviceToHost), "d2h counters");
+        b->timing.attempts = (int64_t)(c1[CNT_ACCEPTED] + c1[CNT_REJECTED]) - attempts0;
+        return rc;
+    });
+}
+
+int mgpu_batch_get_timing(mgpu_batch* b, mgpu_timing* out)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!out) {
+            fail(MGPU_INVALID_VALUE, "null output");
+        }
+        *out = b->timing;
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_reset(mgpu_batch* b, double t0)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        const int64_t n = std::max<int64_t>(
+            std::max<int64_t>(b->state_total, b->dev.num_nodes),
+            std::max<int64_t>(b->dev.num_edges, (int64_t)b->num_graphs));
+        k_reset<<<(unsigned)((n + 255) / 256), 256, 0, b->ctx->stream>>>(b->dev, b->init_state, b->state_total, t0,
+                                                                          b->dt0);
+        ++b->launches;
+        ck(cudaGetLastError(), "k_reset");
+        ck(cudaStreamSynchronize(b->ctx->stream), "sync");
+        b->t_host.assign(b->num_graphs, t0);
+        b->tmax_host.assign(b->num_graphs, t0);
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_get_state(mgpu_batch* b, double* out)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!out) {
+            fail(MGPU_INVALID_VALUE, "null output");
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        ck(cudaMemcpyAsync(out, b->dev.state, sizeof(double) * b->state_total, cudaMemcpyDeviceToHost,
+                           b->ctx->stream),
+           "d2h state");
+        ck(cudaStreamSynchronize(b->ctx->stream), "sync");
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_set_state(mgpu_batch* b, const double* state)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!state) {
+            fail(MGPU_INVALID_VALUE, "null input");
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        ck(cudaMemcpyAsync(b->dev.state, state, sizeof(double) * b->state_total, cudaMemcpyHostToDevice,
+                           b->ctx->stream),
+           "h2d state");
+        ck(cudaStreamSynchronize(b->ctx->stream), "sync");
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_get_time(mgpu_batch* b, double* out)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!out) {
+            fail(MGPU_INVALID_VALUE, "null output");
+        }
+        std::copy(b->t_host.begin(), b->t_host.end(), out);
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_get_stats(mgpu_batch* b, mgpu_stats* out)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!out) {
+            fail(MGPU_INVALID_VALUE, "null output");
+        }
+        unsigned long long c[CNT_NUM];
+        ck(cudaMemcpyAsync(c, b->dev.counters, sizeof(c), cudaMemcpyDeviceToHost, b->ctx->stream), "d2h");
+        ck(cudaStreamSynchronize(b->ctx->stream), "sync");
+        out->accepted_steps       = (int64_t)c[CNT_ACCEPTED];
+        out->rejected_steps       = (int64_t)c[CNT_REJECTED];
+        out->failed_steps         = (int64_t)c[CNT_FAILED];
+        out->underflow_fixes      = (int64_t)c[CNT_UNDERFLOW];
+        out->sequential_exchanges = (int64_t)c[CNT_SEQUENTIAL];
+        out->phases               = b->phases;
+        out->kernel_launches      = b->launches;
+        return MGPU_OK;
+    });
+}
+
+int64_t mgpu_batch_device_bytes(const mgpu_batch* b)
+{
+    return b ? b->pool.bytes : 0;
+}
+
+void mgpu_batch_destroy(mgpu_batch* b)
+{
+    if (!b) {
+        return;
+    }
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    delete b;
+}
+
+} // extern "C"

@@ -1,0 +1,408 @@
+// mgpu_internal.cuh — device-side data structures and the FP64 thread-level
+// ODE-SECIR model shared by the kernels of libmiogpu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/miogpu.h"
+
+namespace mgpu
+{
+
+constexpr int kC = MGPU_NUM_COMPARTMENTS;
+constexpr int kF = MGPU_NUM_FLOWS;
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kZeroTol = 1e-12; // Limits<double>::zero_tolerance (memilio/config.h:73-79)
+
+// Device error word bits (per batch).
+enum : int32_t {
+    ERR_STEP_CAP   = 1, // an instance exceeded max steps in one interval
+    ERR_NONFINITE  = 2, // NaN/Inf in a state
+    ERR_BAD_GRAPH  = 4, // inconsistent graph descriptor met on the device
+    ERR_SEQ_BOUNDS = 8  // sequential exchange met an out-of-range index
+};
+
+// Immutable per-graph descriptor (offsets into the batch pools).
+struct DevGraph {
+    int32_t N, G, E, M, K, Ke;
+    int32_t n;      // 10 G
+    int32_t method; // integrator
+    int64_t node0;  // first global node id
+    int64_t edge0;  // first global edge id
+    int64_t param_off;   // doubles, [N][stride(G)]
+    int64_t contact_off; // doubles, [N][M][2][G][G] (baseline, minimum)
+    int64_t dtime_off;   // doubles, [N][M][K]
+    int64_t dval_off;    // doubles, [N][M][K][G][G]
+    int64_t state_off;   // doubles, [N][n] (state, v0, ypre, ynew pools share it)
+    int64_t ecoef_off;   // doubles, [E][2][n] (baseline, minimum)
+    int64_t edt_off;     // doubles, [E][Ke]
+    int64_t edv_off;     // doubles, [E][Ke][n]
+};
+
+// Mutable per-graph state (GraphSimulation::m_t and the edges' shared return flag).
+struct GraphRt {
+    double t;          // graph time
+    double t_next;     // end of the current interval
+    double dt;         // length of the current interval
+    double tmax;       // horizon
+    double t_dep;      // time of the pending departure
+    double t_ret;      // its return time (t_dep + dt at departure)
+    int32_t return_mobile; // MobilityEdge::m_return_mobile_population (identical for all edges)
+    int32_t active;    // takes part in the current interval
+    int32_t fallback;  // current return needs the sequential path
+    int32_t has_pending; // travelers are away
+    int32_t do_return; // current interval ends with returns
+    int32_t do_depart; // current interval ends with departures
+    int32_t pad0, pad1;
+};
+
+// Integrator options on the device.
+struct DevOpts {
+    double abs_tol, rel_tol, dt_min, dt_max;
+    int32_t max_steps;
+    int32_t method;
+};
+
+// All device pointers of a batch.
+struct BatchDev {
+    int32_t num_graphs;
+    int64_t num_nodes, num_edges;
+    const DevGraph* graphs;
+    GraphRt* rt;
+    const int32_t* node_graph;   // [num_nodes]
+    const int32_t* edge_graph;   // [num_edges]
+    const double* params;
+    const double* contact;
+    const double* dtimes;
+    const double* dvals;
+    double* state;               // result last values
+    double* v0;                  // post-departure snapshot (destination state at t_dep)
+    double* ypre;                // pre-exchange snapshot
+    double* ynew;                // scratch for the parallel return
+    double* node_t;              // integrator time per node
+    double* node_dt;             // integrator step per node
+    const int32_t* edge_src;     // global node ids
+    const int32_t* edge_dst;
+    const double* ecoef;
+    const double* edt;
+    const double* edv;
+    const uint8_t* edge_static_any; // coefficients constant and some > 0 (Ke == 0)
+    uint8_t* edge_pending;       // travelers away on this edge
+    double* trav;                // [sum_e n_e] stored travelers
+    const int64_t* trav_off;     // [num_edges] offset of each edge's travelers
+    const int64_t* out_ptr;      // [num_nodes+1] CSR (edges sorted by (src, dst))
+    const int64_t* in_ptr;       // [num_nodes+1] CSC
+    const int64_t* in_edges;     // [num_edges] edge ids sorted by (dst, src)
+    double* scratch;             // plain ODE stage vectors, [8][scratch_nmax][scratch_stride]
+    int64_t scratch_stride;      // node slots (distance between consecutive components)
+    int32_t scratch_nmax;        // components per scratch vector
+    DevOpts opts;
+    int32_t* err;                // device error word
+    unsigned long long* counters; // [8]: accepted, rejected, failed, underflow, sequential
+};
+
+enum { CNT_ACCEPTED = 0, CNT_REJECTED, CNT_FAILED, CNT_UNDERFLOW, CNT_SEQUENTIAL, CNT_NUM };
+
+__host__ __device__ inline int param_stride(int G)
+{
+    return MGPU_NUM_SCALAR_PARAMS + MGPU_NUM_GROUP_PARAMS * G;
+}
+
+// Source/target compartment of the 15 flows (osecir Flows typelist, models/ode_secir/model.h:45-59).
+__device__ __constant__ const int8_t kFlowSrc[kF] = {MGPU_S,    MGPU_E,    MGPU_INS,  MGPU_INS,  MGPU_INSC,
+                                                      MGPU_INSC, MGPU_ISY,  MGPU_ISY,  MGPU_ISYC, MGPU_ISYC,
+                                                      MGPU_ISEV, MGPU_ISEV, MGPU_ISEV, MGPU_ICRI, MGPU_ICRI};
+__device__ __constant__ const int8_t kFlowDst[kF] = {MGPU_E,    MGPU_INS,  MGPU_ISY,  MGPU_R,    MGPU_ISYC,
+                                                      MGPU_R,    MGPU_ISEV, MGPU_R,    MGPU_ISEV, MGPU_R,
+                                                      MGPU_ICRI, MGPU_R,    MGPU_D,    MGPU_D,    MGPU_R};
+
+// The same tables as compile-time functions (fold to register indices in unrolled loops).
+__host__ __device__ __forceinline__ constexpr int kFlowSrcI(int f)
+{
+    return f == 0 ? MGPU_S
+         : f == 1 ? MGPU_E
+         : f <= 3 ? MGPU_INS
+         : f <= 5 ? MGPU_INSC
+         : f <= 7 ? MGPU_ISY
+         : f <= 9 ? MGPU_ISYC
+         : f <= 12 ? MGPU_ISEV
+                   : MGPU_ICRI;
+}
+__host__ __device__ __forceinline__ constexpr int kFlowDstI(int f)
+{
+    return f == 0 ? MGPU_E
+         : f == 1 ? MGPU_INS
+         : f == 2 ? MGPU_ISY
+         : f == 3 ? MGPU_R
+         : f == 4 ? MGPU_ISYC
+         : f == 5 ? MGPU_R
+         : f == 6 ? MGPU_ISEV
+         : f == 7 ? MGPU_R
+         : f == 8 ? MGPU_ISEV
+         : f == 9 ? MGPU_R
+         : f == 10 ? MGPU_ICRI
+         : f == 11 ? MGPU_R
+         : f == 12 ? MGPU_D
+         : f == 13 ? MGPU_D
+                   : MGPU_R;
+}
+
+// smoother_cosine (memilio/math/smoother.h:46-60).
+template <class R>
+__device__ __forceinline__ R smoother_cosine(R x, R xleft, R xright, R yleft, R yright)
+{
+    if (x <= xleft) {
+        return yleft;
+    }
+    if (x >= xright) {
+        return yright;
+    }
+    return R(0.5) * (yleft - yright) * cos(R(kPi) / (xright - xleft) * (x - xleft)) + R(0.5) * (yleft + yright);
+}
+
+// The branch of a cosine smoother, shared by all coefficients that use the
+// same x and interval: 0 = left value, 1 = right value, 2 = ramp with cosine c.
+struct Ramp {
+    int mode;
+    double c;
+};
+
+__device__ __forceinline__ Ramp ramp_at(double x, double xleft, double xright)
+{
+    Ramp r;
+    if (x <= xleft) {
+        r.mode = 0;
+        r.c    = 0.0;
+    }
+    else if (x >= xright) {
+        r.mode = 1;
+        r.c    = 0.0;
+    }
+    else {
+        r.mode = 2;
+        r.c    = cos(kPi / (xright - xleft) * (x - xleft));
+    }
+    return r;
+}
+
+__device__ __forceinline__ double ramp_apply(const Ramp& r, double yleft, double yright)
+{
+    return r.mode == 0 ? yleft : (r.mode == 1 ? yright : 0.5 * (yleft - yright) * r.c + 0.5 * (yleft + yright));
+}
+
+// Position in a damping cache (Dampings::get_matrix_at, memilio/epidemiology/damping.h:381-396):
+// ub = first point with time > t; the matrix is a cosine ramp over [t_ub - 1, t_ub].
+__device__ __forceinline__ int damping_upper_bound(const double* times, int K, double t)
+{
+    int ub = 0;
+    while (ub < K && !(t < times[ub])) {
+        ++ub;
+    }
+    return ub < K ? ub : K - 1;
+}
+
+// Node model accessor over the batch pools.
+struct NodeModel {
+    int G, M, K;
+    const double* p;      // parameter record
+    const double* cm;     // [M][2][G][G]
+    const double* dtimes; // [M][K]
+    const double* dvals;  // [M][K][G][G]
+    __device__ double scalar(int w) const
+    {
+        return p[w];
+    }
+    __device__ double gp(int w, int g) const
+    {
+        return p[MGPU_NUM_SCALAR_PARAMS + w * G + g];
+    }
+};
+
+__device__ __forceinline__ NodeModel node_model(const BatchDev& B, const DevGraph& g, int64_t local)
+{
+    NodeModel m;
+    m.G            = g.G;
+    m.M            = g.M;
+    m.K            = g.K;
+    const long GG  = (long)g.G * g.G;
+    m.p            = B.params + g.param_off + local * param_stride(g.G);
+    m.cm           = B.contact + g.contact_off + local * g.M * 2 * GG;
+    m.dtimes       = g.K ? B.dtimes + g.dtime_off + local * g.M * g.K : nullptr;
+    m.dvals        = g.K ? B.dvals + g.dval_off + local * g.M * g.K * GG : nullptr;
+    return m;
+}
+
+// Strided vector view (SoA scratch or contiguous rows).
+struct SVec {
+    double* p;
+    int64_t s;
+    __device__ __forceinline__ double& operator[](int i) const
+    {
+        return p[(int64_t)i * s];
+    }
+};
+struct CVec {
+    const double* p;
+    int64_t s;
+    __device__ __forceinline__ double operator[](int i) const
+    {
+        return p[(int64_t)i * s];
+    }
+};
+
+// ContactMatrixGroup::get_matrix_at(t) element (i, j) times the seasonality
+// factor, for all (i, j) at once (contact_matrix.h:190-194,392-399).
+// `C` receives G*G values (row-major).
+__device__ inline void contact_matrix_at(const NodeModel& nm, double t, double* C)
+{
+    const int G   = nm.G;
+    const long GG = (long)G * G;
+    for (int k = 0; k < GG; ++k) {
+        C[k] = 0.0;
+    }
+    for (int m = 0; m < nm.M; ++m) {
+        const double* B = nm.cm + m * 2 * GG;
+        const double* L = B + GG;
+        if (nm.K) {
+            const double* T  = nm.dtimes + m * nm.K;
+            const int ub     = damping_upper_bound(T, nm.K, t);
+            const Ramp r     = ramp_at(t, T[ub] - 1.0, T[ub]);
+            const double* Dl = nm.dvals + ((long)m * nm.K + ub - 1) * GG;
+            const double* Dr = Dl + GG;
+            for (int k = 0; k < GG; ++k) {
+                const double D = ramp_apply(r, Dl[k], Dr[k]);
+                C[k]           = C[k] + (B[k] - D * (B[k] - L[k]));
+            }
+        }
+        else {
+            for (int k = 0; k < GG; ++k) {
+                C[k] = C[k] + (B[k] - 0.0 * (B[k] - L[k]));
+            }
+        }
+    }
+}
+
+// osecir::Model::get_flows + FlowModel::get_derivatives (models/ode_secir/model.h:82-214,
+// compartments/flow_model.h:112-144) for one node, FP64, one thread. The
+// contact matrix, seasonality and risk smoother are evaluated once per call
+// (they depend on t and pop only) instead of once per (i, j).
+template <class PopV, class YV, class OutV>
+__device__ void secir_rhs(const NodeModel& nm, const PopV& pop, const YV& y, double t, const OutV& dydt)
+{
+    const int G = nm.G;
+    double C[MGPU_MAX_GROUPS * MGPU_MAX_GROUPS];
+    contact_matrix_at(nm, t, C);
+    double icu = 0.0, tnt = 0.0;
+    for (int i = 0; i < G; ++i) {
+        tnt += (1 - nm.gp(MGPU_G_RECOVERED_PER_INS, i)) / nm.gp(MGPU_G_TIME_INS, i) * pop[i * kC + MGPU_INS];
+        icu += pop[i * kC + MGPU_ICRI];
+    }
+    const double cap    = nm.scalar(MGPU_P_TNT_CAPACITY);
+    const Ramp rrisk    = ramp_at(tnt, cap, cap * nm.scalar(MGPU_P_TNT_MAX_RISK));
+    const double season = (1 + nm.scalar(MGPU_P_SEASONALITY) *
+                                   sin(kPi * ((nm.scalar(MGPU_P_START_DAY) + t) / 182.5 + 0.5)));
+    const double icu_cap = nm.scalar(MGPU_P_ICU_CAPACITY);
+    const Ramp ricu      = ramp_at(icu, 0.90 * icu_cap, icu_cap);
+    // per source group j: 1/N_j and the infectious pressure
+    double divN[MGPU_MAX_GROUPS], press[MGPU_MAX_GROUPS];
+    for (int j = 0; j < G; ++j) {
+        const int o = j * kC;
+        const double Nj = pop[o + MGPU_S] + pop[o + MGPU_E] + pop[o + MGPU_INS] + pop[o + MGPU_ISY] +
+                          pop[o + MGPU_ISEV] + pop[o + MGPU_ICRI] + pop[o + MGPU_R];
+        divN[j]           = (Nj < kZeroTol) ? 0.0 : 1.0 / Nj;
+        const double risk = ramp_apply(rrisk, nm.gp(MGPU_G_RISK_FROM_SYMPTOMATIC, j),
+                                       nm.gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, j));
+        press[j] = nm.gp(MGPU_G_REL_TRANSMISSION_NS, j) * pop[o + MGPU_INS] + risk * pop[o + MGPU_ISY];
+    }
+    for (int k = 0; k < G * kC; ++k) {
+        dydt[k] = 0.0;
+    }
+    for (int i = 0; i < G; ++i) {
+        const int o       = i * kC;
+        const double beta = nm.gp(MGPU_G_TRANSMISSION_PROB, i);
+        double f[kF];
+        f[0] = 0.0;
+        for (int j = 0; j < G; ++j) {
+            const double cont = season * C[i * G + j];
+            f[0] += y[o + MGPU_S] * cont * divN[j] * beta * press[j];
+        }
+        const double cps       = nm.gp(MGPU_G_CRITICAL_PER_SEVERE, i);
+        const double crit_adj  = ramp_apply(ricu, cps, 0.0);
+        const double death_adj = cps - crit_adj;
+        const double mu        = nm.gp(MGPU_G_RECOVERED_PER_INS, i);
+        const double tins      = nm.gp(MGPU_G_TIME_INS, i);
+        const double sev       = nm.gp(MGPU_G_SEVERE_PER_ISY, i);
+        const double tisy      = nm.gp(MGPU_G_TIME_ISY, i);
+        const double tisev     = nm.gp(MGPU_G_TIME_ISEV, i);
+        const double dps       = nm.gp(MGPU_G_DEATHS_PER_SEVERE, i);
+        const double dpc       = nm.gp(MGPU_G_DEATHS_PER_CRITICAL, i);
+        const double ticri     = nm.gp(MGPU_G_TIME_ICRI, i);
+        f[1]  = (1.0 / nm.gp(MGPU_G_TIME_EXPOSED, i)) * y[o + MGPU_E];
+        f[2]  = (1 - mu) * (1 / tins) * y[o + MGPU_INS];
+        f[3]  = mu * (1.0 / tins) * y[o + MGPU_INS];
+        f[4]  = (1.0 - mu) * (1.0 / tins) * y[o + MGPU_INSC];
+        f[5]  = mu * (1.0 / tins) * y[o + MGPU_INSC];
+        f[6]  = sev / tisy * y[o + MGPU_ISY];
+        f[7]  = (1 - sev) / tisy * y[o + MGPU_ISY];
+        f[8]  = sev / tisy * y[o + MGPU_ISYC];
+        f[9]  = (1.0 - sev) / tisy * y[o + MGPU_ISYC];
+        f[10] = crit_adj / tisev * y[o + MGPU_ISEV];
+        f[11] = (1.0 - cps - dps) / tisev * y[o + MGPU_ISEV];
+        f[12] = (dps + death_adj) / tisev * y[o + MGPU_ISEV];
+        f[13] = dpc / ticri * y[o + MGPU_ICRI];
+        f[14] = (1.0 - dpc) / ticri * y[o + MGPU_ICRI];
+#pragma unroll
+        for (int k = 0; k < kF; ++k) {
+            dydt[o + kFlowSrc[k]] -= f[k];
+            dydt[o + kFlowDst[k]] += f[k];
+        }
+    }
+}
+
+// Mobility risk factor of the ISy compartments (get_mobility_factors,
+// models/ode_secir/model.h:687-715) for group g, from state y.
+template <class YV>
+__device__ inline double mobility_isy_factor(const NodeModel& nm, const YV& y, int g)
+{
+    double tnt = 0.0;
+    for (int i = 0; i < nm.G; ++i) {
+        tnt += (1 - nm.gp(MGPU_G_RECOVERED_PER_INS, i)) / nm.gp(MGPU_G_TIME_INS, i) * y[i * kC + MGPU_INS];
+    }
+    const double cap = nm.scalar(MGPU_P_TNT_CAPACITY);
+    return smoother_cosine(tnt, cap, cap * nm.scalar(MGPU_P_TNT_MAX_RISK), nm.gp(MGPU_G_RISK_FROM_SYMPTOMATIC, g),
+                           nm.gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, g));
+}
+
+// Coefficient j of edge e at time t (MobilityCoefficientGroup::get_matrix_at with one matrix).
+__device__ inline double edge_coeff_at(const BatchDev& B, const DevGraph& g, int64_t local_e, int j, double t)
+{
+    const double* base = B.ecoef + g.ecoef_off + local_e * 2 * g.n;
+    const double Bv    = base[j];
+    const double Lv    = base[g.n + j];
+    double D           = 0.0;
+    if (g.Ke) {
+        const double* T  = B.edt + g.edt_off + local_e * g.Ke;
+        const int ub     = damping_upper_bound(T, g.Ke, t);
+        const Ramp r     = ramp_at(t, T[ub] - 1.0, T[ub]);
+        const double* Dv = B.edv + g.edv_off + local_e * g.Ke * g.n;
+        D                = ramp_apply(r, Dv[(ub - 1) * g.n + j], Dv[ub * g.n + j]);
+    }
+    return 0.0 + (Bv - D * (Bv - Lv));
+}
+
+// Launchers (defined in the .cu files).
+void launch_ode_plain(const BatchDev& B, int64_t node_begin, int64_t node_end, cudaStream_t s);
+void launch_simulate(const BatchDev& B, const int32_t* d_nodes, int count, double t0, double tmax, double dt0,
+                     int max_points, double* d_out_t, double* d_out_y, int32_t* d_num_points, cudaStream_t s);
+void launch_eval_rhs(const BatchDev& B, const int32_t* d_nodes, int count, const double* d_pop, const double* d_y,
+                     const double* d_t, double* d_dydt, cudaStream_t s);
+int launch_ode_batched(const BatchDev& B, int G, int precision, const int32_t* d_instances, int64_t count,
+                       int instances_per_block, int grid_blocks, cudaStream_t s);
+void launch_phase_begin(const BatchDev& B, double dt_exchange, cudaStream_t s);
+void launch_exchange(const BatchDev& B, int64_t max_n, cudaStream_t s, int64_t* launches);
+void launch_exchange_range(const BatchDev& B, int g0, int ng, int64_t n0, int64_t nn, int64_t e0, int64_t ne,
+                           int64_t n_max, cudaStream_t s, int64_t* launches);
+void launch_phase_end(const BatchDev& B, cudaStream_t s);
+
+} // namespace mgpu

@@ -1,0 +1,554 @@
+// ode_batched.cu — batched node solver: one exchange interval of many node
+// instances (all nodes of all graphs of a batch) per launch.
+//
+// Work mapping: one lane per age group. A node instance with G groups is a
+// segment of G consecutive lanes; a warp carries floor(32/G) instances
+// (G = 6: 5 instances on 30 lanes). Every lane keeps its group's 10
+// compartments in registers; the force of infection is a G-term contraction
+// whose source terms come from the other lanes of the segment by
+// __shfl_sync, and the embedded error norm is a max-reduction over the
+// segment. Each instance has its own adaptive dt: segments of one warp step
+// independently.
+//
+// Arithmetic (template Real):
+//   Real = double : FP64 throughout, the reference's evaluation order.
+//   Real = float  : flows, stage states and stage combinations in FP32;
+//                   the state, its update, the error norm's max and the
+//                   step-size controller in FP64. The update is applied in
+//                   flow space (each flow increment leaves its source and
+//                   enters its target with the same FP64 value), so every
+//                   node conserves its population to FP64 rounding.
+//
+// Integrator: ControlledStepperWrapper<cash_karp54> inside
+// SystemIntegrator::advance (memilio/math/stepper_wrapper.h:112-163,
+// memilio/math/integrator.h:184-249), same controller rules as ode_plain.cu.
+#include "mgpu_internal.cuh"
+
+#include <type_traits>
+
+namespace mgpu
+{
+namespace
+{
+
+__device__ __constant__ const double bk_c[6]    = {0.0, 1.0 / 5.0, 3.0 / 10.0, 3.0 / 5.0, 1.0, 7.0 / 8.0};
+__device__ __constant__ const double bk_a[6][5] = {
+    {0, 0, 0, 0, 0},
+    {1.0 / 5.0, 0, 0, 0, 0},
+    {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0},
+    {3.0 / 10.0, -9.0 / 10.0, 6.0 / 5.0, 0, 0},
+    {-11.0 / 54.0, 5.0 / 2.0, -70.0 / 27.0, 35.0 / 27.0, 0},
+    {1631.0 / 55296.0, 175.0 / 512.0, 575.0 / 13824.0, 44275.0 / 110592.0, 253.0 / 4096.0}};
+__device__ __constant__ const double bk_b5[6] = {37.0 / 378.0, 0.0, 250.0 / 621.0, 125.0 / 594.0, 0.0, 512.0 / 1771.0};
+__device__ __constant__ const double bk_db[6] = {
+    37.0 / 378.0 - 2825.0 / 27648.0, 0.0, 250.0 / 621.0 - 18575.0 / 48384.0, 125.0 / 594.0 - 13525.0 / 55296.0,
+    0.0 - 277.0 / 14336.0, 512.0 / 1771.0 - 1.0 / 4.0};
+
+constexpr int S_ = MGPU_S, E_ = MGPU_E, INS_ = MGPU_INS, INSC_ = MGPU_INSC, ISY_ = MGPU_ISY, ISYC_ = MGPU_ISYC,
+              ISEV_ = MGPU_ISEV, ICRI_ = MGPU_ICRI, R_ = MGPU_R, D_ = MGPU_D;
+
+// Row i of ContactMatrixGroup::get_matrix_at(t) in FP64 (contact_matrix.h:190-194,392-399).
+__device__ inline void contact_row_at(const NodeModel& nm, int i, double t, double* C)
+{
+    const int G   = nm.G;
+    const long GG = (long)G * G;
+    for (int j = 0; j < G; ++j) {
+        C[j] = 0.0;
+    }
+    for (int m = 0; m < nm.M; ++m) {
+        const double* Bm = nm.cm + m * 2 * GG + (long)i * G;
+        const double* Lm = Bm + GG;
+        if (nm.K) {
+            const double* T  = nm.dtimes + m * nm.K;
+            const int ub     = damping_upper_bound(T, nm.K, t);
+            const Ramp r     = ramp_at(t, T[ub] - 1.0, T[ub]);
+            const double* Dl = nm.dvals + ((long)m * nm.K + ub - 1) * GG + (long)i * G;
+            const double* Dr = Dl + GG;
+            for (int j = 0; j < G; ++j) {
+                const double D = ramp_apply(r, Dl[j], Dr[j]);
+                C[j]           = C[j] + (Bm[j] - D * (Bm[j] - Lm[j]));
+            }
+        }
+        else {
+            for (int j = 0; j < G; ++j) {
+                C[j] = C[j] + (Bm[j] - 0.0 * (Bm[j] - Lm[j]));
+            }
+        }
+    }
+}
+
+// Per-lane constants of one node instance for one interval.
+template <int G, class Real>
+struct Seg {
+    int base;
+    unsigned mask;
+    int gi;
+    NodeModel nm;
+    // own group
+    Real a_tnt, beta, xi, rho, rho_max;
+    Real r1, r2, r3, r6, r7, r11, r13, r14, r10l, r12l, cps, dps, tisev;
+    // scalars
+    Real tnt_cap, tnt_cap2, icu_lo, icu_cap;
+    double season_k, start_day;
+    // contact row as P + Q c(t) on [t_lo, t_hi) (single contact matrix only)
+    bool fast;
+    Real P[G], Q[G];
+    double t_lo, t_hi, ramp_xl;
+    Real ramp_scale;
+};
+
+template <int G, class Real>
+__device__ void seg_load_contact(Seg<G, Real>& X, double t)
+{
+    const NodeModel& nm = X.nm;
+    const long GG       = (long)G * G;
+    const double* Bm    = nm.cm + (long)X.gi * G;
+    const double* Lm    = Bm + GG;
+    if (nm.K == 0) {
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+            X.P[j] = (Real)(Bm[j] - 0.0 * (Bm[j] - Lm[j]));
+            X.Q[j] = (Real)0;
+        }
+        X.t_lo       = -INFINITY;
+        X.t_hi       = INFINITY;
+        X.ramp_xl    = INFINITY;
+        X.ramp_scale = (Real)0;
+        return;
+    }
+    const double* T  = nm.dtimes;
+    const int ub     = damping_upper_bound(T, nm.K, t);
+    const double* Dl = nm.dvals + (long)(ub - 1) * GG + (long)X.gi * G;
+    const double* Dr = Dl + GG;
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+        const double BL = Bm[j] - Lm[j];
+        X.P[j]          = (Real)(Bm[j] - (0.5 * (Dl[j] + Dr[j])) * BL);
+        X.Q[j]          = (Real)(-(0.5 * (Dl[j] - Dr[j])) * BL);
+    }
+    X.t_lo       = T[ub - 1];
+    X.t_hi       = T[ub];
+    X.ramp_xl    = T[ub] - 1.0;
+    X.ramp_scale = (Real)(1.0 / (T[ub] - X.ramp_xl));
+}
+
+template <int G, class Real>
+__device__ void seg_load(Seg<G, Real>& X, const BatchDev& B, const DevGraph& g, int64_t local, double t)
+{
+    X.nm                 = node_model(B, g, local);
+    const NodeModel& nm  = X.nm;
+    const int i          = X.gi;
+    const double mu      = nm.gp(MGPU_G_RECOVERED_PER_INS, i);
+    const double tins    = nm.gp(MGPU_G_TIME_INS, i);
+    const double sev     = nm.gp(MGPU_G_SEVERE_PER_ISY, i);
+    const double tisy    = nm.gp(MGPU_G_TIME_ISY, i);
+    const double tisev   = nm.gp(MGPU_G_TIME_ISEV, i);
+    const double cps     = nm.gp(MGPU_G_CRITICAL_PER_SEVERE, i);
+    const double dps     = nm.gp(MGPU_G_DEATHS_PER_SEVERE, i);
+    const double dpc     = nm.gp(MGPU_G_DEATHS_PER_CRITICAL, i);
+    const double ticri   = nm.gp(MGPU_G_TIME_ICRI, i);
+    X.a_tnt              = (Real)((1 - mu) / tins);
+    X.beta               = (Real)nm.gp(MGPU_G_TRANSMISSION_PROB, i);
+    X.xi                 = (Real)nm.gp(MGPU_G_REL_TRANSMISSION_NS, i);
+    X.rho                = (Real)nm.gp(MGPU_G_RISK_FROM_SYMPTOMATIC, i);
+    X.rho_max            = (Real)nm.gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, i);
+    X.r1                 = (Real)(1.0 / nm.gp(MGPU_G_TIME_EXPOSED, i));
+    X.r2                 = (Real)((1 - mu) * (1 / tins));
+    X.r3                 = (Real)(mu * (1.0 / tins));
+    X.r6                 = (Real)(sev / tisy);
+    X.r7                 = (Real)((1 - sev) / tisy);
+    X.r11                = (Real)((1.0 - cps - dps) / tisev);
+    X.r13                = (Real)(dpc / ticri);
+    X.r14                = (Real)((1.0 - dpc) / ticri);
+    X.r10l               = (Real)(cps / tisev);
+    X.r12l               = (Real)((dps + (cps - cps)) / tisev);
+    X.cps                = (Real)cps;
+    X.dps                = (Real)dps;
+    X.tisev              = (Real)tisev;
+    const double cap     = nm.scalar(MGPU_P_TNT_CAPACITY);
+    X.tnt_cap            = (Real)cap;
+    X.tnt_cap2           = (Real)(cap * nm.scalar(MGPU_P_TNT_MAX_RISK));
+    const double icu_cap = nm.scalar(MGPU_P_ICU_CAPACITY);
+    X.icu_lo             = (Real)(0.90 * icu_cap);
+    X.icu_cap            = (Real)icu_cap;
+    X.season_k           = nm.scalar(MGPU_P_SEASONALITY);
+    X.start_day          = nm.scalar(MGPU_P_START_DAY);
+    X.fast               = std::is_same<Real, float>::value && nm.M == 1;
+    if (X.fast) {
+        seg_load_contact(X, t);
+    }
+}
+
+template <int G, class Real>
+__device__ __forceinline__ Real seg_sum(const Seg<G, Real>& X, Real v)
+{
+    Real s = (Real)0;
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+        s += __shfl_sync(X.mask, v, X.base + k);
+    }
+    return s;
+}
+
+// Flows of the lane's age group (osecir::Model::get_flows, models/ode_secir/model.h:82-214)
+// and the derivative of its 10 compartments (FlowModel::get_derivatives, flow_model.h:112-125).
+template <int G, class Real>
+__device__ __forceinline__ void seg_rhs(Seg<G, Real>& X, const Real (&u)[kC], double tau, Real (&fl)[kF],
+                                        Real (&kc)[kC])
+{
+    constexpr bool fp64 = std::is_same<Real, double>::value;
+    const Real tnt      = seg_sum(X, X.a_tnt * u[INS_]);
+    const Real icu      = seg_sum(X, u[ICRI_]);
+    // own group as source j of the contact sum
+    const Real risk  = smoother_cosine(tnt, X.tnt_cap, X.tnt_cap2, X.rho, X.rho_max);
+    const Real Nj    = u[S_] + u[E_] + u[INS_] + u[ISY_] + u[ISEV_] + u[ICRI_] + u[R_];
+    const Real divN  = (Nj < (Real)kZeroTol) ? (Real)0 : (Real)1 / Nj;
+    const Real press = X.xi * u[INS_] + risk * u[ISY_];
+    Real f0          = (Real)0;
+    if constexpr (fp64) {
+        const double season =
+            X.season_k == 0.0 ? 1.0 : (1 + X.season_k * sin(kPi * ((X.start_day + tau) / 182.5 + 0.5)));
+        double C[G];
+        contact_row_at(X.nm, X.gi, tau, C);
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+            const double dN = __shfl_sync(X.mask, divN, X.base + j);
+            const double pr = __shfl_sync(X.mask, press, X.base + j);
+            const double cont = season * C[j];
+            f0 += u[S_] * cont * dN * X.beta * pr;
+        }
+    }
+    else {
+        const float season =
+            X.season_k == 0.0 ? 1.0f
+                              : 1.0f + (float)X.season_k * sinpif((float)((X.start_day + tau) * (1.0 / 182.5) + 0.5));
+        const float w = divN * press;
+        float acc     = 0.0f;
+        if (X.fast) {
+            if (!(tau >= X.t_lo && tau < X.t_hi)) {
+                seg_load_contact(X, tau);
+            }
+            const float c = (tau <= X.ramp_xl) ? 1.0f : cospif((float)(tau - X.ramp_xl) * X.ramp_scale);
+#pragma unroll
+            for (int j = 0; j < G; ++j) {
+                acc += (X.P[j] + X.Q[j] * c) * __shfl_sync(X.mask, w, X.base + j);
+            }
+        }
+        else {
+            double C[G];
+            contact_row_at(X.nm, X.gi, tau, C);
+#pragma unroll
+            for (int j = 0; j < G; ++j) {
+                acc += (float)C[j] * __shfl_sync(X.mask, w, X.base + j);
+            }
+        }
+        f0 = u[S_] * X.beta * season * acc;
+    }
+    // ICU smoother for CriticalPerSevere
+    Real r10 = X.r10l, r12 = X.r12l;
+    if (!(icu <= X.icu_lo)) {
+        const Real crit_adj = smoother_cosine(icu, X.icu_lo, X.icu_cap, X.cps, (Real)0);
+        r10                 = crit_adj / X.tisev;
+        r12                 = (X.dps + (X.cps - crit_adj)) / X.tisev;
+    }
+    fl[0]  = f0;
+    fl[1]  = X.r1 * u[E_];
+    fl[2]  = X.r2 * u[INS_];
+    fl[3]  = X.r3 * u[INS_];
+    fl[4]  = X.r2 * u[INSC_];
+    fl[5]  = X.r3 * u[INSC_];
+    fl[6]  = X.r6 * u[ISY_];
+    fl[7]  = X.r7 * u[ISY_];
+    fl[8]  = X.r6 * u[ISYC_];
+    fl[9]  = X.r7 * u[ISYC_];
+    fl[10] = r10 * u[ISEV_];
+    fl[11] = X.r11 * u[ISEV_];
+    fl[12] = r12 * u[ISEV_];
+    fl[13] = X.r13 * u[ICRI_];
+    fl[14] = X.r14 * u[ICRI_];
+    // derivative scatter in flow order
+    kc[S_]    = -fl[0];
+    kc[E_]    = fl[0] - fl[1];
+    kc[INS_]  = (fl[1] - fl[2]) - fl[3];
+    kc[INSC_] = -fl[4] - fl[5];
+    kc[ISY_]  = (fl[2] - fl[6]) - fl[7];
+    kc[ISYC_] = (fl[4] - fl[8]) - fl[9];
+    kc[ISEV_] = (((fl[6] + fl[8]) - fl[10]) - fl[11]) - fl[12];
+    kc[ICRI_] = (fl[10] - fl[13]) - fl[14];
+    kc[R_]    = ((((fl[3] + fl[5]) + fl[7]) + fl[9]) + fl[11]) + fl[14];
+    kc[D_]    = fl[12] + fl[13];
+}
+
+template <int G, class Real>
+__device__ __forceinline__ double seg_max(const Seg<G, Real>& X, double v)
+{
+    double m = v;
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+        m = fmax(m, __shfl_sync(X.mask, v, X.base + k));
+    }
+    return m;
+}
+
+template <int G, class Real>
+__global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* inst, int64_t count)
+{
+    constexpr bool fp64 = std::is_same<Real, double>::value;
+    constexpr int IPW   = 32 / G;
+    const int lane      = threadIdx.x & 31;
+    const int seg       = lane / G;
+    if (seg >= IPW) {
+        return;
+    }
+    Seg<G, Real> X;
+    X.gi   = lane - seg * G;
+    X.base = seg * G;
+    X.mask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << X.base);
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw  = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const DevOpts o   = B.opts;
+    unsigned long long n_acc = 0, n_rej = 0, n_fail = 0;
+    bool cap_hit = false, nonfinite = false;
+
+    for (int64_t slot = wid * IPW + seg; slot < count; slot += nw * IPW) {
+        const int64_t node = inst[slot];
+        const int gidx     = B.node_graph[node];
+        const DevGraph& g  = B.graphs[gidx];
+        const GraphRt& rt  = B.rt[gidx];
+        if (!rt.active) {
+            continue;
+        }
+        const int64_t local = node - g.node0;
+        double* yp          = B.state + g.state_off + local * g.n + X.gi * kC;
+        double y[kC];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            y[c] = yp[c];
+        }
+        double t          = B.node_t[node];
+        double dt         = B.node_dt[node];
+        const double tmax = rt.t_next;
+        seg_load(X, B, g, local, t);
+
+        // SystemIntegrator::advance
+        const double t0   = t;
+        double dt_restore = 0.0;
+        double dt_min     = o.dt_min;
+        int steps         = 0;
+        while (fabs((tmax - t) / (tmax - t0)) > kZeroTol) {
+            if (steps++ >= o.max_steps) {
+                cap_hit = true;
+                break;
+            }
+            if (dt > tmax - t) {
+                dt_restore = dt;
+                dt         = tmax - t;
+                dt_min     = fmin(tmax - t, dt_min);
+            }
+            // ControlledStepperWrapper::step
+            bool success     = false;
+            bool is_dt_valid = true;
+            double dt_used   = dt;
+            Real phi[kF];   // mixed: flow increments of the attempt
+            double yn[kC];  // fp64: 5th-order result
+            while (!success && is_dt_valid) {
+                if (dt < dt_min) {
+                    is_dt_valid = false;
+                    dt          = dt_min;
+                }
+                if (o.dt_max != 0.0 && fabs(dt) > o.dt_max) {
+                    dt = o.dt_max;
+                    ++n_rej;
+                    continue;
+                }
+                dt_used = dt;
+                // ---- one Cash-Karp attempt ----
+                Real k[5][kC];
+                Real kc[kC], fl[kF], xe[kC];
+                Real y0[kC];
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    y0[c] = (Real)y[c];
+                }
+                seg_rhs(X, y0, t, fl, kc);
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    k[0][c] = kc[c];
+                    xe[c]   = (Real)(bk_db[0] * dt) * kc[c];
+                }
+                if constexpr (!fp64) {
+#pragma unroll
+                    for (int f = 0; f < kF; ++f) {
+                        phi[f] = (Real)(bk_b5[0] * dt) * fl[f];
+                    }
+                }
+                if constexpr (fp64) {
+#pragma unroll
+                    for (int c = 0; c < kC; ++c) {
+                        yn[c] = y[c] + (bk_b5[0] * dt) * kc[c];
+                    }
+                }
+#pragma unroll
+                for (int s = 1; s < 6; ++s) {
+                    Real u[kC];
+#pragma unroll
+                    for (int c = 0; c < kC; ++c) {
+                        Real v = y0[c];
+#pragma unroll
+                        for (int j = 0; j < s; ++j) {
+                            v = v + (Real)(bk_a[s][j] * dt) * k[j][c];
+                        }
+                        u[c] = v;
+                    }
+                    seg_rhs(X, u, t + bk_c[s] * dt, fl, kc);
+#pragma unroll
+                    for (int c = 0; c < kC; ++c) {
+                        xe[c] = xe[c] + (Real)(bk_db[s] * dt) * kc[c];
+                        if (s < 5) {
+                            k[s][c] = kc[c];
+                        }
+                    }
+                    if constexpr (fp64) {
+#pragma unroll
+                        for (int c = 0; c < kC; ++c) {
+                            yn[c] = yn[c] + (bk_b5[s] * dt) * kc[c];
+                        }
+                    }
+                    else {
+                        if (s == 2 || s == 3 || s == 5) {
+#pragma unroll
+                            for (int f = 0; f < kF; ++f) {
+                                phi[f] = phi[f] + (Real)(bk_b5[s] * dt) * fl[f];
+                            }
+                        }
+                    }
+                }
+                // Odeint error measure, max over the instance
+                double el = 0.0;
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    const Real r = fabs(xe[c]) / ((Real)o.abs_tol +
+                                                  (Real)o.rel_tol * (fabs(y0[c]) + (Real)dt * fabs(k[0][c])));
+                    el           = fmax(el, (double)r);
+                }
+                const double err = seg_max(X, el);
+                // ---- controller ----
+                if (err > 1.0) {
+                    dt *= fmax(0.9 * pow(err, -1.0 / 3.0), 0.2);
+                    if (o.dt_max != 0.0) {
+                        dt = fmin(dt, o.dt_max);
+                    }
+                    ++n_rej;
+                }
+                else {
+                    t += dt;
+                    if (err < 0.5) {
+                        const double e = fmax(0.00032 /* 5^-5 */, err);
+                        dt *= 0.9 * pow(e, -1.0 / 5.0);
+                        if (o.dt_max != 0.0) {
+                            dt = fmin(dt, o.dt_max);
+                        }
+                    }
+                    success = true;
+                }
+            }
+            dt = fmax(dt, dt_min);
+            if (!success) {
+                t += dt_min;
+                ++n_fail;
+            }
+            else {
+                ++n_acc;
+            }
+            (void)dt_used;
+            // apply the (last) attempt
+            if constexpr (fp64) {
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    y[c] = yn[c];
+                }
+            }
+            else {
+#pragma unroll
+                for (int f = 0; f < kF; ++f) {
+                    const double p = (double)phi[f];
+                    y[kFlowSrcI(f)] -= p;
+                    y[kFlowDstI(f)] += p;
+                }
+            }
+        }
+        dt = fmax(dt, dt_restore);
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            yp[c]     = y[c];
+            nonfinite = nonfinite || !isfinite(y[c]);
+        }
+        if (X.gi == 0) {
+            B.node_t[node]  = t;
+            B.node_dt[node] = dt;
+        }
+    }
+    if (cap_hit) {
+        atomicOr(B.err, ERR_STEP_CAP);
+    }
+    if (nonfinite) {
+        atomicOr(B.err, ERR_NONFINITE);
+    }
+    if (X.gi == 0) {
+        if (n_acc) {
+            atomicAdd(&B.counters[CNT_ACCEPTED], n_acc);
+        }
+        if (n_rej) {
+            atomicAdd(&B.counters[CNT_REJECTED], n_rej);
+        }
+        if (n_fail) {
+            atomicAdd(&B.counters[CNT_FAILED], n_fail);
+        }
+    }
+}
+
+template <int G>
+int launch_g(const BatchDev& B, int precision, const int32_t* inst, int64_t count, int ipb, int grid, cudaStream_t s)
+{
+    constexpr int IPW  = 32 / G;
+    const int warps    = ipb > 0 ? (ipb + IPW - 1) / IPW : 4;
+    const int threads  = 32 * (warps < 1 ? 1 : (warps > 32 ? 32 : warps));
+    const int64_t per  = (int64_t)(threads / 32) * IPW;
+    int64_t blocks     = (count + per - 1) / per;
+    if (grid > 0 && blocks > grid) {
+        blocks = grid;
+    }
+    if (blocks < 1) {
+        blocks = 1;
+    }
+    if (precision == MGPU_PRECISION_MIXED) {
+        k_ode_batched<G, float><<<(unsigned)blocks, threads, 0, s>>>(B, inst, count);
+    }
+    else {
+        k_ode_batched<G, double><<<(unsigned)blocks, threads, 0, s>>>(B, inst, count);
+    }
+    return 0;
+}
+
+} // namespace
+
+int launch_ode_batched(const BatchDev& B, int G, int precision, const int32_t* d_instances, int64_t count,
+                       int instances_per_block, int grid_blocks, cudaStream_t s)
+{
+    if (count <= 0) {
+        return 0;
+    }
+    switch (G) {
+    case 1: return launch_g<1>(B, precision, d_instances, count, instances_per_block, grid_blocks, s);
+    case 2: return launch_g<2>(B, precision, d_instances, count, instances_per_block, grid_blocks, s);
+    case 3: return launch_g<3>(B, precision, d_instances, count, instances_per_block, grid_blocks, s);
+    case 4: return launch_g<4>(B, precision, d_instances, count, instances_per_block, grid_blocks, s);
+    case 5: return launch_g<5>(B, precision, d_instances, count, instances_per_block, grid_blocks, s);
+    case 6: return launch_g<6>(B, precision, d_instances, count, instances_per_block, grid_blocks, s);
+    case 7: return launch_g<7>(B, precision, d_instances, count, instances_per_block, grid_blocks, s);
+    case 8: return launch_g<8>(B, precision, d_instances, count, instances_per_block, grid_blocks, s);
+    default: return -1;
+    }
+}
+
+} // namespace mgpu
