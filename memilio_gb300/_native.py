@@ -14,7 +14,7 @@ import numpy as np
 from .layout import GraphArrays, MgpuGraph, MgpuIntegratorOpts, integrator_opts
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "lib", "libmiogpu.so")
+LIB_PATH = os.environ.get("MIOGPU_LIB") or os.path.join(HERE, "lib", "libmiogpu.so")
 
 OK = 0
 STATUS_NAMES = {0: "OK", 1: "UnknownError", 2: "OutOfRange", 3: "InvalidValue", 4: "InvalidFileFormat",

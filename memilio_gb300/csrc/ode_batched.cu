@@ -507,6 +507,416 @@ __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed-precision solver. GB300 executes FP64 at ~1/64 of the FP32 rate, so
+// inside an interval everything runs in FP32 except the clock (t, dt) and the
+// state accumulator: each lane holds its 10 compartments as float-float pairs
+// (hi + lo, ~48-bit significand, error-free TwoSum updates). Every flow
+// increment is subtracted from its source and added to its target through
+// the same exact TwoSum, so populations are conserved to ~2^-48 per step.
+// The state is loaded from and stored to FP64 HBM once per interval.
+
+__device__ __constant__ const float fk_c[6]    = {0.0f, 1.0f / 5.0f, 3.0f / 10.0f, 3.0f / 5.0f, 1.0f, 7.0f / 8.0f};
+__device__ __constant__ const float fk_a[6][5] = {
+    {0, 0, 0, 0, 0},
+    {1.0f / 5.0f, 0, 0, 0, 0},
+    {3.0f / 40.0f, 9.0f / 40.0f, 0, 0, 0},
+    {3.0f / 10.0f, -9.0f / 10.0f, 6.0f / 5.0f, 0, 0},
+    {-11.0f / 54.0f, 5.0f / 2.0f, -70.0f / 27.0f, 35.0f / 27.0f, 0},
+    {1631.0f / 55296.0f, 175.0f / 512.0f, 575.0f / 13824.0f, 44275.0f / 110592.0f, 253.0f / 4096.0f}};
+__device__ __constant__ const float fk_b5[6] = {(float)(37.0 / 378.0), 0.0f, (float)(250.0 / 621.0),
+                                                (float)(125.0 / 594.0), 0.0f, (float)(512.0 / 1771.0)};
+__device__ __constant__ const float fk_db[6] = {
+    (float)(37.0 / 378.0 - 2825.0 / 27648.0), 0.0f, (float)(250.0 / 621.0 - 18575.0 / 48384.0),
+    (float)(125.0 / 594.0 - 13525.0 / 55296.0), (float)(0.0 - 277.0 / 14336.0), (float)(512.0 / 1771.0 - 1.0 / 4.0)};
+
+// Error-free a + b (Knuth's TwoSum): hi takes the rounded sum, lo the rounding error.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float b)
+{
+    const float s  = __fadd_rn(hi, b);
+    const float bb = __fsub_rn(s, hi);
+    const float e  = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    hi             = s;
+    lo             = __fadd_rn(lo, e);
+}
+
+__device__ __forceinline__ void df_renorm(float& hi, float& lo)
+{
+    const float s = __fadd_rn(hi, lo);
+    lo            = __fsub_rn(lo, __fsub_rn(s, hi));
+    hi            = s;
+}
+
+template <int G>
+struct SegF {
+    int base;
+    unsigned mask;
+    int gi;
+    NodeModel nm;
+    float a_tnt, beta, xi, rho, rho_max;
+    float r1, r2, r3, r6, r7, r11, r13, r14, r10l, r12l, cps, dps, inv_tisev;
+    float tnt_cap, tnt_cap2, icu_lo, icu_cap;
+    float season_k, season_s0;
+    bool fast;
+    float P[G], Q[G];
+    float t_lo, t_hi, xl, scale; // damping segment and ramp, relative to t_base
+    double t_base;
+};
+
+template <int G>
+__device__ void segf_load_contact(SegF<G>& X, float tau_rel)
+{
+    const NodeModel& nm = X.nm;
+    const long GG       = (long)G * G;
+    const double* Bm    = nm.cm + (long)X.gi * G;
+    const double* Lm    = Bm + GG;
+    if (nm.K == 0) {
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+            X.P[j] = (float)Bm[j];
+            X.Q[j] = 0.0f;
+        }
+        X.t_lo  = -INFINITY;
+        X.t_hi  = INFINITY;
+        X.xl    = INFINITY;
+        X.scale = 0.0f;
+        return;
+    }
+    const double tau = X.t_base + (double)tau_rel;
+    const double* T  = nm.dtimes;
+    const int ub     = damping_upper_bound(T, nm.K, tau);
+    const double* Dl = nm.dvals + (long)(ub - 1) * GG + (long)X.gi * G;
+    const double* Dr = Dl + GG;
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+        const double BL = Bm[j] - Lm[j];
+        X.P[j]          = (float)(Bm[j] - (0.5 * (Dl[j] + Dr[j])) * BL);
+        X.Q[j]          = (float)(-(0.5 * (Dl[j] - Dr[j])) * BL);
+    }
+    // times relative to the interval start; far sentinels saturate to +-inf
+    X.t_lo  = (float)(T[ub - 1] - X.t_base);
+    X.t_hi  = (float)(T[ub] - X.t_base);
+    X.xl    = (float)((T[ub] - 1.0) - X.t_base);
+    X.scale = (float)(1.0 / (T[ub] - (T[ub] - 1.0)));
+}
+
+template <int G>
+__device__ void segf_load(SegF<G>& X, const BatchDev& B, const DevGraph& g, int64_t local, double t_base)
+{
+    X.nm                 = node_model(B, g, local);
+    const NodeModel& nm  = X.nm;
+    const int i          = X.gi;
+    const double mu      = nm.gp(MGPU_G_RECOVERED_PER_INS, i);
+    const double tins    = nm.gp(MGPU_G_TIME_INS, i);
+    const double sev     = nm.gp(MGPU_G_SEVERE_PER_ISY, i);
+    const double tisy    = nm.gp(MGPU_G_TIME_ISY, i);
+    const double tisev   = nm.gp(MGPU_G_TIME_ISEV, i);
+    const double cps     = nm.gp(MGPU_G_CRITICAL_PER_SEVERE, i);
+    const double dps     = nm.gp(MGPU_G_DEATHS_PER_SEVERE, i);
+    const double dpc     = nm.gp(MGPU_G_DEATHS_PER_CRITICAL, i);
+    const double ticri   = nm.gp(MGPU_G_TIME_ICRI, i);
+    X.t_base             = t_base;
+    X.a_tnt              = (float)((1 - mu) / tins);
+    X.beta               = (float)nm.gp(MGPU_G_TRANSMISSION_PROB, i);
+    X.xi                 = (float)nm.gp(MGPU_G_REL_TRANSMISSION_NS, i);
+    X.rho                = (float)nm.gp(MGPU_G_RISK_FROM_SYMPTOMATIC, i);
+    X.rho_max            = (float)nm.gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, i);
+    X.r1                 = (float)(1.0 / nm.gp(MGPU_G_TIME_EXPOSED, i));
+    X.r2                 = (float)((1 - mu) * (1 / tins));
+    X.r3                 = (float)(mu * (1.0 / tins));
+    X.r6                 = (float)(sev / tisy);
+    X.r7                 = (float)((1 - sev) / tisy);
+    X.r11                = (float)((1.0 - cps - dps) / tisev);
+    X.r13                = (float)(dpc / ticri);
+    X.r14                = (float)((1.0 - dpc) / ticri);
+    X.r10l               = (float)(cps / tisev);
+    X.r12l               = (float)((dps + (cps - cps)) / tisev);
+    X.cps                = (float)cps;
+    X.dps                = (float)dps;
+    X.inv_tisev          = (float)(1.0 / tisev);
+    const double cap     = nm.scalar(MGPU_P_TNT_CAPACITY);
+    X.tnt_cap            = (float)cap;
+    X.tnt_cap2           = (float)(cap * nm.scalar(MGPU_P_TNT_MAX_RISK));
+    const double icu_cap = nm.scalar(MGPU_P_ICU_CAPACITY);
+    X.icu_lo             = (float)(0.90 * icu_cap);
+    X.icu_cap            = (float)icu_cap;
+    X.season_k           = (float)nm.scalar(MGPU_P_SEASONALITY);
+    X.season_s0          = (float)((nm.scalar(MGPU_P_START_DAY) + t_base) / 182.5 + 0.5);
+    X.fast               = nm.M == 1;
+    if (X.fast) {
+        segf_load_contact(X, 0.0f);
+    }
+}
+
+template <int G>
+__device__ __forceinline__ float segf_sum(const SegF<G>& X, float v)
+{
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+        s += __shfl_sync(X.mask, v, X.base + k);
+    }
+    return s;
+}
+
+// Flows and derivative of the lane's age group in FP32 (same model as seg_rhs).
+template <int G>
+__device__ __forceinline__ void segf_rhs(SegF<G>& X, const float (&u)[kC], float tau_rel, float (&fl)[kF],
+                                         float (&kc)[kC])
+{
+    const float tnt   = segf_sum(X, X.a_tnt * u[INS_]);
+    const float icu   = segf_sum(X, u[ICRI_]);
+    const float risk  = smoother_cosine(tnt, X.tnt_cap, X.tnt_cap2, X.rho, X.rho_max);
+    const float Nj    = u[S_] + u[E_] + u[INS_] + u[ISY_] + u[ISEV_] + u[ICRI_] + u[R_];
+    const float divN  = (Nj < (float)kZeroTol) ? 0.0f : __frcp_rn(Nj);
+    const float w     = divN * (X.xi * u[INS_] + risk * u[ISY_]);
+    const float season =
+        X.season_k == 0.0f ? 1.0f : 1.0f + X.season_k * sinpif(X.season_s0 + tau_rel * (float)(1.0 / 182.5));
+    float acc = 0.0f;
+    if (X.fast) {
+        if (!(tau_rel >= X.t_lo && tau_rel < X.t_hi)) {
+            segf_load_contact(X, tau_rel);
+        }
+        const float c = (tau_rel <= X.xl) ? 1.0f : cospif((tau_rel - X.xl) * X.scale);
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+            acc += (X.P[j] + X.Q[j] * c) * __shfl_sync(X.mask, w, X.base + j);
+        }
+    }
+    else {
+        double C[G];
+        contact_row_at(X.nm, X.gi, X.t_base + (double)tau_rel, C);
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+            acc += (float)C[j] * __shfl_sync(X.mask, w, X.base + j);
+        }
+    }
+    float r10 = X.r10l, r12 = X.r12l;
+    if (!(icu <= X.icu_lo)) {
+        const float crit_adj = smoother_cosine(icu, X.icu_lo, X.icu_cap, X.cps, 0.0f);
+        r10                  = crit_adj * X.inv_tisev;
+        r12                  = (X.dps + (X.cps - crit_adj)) * X.inv_tisev;
+    }
+    fl[0]  = u[S_] * X.beta * season * acc;
+    fl[1]  = X.r1 * u[E_];
+    fl[2]  = X.r2 * u[INS_];
+    fl[3]  = X.r3 * u[INS_];
+    fl[4]  = X.r2 * u[INSC_];
+    fl[5]  = X.r3 * u[INSC_];
+    fl[6]  = X.r6 * u[ISY_];
+    fl[7]  = X.r7 * u[ISY_];
+    fl[8]  = X.r6 * u[ISYC_];
+    fl[9]  = X.r7 * u[ISYC_];
+    fl[10] = r10 * u[ISEV_];
+    fl[11] = X.r11 * u[ISEV_];
+    fl[12] = r12 * u[ISEV_];
+    fl[13] = X.r13 * u[ICRI_];
+    fl[14] = X.r14 * u[ICRI_];
+    kc[S_]    = -fl[0];
+    kc[E_]    = fl[0] - fl[1];
+    kc[INS_]  = (fl[1] - fl[2]) - fl[3];
+    kc[INSC_] = -fl[4] - fl[5];
+    kc[ISY_]  = (fl[2] - fl[6]) - fl[7];
+    kc[ISYC_] = (fl[4] - fl[8]) - fl[9];
+    kc[ISEV_] = (((fl[6] + fl[8]) - fl[10]) - fl[11]) - fl[12];
+    kc[ICRI_] = (fl[10] - fl[13]) - fl[14];
+    kc[R_]    = ((((fl[3] + fl[5]) + fl[7]) + fl[9]) + fl[11]) + fl[14];
+    kc[D_]    = fl[12] + fl[13];
+}
+
+template <int G>
+__global__ void __launch_bounds__(128) k_ode_mixed(BatchDev B, const int32_t* inst, int64_t count)
+{
+    constexpr int IPW = 32 / G;
+    const int lane    = threadIdx.x & 31;
+    const int seg     = lane / G;
+    if (seg >= IPW) {
+        return;
+    }
+    SegF<G> X;
+    X.gi              = lane - seg * G;
+    X.base            = seg * G;
+    X.mask            = (((1u << G) - 1u) << X.base);
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw  = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const DevOpts o   = B.opts;
+    const float abs_f = (float)o.abs_tol, rel_f = (float)o.rel_tol;
+    unsigned long long n_acc = 0, n_rej = 0, n_fail = 0;
+    bool cap_hit = false, nonfinite = false;
+
+    for (int64_t slot = wid * IPW + seg; slot < count; slot += nw * IPW) {
+        const int64_t node = inst[slot];
+        const int gidx     = B.node_graph[node];
+        const DevGraph& g  = B.graphs[gidx];
+        const GraphRt& rt  = B.rt[gidx];
+        if (!rt.active) {
+            continue;
+        }
+        const int64_t local = node - g.node0;
+        double* yp          = B.state + g.state_off + local * g.n + X.gi * kC;
+        float hi[kC], lo[kC];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            const double v = yp[c];
+            hi[c]          = (float)v;
+            lo[c]          = (float)(v - (double)hi[c]);
+        }
+        double t          = B.node_t[node];
+        double dt         = B.node_dt[node];
+        const double tmax = rt.t_next;
+        segf_load(X, B, g, local, t);
+
+        // SystemIntegrator::advance
+        const double t0   = t;
+        double dt_restore = 0.0;
+        double dt_min     = o.dt_min;
+        int steps         = 0;
+        while (fabs((tmax - t) / (tmax - t0)) > kZeroTol) {
+            if (steps++ >= o.max_steps) {
+                cap_hit = true;
+                break;
+            }
+            if (dt > tmax - t) {
+                dt_restore = dt;
+                dt         = tmax - t;
+                dt_min     = fmin(tmax - t, dt_min);
+            }
+            // ControlledStepperWrapper::step
+            bool success     = false;
+            bool is_dt_valid = true;
+            float phi[kF];
+            while (!success && is_dt_valid) {
+                if (dt < dt_min) {
+                    is_dt_valid = false;
+                    dt          = dt_min;
+                }
+                if (o.dt_max != 0.0 && fabs(dt) > o.dt_max) {
+                    dt = o.dt_max;
+                    ++n_rej;
+                    continue;
+                }
+                const float dtf  = (float)dt;
+                const float trel = (float)(t - X.t_base);
+                float k[5][kC];
+                float kc[kC], fl[kF], xe[kC];
+                segf_rhs(X, hi, trel, fl, kc);
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    k[0][c] = kc[c];
+                    xe[c]   = (fk_db[0] * dtf) * kc[c];
+                }
+#pragma unroll
+                for (int f = 0; f < kF; ++f) {
+                    phi[f] = (fk_b5[0] * dtf) * fl[f];
+                }
+#pragma unroll
+                for (int s = 1; s < 6; ++s) {
+                    float u[kC];
+#pragma unroll
+                    for (int c = 0; c < kC; ++c) {
+                        float v = hi[c];
+#pragma unroll
+                        for (int j = 0; j < s; ++j) {
+                            v = v + (fk_a[s][j] * dtf) * k[j][c];
+                        }
+                        u[c] = v;
+                    }
+                    segf_rhs(X, u, trel + fk_c[s] * dtf, fl, kc);
+#pragma unroll
+                    for (int c = 0; c < kC; ++c) {
+                        xe[c] = xe[c] + (fk_db[s] * dtf) * kc[c];
+                        if (s < 5) {
+                            k[s][c] = kc[c];
+                        }
+                    }
+                    if (s == 2 || s == 3 || s == 5) {
+#pragma unroll
+                        for (int f = 0; f < kF; ++f) {
+                            phi[f] = phi[f] + (fk_b5[s] * dtf) * fl[f];
+                        }
+                    }
+                }
+                // Odeint error measure, max over the instance
+                float el = 0.0f;
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    const float den = abs_f + rel_f * (fabsf(hi[c]) + dtf * fabsf(k[0][c]));
+                    el              = fmaxf(el, fabsf(xe[c]) * __frcp_rn(den));
+                }
+#pragma unroll
+                for (int q = 0; q < G; ++q) {
+                    el = fmaxf(el, __shfl_sync(X.mask, el, X.base + q));
+                }
+                // controller: FP64 clock, FP32 step-size factor
+                if (el > 1.0f) {
+                    dt *= (double)fmaxf(0.9f * exp2f(__log2f(el) * (-1.0f / 3.0f)), 0.2f);
+                    if (o.dt_max != 0.0) {
+                        dt = fmin(dt, o.dt_max);
+                    }
+                    ++n_rej;
+                }
+                else {
+                    t += dt;
+                    if (el < 0.5f) {
+                        const float e = fmaxf(0.00032f /* 5^-5 */, el);
+                        dt *= (double)(0.9f * exp2f(__log2f(e) * -0.2f));
+                        if (o.dt_max != 0.0) {
+                            dt = fmin(dt, o.dt_max);
+                        }
+                    }
+                    success = true;
+                }
+            }
+            dt = fmax(dt, dt_min);
+            if (!success) {
+                t += dt_min;
+                ++n_fail;
+            }
+            else {
+                ++n_acc;
+            }
+            // flow-space update of the (last) attempt: exact TwoSum on both ends of each flow
+#pragma unroll
+            for (int f = 0; f < kF; ++f) {
+                df_add(hi[kFlowSrcI(f)], lo[kFlowSrcI(f)], -phi[f]);
+                df_add(hi[kFlowDstI(f)], lo[kFlowDstI(f)], phi[f]);
+            }
+#pragma unroll
+            for (int c = 0; c < kC; ++c) {
+                df_renorm(hi[c], lo[c]);
+            }
+        }
+        dt = fmax(dt, dt_restore);
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            const double v = (double)hi[c] + (double)lo[c];
+            yp[c]          = v;
+            nonfinite      = nonfinite || !isfinite(v);
+        }
+        if (X.gi == 0) {
+            B.node_t[node]  = t;
+            B.node_dt[node] = dt;
+        }
+    }
+    if (cap_hit) {
+        atomicOr(B.err, ERR_STEP_CAP);
+    }
+    if (nonfinite) {
+        atomicOr(B.err, ERR_NONFINITE);
+    }
+    if (X.gi == 0) {
+        if (n_acc) {
+            atomicAdd(&B.counters[CNT_ACCEPTED], n_acc);
+        }
+        if (n_rej) {
+            atomicAdd(&B.counters[CNT_REJECTED], n_rej);
+        }
+        if (n_fail) {
+            atomicAdd(&B.counters[CNT_FAILED], n_fail);
+        }
+    }
+}
+
 template <int G>
 int launch_g(const BatchDev& B, int precision, const int32_t* inst, int64_t count, int ipb, int grid, cudaStream_t s)
 {
@@ -522,7 +932,7 @@ int launch_g(const BatchDev& B, int precision, const int32_t* inst, int64_t coun
         blocks = 1;
     }
     if (precision == MGPU_PRECISION_MIXED) {
-        k_ode_batched<G, float><<<(unsigned)blocks, threads, 0, s>>>(B, inst, count);
+        k_ode_mixed<G><<<(unsigned)blocks, threads, 0, s>>>(B, inst, count);
     }
     else {
         k_ode_batched<G, double><<<(unsigned)blocks, threads, 0, s>>>(B, inst, count);
