@@ -417,7 +417,14 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.edge_static_any = b->pool.upload(h_any);
     B.edge_pending    = b->pool.alloc<uint8_t>(edges);
     ck(cudaMemsetAsync(B.edge_pending, 0, std::max<int64_t>(edges, 1), ctx->stream), "memset");
-    B.trav     = b->pool.alloc<double>(tr);
+    B.trav       = b->pool.alloc<double>(tr);
+    B.mfix       = b->pool.alloc<double>(tr);
+    B.edge_fixed = b->pool.alloc<int32_t>(edges);
+    B.node_flag  = b->pool.alloc<uint8_t>(nodes);
+    B.node_dirty = b->pool.alloc<uint8_t>(2 * nodes);
+    ck(cudaMemsetAsync(B.edge_fixed, 0, sizeof(int32_t) * std::max<int64_t>(edges, 1), ctx->stream), "memset");
+    ck(cudaMemsetAsync(B.node_flag, 0, std::max<int64_t>(nodes, 1), ctx->stream), "memset");
+    ck(cudaMemsetAsync(B.node_dirty, 0, std::max<int64_t>(2 * nodes, 1), ctx->stream), "memset");
     B.trav_off = b->pool.upload(h_trav_off);
     B.out_ptr  = b->pool.upload(h_out_ptr);
     B.in_ptr   = b->pool.upload(h_in_ptr);
@@ -869,7 +876,7 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
                 nev += 3;
                 ode_launches += (int64_t)b->inst_by_G.size();
             }
-            b->launches += P * (3 + (int64_t)b->inst_by_G.size() + (B.num_edges > 0 ? 7 : 1));
+            b->launches += P * (2 + (int64_t)b->inst_by_G.size() + exchange_launches(B.num_edges > 0));
             b->phases += P;
         }
         else {
@@ -889,7 +896,7 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
                     b->graph_exec   = nullptr;
                 }
             }
-            const int64_t per_phase = 3 + (int64_t)b->inst_by_G.size() + (B.num_edges > 0 ? 7 : 1);
+            const int64_t per_phase = 2 + (int64_t)b->inst_by_G.size() + exchange_launches(B.num_edges > 0);
             for (int64_t p = 0; p < P; ++p) {
                 if (b->graph_exec) {
                     ck(cudaGraphLaunch(b->graph_exec, s), "cudaGraphLaunch");

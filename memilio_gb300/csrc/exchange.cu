@@ -17,6 +17,8 @@
 // which the bound fails anywhere is redone by an exact sequential pass.
 #include "mgpu_internal.cuh"
 
+#include <cstdio>
+
 namespace mgpu
 {
 namespace
@@ -307,8 +309,204 @@ __global__ void k_return_nodes(BatchDev B, int n_max, int64_t n0, int64_t nn)
     // the serial loop fixes strictly negative remainders only; the margin covers
     // the different rounding of this bound against the serial partial sums
     if (bound < 1e-12 * mag) {
+#ifdef MGPU_DEBUG_BOUND
+        printf("bound: graph %d node %lld j %d y %.17g bound %.17g mag %.17g t %g\n", gi,
+               (long long)(node - g.node0), j, y0, bound, mag, rt.t_next);
+#endif
+        B.node_flag[node] = 1;
+    }
+}
+
+// Exact serial return semantics restricted to one node (one warp, lanes over
+// compartments): the node's incident edges in serial order, the underflow
+// fix of each in-edge against the node's running state, the node's own
+// returning travelers (fixed at their destinations when needed) added at
+// their place in the order. An in-edge whose fixed travelers change marks its
+// source for a rescan (the source's state includes them). Pass 0 scans the
+// flagged nodes, later passes the nodes marked in the previous pass.
+__global__ void k_return_scan(BatchDev B, int64_t n0, int64_t nn, int pass)
+{
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane  = threadIdx.x & 31;
+    if (w >= nn) {
+        return;
+    }
+    const int64_t node = n0 + w;
+    const int gi       = B.node_graph[node];
+    const DevGraph& g  = B.graphs[gi];
+    const GraphRt& rt  = B.rt[gi];
+    if (!returning(rt)) {
+        return;
+    }
+    uint8_t* dirty_in  = B.node_dirty + (pass & 1) * B.num_nodes;
+    uint8_t* dirty_out = B.node_dirty + ((pass + 1) & 1) * B.num_nodes;
+    const bool todo    = pass == 0 ? B.node_flag[node] != 0 : dirty_in[node] != 0;
+    if (!todo) {
+        return;
+    }
+    if (pass > 0 && lane == 0) {
+        dirty_in[node] = 0;
+    }
+    __shared__ double sm_m[4][MGPU_MAX_GROUPS * kC];
+    __shared__ double sm_r[4][MGPU_MAX_GROUPS * kC];
+    double* m   = sm_m[(threadIdx.x >> 5) & 3];
+    double* rem = sm_r[(threadIdx.x >> 5) & 3];
+    const int n = g.n;
+    double y[3];
+    const double* ys = B.state + g.state_off + (node - g.node0) * n;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const int j = lane + 32 * q;
+        y[q]        = j < n ? ys[j] : 0.0;
+    }
+    auto in_edge = [&](int64_t e) {
+        if (!B.edge_pending[e]) {
+            return;
+        }
+        const double* me = B.trav + B.trav_off[e];
+        bool neg         = false;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const int j = lane + 32 * q;
+            if (j < n) {
+                m[j]   = me[j];
+                rem[j] = y[q] - m[j];
+                neg    = neg || (rem[j] < 0);
+            }
+        }
+        neg = __any_sync(0xffffffffu, neg);
+        __syncwarp();
+        if (neg) {
+            if (lane == 0) {
+                int fixes = 0;
+                for (int j = 0; j < n; ++j) {
+                    if (rem[j] < 0) {
+                        const int group = j / kC;
+                        int max_index   = 0;
+                        for (int c = 1; c < kC; ++c) {
+                            if (rem[group * kC + c] > rem[group * kC + max_index]) {
+                                max_index = c;
+                            }
+                        }
+                        max_index += group * kC;
+                        m[max_index] -= rem[j];
+                        m[j] += rem[j];
+                        ++fixes;
+                    }
+                }
+                rem[0] = (double)fixes;
+            }
+            __syncwarp();
+            const int fixes = (int)rem[0];
+            double* mf      = B.mfix + B.trav_off[e];
+            bool changed    = B.edge_fixed[e] == 0;
+            for (int q = 0; q < 3; ++q) {
+                const int j = lane + 32 * q;
+                if (j < n) {
+                    changed = changed || (__ldcg(mf + j) != m[j]);
+                    __stcg(mf + j, m[j]);
+                }
+            }
+            changed = __any_sync(0xffffffffu, changed);
+            __threadfence();
+            if (lane == 0) {
+                B.edge_fixed[e] = fixes;
+                if (changed) {
+                    dirty_out[B.edge_src[e]] = 1;
+                }
+            }
+        }
+        else if (B.edge_fixed[e] != 0) {
+            if (lane == 0) {
+                B.edge_fixed[e]          = 0;
+                dirty_out[B.edge_src[e]] = 1;
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const int j = lane + 32 * q;
+            if (j < n) {
+                y[q] -= m[j];
+            }
+        }
+        __syncwarp();
+    };
+    const int64_t ib = B.in_ptr[node], ie = B.in_ptr[node + 1];
+    int64_t k        = ib;
+    for (; k < ie; ++k) {
+        const int64_t e = B.in_edges[k];
+        if (B.edge_src[e] > node) {
+            break;
+        }
+        in_edge(e);
+    }
+    for (int64_t e = B.out_ptr[node]; e < B.out_ptr[node + 1]; ++e) {
+        if (!B.edge_pending[e]) {
+            continue;
+        }
+        // fixed travelers are published by another warp (possibly in this pass):
+        // read the flag and the values past L1
+        const bool fixed  = ((volatile int32_t*)B.edge_fixed)[e] != 0;
+        const double* src = fixed ? B.mfix + B.trav_off[e] : B.trav + B.trav_off[e];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const int j = lane + 32 * q;
+            if (j < n) {
+                y[q] += __ldcg(src + j);
+            }
+        }
+    }
+    for (; k < ie; ++k) {
+        in_edge(B.in_edges[k]);
+    }
+    double* yn = B.ynew + g.state_off + (node - g.node0) * n;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const int j = lane + 32 * q;
+        if (j < n) {
+            yn[j] = y[q];
+        }
+    }
+}
+
+// Graphs with a node still marked after the last scan pass take the exact
+// sequential path; flags are cleared.
+__global__ void k_return_scan_done(BatchDev B, int64_t n0, int64_t nn, int pass_end)
+{
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= nn) {
+        return;
+    }
+    const int64_t node = n0 + tid;
+    const int gi       = B.node_graph[node];
+    GraphRt& rt        = B.rt[gi];
+    uint8_t* dirty     = B.node_dirty + (pass_end & 1) * B.num_nodes;
+    if (returning(rt) && dirty[node]) {
         atomicOr(&rt.fallback, 1);
     }
+    dirty[node]                                        = 0;
+    B.node_dirty[((pass_end + 1) & 1) * B.num_nodes + node] = 0;
+    B.node_flag[node]                                  = 0;
+}
+
+// Underflow-fix counts of the parallel path; clears the per-edge fix state.
+__global__ void k_return_cleanup(BatchDev B, int64_t e0, int64_t ne)
+{
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= ne) {
+        return;
+    }
+    const int64_t e = e0 + tid;
+    const int f     = B.edge_fixed[e];
+    if (f == 0) {
+        return;
+    }
+    const GraphRt& rt = B.rt[B.edge_graph[e]];
+    if (!rt.fallback) {
+        atomicAdd(&B.counters[CNT_UNDERFLOW], (unsigned long long)f);
+    }
+    B.edge_fixed[e] = 0;
 }
 
 __global__ void k_return_commit(BatchDev B, int n_max, int64_t n0, int64_t nn)
@@ -406,6 +604,10 @@ inline int blocks_for(int64_t n, int threads)
     return (int)((n + threads - 1) / threads);
 }
 
+// Passes of the per-node exact scan before a graph falls back to the
+// sequential pass (each pass resolves one more level of the dependency chain).
+constexpr int kScanPasses = 4;
+
 } // namespace
 
 void launch_phase_begin(const BatchDev& B, double dt_exchange, cudaStream_t s)
@@ -433,15 +635,25 @@ void launch_exchange_range(const BatchDev& B, int g0, int ng, int64_t n0, int64_
     if (ne > 0) {
         k_return_edges<<<blocks_for(ne, 128), 128, 0, s>>>(B, e0, ne);
         k_return_nodes<<<blocks_for(nthr, T), T, 0, s>>>(B, (int)n_max, n0, nn);
+        for (int pass = 0; pass < kScanPasses; ++pass) {
+            k_return_scan<<<blocks_for(nn * 32, 128), 128, 0, s>>>(B, n0, nn, pass);
+        }
+        k_return_scan_done<<<blocks_for(nn, T), T, 0, s>>>(B, n0, nn, kScanPasses);
         k_return_commit<<<blocks_for(nthr, T), T, 0, s>>>(B, (int)n_max, n0, nn);
         k_return_sequential<<<ng, 32, 0, s>>>(B, g0, ng);
+        k_return_cleanup<<<blocks_for(ne, T), T, 0, s>>>(B, e0, ne);
         k_depart_edges<<<blocks_for(ne, 128), 128, 0, s>>>(B, e0, ne);
         k_depart_nodes<<<blocks_for(nthr, T), T, 0, s>>>(B, (int)n_max, n0, nn);
-        *launches += 7;
+        *launches += 9 + kScanPasses;
     }
     else {
         *launches += 1;
     }
+}
+
+int exchange_launches(bool has_edges)
+{
+    return has_edges ? 9 + kScanPasses : 1;
 }
 
 void launch_exchange(const BatchDev& B, int64_t n_max, cudaStream_t s, int64_t* launches)

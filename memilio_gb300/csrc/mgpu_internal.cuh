@@ -90,6 +90,10 @@ struct BatchDev {
     const uint8_t* edge_static_any; // coefficients constant and some > 0 (Ke == 0)
     uint8_t* edge_pending;       // travelers away on this edge
     double* trav;                // [sum_e n_e] stored travelers
+    double* mfix;                // [sum_e n_e] travelers after an underflow fix at the destination
+    int32_t* edge_fixed;         // [num_edges] number of fixed compartments (0: mfix unused)
+    uint8_t* node_flag;          // [num_nodes] return needs the exact per-node scan
+    uint8_t* node_dirty;         // [2][num_nodes] an out-edge changed: rescan (double-buffered)
     const int64_t* trav_off;     // [num_edges] offset of each edge's travelers
     const int64_t* out_ptr;      // [num_nodes+1] CSR (edges sorted by (src, dst))
     const int64_t* in_ptr;       // [num_nodes+1] CSC
@@ -401,6 +405,7 @@ int launch_ode_batched(const BatchDev& B, int G, int precision, const int32_t* d
                        int instances_per_block, int grid_blocks, cudaStream_t s);
 void launch_phase_begin(const BatchDev& B, double dt_exchange, cudaStream_t s);
 void launch_exchange(const BatchDev& B, int64_t max_n, cudaStream_t s, int64_t* launches);
+int exchange_launches(bool has_edges);
 void launch_exchange_range(const BatchDev& B, int g0, int ng, int64_t n0, int64_t nn, int64_t e0, int64_t ne,
                            int64_t n_max, cudaStream_t s, int64_t* launches);
 void launch_phase_end(const BatchDev& B, cudaStream_t s);
