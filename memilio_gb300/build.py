@@ -19,7 +19,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIB_DIR, "libmiogpu.so")
 
-SOURCES = ["capi.cu", "ode_plain.cu", "ode_batched.cu", "exchange.cu"]
+SOURCES = ["capi.cu", "ode_plain.cu", "ode_batched.cu", "exchange.cu", "exchange_batched.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "--expt-relaxed-constexpr"]

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <exception>
 #include <map>
+#include <tuple>
 #include <new>
 #include <string>
 #include <vector>
@@ -165,6 +166,7 @@ struct mgpu_batch {
     // batched solver work lists per age-group count
     std::map<int, std::pair<int32_t*, int64_t>> inst_by_G;
     int instances_per_block = 0;
+    bool any_edge_dampings  = false;
     int64_t launches        = 0;
     int64_t phases          = 0;
     int64_t seq_exchanges   = 0;
@@ -246,7 +248,13 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     b->pool.ctx       = ctx;
     b->num_graphs     = num_graphs;
     std::vector<DevGraph> dg(num_graphs);
-    int64_t nodes = 0, edges = 0, par = 0, con = 0, dtt = 0, dtv = 0, st = 0, ec = 0, edt = 0, edv = 0, tr = 0;
+    int64_t nodes = 0, edges = 0, par = 0, con = 0, dtt = 0, dtv = 0, st = 0, ec = 0, edt = 0, edv = 0, tr = 0,
+            ecf = 0;
+    // Arrays that several graphs pass by the same host pointer (the shared
+    // topology, contacts and coefficients of an ensemble) are uploaded once.
+    using Key = std::tuple<const void*, const void*, const void*, const void*, int64_t, int64_t, int64_t>;
+    std::map<Key, int> contact_first, damping_first, coeff_first;
+    std::vector<char> own_contact(num_graphs, 1), own_damping(num_graphs, 1), own_coeff(num_graphs, 1);
     b->N.resize(num_graphs);
     b->G.resize(num_graphs);
     b->n.resize(num_graphs);
@@ -273,24 +281,58 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         d.node0       = nodes;
         d.edge0       = edges;
         d.param_off   = par;
-        d.contact_off = con;
-        d.dtime_off   = dtt;
-        d.dval_off    = dtv;
         d.state_off   = st;
-        d.ecoef_off   = ec;
-        d.edt_off     = edt;
-        d.edv_off     = edv;
         nodes += g.num_nodes;
         edges += E;
         par += (int64_t)g.num_nodes * param_stride(G);
-        con += (int64_t)g.num_nodes * d.M * 2 * GG;
-        dtt += (int64_t)g.num_nodes * d.M * d.K;
-        dtv += (int64_t)g.num_nodes * d.M * d.K * GG;
         st += (int64_t)g.num_nodes * n;
-        ec += (int64_t)E * 2 * n;
-        edt += (int64_t)E * d.Ke;
-        edv += (int64_t)E * d.Ke * n;
         tr += (int64_t)E * n;
+        const Key kc{g.contact_baseline, g.contact_minimum, nullptr, nullptr, g.num_nodes, d.M, G};
+        auto itc = contact_first.find(kc);
+        if (itc != contact_first.end()) {
+            d.contact_off  = dg[itc->second].contact_off;
+            own_contact[i] = 0;
+        }
+        else {
+            contact_first[kc] = i;
+            d.contact_off     = con;
+            con += (int64_t)g.num_nodes * d.M * 2 * GG;
+        }
+        const Key kd{g.damping_times, g.damping_values, nullptr, nullptr, g.num_nodes, d.M * 64 + d.K, G};
+        auto itd = damping_first.find(kd);
+        if (d.K && itd != damping_first.end()) {
+            d.dtime_off    = dg[itd->second].dtime_off;
+            d.dval_off     = dg[itd->second].dval_off;
+            own_damping[i] = 0;
+        }
+        else {
+            damping_first[kd] = i;
+            d.dtime_off       = dtt;
+            d.dval_off        = dtv;
+            dtt += (int64_t)g.num_nodes * d.M * d.K;
+            dtv += (int64_t)g.num_nodes * d.M * d.K * GG;
+        }
+        const Key ke{g.edge_coeff_baseline, g.edge_coeff_minimum, g.edge_damping_times, g.edge_damping_values, E,
+                     d.Ke, n};
+        auto ite = coeff_first.find(ke);
+        if (E && ite != coeff_first.end()) {
+            d.ecoef_off   = dg[ite->second].ecoef_off;
+            d.edt_off     = dg[ite->second].edt_off;
+            d.edv_off     = dg[ite->second].edv_off;
+            d.ecoef_f_off = dg[ite->second].ecoef_f_off;
+            own_coeff[i]  = 0;
+        }
+        else {
+            coeff_first[ke] = i;
+            d.ecoef_off     = ec;
+            d.edt_off       = edt;
+            d.edv_off       = edv;
+            d.ecoef_f_off   = ecf;
+            ec += (int64_t)E * 2 * n;
+            edt += (int64_t)E * d.Ke;
+            edv += (int64_t)E * d.Ke * n;
+            ecf += (int64_t)E * n;
+        }
         b->N[i]         = g.num_nodes;
         b->G[i]         = G;
         b->n[i]         = n;
@@ -303,6 +345,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     // host staging
     std::vector<double> h_par(par), h_con(con), h_dtt(dtt), h_dtv(dtv), h_state(st), h_ec(ec), h_edt(edt),
         h_edv(edv);
+    std::vector<float> h_ecf(ecf);
     std::vector<int32_t> h_node_graph(nodes), h_edge_graph(edges), h_src(edges), h_dst(edges);
     std::vector<uint8_t> h_any(edges);
     std::vector<int64_t> h_trav_off(edges), h_out_ptr(nodes + 1, 0), h_in_ptr(nodes + 1, 0), h_in_edges(edges);
@@ -313,7 +356,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         const int G = d.G, n = d.n;
         const long GG = (long)G * G;
         std::memcpy(h_par.data() + d.param_off, g.params, sizeof(double) * (size_t)g.num_nodes * param_stride(G));
-        for (long v = 0; v < g.num_nodes; ++v) {
+        for (long v = 0; own_contact[i] && v < g.num_nodes; ++v) {
             for (int m = 0; m < d.M; ++m) {
                 double* dst      = h_con.data() + d.contact_off + (v * d.M + m) * 2 * GG;
                 const double* Bs = g.contact_baseline + (v * d.M + m) * GG;
@@ -326,7 +369,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
                 }
             }
         }
-        if (d.K) {
+        if (d.K && own_damping[i]) {
             std::memcpy(h_dtt.data() + d.dtime_off, g.damping_times, sizeof(double) * (size_t)g.num_nodes * d.M * d.K);
             std::memcpy(h_dtv.data() + d.dval_off, g.damping_values,
                         sizeof(double) * (size_t)g.num_nodes * d.M * d.K * GG);
@@ -344,20 +387,26 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
             h_dst[ge]        = (int32_t)(d.node0 + g.edge_dst[e]);
             h_out_ptr[d.node0 + g.edge_src[e] + 1]++;
             indeg[g.edge_dst[e] + 1]++;
-            double* dc = h_ec.data() + d.ecoef_off + (int64_t)e * 2 * n;
-            std::memcpy(dc, g.edge_coeff_baseline + (int64_t)e * n, sizeof(double) * n);
-            if (g.edge_coeff_minimum) {
-                std::memcpy(dc + n, g.edge_coeff_minimum + (int64_t)e * n, sizeof(double) * n);
-            }
-            else {
-                std::fill(dc + n, dc + 2 * n, 0.0);
+            const double* cb = g.edge_coeff_baseline + (int64_t)e * n;
+            if (own_coeff[i]) {
+                double* dc = h_ec.data() + d.ecoef_off + (int64_t)e * 2 * n;
+                std::memcpy(dc, cb, sizeof(double) * n);
+                if (g.edge_coeff_minimum) {
+                    std::memcpy(dc + n, g.edge_coeff_minimum + (int64_t)e * n, sizeof(double) * n);
+                }
+                else {
+                    std::fill(dc + n, dc + 2 * n, 0.0);
+                }
+                for (int j = 0; j < n; ++j) {
+                    h_ecf[d.ecoef_f_off + (int64_t)e * n + j] = (float)cb[j];
+                }
             }
             bool any = false;
             for (int j = 0; j < n; ++j) {
-                any = any || (dc[j] > 0.0);
+                any = any || (cb[j] > 0.0);
             }
             h_any[ge] = any ? 1 : 0;
-            if (d.Ke) {
+            if (d.Ke && own_coeff[i]) {
                 std::memcpy(h_edt.data() + d.edt_off + (int64_t)e * d.Ke, g.edge_damping_times + (int64_t)e * d.Ke,
                             sizeof(double) * d.Ke);
                 std::memcpy(h_edv.data() + d.edv_off + (int64_t)e * d.Ke * n,
@@ -417,8 +466,77 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.edge_static_any = b->pool.upload(h_any);
     B.edge_pending    = b->pool.alloc<uint8_t>(edges);
     ck(cudaMemsetAsync(B.edge_pending, 0, std::max<int64_t>(edges, 1), ctx->stream), "memset");
-    B.trav       = b->pool.alloc<double>(tr);
+    const bool plain = b->opts.precision == MGPU_PRECISION_FP64_PLAIN;
+    B.trav       = plain ? b->pool.alloc<double>(tr) : nullptr; // the batched exchange recomputes travelers
     B.mfix       = b->pool.alloc<double>(tr);
+    B.state_total = st;
+    B.ysnap      = plain ? nullptr : b->pool.alloc<double>(2 * st);
+    B.ysnap_f    = plain ? nullptr : b->pool.alloc<float>(2 * st);
+    B.risk       = plain ? nullptr : (void*)b->pool.alloc<double>(2 * nodes * MGPU_MAX_GROUPS);
+    B.aux        = plain ? nullptr : (void*)b->pool.alloc<double>(nodes * MGPU_MAX_GROUPS * 12);
+    B.ecoef_f    = b->pool.upload(h_ecf);
+    B.tab_f      = nullptr;
+    B.contact_f  = nullptr;
+    B.dvals_f    = nullptr;
+    if (b->opts.precision == MGPU_PRECISION_MIXED) {
+        // FP32 node constants, contact and damping pools of the mixed solver
+        std::vector<float> tab((size_t)nodes * MGPU_MAX_GROUPS * kTabF, 0.0f);
+        for (int i = 0; i < num_graphs; ++i) {
+            const DevGraph& d = dg[i];
+            const int G       = d.G;
+            for (int64_t v = 0; v < d.N; ++v) {
+                const double* p = h_par.data() + d.param_off + v * param_stride(G);
+                auto gp         = [&](int w, int gr) {
+                    return p[MGPU_NUM_SCALAR_PARAMS + w * G + gr];
+                };
+                for (int gr = 0; gr < G; ++gr) {
+                    float* T           = tab.data() + ((d.node0 + v) * MGPU_MAX_GROUPS + gr) * kTabF;
+                    const double mu    = gp(MGPU_G_RECOVERED_PER_INS, gr);
+                    const double tins  = gp(MGPU_G_TIME_INS, gr);
+                    const double sev   = gp(MGPU_G_SEVERE_PER_ISY, gr);
+                    const double tisy  = gp(MGPU_G_TIME_ISY, gr);
+                    const double tisev = gp(MGPU_G_TIME_ISEV, gr);
+                    const double cps   = gp(MGPU_G_CRITICAL_PER_SEVERE, gr);
+                    const double dps   = gp(MGPU_G_DEATHS_PER_SEVERE, gr);
+                    const double dpc   = gp(MGPU_G_DEATHS_PER_CRITICAL, gr);
+                    const double ticri = gp(MGPU_G_TIME_ICRI, gr);
+                    T[TF_A_TNT]        = (float)((1 - mu) / tins);
+                    T[TF_BETA]         = (float)gp(MGPU_G_TRANSMISSION_PROB, gr);
+                    T[TF_XI]           = (float)gp(MGPU_G_REL_TRANSMISSION_NS, gr);
+                    T[TF_RHO]          = (float)gp(MGPU_G_RISK_FROM_SYMPTOMATIC, gr);
+                    T[TF_RHO_MAX]      = (float)gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, gr);
+                    T[TF_R1]           = (float)(1.0 / gp(MGPU_G_TIME_EXPOSED, gr));
+                    T[TF_R2]           = (float)((1 - mu) * (1 / tins));
+                    T[TF_R3]           = (float)(mu * (1.0 / tins));
+                    T[TF_R6]           = (float)(sev / tisy);
+                    T[TF_R7]           = (float)((1 - sev) / tisy);
+                    T[TF_R11]          = (float)((1.0 - cps - dps) / tisev);
+                    T[TF_R13]          = (float)(dpc / ticri);
+                    T[TF_R14]          = (float)((1.0 - dpc) / ticri);
+                    T[TF_R10L]         = (float)(cps / tisev);
+                    T[TF_R12L]         = (float)((dps + (cps - cps)) / tisev);
+                    T[TF_CPS]          = (float)cps;
+                    T[TF_DPS]          = (float)dps;
+                    T[TF_INV_TISEV]    = (float)(1.0 / tisev);
+                    const double cap   = p[MGPU_P_TNT_CAPACITY];
+                    T[TF_TNT_CAP]      = (float)cap;
+                    T[TF_TNT_CAP2]     = (float)(cap * p[MGPU_P_TNT_MAX_RISK]);
+                    const double icu   = p[MGPU_P_ICU_CAPACITY];
+                    T[TF_ICU_LO]       = (float)(0.90 * icu);
+                    T[TF_ICU_CAP]      = (float)icu;
+                    T[TF_SEASON_K]     = (float)p[MGPU_P_SEASONALITY];
+                }
+            }
+        }
+        B.tab_f = b->pool.upload(tab);
+        std::vector<float> cf(h_con.begin(), h_con.end()), df(h_dtv.begin(), h_dtv.end());
+        B.contact_f = b->pool.upload(cf);
+        B.dvals_f   = b->pool.upload(df);
+    }
+    b->any_edge_dampings = false;
+    for (int i = 0; i < num_graphs; ++i) {
+        b->any_edge_dampings = b->any_edge_dampings || (dg[i].Ke > 0 && dg[i].E > 0);
+    }
     B.edge_fixed = b->pool.alloc<int32_t>(edges);
     B.node_flag  = b->pool.alloc<uint8_t>(nodes);
     B.node_dirty = b->pool.alloc<uint8_t>(2 * nodes);
@@ -492,7 +610,7 @@ void enqueue_batched_phase(mgpu_batch* b, cudaStream_t s, cudaEvent_t* ev = null
         ck(cudaEventRecord(ev[1], s), "cudaEventRecord");
     }
     int64_t l = 0;
-    launch_exchange(B, b->n_max, s, &l);
+    launch_exchange_batched(B, b->opts.precision, b->n_max, b->any_edge_dampings, s, &l);
     launch_phase_end(B, s);
     if (ev) {
         ck(cudaEventRecord(ev[2], s), "cudaEventRecord");
@@ -876,7 +994,8 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
                 nev += 3;
                 ode_launches += (int64_t)b->inst_by_G.size();
             }
-            b->launches += P * (2 + (int64_t)b->inst_by_G.size() + exchange_launches(B.num_edges > 0));
+            b->launches +=
+                P * (2 + (int64_t)b->inst_by_G.size() + exchange_batched_launches(B.num_edges > 0, b->any_edge_dampings));
             b->phases += P;
         }
         else {
@@ -896,7 +1015,8 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
                     b->graph_exec   = nullptr;
                 }
             }
-            const int64_t per_phase = 2 + (int64_t)b->inst_by_G.size() + exchange_launches(B.num_edges > 0);
+            const int64_t per_phase = 2 + (int64_t)b->inst_by_G.size() +
+                                      exchange_batched_launches(B.num_edges > 0, b->any_edge_dampings);
             for (int64_t p = 0; p < P; ++p) {
                 if (b->graph_exec) {
                     ck(cudaGraphLaunch(b->graph_exec, s), "cudaGraphLaunch");

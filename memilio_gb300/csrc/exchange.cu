@@ -78,6 +78,7 @@ __global__ void k_phase_end(BatchDev B)
         rt.has_pending = 1;
         rt.t_dep       = rt.t_next;
         rt.t_ret       = rt.t_next + rt.dt;
+        rt.snap_slot ^= 1;
     }
     rt.return_mobile = !rt.return_mobile;
     rt.active        = 0;

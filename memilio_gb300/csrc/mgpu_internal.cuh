@@ -38,6 +38,7 @@ struct DevGraph {
     int64_t ecoef_off;   // doubles, [E][2][n] (baseline, minimum)
     int64_t edt_off;     // doubles, [E][Ke]
     int64_t edv_off;     // doubles, [E][Ke][n]
+    int64_t ecoef_f_off; // floats, [E][n] coefficients (Ke == 0) for the mixed exchange
 };
 
 // Mutable per-graph state (GraphSimulation::m_t and the edges' shared return flag).
@@ -54,7 +55,8 @@ struct GraphRt {
     int32_t has_pending; // travelers are away
     int32_t do_return; // current interval ends with returns
     int32_t do_depart; // current interval ends with departures
-    int32_t pad0, pad1;
+    int32_t snap_slot; // snapshot slot of the pending departure (batched exchange)
+    int32_t pad1;
 };
 
 // Integrator options on the device.
@@ -98,6 +100,15 @@ struct BatchDev {
     const int64_t* out_ptr;      // [num_nodes+1] CSR (edges sorted by (src, dst))
     const int64_t* in_ptr;       // [num_nodes+1] CSC
     const int64_t* in_edges;     // [num_edges] edge ids sorted by (dst, src)
+    int64_t state_total;         // doubles in a state pool
+    double* ysnap;               // [2][state_total] departure snapshots (batched exchange)
+    float* ysnap_f;              // [2][state_total] the same in FP32
+    void* risk;                  // [2][num_nodes][MAX_GROUPS] ISy mobility factor at departure (R)
+    void* aux;                   // [num_nodes][MAX_GROUPS][12] return-time force of infection and rates (R)
+    const float* ecoef_f;        // FP32 coefficients of edges without dampings
+    const float* tab_f;          // [num_nodes][MAX_GROUPS][kTabF] FP32 node constants (mixed solver)
+    const float* contact_f;      // FP32 copy of the contact pool
+    const float* dvals_f;        // FP32 copy of the damping-value pool
     double* scratch;             // plain ODE stage vectors, [8][scratch_nmax][scratch_stride]
     int64_t scratch_stride;      // node slots (distance between consecutive components)
     int32_t scratch_nmax;        // components per scratch vector
@@ -107,6 +118,14 @@ struct BatchDev {
 };
 
 enum { CNT_ACCEPTED = 0, CNT_REJECTED, CNT_FAILED, CNT_UNDERFLOW, CNT_SEQUENTIAL, CNT_NUM };
+
+// FP32 per-(node, age group) constants of the mixed solver, computed once from
+// the FP64 parameters (rates as the reference forms them: (1-mu)*(1/T) etc.).
+enum {
+    TF_A_TNT = 0, TF_BETA, TF_XI, TF_RHO, TF_RHO_MAX, TF_R1, TF_R2, TF_R3, TF_R6, TF_R7, TF_R11, TF_R13, TF_R14,
+    TF_R10L, TF_R12L, TF_CPS, TF_DPS, TF_INV_TISEV, TF_TNT_CAP, TF_TNT_CAP2, TF_ICU_LO, TF_ICU_CAP, TF_SEASON_K,
+    kTabF = 24
+};
 
 __host__ __device__ inline int param_stride(int G)
 {
@@ -406,6 +425,9 @@ int launch_ode_batched(const BatchDev& B, int G, int precision, const int32_t* d
 void launch_phase_begin(const BatchDev& B, double dt_exchange, cudaStream_t s);
 void launch_exchange(const BatchDev& B, int64_t max_n, cudaStream_t s, int64_t* launches);
 int exchange_launches(bool has_edges);
+void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,
+                             cudaStream_t s, int64_t* launches);
+int exchange_batched_launches(bool has_edges, bool any_edge_dampings);
 void launch_exchange_range(const BatchDev& B, int g0, int ng, int64_t n0, int64_t nn, int64_t e0, int64_t ne,
                            int64_t n_max, cudaStream_t s, int64_t* launches);
 void launch_phase_end(const BatchDev& B, cudaStream_t s);

@@ -561,6 +561,8 @@ struct SegF {
     float P[G], Q[G];
     float t_lo, t_hi, xl, scale; // damping segment and ramp, relative to t_base
     double t_base;
+    const float* cm_f; // the node's contact matrix (baseline, minimum) in FP32
+    const float* dv_f; // the node's damping cache values in FP32
 };
 
 template <int G>
@@ -568,12 +570,12 @@ __device__ void segf_load_contact(SegF<G>& X, float tau_rel)
 {
     const NodeModel& nm = X.nm;
     const long GG       = (long)G * G;
-    const double* Bm    = nm.cm + (long)X.gi * G;
-    const double* Lm    = Bm + GG;
+    const float* Bm     = X.cm_f + (long)X.gi * G;
+    const float* Lm     = Bm + GG;
     if (nm.K == 0) {
 #pragma unroll
         for (int j = 0; j < G; ++j) {
-            X.P[j] = (float)Bm[j];
+            X.P[j] = Bm[j];
             X.Q[j] = 0.0f;
         }
         X.t_lo  = -INFINITY;
@@ -585,13 +587,13 @@ __device__ void segf_load_contact(SegF<G>& X, float tau_rel)
     const double tau = X.t_base + (double)tau_rel;
     const double* T  = nm.dtimes;
     const int ub     = damping_upper_bound(T, nm.K, tau);
-    const double* Dl = nm.dvals + (long)(ub - 1) * GG + (long)X.gi * G;
-    const double* Dr = Dl + GG;
+    const float* Dl  = X.dv_f + (long)(ub - 1) * GG + (long)X.gi * G;
+    const float* Dr  = Dl + GG;
 #pragma unroll
     for (int j = 0; j < G; ++j) {
-        const double BL = Bm[j] - Lm[j];
-        X.P[j]          = (float)(Bm[j] - (0.5 * (Dl[j] + Dr[j])) * BL);
-        X.Q[j]          = (float)(-(0.5 * (Dl[j] - Dr[j])) * BL);
+        const float BL = Bm[j] - Lm[j];
+        X.P[j]         = Bm[j] - (0.5f * (Dl[j] + Dr[j])) * BL;
+        X.Q[j]         = -(0.5f * (Dl[j] - Dr[j])) * BL;
     }
     // times relative to the interval start; far sentinels saturate to +-inf
     X.t_lo  = (float)(T[ub - 1] - X.t_base);
@@ -603,46 +605,39 @@ __device__ void segf_load_contact(SegF<G>& X, float tau_rel)
 template <int G>
 __device__ void segf_load(SegF<G>& X, const BatchDev& B, const DevGraph& g, int64_t local, double t_base)
 {
-    X.nm                 = node_model(B, g, local);
-    const NodeModel& nm  = X.nm;
-    const int i          = X.gi;
-    const double mu      = nm.gp(MGPU_G_RECOVERED_PER_INS, i);
-    const double tins    = nm.gp(MGPU_G_TIME_INS, i);
-    const double sev     = nm.gp(MGPU_G_SEVERE_PER_ISY, i);
-    const double tisy    = nm.gp(MGPU_G_TIME_ISY, i);
-    const double tisev   = nm.gp(MGPU_G_TIME_ISEV, i);
-    const double cps     = nm.gp(MGPU_G_CRITICAL_PER_SEVERE, i);
-    const double dps     = nm.gp(MGPU_G_DEATHS_PER_SEVERE, i);
-    const double dpc     = nm.gp(MGPU_G_DEATHS_PER_CRITICAL, i);
-    const double ticri   = nm.gp(MGPU_G_TIME_ICRI, i);
-    X.t_base             = t_base;
-    X.a_tnt              = (float)((1 - mu) / tins);
-    X.beta               = (float)nm.gp(MGPU_G_TRANSMISSION_PROB, i);
-    X.xi                 = (float)nm.gp(MGPU_G_REL_TRANSMISSION_NS, i);
-    X.rho                = (float)nm.gp(MGPU_G_RISK_FROM_SYMPTOMATIC, i);
-    X.rho_max            = (float)nm.gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, i);
-    X.r1                 = (float)(1.0 / nm.gp(MGPU_G_TIME_EXPOSED, i));
-    X.r2                 = (float)((1 - mu) * (1 / tins));
-    X.r3                 = (float)(mu * (1.0 / tins));
-    X.r6                 = (float)(sev / tisy);
-    X.r7                 = (float)((1 - sev) / tisy);
-    X.r11                = (float)((1.0 - cps - dps) / tisev);
-    X.r13                = (float)(dpc / ticri);
-    X.r14                = (float)((1.0 - dpc) / ticri);
-    X.r10l               = (float)(cps / tisev);
-    X.r12l               = (float)((dps + (cps - cps)) / tisev);
-    X.cps                = (float)cps;
-    X.dps                = (float)dps;
-    X.inv_tisev          = (float)(1.0 / tisev);
-    const double cap     = nm.scalar(MGPU_P_TNT_CAPACITY);
-    X.tnt_cap            = (float)cap;
-    X.tnt_cap2           = (float)(cap * nm.scalar(MGPU_P_TNT_MAX_RISK));
-    const double icu_cap = nm.scalar(MGPU_P_ICU_CAPACITY);
-    X.icu_lo             = (float)(0.90 * icu_cap);
-    X.icu_cap            = (float)icu_cap;
-    X.season_k           = (float)nm.scalar(MGPU_P_SEASONALITY);
-    X.season_s0          = (float)((nm.scalar(MGPU_P_START_DAY) + t_base) / 182.5 + 0.5);
-    X.fast               = nm.M == 1;
+    X.nm                = node_model(B, g, local);
+    const NodeModel& nm = X.nm;
+    const long GG       = (long)G * G;
+    X.cm_f              = B.contact_f + g.contact_off + local * g.M * 2 * GG;
+    X.dv_f              = g.K ? B.dvals_f + g.dval_off + local * g.M * g.K * GG : nullptr;
+    // per-(node, group) constants precomputed in FP32 at upload (no FP64 division here)
+    const float* T = B.tab_f + ((g.node0 + local) * MGPU_MAX_GROUPS + X.gi) * kTabF;
+    X.t_base       = t_base;
+    X.a_tnt        = T[TF_A_TNT];
+    X.beta         = T[TF_BETA];
+    X.xi           = T[TF_XI];
+    X.rho          = T[TF_RHO];
+    X.rho_max      = T[TF_RHO_MAX];
+    X.r1           = T[TF_R1];
+    X.r2           = T[TF_R2];
+    X.r3           = T[TF_R3];
+    X.r6           = T[TF_R6];
+    X.r7           = T[TF_R7];
+    X.r11          = T[TF_R11];
+    X.r13          = T[TF_R13];
+    X.r14          = T[TF_R14];
+    X.r10l         = T[TF_R10L];
+    X.r12l         = T[TF_R12L];
+    X.cps          = T[TF_CPS];
+    X.dps          = T[TF_DPS];
+    X.inv_tisev    = T[TF_INV_TISEV];
+    X.tnt_cap      = T[TF_TNT_CAP];
+    X.tnt_cap2     = T[TF_TNT_CAP2];
+    X.icu_lo       = T[TF_ICU_LO];
+    X.icu_cap      = T[TF_ICU_CAP];
+    X.season_k     = T[TF_SEASON_K];
+    X.season_s0    = (float)((nm.scalar(MGPU_P_START_DAY) + t_base) * (1.0 / 182.5) + 0.5);
+    X.fast         = nm.M == 1;
     if (X.fast) {
         segf_load_contact(X, 0.0f);
     }
@@ -766,12 +761,13 @@ __global__ void __launch_bounds__(128) k_ode_mixed(BatchDev B, const int32_t* in
         const double tmax = rt.t_next;
         segf_load(X, B, g, local, t);
 
-        // SystemIntegrator::advance
-        const double t0   = t;
-        double dt_restore = 0.0;
-        double dt_min     = o.dt_min;
-        int steps         = 0;
-        while (fabs((tmax - t) / (tmax - t0)) > kZeroTol) {
+        // SystemIntegrator::advance; |(tmax - t) / (tmax - t0)| > eps without the FP64 division
+        const double t0    = t;
+        const double eps_t = kZeroTol * fabs(tmax - t0);
+        double dt_restore  = 0.0;
+        double dt_min      = o.dt_min;
+        int steps          = 0;
+        while (fabs(tmax - t) > eps_t) {
             if (steps++ >= o.max_steps) {
                 cap_hit = true;
                 break;
