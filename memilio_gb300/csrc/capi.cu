@@ -472,7 +472,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.state_total = st;
     B.ysnap      = plain ? nullptr : b->pool.alloc<double>(2 * st);
     B.ysnap_f    = plain ? nullptr : b->pool.alloc<float>(2 * st);
-    B.risk       = plain ? nullptr : (void*)b->pool.alloc<double>(2 * nodes * MGPU_MAX_GROUPS);
+    B.risk       = plain ? nullptr : (void*)b->pool.alloc<double>(2 * nodes * MGPU_MAX_GROUPS * 2);
     B.aux        = plain ? nullptr : (void*)b->pool.alloc<double>(nodes * MGPU_MAX_GROUPS * 12);
     B.ecoef_f    = b->pool.upload(h_ecf);
     B.tab_f      = nullptr;

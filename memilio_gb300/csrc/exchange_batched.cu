@@ -165,18 +165,14 @@ template <class R, bool orig = false>
 __device__ __forceinline__ void depart_travelers(const BatchDev& B, const DevGraph& g, int64_t e, int gr, int slot,
                                                  double t, R (&m)[kC])
 {
-    const int64_t u     = B.edge_src[e];
-    const int64_t lu    = u - g.node0;
-    const int64_t le    = e - g.edge0;
-    const R* y          = snap_ptr<R>(B, slot) + g.state_off + lu * g.n + gr * kC;
-    const R risk        = reinterpret_cast<const R*>(B.risk)[((int64_t)slot * B.num_nodes + u) * MGPU_MAX_GROUPS + gr];
-    R nd                = (R)1;
-    if (!orig) {
-        const double* p = B.params + g.param_off + lu * param_stride(g.G);
-        if (t >= p[MGPU_P_START_COMMUTER_DETECTION] && t < p[MGPU_P_END_COMMUTER_DETECTION]) {
-            nd = (R)p[MGPU_P_COMMUTER_NONDETECTION];
-        }
-    }
+    const int64_t u  = B.edge_src[e];
+    const int64_t lu = u - g.node0;
+    const int64_t le = e - g.edge0;
+    const R* y       = snap_ptr<R>(B, slot) + g.state_off + lu * g.n + gr * kC;
+    const R* fac     = reinterpret_cast<const R*>(B.risk) + (((int64_t)slot * B.num_nodes + u) * MGPU_MAX_GROUPS + gr) * 2;
+    const R risk     = fac[0];
+    const R nd       = orig ? (R)1 : fac[1];
+    (void)t;
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
         const R cf = xb_coeff<R>(B, g, le, gr * kC + c, t);
@@ -365,10 +361,17 @@ __global__ void k_xb_prep(BatchDev B, int64_t n0, int64_t nn)
             yd[j]          = v;
             yf[j]          = (float)v;
         }
-        R* risk = reinterpret_cast<R*>(B.risk) + ((int64_t)ws * B.num_nodes + node) * MGPU_MAX_GROUPS;
+        // per age group: ISy mobility factor and commuter nondetection at this departure
+        R* fac = reinterpret_cast<R*>(B.risk) + ((int64_t)ws * B.num_nodes + node) * MGPU_MAX_GROUPS * 2;
         const CVec y{B.state + so, 1};
+        const double t    = rt.t_next;
+        const double nd   = (t >= nm.scalar(MGPU_P_START_COMMUTER_DETECTION) &&
+                           t < nm.scalar(MGPU_P_END_COMMUTER_DETECTION))
+                                ? nm.scalar(MGPU_P_COMMUTER_NONDETECTION)
+                                : 1.0;
         for (int gr = 0; gr < g.G; ++gr) {
-            risk[gr] = (R)mobility_isy_factor(nm, y, gr);
+            fac[2 * gr]     = (R)mobility_isy_factor(nm, y, gr);
+            fac[2 * gr + 1] = (R)nd;
         }
     }
 }
@@ -409,6 +412,9 @@ __global__ void k_xb_depart(BatchDev B, int64_t n0, int64_t nn)
     const GraphRt& rt = B.rt[gi];
     if (gr >= g.G || !xb_departing(rt)) {
         return;
+    }
+    if (std::is_same<R, float>::value && g.Ke == 0) {
+        return; // k_xf_depart
     }
     const int ws     = rt.snap_slot ^ 1;
     const double t   = rt.t_next;
@@ -493,6 +499,9 @@ __global__ void k_xb_return(BatchDev B, int64_t n0, int64_t nn)
     if (gr >= g.G || !xb_returning(rt)) {
         return;
     }
+    if (std::is_same<R, float>::value && g.Ke == 0) {
+        return; // k_xf_return
+    }
     const int64_t lv = node - g.node0;
     const double* yv = B.state + g.state_off + lv * g.n + gr * kC;
     Acc<R> acc[kC];
@@ -570,6 +579,267 @@ __global__ void k_xb_return(BatchDev B, int64_t n0, int64_t nn)
     for (int c = 0; c < kC; ++c) {
         yn[c] = acc[c].get();
         flag  = flag || (bound[c] < margin * mag[c]);
+    }
+    if (flag) {
+        B.node_flag[node] = 1;
+    }
+}
+
+// ---- FP32 node passes of the mixed solver ------------------------------------
+// Per edge: 22 loads (source snapshot, source factors, coefficients), the
+// traveler products, and 10 exact TwoSum updates; everything about the node
+// itself (its snapshot and factors for out-edges, its force of infection and
+// rates for in-edges) is loaded once.
+
+struct GroupSnap {
+    float y[kC];
+    float risk, nd;
+};
+
+__device__ __forceinline__ void load_group_snap(const BatchDev& B, const DevGraph& g, int64_t node, int gr, int slot,
+                                                GroupSnap& s)
+{
+    const float* y = B.ysnap_f + (int64_t)slot * B.state_total + g.state_off + (node - g.node0) * g.n + gr * kC;
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        s.y[c] = y[c];
+    }
+    const float* fac = reinterpret_cast<const float*>(B.risk) + (((int64_t)slot * B.num_nodes + node) * MGPU_MAX_GROUPS + gr) * 2;
+    s.risk           = fac[0];
+    s.nd             = fac[1];
+}
+
+// m = ((y o c) o f) with the nondetection factor on INS and ISy (same operations as depart_travelers<float>)
+__device__ __forceinline__ void travelers_f(const BatchDev& B, const DevGraph& g, int64_t e, int gr,
+                                            const GroupSnap& s, float (&m)[kC])
+{
+    const float* cf = B.ecoef_f + g.ecoef_f_off + (e - g.edge0) * g.n + gr * kC;
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        float v = __fmul_rn(__fmul_rn(s.y[c], cf[c]), c == MGPU_ISY ? s.risk : 1.0f);
+        if (c == MGPU_INS || c == MGPU_ISY) {
+            v = __fmul_rn(v, s.nd);
+        }
+        m[c] = v;
+    }
+}
+
+__device__ __forceinline__ void flows_f(const float* a, float dt, const float (&m)[kC], float (&phi)[kF])
+{
+    const float s[kF] = {m[MGPU_S],    m[MGPU_E],    m[MGPU_INS],  m[MGPU_INS],  m[MGPU_INSC],
+                         m[MGPU_INSC], m[MGPU_ISY],  m[MGPU_ISY],  m[MGPU_ISYC], m[MGPU_ISYC],
+                         m[MGPU_ISEV], m[MGPU_ISEV], m[MGPU_ISEV], m[MGPU_ICRI], m[MGPU_ICRI]};
+    const int ai[kF] = {0, 1, 2, 3, 2, 3, 4, 5, 4, 5, 6, 7, 8, 9, 10};
+#pragma unroll
+    for (int k = 0; k < kF; ++k) {
+        phi[k] = __fmul_rn(dt, __fmul_rn(a[ai[k]], s[k]));
+    }
+}
+
+__global__ void k_xf_depart(BatchDev B, int64_t n0, int64_t nn)
+{
+    const int64_t tid  = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t node = n0 + tid / MGPU_MAX_GROUPS;
+    const int gr       = (int)(tid % MGPU_MAX_GROUPS);
+    if (tid >= nn * MGPU_MAX_GROUPS) {
+        return;
+    }
+    const int gi      = B.node_graph[node];
+    const DevGraph& g = B.graphs[gi];
+    const GraphRt& rt = B.rt[gi];
+    if (gr >= g.G || !xb_departing(rt) || g.Ke != 0) {
+        return;
+    }
+    const int ws     = rt.snap_slot ^ 1;
+    const int64_t lv = node - g.node0;
+    double* yv       = B.state + g.state_off + lv * g.n + gr * kC;
+    Acc<float> acc[kC];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        acc[c].init(yv[c]);
+    }
+    GroupSnap own, src;
+    load_group_snap(B, g, node, gr, ws, own);
+    float m[kC];
+    const int64_t ib = B.in_ptr[node], ie = B.in_ptr[node + 1];
+    int64_t k        = ib;
+    for (; k < ie; ++k) {
+        const int64_t e = B.in_edges[k];
+        const int64_t u = B.edge_src[e];
+        if (u > node) {
+            break;
+        }
+        if (B.edge_static_any[e]) {
+            load_group_snap(B, g, u, gr, ws, src);
+            travelers_f(B, g, e, gr, src, m);
+#pragma unroll
+            for (int c = 0; c < kC; ++c) {
+                acc[c].add(m[c]);
+            }
+        }
+    }
+    const bool detect = own.nd != 1.0f;
+    const float q     = 1.0f - own.nd;
+    for (int64_t e = B.out_ptr[node]; e < B.out_ptr[node + 1]; ++e) {
+        if (!B.edge_static_any[e]) {
+            continue;
+        }
+        if (detect) {
+            // test_commuters: detected commuters move to the confirmed compartments first
+            GroupSnap o = own;
+            o.nd        = 1.0f;
+            float mo[kC];
+            travelers_f(B, g, e, gr, o, mo);
+            acc[MGPU_INS].add(-__fmul_rn(mo[MGPU_INS], q));
+            acc[MGPU_INSC].add(__fmul_rn(mo[MGPU_INS], q));
+            acc[MGPU_ISY].add(-__fmul_rn(mo[MGPU_ISY], q));
+            acc[MGPU_ISYC].add(__fmul_rn(mo[MGPU_ISY], q));
+        }
+        travelers_f(B, g, e, gr, own, m);
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            acc[c].add(-m[c]);
+        }
+    }
+    for (; k < ie; ++k) {
+        const int64_t e = B.in_edges[k];
+        if (B.edge_static_any[e]) {
+            load_group_snap(B, g, B.edge_src[e], gr, ws, src);
+            travelers_f(B, g, e, gr, src, m);
+#pragma unroll
+            for (int c = 0; c < kC; ++c) {
+                acc[c].add(m[c]);
+            }
+        }
+    }
+    double* v0 = B.v0 + g.state_off + lv * g.n + gr * kC;
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        const double v = acc[c].get();
+        yv[c]          = v;
+        v0[c]          = v;
+    }
+}
+
+__global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
+{
+    const int64_t tid  = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t node = n0 + tid / MGPU_MAX_GROUPS;
+    const int gr       = (int)(tid % MGPU_MAX_GROUPS);
+    if (tid >= nn * MGPU_MAX_GROUPS) {
+        return;
+    }
+    const int gi      = B.node_graph[node];
+    const DevGraph& g = B.graphs[gi];
+    const GraphRt& rt = B.rt[gi];
+    if (gr >= g.G || !xb_returning(rt) || g.Ke != 0) {
+        return;
+    }
+    const int slot   = rt.snap_slot;
+    const float dt   = (float)rt.dt;
+    const int64_t lv = node - g.node0;
+    const double* yv = B.state + g.state_off + lv * g.n + gr * kC;
+    Acc<float> acc[kC];
+    float yf[kC], min_in[kC], phi_in[kF], phi_out[kF];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        acc[c].init(yv[c]);
+        yf[c]     = acc[c].hi;
+        min_in[c] = 0.0f;
+    }
+#pragma unroll
+    for (int f = 0; f < kF; ++f) {
+        phi_in[f]  = 0.0f;
+        phi_out[f] = 0.0f;
+    }
+    const float* aux = reinterpret_cast<const float*>(B.aux);
+    float a_own[kAux];
+#pragma unroll
+    for (int q = 0; q < kAux; ++q) {
+        a_own[q] = aux[(node * MGPU_MAX_GROUPS + gr) * kAux + q];
+    }
+    GroupSnap own, src;
+    load_group_snap(B, g, node, gr, slot, own);
+    float m[kC], phi[kF];
+    float lowest = 0.0f; // a negative traveler or increment voids the bound
+    auto in_edge = [&](int64_t e, int64_t u) {
+        load_group_snap(B, g, u, gr, slot, src);
+        travelers_f(B, g, e, gr, src, m);
+        flows_f(a_own, dt, m, phi);
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            acc[c].add(-m[c]);
+            min_in[c] += m[c];
+            lowest = fminf(lowest, m[c]);
+        }
+#pragma unroll
+        for (int f = 0; f < kF; ++f) {
+            phi_in[f] += phi[f];
+            lowest = fminf(lowest, phi[f]);
+        }
+    };
+    const int64_t ib = B.in_ptr[node], ie = B.in_ptr[node + 1];
+    int64_t k        = ib;
+    for (; k < ie; ++k) {
+        const int64_t e = B.in_edges[k];
+        const int64_t u = B.edge_src[e];
+        if (u > node) {
+            break;
+        }
+        if (B.edge_static_any[e]) {
+            in_edge(e, u);
+        }
+    }
+    for (int64_t e = B.out_ptr[node]; e < B.out_ptr[node + 1]; ++e) {
+        if (!B.edge_static_any[e]) {
+            continue;
+        }
+        travelers_f(B, g, e, gr, own, m);
+        flows_f(aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux, dt, m, phi);
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            acc[c].add(m[c]);
+            lowest = fminf(lowest, m[c]);
+        }
+#pragma unroll
+        for (int f = 0; f < kF; ++f) {
+            phi_out[f] += phi[f];
+            lowest = fminf(lowest, phi[f]);
+        }
+    }
+    for (; k < ie; ++k) {
+        const int64_t e = B.in_edges[k];
+        if (B.edge_static_any[e]) {
+            in_edge(e, B.edge_src[e]);
+        }
+    }
+    // flow increments: in-edges take travelers away (their increments count
+    // with the opposite sign), out-edges bring them home
+    float in_c[kC], out_c[kC];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        in_c[c]  = min_in[c];
+        out_c[c] = 0.0f;
+    }
+#pragma unroll
+    for (int f = 0; f < kF; ++f) {
+        acc[kFlowSrcI(f)].add(phi_in[f]);
+        acc[kFlowDstI(f)].add(-phi_in[f]);
+        acc[kFlowSrcI(f)].add(-phi_out[f]);
+        acc[kFlowDstI(f)].add(phi_out[f]);
+        in_c[kFlowDstI(f)] += phi_in[f];
+        out_c[kFlowSrcI(f)] += phi_out[f];
+    }
+    // conservative no-underflow bound: with nonnegative travelers and increments,
+    // every partial state of the serial order is at least y - in - out
+    bool flag = lowest < 0.0f;
+    double* yn = B.ynew + g.state_off + lv * g.n + gr * kC;
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        yn[c]             = acc[c].get();
+        const float bound = yf[c] - in_c[c] - out_c[c];
+        const float mag   = fabsf(yf[c]) + in_c[c] + out_c[c];
+        flag              = flag || (bound < 1e-5f * mag);
     }
     if (flag) {
         B.node_flag[node] = 1;
@@ -900,8 +1170,16 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
     if (ne == 0) {
         return;
     }
-    const int64_t ng = nn * MGPU_MAX_GROUPS;
-    k_xb_return<R><<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
+    const int64_t ng  = nn * MGPU_MAX_GROUPS;
+    const bool mixed  = std::is_same<R, float>::value;
+    if (mixed) {
+        k_xf_return<<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
+        *launches += 1;
+    }
+    if (!mixed || any_edge_dampings) {
+        k_xb_return<R><<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
+        *launches += 1;
+    }
     for (int pass = 0; pass < kXbScanPasses; ++pass) {
         k_xb_scan<R><<<blocks_of(nn * 32, 128), 128, 0, s>>>(B, 0, nn, pass);
     }
@@ -913,15 +1191,22 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
         k_xb_edge_flags<<<blocks_of(ne, 256), 256, 0, s>>>(B, 0, ne);
         *launches += 1;
     }
-    k_xb_depart<R><<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
-    *launches += 7 + kXbScanPasses;
+    if (mixed) {
+        k_xf_depart<<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
+        *launches += 1;
+    }
+    if (!mixed || any_edge_dampings) {
+        k_xb_depart<R><<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
+        *launches += 1;
+    }
+    *launches += 5 + kXbScanPasses;
 }
 
 } // namespace
 
 int exchange_batched_launches(bool has_edges, bool any_edge_dampings)
 {
-    return has_edges ? 8 + kXbScanPasses + (any_edge_dampings ? 1 : 0) : 1;
+    return has_edges ? 8 + kXbScanPasses + (any_edge_dampings ? 3 : 0) : 1;
 }
 
 void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,

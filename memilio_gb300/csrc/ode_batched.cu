@@ -720,7 +720,11 @@ __device__ __forceinline__ void segf_rhs(SegF<G>& X, const float (&u)[kC], float
 }
 
 template <int G>
-__global__ void __launch_bounds__(128) k_ode_mixed(BatchDev B, const int32_t* inst, int64_t count)
+#ifndef MGPU_MIXED_MIN_BLOCKS
+#define MGPU_MIXED_MIN_BLOCKS 1 // resident 128-thread blocks per SM the register budget must allow
+#endif
+__global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchDev B, const int32_t* inst,
+                                                                         int64_t count)
 {
     constexpr int IPW = 32 / G;
     const int lane    = threadIdx.x & 31;
@@ -734,8 +738,10 @@ __global__ void __launch_bounds__(128) k_ode_mixed(BatchDev B, const int32_t* in
     X.mask            = (((1u << G) - 1u) << X.base);
     const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw  = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const DevOpts o   = B.opts;
-    const float abs_f = (float)o.abs_tol, rel_f = (float)o.rel_tol;
+    const DevOpts o      = B.opts;
+    const float abs_f    = (float)o.abs_tol, rel_f = (float)o.rel_tol;
+    const float o_dt_min = (float)o.dt_min; // DBL_MIN becomes 0: no lower bound, as in FP64
+    const float o_dt_max = (float)o.dt_max; // DBL_MAX becomes +inf
     unsigned long long n_acc = 0, n_rej = 0, n_fail = 0;
     bool cap_hit = false, nonfinite = false;
 
@@ -756,43 +762,51 @@ __global__ void __launch_bounds__(128) k_ode_mixed(BatchDev B, const int32_t* in
             hi[c]          = (float)v;
             lo[c]          = (float)(v - (double)hi[c]);
         }
-        double t          = B.node_t[node];
-        double dt         = B.node_dt[node];
-        const double tmax = rt.t_next;
-        segf_load(X, B, g, local, t);
+        const double t_start = B.node_t[node];
+        const double tmax    = rt.t_next;
+        segf_load(X, B, g, local, t_start);
 
-        // SystemIntegrator::advance; |(tmax - t) / (tmax - t0)| > eps without the FP64 division
-        const double t0    = t;
-        const double eps_t = kZeroTol * fabs(tmax - t0);
-        double dt_restore  = 0.0;
-        double dt_min      = o.dt_min;
-        int steps          = 0;
-        while (fabs(tmax - t) > eps_t) {
+        // SystemIntegrator::advance on an interval-relative FP32 clock: tr runs
+        // from 0 to span (0.5 days is exact in FP32); a step clipped to the
+        // remaining span lands exactly on it.
+        const float span  = (float)(tmax - t_start);
+        const float eps_t = (float)kZeroTol * span;
+        float tr          = 0.0f;
+        float dt          = (float)B.node_dt[node];
+        float dt_restore  = 0.0f;
+        float dt_min      = o_dt_min;
+        int steps         = 0;
+        while (span - tr > eps_t) {
             if (steps++ >= o.max_steps) {
                 cap_hit = true;
                 break;
             }
-            if (dt > tmax - t) {
-                dt_restore = dt;
-                dt         = tmax - t;
-                dt_min     = fmin(tmax - t, dt_min);
+            bool last = false;
+            if (dt >= span - tr) {
+                if (dt > span - tr) {
+                    dt_restore = dt;
+                }
+                dt     = span - tr;
+                dt_min = fminf(span - tr, dt_min);
+                last   = true;
             }
             // ControlledStepperWrapper::step
             bool success     = false;
             bool is_dt_valid = true;
             float phi[kF];
+            const float dt_try0 = dt;
             while (!success && is_dt_valid) {
                 if (dt < dt_min) {
                     is_dt_valid = false;
                     dt          = dt_min;
                 }
-                if (o.dt_max != 0.0 && fabs(dt) > o.dt_max) {
-                    dt = o.dt_max;
+                if (o_dt_max != 0.0f && fabsf(dt) > o_dt_max) {
+                    dt = o_dt_max;
                     ++n_rej;
                     continue;
                 }
-                const float dtf  = (float)dt;
-                const float trel = (float)(t - X.t_base);
+                const float dtf  = dt;
+                const float trel = tr;
                 float k[5][kC];
                 float kc[kC], fl[kF], xe[kC];
                 segf_rhs(X, hi, trel, fl, kc);
@@ -843,29 +857,30 @@ __global__ void __launch_bounds__(128) k_ode_mixed(BatchDev B, const int32_t* in
                 for (int q = 0; q < G; ++q) {
                     el = fmaxf(el, __shfl_sync(X.mask, el, X.base + q));
                 }
-                // controller: FP64 clock, FP32 step-size factor
+                // controller (Odeint rules) on the FP32 clock
                 if (el > 1.0f) {
-                    dt *= (double)fmaxf(0.9f * exp2f(__log2f(el) * (-1.0f / 3.0f)), 0.2f);
-                    if (o.dt_max != 0.0) {
-                        dt = fmin(dt, o.dt_max);
+                    dt *= fmaxf(0.9f * exp2f(__log2f(el) * (-1.0f / 3.0f)), 0.2f);
+                    if (o_dt_max != 0.0f) {
+                        dt = fminf(dt, o_dt_max);
                     }
                     ++n_rej;
                 }
                 else {
-                    t += dt;
+                    // the step taken with the clipped size reaches the boundary exactly
+                    tr = (last && dt == dt_try0) ? span : tr + dt;
                     if (el < 0.5f) {
                         const float e = fmaxf(0.00032f /* 5^-5 */, el);
-                        dt *= (double)(0.9f * exp2f(__log2f(e) * -0.2f));
-                        if (o.dt_max != 0.0) {
-                            dt = fmin(dt, o.dt_max);
+                        dt *= 0.9f * exp2f(__log2f(e) * -0.2f);
+                        if (o_dt_max != 0.0f) {
+                            dt = fminf(dt, o_dt_max);
                         }
                     }
                     success = true;
                 }
             }
-            dt = fmax(dt, dt_min);
+            dt = fmaxf(dt, dt_min);
             if (!success) {
-                t += dt_min;
+                tr += dt_min;
                 ++n_fail;
             }
             else {
@@ -882,7 +897,7 @@ __global__ void __launch_bounds__(128) k_ode_mixed(BatchDev B, const int32_t* in
                 df_renorm(hi[c], lo[c]);
             }
         }
-        dt = fmax(dt, dt_restore);
+        dt = fmaxf(dt, dt_restore);
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
             const double v = (double)hi[c] + (double)lo[c];
@@ -890,8 +905,8 @@ __global__ void __launch_bounds__(128) k_ode_mixed(BatchDev B, const int32_t* in
             nonfinite      = nonfinite || !isfinite(v);
         }
         if (X.gi == 0) {
-            B.node_t[node]  = t;
-            B.node_dt[node] = dt;
+            B.node_t[node]  = (tr >= span) ? tmax : t_start + (double)tr;
+            B.node_dt[node] = (double)dt;
         }
     }
     if (cap_hit) {
