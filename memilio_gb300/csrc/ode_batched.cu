@@ -742,6 +742,10 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
     const float abs_f    = (float)o.abs_tol, rel_f = (float)o.rel_tol;
     const float o_dt_min = (float)o.dt_min; // DBL_MIN becomes 0: no lower bound, as in FP64
     const float o_dt_max = (float)o.dt_max; // DBL_MAX becomes +inf
+    // stage derivatives k_0..k_4: [warp][stage*10 + c][lane] (conflict-free columns)
+    extern __shared__ float ode_smem[];
+    float* skw = ode_smem + (threadIdx.x >> 5) * (5 * kC * 32);
+#define SK(s, c) skw[((s) * kC + (c)) * 32 + lane]
     unsigned long long n_acc = 0, n_rej = 0, n_fail = 0;
     bool cap_hit = false, nonfinite = false;
 
@@ -807,42 +811,51 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
                 }
                 const float dtf  = dt;
                 const float trel = tr;
-                float k[5][kC];
                 float kc[kC], fl[kF], xe[kC];
                 segf_rhs(X, hi, trel, fl, kc);
 #pragma unroll
                 for (int c = 0; c < kC; ++c) {
-                    k[0][c] = kc[c];
-                    xe[c]   = (fk_db[0] * dtf) * kc[c];
+                    SK(0, c) = kc[c];
+                    xe[c]    = (fk_db[0] * dtf) * kc[c];
                 }
 #pragma unroll
                 for (int f = 0; f < kF; ++f) {
                     phi[f] = (fk_b5[0] * dtf) * fl[f];
                 }
-#pragma unroll
+                // stages 2..6: one copy of the right-hand side in the code, stage
+                // derivatives in this lane's shared-memory column
+#pragma unroll 1
                 for (int s = 1; s < 6; ++s) {
                     float u[kC];
 #pragma unroll
                     for (int c = 0; c < kC; ++c) {
-                        float v = hi[c];
+                        u[c] = hi[c];
+                    }
+#pragma unroll 1
+                    for (int j = 0; j < s; ++j) {
+                        const float a = fk_a[s][j] * dtf;
 #pragma unroll
-                        for (int j = 0; j < s; ++j) {
-                            v = v + (fk_a[s][j] * dtf) * k[j][c];
+                        for (int c = 0; c < kC; ++c) {
+                            u[c] = u[c] + a * SK(j, c);
                         }
-                        u[c] = v;
                     }
                     segf_rhs(X, u, trel + fk_c[s] * dtf, fl, kc);
+                    const float db = fk_db[s] * dtf;
 #pragma unroll
                     for (int c = 0; c < kC; ++c) {
-                        xe[c] = xe[c] + (fk_db[s] * dtf) * kc[c];
-                        if (s < 5) {
-                            k[s][c] = kc[c];
+                        xe[c] = xe[c] + db * kc[c];
+                    }
+                    if (s < 5) {
+#pragma unroll
+                        for (int c = 0; c < kC; ++c) {
+                            SK(s, c) = kc[c];
                         }
                     }
-                    if (s == 2 || s == 3 || s == 5) {
+                    const float b5 = fk_b5[s] * dtf;
+                    if (b5 != 0.0f) {
 #pragma unroll
                         for (int f = 0; f < kF; ++f) {
-                            phi[f] = phi[f] + (fk_b5[s] * dtf) * fl[f];
+                            phi[f] = phi[f] + b5 * fl[f];
                         }
                     }
                 }
@@ -850,7 +863,7 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
                 float el = 0.0f;
 #pragma unroll
                 for (int c = 0; c < kC; ++c) {
-                    const float den = abs_f + rel_f * (fabsf(hi[c]) + dtf * fabsf(k[0][c]));
+                    const float den = abs_f + rel_f * (fabsf(hi[c]) + dtf * fabsf(SK(0, c)));
                     el              = fmaxf(el, fabsf(xe[c]) * __frcp_rn(den));
                 }
 #pragma unroll
@@ -943,7 +956,8 @@ int launch_g(const BatchDev& B, int precision, const int32_t* inst, int64_t coun
         blocks = 1;
     }
     if (precision == MGPU_PRECISION_MIXED) {
-        k_ode_mixed<G><<<(unsigned)blocks, threads, 0, s>>>(B, inst, count);
+        const size_t smem = (size_t)(threads / 32) * 5 * kC * 32 * sizeof(float);
+        k_ode_mixed<G><<<(unsigned)blocks, threads, smem, s>>>(B, inst, count);
     }
     else {
         k_ode_batched<G, double><<<(unsigned)blocks, threads, 0, s>>>(B, inst, count);
