@@ -159,6 +159,9 @@ struct mgpu_batch {
     std::vector<int64_t> node0, edge0, state_off;
     int64_t state_total = 0;
     double* init_state  = nullptr; // initial states (for reset)
+    float* init_hi      = nullptr; // the same as float-float pairs (mixed solver)
+    float* init_lo      = nullptr;
+    bool pairs          = false;   // node states are float-float pairs on the device
     double dt0          = 0.1;
     std::vector<double> t_host;  // mirror of rt.t
     std::vector<double> tmax_host;
@@ -217,12 +220,28 @@ __global__ void k_set_tmax(GraphRt* rt, const double* tmax, int num_graphs)
     }
 }
 
+// FP64 value -> float-float pair (hi = nearest float, lo = the rest rounded)
+void split_pairs(const double* v, int64_t n, float* hi, float* lo)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        hi[i] = (float)v[i];
+        lo[i] = (float)(v[i] - (double)hi[i]);
+    }
+}
+
 // Restart: graph clocks and flags, node clocks, states, pending travelers.
-__global__ void k_reset(BatchDev B, const double* init_state, int64_t state_total, double t0, double dt0)
+__global__ void k_reset(BatchDev B, const double* init_state, const float* init_hi, const float* init_lo,
+                        int64_t state_total, double t0, double dt0)
 {
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (tid < state_total) {
-        B.state[tid] = init_state[tid];
+        if (B.st_hi) {
+            B.st_hi[tid] = init_hi[tid];
+            B.st_lo[tid] = init_lo[tid];
+        }
+        else {
+            B.state[tid] = init_state[tid];
+        }
     }
     if (tid < B.num_nodes) {
         B.node_t[tid]  = t0;
@@ -449,12 +468,32 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.contact    = b->pool.upload(h_con);
     B.dtimes     = b->pool.upload(h_dtt);
     B.dvals      = b->pool.upload(h_dtv);
-    B.state      = b->pool.upload(h_state);
-    b->init_state = b->pool.upload(h_state);
-    b->dt0        = dt0;
-    B.v0         = b->pool.alloc<double>(st);
-    B.ypre       = b->pool.alloc<double>(st);
-    B.ynew       = b->pool.alloc<double>(std::max<int64_t>(st, scratch_slots * b->n_max));
+    b->dt0     = dt0;
+    b->pairs   = b->opts.precision == MGPU_PRECISION_MIXED;
+    B.st_hi    = B.st_lo = B.v0_hi = B.v0_lo = B.yn_hi = B.yn_lo = nullptr;
+    B.state    = nullptr;
+    B.v0       = nullptr;
+    B.ynew     = nullptr;
+    if (b->pairs) {
+        // the mixed solver keeps node states as float-float pairs on the device
+        std::vector<float> hi(st), lo(st);
+        split_pairs(h_state.data(), st, hi.data(), lo.data());
+        B.st_hi       = b->pool.upload(hi);
+        B.st_lo       = b->pool.upload(lo);
+        b->init_hi    = b->pool.upload(hi);
+        b->init_lo    = b->pool.upload(lo);
+        B.v0_hi       = b->pool.alloc<float>(st);
+        B.v0_lo       = b->pool.alloc<float>(st);
+        B.yn_hi       = b->pool.alloc<float>(st);
+        B.yn_lo       = b->pool.alloc<float>(st);
+    }
+    else {
+        B.state       = b->pool.upload(h_state);
+        b->init_state = b->pool.upload(h_state);
+        B.v0          = b->pool.alloc<double>(st);
+        B.ynew        = b->pool.alloc<double>(std::max<int64_t>(st, scratch_slots * b->n_max));
+    }
+    B.ypre = b->opts.precision == MGPU_PRECISION_FP64_PLAIN ? b->pool.alloc<double>(st) : nullptr;
     std::vector<double> h_t(nodes, t0), h_dt(nodes, dt0);
     B.node_t          = b->pool.upload(h_t);
     B.node_dt         = b->pool.upload(h_dt);
@@ -763,6 +802,7 @@ int mgpu_eval_rhs(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, con
         mgpu_batch b;
         b.ctx = ctx;
         mgpu_default_solver_opts(&b.opts);
+        b.opts.precision = MGPU_PRECISION_FP64_PLAIN; // FP64 states, one thread per node
         build_batch(&b, &g, 1, 0.0, 0.1, false, 0);
         const int n = g.num_groups * kC;
         DevPool io;
@@ -818,6 +858,7 @@ int mgpu_simulate(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, con
         mgpu_batch b;
         b.ctx = ctx;
         mgpu_default_solver_opts(&b.opts);
+        b.opts.precision = MGPU_PRECISION_FP64_PLAIN; // FP64 states, one thread per node
         b.opts.integrator = *opts;
         build_batch(&b, &g, 1, t0, dt0, false, count);
         const int n = g.num_groups * kC;
@@ -1077,7 +1118,8 @@ int mgpu_batch_reset(mgpu_batch* b, double t0)
         const int64_t n = std::max<int64_t>(
             std::max<int64_t>(b->state_total, b->dev.num_nodes),
             std::max<int64_t>(b->dev.num_edges, (int64_t)b->num_graphs));
-        k_reset<<<(unsigned)((n + 255) / 256), 256, 0, b->ctx->stream>>>(b->dev, b->init_state, b->state_total, t0,
+        k_reset<<<(unsigned)((n + 255) / 256), 256, 0, b->ctx->stream>>>(b->dev, b->init_state, b->init_hi,
+                                                                          b->init_lo, b->state_total, t0,
                                                                           b->dt0);
         ++b->launches;
         ck(cudaGetLastError(), "k_reset");
@@ -1098,6 +1140,21 @@ int mgpu_batch_get_state(mgpu_batch* b, double* out)
             fail(MGPU_INVALID_VALUE, "null output");
         }
         ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        if (b->pairs) {
+            // float-float pairs, combined in FP64 on the host
+            std::vector<float> hi(b->state_total), lo(b->state_total);
+            ck(cudaMemcpyAsync(hi.data(), b->dev.st_hi, sizeof(float) * b->state_total, cudaMemcpyDeviceToHost,
+                               b->ctx->stream),
+               "d2h state");
+            ck(cudaMemcpyAsync(lo.data(), b->dev.st_lo, sizeof(float) * b->state_total, cudaMemcpyDeviceToHost,
+                               b->ctx->stream),
+               "d2h state");
+            ck(cudaStreamSynchronize(b->ctx->stream), "sync");
+            for (int64_t i = 0; i < b->state_total; ++i) {
+                out[i] = (double)hi[i] + (double)lo[i];
+            }
+            return MGPU_OK;
+        }
         ck(cudaMemcpyAsync(out, b->dev.state, sizeof(double) * b->state_total, cudaMemcpyDeviceToHost,
                            b->ctx->stream),
            "d2h state");
@@ -1116,6 +1173,18 @@ int mgpu_batch_set_state(mgpu_batch* b, const double* state)
             fail(MGPU_INVALID_VALUE, "null input");
         }
         ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        if (b->pairs) {
+            std::vector<float> hi(b->state_total), lo(b->state_total);
+            split_pairs(state, b->state_total, hi.data(), lo.data());
+            ck(cudaMemcpyAsync(b->dev.st_hi, hi.data(), sizeof(float) * b->state_total, cudaMemcpyHostToDevice,
+                               b->ctx->stream),
+               "h2d state");
+            ck(cudaMemcpyAsync(b->dev.st_lo, lo.data(), sizeof(float) * b->state_total, cudaMemcpyHostToDevice,
+                               b->ctx->stream),
+               "h2d state");
+            ck(cudaStreamSynchronize(b->ctx->stream), "sync");
+            return MGPU_OK;
+        }
         ck(cudaMemcpyAsync(b->dev.state, state, sizeof(double) * b->state_total, cudaMemcpyHostToDevice,
                            b->ctx->stream),
            "h2d state");

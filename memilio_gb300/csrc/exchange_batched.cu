@@ -123,6 +123,18 @@ struct Acc<float> {
     {
         return (double)hi + (double)lo;
     }
+    __device__ void init_pair(float h, float l)
+    {
+        hi = h;
+        lo = l;
+    }
+    // renormalised pair (|lo| <= ulp(hi)/2)
+    __device__ void store(float* h, float* l) const
+    {
+        const float s = __fadd_rn(hi, lo);
+        *l            = __fsub_rn(lo, __fsub_rn(s, hi));
+        *h            = s;
+    }
 };
 
 // Coefficient of edge e (local le) for compartment j at time t, in R.
@@ -295,8 +307,12 @@ __global__ void k_xb_prep(BatchDev B, int64_t n0, int64_t nn)
     const NodeModel nm = node_model(B, g, lv);
     const int64_t so   = g.state_off + lv * g.n;
     if (xb_returning(rt)) {
-        const CVec pop{B.v0 + so, 1};
-        const int G = g.G;
+        double popv[MGPU_MAX_GROUPS * kC];
+        for (int j = 0; j < g.n; ++j) {
+            popv[j] = v0_get(B, so + j);
+        }
+        const double* pop = popv;
+        const int G       = g.G;
         double C[MGPU_MAX_GROUPS * MGPU_MAX_GROUPS];
         contact_matrix_at(nm, rt.t_dep, C);
         double icu = 0.0, tnt = 0.0;
@@ -354,16 +370,26 @@ __global__ void k_xb_prep(BatchDev B, int64_t n0, int64_t nn)
     }
     if (xb_departing(rt)) {
         const int ws = rt.snap_slot ^ 1;
-        double* yd   = B.ysnap + (int64_t)ws * B.state_total + so;
         float* yf    = B.ysnap_f + (int64_t)ws * B.state_total + so;
-        for (int j = 0; j < g.n; ++j) {
-            const double v = B.state[so + j];
-            yd[j]          = v;
-            yf[j]          = (float)v;
+        double ys[MGPU_MAX_GROUPS * kC];
+        if (B.st_hi) {
+            for (int j = 0; j < g.n; ++j) {
+                yf[j] = B.st_hi[so + j]; // the FP32 rounding of hi + lo
+                ys[j] = (double)B.st_hi[so + j] + (double)B.st_lo[so + j];
+            }
+        }
+        else {
+            double* yd = B.ysnap + (int64_t)ws * B.state_total + so;
+            for (int j = 0; j < g.n; ++j) {
+                const double v = B.state[so + j];
+                yd[j]          = v;
+                yf[j]          = (float)v;
+                ys[j]          = v;
+            }
         }
         // per age group: ISy mobility factor and commuter nondetection at this departure
         R* fac = reinterpret_cast<R*>(B.risk) + ((int64_t)ws * B.num_nodes + node) * MGPU_MAX_GROUPS * 2;
-        const CVec y{B.state + so, 1};
+        const CVec y{ys, 1};
         const double t    = rt.t_next;
         const double nd   = (t >= nm.scalar(MGPU_P_START_COMMUTER_DETECTION) &&
                            t < nm.scalar(MGPU_P_END_COMMUTER_DETECTION))
@@ -419,11 +445,11 @@ __global__ void k_xb_depart(BatchDev B, int64_t n0, int64_t nn)
     const int ws     = rt.snap_slot ^ 1;
     const double t   = rt.t_next;
     const int64_t lv = node - g.node0;
-    double* yv       = B.state + g.state_off + lv * g.n + gr * kC;
+    const int64_t so = g.state_off + lv * g.n + gr * kC;
     Acc<R> acc[kC];
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
-        acc[c].init(yv[c]);
+        acc[c].init(state_get(B, so + c));
     }
     R m[kC];
     const int64_t ib = B.in_ptr[node], ie = B.in_ptr[node + 1];
@@ -473,12 +499,16 @@ __global__ void k_xb_depart(BatchDev B, int64_t n0, int64_t nn)
             }
         }
     }
-    double* v0 = B.v0 + g.state_off + lv * g.n + gr * kC;
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
         const double v = acc[c].get();
-        yv[c]          = v;
-        v0[c]          = v;
+        state_set(B, so + c, v);
+        if (B.v0_hi) {
+            pair_set(B.v0_hi, B.v0_lo, so + c, v);
+        }
+        else {
+            B.v0[so + c] = v;
+        }
     }
 }
 
@@ -503,14 +533,15 @@ __global__ void k_xb_return(BatchDev B, int64_t n0, int64_t nn)
         return; // k_xf_return
     }
     const int64_t lv = node - g.node0;
-    const double* yv = B.state + g.state_off + lv * g.n + gr * kC;
+    const int64_t so = g.state_off + lv * g.n + gr * kC;
     Acc<R> acc[kC];
     R bound[kC], mag[kC];
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
-        acc[c].init(yv[c]);
-        bound[c] = (R)yv[c];
-        mag[c]   = (R)fabs(yv[c]);
+        const double y = state_get(B, so + c);
+        acc[c].init(y);
+        bound[c] = (R)y;
+        mag[c]   = (R)fabs(y);
     }
     // sign -1: travelers leave this node (in-edge), +1: they come home (out-edge)
     auto edge = [&](int64_t e, int sign) {
@@ -571,14 +602,13 @@ __global__ void k_xb_return(BatchDev B, int64_t n0, int64_t nn)
             edge(e, -1);
         }
     }
-    double* yn = B.ynew + g.state_off + lv * g.n + gr * kC;
     // margin: the bound's own rounding (FP64: 1e-12, float: 4e-6 relative to the summed magnitudes)
     const R margin = std::is_same<R, float>::value ? (R)4e-6 : (R)1e-12;
     bool flag      = false;
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
-        yn[c] = acc[c].get();
-        flag  = flag || (bound[c] < margin * mag[c]);
+        ynew_set(B, so + c, acc[c].get());
+        flag = flag || (bound[c] < margin * mag[c]);
     }
     if (flag) {
         B.node_flag[node] = 1;
@@ -652,11 +682,11 @@ __global__ void k_xf_depart(BatchDev B, int64_t n0, int64_t nn)
     }
     const int ws     = rt.snap_slot ^ 1;
     const int64_t lv = node - g.node0;
-    double* yv       = B.state + g.state_off + lv * g.n + gr * kC;
+    const int64_t so = g.state_off + lv * g.n + gr * kC;
     Acc<float> acc[kC];
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
-        acc[c].init(yv[c]);
+        acc[c].init_pair(B.st_hi[so + c], B.st_lo[so + c]);
     }
     GroupSnap own, src;
     load_group_snap(B, g, node, gr, ws, own);
@@ -712,12 +742,11 @@ __global__ void k_xf_depart(BatchDev B, int64_t n0, int64_t nn)
             }
         }
     }
-    double* v0 = B.v0 + g.state_off + lv * g.n + gr * kC;
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
-        const double v = acc[c].get();
-        yv[c]          = v;
-        v0[c]          = v;
+        acc[c].store(B.st_hi + so + c, B.st_lo + so + c);
+        B.v0_hi[so + c] = B.st_hi[so + c];
+        B.v0_lo[so + c] = B.st_lo[so + c];
     }
 }
 
@@ -738,12 +767,12 @@ __global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
     const int slot   = rt.snap_slot;
     const float dt   = (float)rt.dt;
     const int64_t lv = node - g.node0;
-    const double* yv = B.state + g.state_off + lv * g.n + gr * kC;
+    const int64_t s0 = g.state_off + lv * g.n + gr * kC;
     Acc<float> acc[kC];
     float yf[kC], min_in[kC], phi_in[kF], phi_out[kF];
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
-        acc[c].init(yv[c]);
+        acc[c].init_pair(B.st_hi[s0 + c], B.st_lo[s0 + c]);
         yf[c]     = acc[c].hi;
         min_in[c] = 0.0f;
     }
@@ -833,10 +862,10 @@ __global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
     // conservative no-underflow bound: with nonnegative travelers and increments,
     // every partial state of the serial order is at least y - in - out
     bool flag = lowest < 0.0f;
-    double* yn = B.ynew + g.state_off + lv * g.n + gr * kC;
+    const int64_t so = g.state_off + lv * g.n + gr * kC;
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
-        yn[c]             = acc[c].get();
+        acc[c].store(B.yn_hi + so + c, B.yn_lo + so + c);
         const float bound = yf[c] - in_c[c] - out_c[c];
         const float mag   = fabsf(yf[c]) + in_c[c] + out_c[c];
         flag              = flag || (bound < 1e-5f * mag);
@@ -879,11 +908,11 @@ __global__ void k_xb_scan(BatchDev B, int64_t n0, int64_t nn, int pass)
     double* rem = sm_r[(threadIdx.x >> 5) & 3];
     const int n = g.n;
     double y[3];
-    const double* ys = B.state + g.state_off + (node - g.node0) * n;
+    const int64_t s0 = g.state_off + (node - g.node0) * n;
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
         const int j = lane + 32 * q;
-        y[q]        = j < n ? ys[j] : 0.0;
+        y[q]        = j < n ? state_get(B, s0 + j) : 0.0;
     }
     // lanes 0..G-1 compute one age group's travelers each into shared memory
     auto travelers = [&](int64_t e) {
@@ -1010,12 +1039,11 @@ __global__ void k_xb_scan(BatchDev B, int64_t n0, int64_t nn, int pass)
             in_edge(e);
         }
     }
-    double* yn = B.ynew + g.state_off + (node - g.node0) * n;
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
         const int j = lane + 32 * q;
         if (j < n) {
-            yn[j] = y[q];
+            ynew_set(B, s0 + j, y[q]);
         }
     }
 }
@@ -1051,13 +1079,13 @@ __global__ void k_xb_sequential(BatchDev B, int g0, int ng)
             }
         }
         __syncwarp();
-        const int64_t u = B.edge_src[e] - g.node0;
-        const int64_t v = B.edge_dst[e] - g.node0;
-        double* yu      = B.state + g.state_off + u * n;
-        double* yv      = B.state + g.state_off + v * n;
-        bool neg        = false;
+        const int64_t u  = B.edge_src[e] - g.node0;
+        const int64_t v  = B.edge_dst[e] - g.node0;
+        const int64_t ou = g.state_off + u * n;
+        const int64_t ov = g.state_off + v * n;
+        bool neg         = false;
         for (int j = lane; j < n; j += 32) {
-            rem[j] = yv[j] - m[j];
+            rem[j] = state_get(B, ov + j) - m[j];
             neg    = neg || (rem[j] < 0);
         }
         neg = __any_sync(0xffffffffu, neg);
@@ -1081,11 +1109,11 @@ __global__ void k_xb_sequential(BatchDev B, int g0, int ng)
         }
         __syncwarp();
         for (int j = lane; j < n; j += 32) {
-            yu[j] += m[j];
+            state_set(B, ou + j, state_get(B, ou + j) + m[j]);
         }
         __syncwarp();
         for (int j = lane; j < n; j += 32) {
-            yv[j] -= m[j];
+            state_set(B, ov + j, state_get(B, ov + j) - m[j]);
         }
         __syncwarp();
     }
@@ -1130,7 +1158,13 @@ __global__ void k_xb_commit(BatchDev B, int64_t n0, int64_t nn, int n_max)
         return;
     }
     const int64_t o = g.state_off + (node - g.node0) * g.n + j;
-    B.state[o]      = B.ynew[o];
+    if (B.st_hi) {
+        B.st_hi[o] = B.yn_hi[o];
+        B.st_lo[o] = B.yn_lo[o];
+    }
+    else {
+        B.state[o] = B.ynew[o];
+    }
 }
 
 __global__ void k_xb_cleanup(BatchDev B, int64_t e0, int64_t ne)

@@ -78,10 +78,12 @@ struct BatchDev {
     const double* contact;
     const double* dtimes;
     const double* dvals;
-    double* state;               // result last values
+    double* state;               // result last values (FP64 solvers)
     double* v0;                  // post-departure snapshot (destination state at t_dep)
     double* ypre;                // pre-exchange snapshot
     double* ynew;                // scratch for the parallel return
+    // mixed solver: the same three arrays as float-float pairs (value = hi + lo)
+    float *st_hi, *st_lo, *v0_hi, *v0_lo, *yn_hi, *yn_lo;
     double* node_t;              // integrator time per node
     double* node_dt;             // integrator step per node
     const int32_t* edge_src;     // global node ids
@@ -130,6 +132,41 @@ enum {
 __host__ __device__ inline int param_stride(int G)
 {
     return MGPU_NUM_SCALAR_PARAMS + MGPU_NUM_GROUP_PARAMS * G;
+}
+
+// Node state access for code shared by both representations (FP64 array, or
+// float-float pairs in the mixed solver).
+__device__ __forceinline__ double state_get(const BatchDev& B, int64_t o)
+{
+    return B.st_hi ? (double)B.st_hi[o] + (double)B.st_lo[o] : B.state[o];
+}
+__device__ __forceinline__ void pair_set(float* hi, float* lo, int64_t o, double v)
+{
+    const float h = (float)v;
+    hi[o]         = h;
+    lo[o]         = (float)(v - (double)h);
+}
+__device__ __forceinline__ void state_set(const BatchDev& B, int64_t o, double v)
+{
+    if (B.st_hi) {
+        pair_set(B.st_hi, B.st_lo, o, v);
+    }
+    else {
+        B.state[o] = v;
+    }
+}
+__device__ __forceinline__ double v0_get(const BatchDev& B, int64_t o)
+{
+    return B.v0_hi ? (double)B.v0_hi[o] + (double)B.v0_lo[o] : B.v0[o];
+}
+__device__ __forceinline__ void ynew_set(const BatchDev& B, int64_t o, double v)
+{
+    if (B.yn_hi) {
+        pair_set(B.yn_hi, B.yn_lo, o, v);
+    }
+    else {
+        B.ynew[o] = v;
+    }
 }
 
 // Source/target compartment of the 15 flows (osecir Flows typelist, models/ode_secir/model.h:45-59).

@@ -721,7 +721,7 @@ __device__ __forceinline__ void segf_rhs(SegF<G>& X, const float (&u)[kC], float
 
 template <int G>
 #ifndef MGPU_MIXED_MIN_BLOCKS
-#define MGPU_MIXED_MIN_BLOCKS 1 // resident 128-thread blocks per SM the register budget must allow
+#define MGPU_MIXED_MIN_BLOCKS 3 // resident 128-thread blocks per SM the register budget must allow
 #endif
 __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchDev B, const int32_t* inst,
                                                                          int64_t count)
@@ -758,13 +758,14 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
             continue;
         }
         const int64_t local = node - g.node0;
-        double* yp          = B.state + g.state_off + local * g.n + X.gi * kC;
+        const int64_t so    = g.state_off + local * g.n + X.gi * kC;
+        float* yhi          = B.st_hi + so;
+        float* ylo          = B.st_lo + so;
         float hi[kC], lo[kC];
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
-            const double v = yp[c];
-            hi[c]          = (float)v;
-            lo[c]          = (float)(v - (double)hi[c]);
+            hi[c] = yhi[c];
+            lo[c] = ylo[c];
         }
         const double t_start = B.node_t[node];
         const double tmax    = rt.t_next;
@@ -913,9 +914,9 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
         dt = fmaxf(dt, dt_restore);
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
-            const double v = (double)hi[c] + (double)lo[c];
-            yp[c]          = v;
-            nonfinite      = nonfinite || !isfinite(v);
+            yhi[c]    = hi[c];
+            ylo[c]    = lo[c];
+            nonfinite = nonfinite || !isfinite(hi[c]);
         }
         if (X.gi == 0) {
             B.node_t[node]  = (tr >= span) ? tmax : t_start + (double)tr;
