@@ -227,6 +227,7 @@ def main():
     barrier()
     st1 = batch.stats()
     launches = (st1["kernel_launches"] - st0["kernel_launches"])
+    exchange_stats = {k: (st1[k] - st0[k]) // args.steps for k in ("underflow_fixes", "sequential_exchanges")}
     ms_step = float(np.sum(dev_ms)) / args.steps
     ms_max = ms_step
     if world > 1:
@@ -298,6 +299,7 @@ def main():
             "data": "synthetic (seeded)", "config": workload_config(args), "clocks": clocks,
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
             "attempts_per_node_day": attempts_step / nd_step, "wall_s_timed": t_wall,
+            "exchange_per_step": exchange_stats,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -366,6 +366,13 @@ __global__ void k_xb_prep(BatchDev B, int64_t n0, int64_t nn)
             ai[8]                  = (R)((dps + death_adj) / tisev);
             ai[9]                  = (R)(dpc / ticri);
             ai[10]                 = (R)((1.0 - dpc) / ticri);
+            // can one Euler step of length dt drive a returning compartment negative?
+            // (it cannot when dt times every compartment's total outflow rate is <= 1)
+            const double out_rate = fmax(fmax(lam, 1.0 / nm.gp(MGPU_G_TIME_EXPOSED, i)),
+                                         fmax(fmax((double)ai[2] + (double)ai[3], (double)ai[4] + (double)ai[5]),
+                                              fmax((double)ai[6] + (double)ai[7] + (double)ai[8],
+                                                   (double)ai[9] + (double)ai[10])));
+            ai[11] = (R)((rt.dt * out_rate > 1.0) ? 1 : 0);
         }
     }
     if (xb_departing(rt)) {
@@ -790,21 +797,29 @@ __global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
     GroupSnap own, src;
     load_group_snap(B, g, node, gr, slot, own);
     float m[kC], phi[kF];
-    float lowest = 0.0f; // a negative traveler or increment voids the bound
+    float lowest = 0.0f; // a negative traveler voids the bound
+    bool unsafe  = false; // a destination whose Euler step may drive travelers negative
     auto in_edge = [&](int64_t e, int64_t u) {
         load_group_snap(B, g, u, gr, slot, src);
         travelers_f(B, g, e, gr, src, m);
         flows_f(a_own, dt, m, phi);
+        // returning amounts t_c = m_c + inflows - outflows (for the bound only)
+        float t[kC];
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
             acc[c].add(-m[c]);
-            min_in[c] += m[c];
+            t[c]   = m[c];
             lowest = fminf(lowest, m[c]);
         }
 #pragma unroll
         for (int f = 0; f < kF; ++f) {
             phi_in[f] += phi[f];
-            lowest = fminf(lowest, phi[f]);
+            t[kFlowSrcI(f)] -= phi[f];
+            t[kFlowDstI(f)] += phi[f];
+        }
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            min_in[c] += fmaxf(t[c], 0.0f);
         }
     };
     const int64_t ib = B.in_ptr[node], ie = B.in_ptr[node + 1];
@@ -823,8 +838,10 @@ __global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
         if (!B.edge_static_any[e]) {
             continue;
         }
+        const float* ax = aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux;
         travelers_f(B, g, e, gr, own, m);
-        flows_f(aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux, dt, m, phi);
+        flows_f(ax, dt, m, phi);
+        unsafe = unsafe || ax[11] != 0.0f;
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
             acc[c].add(m[c]);
@@ -833,7 +850,6 @@ __global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
 #pragma unroll
         for (int f = 0; f < kF; ++f) {
             phi_out[f] += phi[f];
-            lowest = fminf(lowest, phi[f]);
         }
     }
     for (; k < ie; ++k) {
@@ -844,30 +860,23 @@ __global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
     }
     // flow increments: in-edges take travelers away (their increments count
     // with the opposite sign), out-edges bring them home
-    float in_c[kC], out_c[kC];
-#pragma unroll
-    for (int c = 0; c < kC; ++c) {
-        in_c[c]  = min_in[c];
-        out_c[c] = 0.0f;
-    }
 #pragma unroll
     for (int f = 0; f < kF; ++f) {
         acc[kFlowSrcI(f)].add(phi_in[f]);
         acc[kFlowDstI(f)].add(-phi_in[f]);
         acc[kFlowSrcI(f)].add(-phi_out[f]);
         acc[kFlowDstI(f)].add(phi_out[f]);
-        in_c[kFlowDstI(f)] += phi_in[f];
-        out_c[kFlowSrcI(f)] += phi_out[f];
     }
-    // conservative no-underflow bound: with nonnegative travelers and increments,
-    // every partial state of the serial order is at least y - in - out
-    bool flag = lowest < 0.0f;
+    // conservative no-underflow bound: with nonnegative travelers whose Euler
+    // step stays nonnegative, every partial state of the serial order is at
+    // least y minus the positive parts of all returning in-edge amounts
+    bool flag = lowest < 0.0f || unsafe;
     const int64_t so = g.state_off + lv * g.n + gr * kC;
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
         acc[c].store(B.yn_hi + so + c, B.yn_lo + so + c);
-        const float bound = yf[c] - in_c[c] - out_c[c];
-        const float mag   = fabsf(yf[c]) + in_c[c] + out_c[c];
+        const float bound = yf[c] - min_in[c];
+        const float mag   = fabsf(yf[c]) + min_in[c];
         flag              = flag || (bound < 1e-5f * mag);
     }
     if (flag) {
