@@ -227,7 +227,7 @@ def main():
     barrier()
     st1 = batch.stats()
     launches = (st1["kernel_launches"] - st0["kernel_launches"])
-    exchange_stats = {k: (st1[k] - st0[k]) // args.steps for k in ("underflow_fixes", "sequential_exchanges")}
+    exchange_stats = {k: (st1[k] - st0[k]) // args.steps for k in ("underflow_fixes", "sequential_exchanges", "scan_items")}
     ms_step = float(np.sum(dev_ms)) / args.steps
     ms_max = ms_step
     if world > 1:

@@ -76,6 +76,8 @@ typedef struct mgpu_stats {
     int64_t sequential_exchanges; /* graph exchanges that took the exact sequential path */
     int64_t phases;           /* exchange intervals simulated */
     int64_t kernel_launches;  /* kernels launched by this batch */
+    int64_t scan_items;       /* (node, age group) items the exact underflow scan of the
+                                 batched exchange visited */
 } mgpu_stats;
 
 /* Default solver options: Cash-Karp 5(4) with the default core's tolerances

@@ -67,6 +67,7 @@ class MgpuStats(ctypes.Structure):
         ("sequential_exchanges", ctypes.c_int64),
         ("phases", ctypes.c_int64),
         ("kernel_launches", ctypes.c_int64),
+        ("scan_items", ctypes.c_int64),
     ]
 
     def as_dict(self):

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <exception>
 #include <map>
@@ -361,6 +362,9 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         b->n_max        = std::max<int64_t>(b->n_max, n);
     }
     b->state_total = st;
+    if (nodes * MGPU_MAX_GROUPS > INT32_MAX) {
+        fail(MGPU_INVALID_VALUE, "batch too large: more than 2^28 nodes in one batch");
+    }
     // host staging
     std::vector<double> h_par(par), h_con(con), h_dtt(dtt), h_dtv(dtv), h_state(st), h_ec(ec), h_edt(edt),
         h_edv(edv);
@@ -577,6 +581,14 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         b->any_edge_dampings = b->any_edge_dampings || (dg[i].Ke > 0 && dg[i].E > 0);
     }
     B.edge_fixed = b->pool.alloc<int32_t>(edges);
+    B.scan_mark  = b->pool.alloc<int32_t>(3 * nodes * MGPU_MAX_GROUPS);
+    B.scan_list  = b->pool.alloc<int32_t>(3 * nodes * MGPU_MAX_GROUPS);
+    B.scan_count = b->pool.alloc<int32_t>(3);
+    B.fix_cnt    = b->pool.alloc<uint8_t>(edges * MGPU_MAX_GROUPS);
+    ck(cudaMemsetAsync(B.scan_mark, 0, sizeof(int32_t) * std::max<int64_t>(3 * nodes * MGPU_MAX_GROUPS, 1), ctx->stream),
+       "memset");
+    ck(cudaMemsetAsync(B.scan_count, 0, sizeof(int32_t) * 3, ctx->stream), "memset");
+    ck(cudaMemsetAsync(B.fix_cnt, 0, std::max<int64_t>(edges * MGPU_MAX_GROUPS, 1), ctx->stream), "memset");
     B.node_flag  = b->pool.alloc<uint8_t>(nodes);
     B.node_dirty = b->pool.alloc<uint8_t>(2 * nodes);
     ck(cudaMemsetAsync(B.edge_fixed, 0, sizeof(int32_t) * std::max<int64_t>(edges, 1), ctx->stream), "memset");
@@ -1036,7 +1048,7 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
                 ode_launches += (int64_t)b->inst_by_G.size();
             }
             b->launches +=
-                P * (2 + (int64_t)b->inst_by_G.size() + exchange_batched_launches(B.num_edges > 0, b->any_edge_dampings));
+                P * (2 + (int64_t)b->inst_by_G.size() + exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings));
             b->phases += P;
         }
         else {
@@ -1057,7 +1069,7 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
                 }
             }
             const int64_t per_phase = 2 + (int64_t)b->inst_by_G.size() +
-                                      exchange_batched_launches(B.num_edges > 0, b->any_edge_dampings);
+                                      exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings);
             for (int64_t p = 0; p < P; ++p) {
                 if (b->graph_exec) {
                     ck(cudaGraphLaunch(b->graph_exec, s), "cudaGraphLaunch");
@@ -1224,6 +1236,7 @@ int mgpu_batch_get_stats(mgpu_batch* b, mgpu_stats* out)
         out->failed_steps         = (int64_t)c[CNT_FAILED];
         out->underflow_fixes      = (int64_t)c[CNT_UNDERFLOW];
         out->sequential_exchanges = (int64_t)c[CNT_SEQUENTIAL];
+        out->scan_items           = (int64_t)c[CNT_SCANNED];
         out->phases               = b->phases;
         out->kernel_launches      = b->launches;
         return MGPU_OK;

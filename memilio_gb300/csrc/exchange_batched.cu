@@ -25,7 +25,7 @@
 //
 // Underflow fixes: a conservative per-node bound flags the nodes whose serial
 // return order might meet a negative remainder; those run the exact
-// per-node scan of exchange.cu semantics in FP64 (k_xb_scan), then the
+// (node, age group) scan of exchange.cu semantics in FP64 (k_xg_scan), then the
 // per-graph sequential pass handles what the scan passes leave unresolved.
 #include "mgpu_internal.cuh"
 
@@ -51,6 +51,39 @@ __device__ __forceinline__ bool xb_returning(const GraphRt& rt)
 __device__ __forceinline__ bool edge_departed(const BatchDev& B, const DevGraph& g, int64_t e)
 {
     return g.Ke == 0 ? B.edge_static_any[e] != 0 : B.edge_pending[e] != 0;
+}
+
+// append a (node, age group) item, node * MAX_GROUPS + group, to exact-scan
+// work list `list` once
+__device__ __forceinline__ void list_push(const BatchDev& B, int list, int64_t item)
+{
+    const int64_t NG = B.num_nodes * MGPU_MAX_GROUPS;
+    if (atomicExch(&B.scan_mark[list * NG + item], 1) == 0) {
+        const int idx               = atomicAdd(&B.scan_count[list], 1);
+        B.scan_list[list * NG + idx] = (int32_t)item;
+    }
+}
+
+// Append item to list 0 when `want`: every (node, group) thread of a return
+// pass appends only its own item, so no mark is needed, and the converged
+// threads of a warp reserve their slots with one atomic.
+__device__ __forceinline__ void list0_push(const BatchDev& B, int64_t item, bool want)
+{
+    const unsigned active = __activemask();
+    const unsigned m      = __ballot_sync(active, want);
+    if (m == 0) {
+        return;
+    }
+    const int lane   = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    int base         = 0;
+    if (lane == leader) {
+        base = atomicAdd(&B.scan_count[0], __popc(m));
+    }
+    base = __shfl_sync(active, base, leader);
+    if (want) {
+        B.scan_list[base + __popc(m & ((1u << lane) - 1u))] = (int32_t)item;
+    }
 }
 
 template <class R>
@@ -288,61 +321,114 @@ __device__ __forceinline__ void return_travelers_ref(const BatchDev& B, const De
     }
 }
 
-// Per node: departure snapshot and ISy factor; return-time force of infection and rates.
+// Row i of the contact matrix at time t (contact_matrix_at, one row), padded
+// to MAX_GROUPS entries.
+__device__ __forceinline__ void contact_row(const NodeModel& nm, int i, double t, double (&Crow)[MGPU_MAX_GROUPS])
+{
+    const int G = nm.G;
+#pragma unroll
+    for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
+        Crow[q] = 0.0;
+    }
+    const long GG = (long)G * G;
+    for (int m = 0; m < nm.M; ++m) {
+        const double* Bm = nm.cm + m * 2 * GG + (long)i * G;
+        const double* Lm = Bm + GG;
+        if (nm.K) {
+            const double* T  = nm.dtimes + m * nm.K;
+            const int ub     = damping_upper_bound(T, nm.K, t);
+            const Ramp r     = ramp_at(t, T[ub] - 1.0, T[ub]);
+            const double* Dl = nm.dvals + ((long)m * nm.K + ub - 1) * GG + (long)i * G;
+            const double* Dr = Dl + GG;
+#pragma unroll
+            for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
+                if (q < G) {
+                    const double D = ramp_apply(r, Dl[q], Dr[q]);
+                    Crow[q]        = Crow[q] + (Bm[q] - D * (Bm[q] - Lm[q]));
+                }
+            }
+        }
+        else {
+#pragma unroll
+            for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
+                if (q < G) {
+                    Crow[q] = Crow[q] + (Bm[q] - 0.0 * (Bm[q] - Lm[q]));
+                }
+            }
+        }
+    }
+}
+
+// Per node, one 8-lane segment with a lane per age group: the departure snapshot
+// and mobility factors; the force of infection and flow rates at the departure
+// time for the return's Euler step. Sums over age groups run in group order
+// (shuffles from lanes 0..G-1), as in the serial right-hand side.
 template <class R>
 __global__ void k_xb_prep(BatchDev B, int64_t n0, int64_t nn)
 {
-    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= nn) {
-        return;
-    }
-    const int64_t node = n0 + tid;
-    const int gi       = B.node_graph[node];
-    const DevGraph& g  = B.graphs[gi];
-    const GraphRt& rt  = B.rt[gi];
-    if (!rt.active) {
-        return;
-    }
-    const int64_t lv   = node - g.node0;
-    const NodeModel nm = node_model(B, g, lv);
-    const int64_t so   = g.state_off + lv * g.n;
-    if (xb_returning(rt)) {
-        double popv[MGPU_MAX_GROUPS * kC];
-        for (int j = 0; j < g.n; ++j) {
-            popv[j] = v0_get(B, so + j);
+    constexpr unsigned kFull = 0xffffffffu;
+    const int64_t tid        = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t seg        = tid / MGPU_MAX_GROUPS;
+    const bool in_range      = seg < nn;
+    const int64_t node       = n0 + (in_range ? seg : nn - 1); // every lane takes part in the shuffles
+    const int lane           = (int)(threadIdx.x % MGPU_MAX_GROUPS);
+    const int gi             = B.node_graph[node];
+    const DevGraph& g        = B.graphs[gi];
+    const GraphRt& rt        = B.rt[gi];
+    const int G              = g.G;
+    const bool mine          = in_range && lane < G;
+    const int i              = lane < G ? lane : 0; // the lane's age group (clamped for idle lanes)
+    const int64_t lv         = node - g.node0;
+    const NodeModel nm       = node_model(B, g, lv);
+    const int64_t so         = g.state_off + lv * g.n + (int64_t)i * kC;
+    const bool ret           = in_range && xb_returning(rt);
+    const bool dep           = in_range && xb_departing(rt);
+    const double tnt_w       = (1 - nm.gp(MGPU_G_RECOVERED_PER_INS, i)) / nm.gp(MGPU_G_TIME_INS, i);
+    const double cap         = nm.scalar(MGPU_P_TNT_CAPACITY);
+    if (__any_sync(kFull, ret)) {
+        double pop[kC];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            pop[c] = v0_get(B, so + c);
         }
-        const double* pop = popv;
-        const int G       = g.G;
-        double C[MGPU_MAX_GROUPS * MGPU_MAX_GROUPS];
-        contact_matrix_at(nm, rt.t_dep, C);
-        double icu = 0.0, tnt = 0.0;
-        for (int i = 0; i < G; ++i) {
-            tnt += (1 - nm.gp(MGPU_G_RECOVERED_PER_INS, i)) / nm.gp(MGPU_G_TIME_INS, i) * pop[i * kC + MGPU_INS];
-            icu += pop[i * kC + MGPU_ICRI];
+        const double tnt_c = tnt_w * pop[MGPU_INS];
+        double tnt = 0.0, icu = 0.0;
+#pragma unroll
+        for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
+            const double a = __shfl_sync(kFull, tnt_c, q, MGPU_MAX_GROUPS);
+            const double b = __shfl_sync(kFull, pop[MGPU_ICRI], q, MGPU_MAX_GROUPS);
+            if (q < G) {
+                tnt += a;
+                icu += b;
+            }
         }
-        const double cap    = nm.scalar(MGPU_P_TNT_CAPACITY);
         const Ramp rrisk    = ramp_at(tnt, cap, cap * nm.scalar(MGPU_P_TNT_MAX_RISK));
         const double season = (1 + nm.scalar(MGPU_P_SEASONALITY) *
                                        sin(kPi * ((nm.scalar(MGPU_P_START_DAY) + rt.t_dep) / 182.5 + 0.5)));
         const double icu_cap = nm.scalar(MGPU_P_ICU_CAPACITY);
         const Ramp ricu      = ramp_at(icu, 0.90 * icu_cap, icu_cap);
-        double divN[MGPU_MAX_GROUPS], press[MGPU_MAX_GROUPS];
-        for (int j = 0; j < G; ++j) {
-            const int o = j * kC;
-            const double Nj = pop[o + MGPU_S] + pop[o + MGPU_E] + pop[o + MGPU_INS] + pop[o + MGPU_ISY] +
-                              pop[o + MGPU_ISEV] + pop[o + MGPU_ICRI] + pop[o + MGPU_R];
-            divN[j]           = (Nj < kZeroTol) ? 0.0 : 1.0 / Nj;
-            const double risk = ramp_apply(rrisk, nm.gp(MGPU_G_RISK_FROM_SYMPTOMATIC, j),
-                                           nm.gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, j));
-            press[j] = nm.gp(MGPU_G_REL_TRANSMISSION_NS, j) * pop[o + MGPU_INS] + risk * pop[o + MGPU_ISY];
-        }
-        R* a = aux_ptr<R>(B) + node * MGPU_MAX_GROUPS * kAux;
-        for (int i = 0; i < G; ++i) {
-            const double beta = nm.gp(MGPU_G_TRANSMISSION_PROB, i);
-            double lam        = 0.0;
-            for (int j = 0; j < G; ++j) {
-                lam += (season * C[i * G + j]) * divN[j] * beta * press[j];
+        // this lane as source group: 1/N and the infectious pressure
+        const double Nj = pop[MGPU_S] + pop[MGPU_E] + pop[MGPU_INS] + pop[MGPU_ISY] + pop[MGPU_ISEV] +
+                          pop[MGPU_ICRI] + pop[MGPU_R];
+        const double divN  = (Nj < kZeroTol) ? 0.0 : 1.0 / Nj;
+        const double risk  = ramp_apply(rrisk, nm.gp(MGPU_G_RISK_FROM_SYMPTOMATIC, i),
+                                        nm.gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, i));
+        const double press = nm.gp(MGPU_G_REL_TRANSMISSION_NS, i) * pop[MGPU_INS] + risk * pop[MGPU_ISY];
+        // this lane as target group: its row of the contact matrix at t_dep
+        // (contact_matrix_at, one row)
+        double Crow[MGPU_MAX_GROUPS];
+        contact_row(nm, i, rt.t_dep, Crow);
+        const double beta = nm.gp(MGPU_G_TRANSMISSION_PROB, i);
+        double lam        = 0.0;
+#pragma unroll
+        for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
+            const double dn = __shfl_sync(kFull, divN, q, MGPU_MAX_GROUPS);
+            const double pr = __shfl_sync(kFull, press, q, MGPU_MAX_GROUPS);
+            if (q < G) {
+                lam += (season * Crow[q]) * dn * beta * pr;
             }
+        }
+        if (ret && mine) {
             const double cps       = nm.gp(MGPU_G_CRITICAL_PER_SEVERE, i);
             const double crit_adj  = ramp_apply(ricu, cps, 0.0);
             const double death_adj = cps - crit_adj;
@@ -354,57 +440,248 @@ __global__ void k_xb_prep(BatchDev B, int64_t n0, int64_t nn)
             const double dps       = nm.gp(MGPU_G_DEATHS_PER_SEVERE, i);
             const double dpc       = nm.gp(MGPU_G_DEATHS_PER_CRITICAL, i);
             const double ticri     = nm.gp(MGPU_G_TIME_ICRI, i);
-            R* ai                  = a + i * kAux;
-            ai[0]                  = (R)lam;
-            ai[1]                  = (R)(1.0 / nm.gp(MGPU_G_TIME_EXPOSED, i));
-            ai[2]                  = (R)((1 - mu) * (1 / tins));
-            ai[3]                  = (R)(mu * (1.0 / tins));
-            ai[4]                  = (R)(sev / tisy);
-            ai[5]                  = (R)((1 - sev) / tisy);
-            ai[6]                  = (R)(crit_adj / tisev);
-            ai[7]                  = (R)((1.0 - cps - dps) / tisev);
-            ai[8]                  = (R)((dps + death_adj) / tisev);
-            ai[9]                  = (R)(dpc / ticri);
-            ai[10]                 = (R)((1.0 - dpc) / ticri);
+            R v[kAux];
+            v[0]  = (R)lam;
+            v[1]  = (R)(1.0 / nm.gp(MGPU_G_TIME_EXPOSED, i));
+            v[2]  = (R)((1 - mu) * (1 / tins));
+            v[3]  = (R)(mu * (1.0 / tins));
+            v[4]  = (R)(sev / tisy);
+            v[5]  = (R)((1 - sev) / tisy);
+            v[6]  = (R)(crit_adj / tisev);
+            v[7]  = (R)((1.0 - cps - dps) / tisev);
+            v[8]  = (R)((dps + death_adj) / tisev);
+            v[9]  = (R)(dpc / ticri);
+            v[10] = (R)((1.0 - dpc) / ticri);
             // can one Euler step of length dt drive a returning compartment negative?
             // (it cannot when dt times every compartment's total outflow rate is <= 1)
             const double out_rate = fmax(fmax(lam, 1.0 / nm.gp(MGPU_G_TIME_EXPOSED, i)),
-                                         fmax(fmax((double)ai[2] + (double)ai[3], (double)ai[4] + (double)ai[5]),
-                                              fmax((double)ai[6] + (double)ai[7] + (double)ai[8],
-                                                   (double)ai[9] + (double)ai[10])));
-            ai[11] = (R)((rt.dt * out_rate > 1.0) ? 1 : 0);
+                                         fmax(fmax((double)v[2] + (double)v[3], (double)v[4] + (double)v[5]),
+                                              fmax((double)v[6] + (double)v[7] + (double)v[8],
+                                                   (double)v[9] + (double)v[10])));
+            v[11] = (R)((rt.dt * out_rate > 1.0) ? 1 : 0);
+            R* ai = aux_ptr<R>(B) + (node * MGPU_MAX_GROUPS + i) * kAux;
+#pragma unroll
+            for (int q = 0; q < kAux; ++q) {
+                ai[q] = v[q];
+            }
         }
     }
-    if (xb_departing(rt)) {
+    if (__any_sync(kFull, dep)) {
         const int ws = rt.snap_slot ^ 1;
-        float* yf    = B.ysnap_f + (int64_t)ws * B.state_total + so;
-        double ys[MGPU_MAX_GROUPS * kC];
+        double ys[kC];
         if (B.st_hi) {
-            for (int j = 0; j < g.n; ++j) {
-                yf[j] = B.st_hi[so + j]; // the FP32 rounding of hi + lo
-                ys[j] = (double)B.st_hi[so + j] + (double)B.st_lo[so + j];
+#pragma unroll
+            for (int c = 0; c < kC; ++c) {
+                const float h = B.st_hi[so + c];
+                ys[c]         = (double)h + (double)B.st_lo[so + c];
+                if (dep && mine) {
+                    B.ysnap_f[(int64_t)ws * B.state_total + so + c] = h; // the FP32 rounding of hi + lo
+                }
             }
         }
         else {
-            double* yd = B.ysnap + (int64_t)ws * B.state_total + so;
-            for (int j = 0; j < g.n; ++j) {
-                const double v = B.state[so + j];
-                yd[j]          = v;
-                yf[j]          = (float)v;
-                ys[j]          = v;
+#pragma unroll
+            for (int c = 0; c < kC; ++c) {
+                ys[c] = B.state[so + c];
+                if (dep && mine) {
+                    B.ysnap[(int64_t)ws * B.state_total + so + c]   = ys[c];
+                    B.ysnap_f[(int64_t)ws * B.state_total + so + c] = (float)ys[c];
+                }
             }
         }
-        // per age group: ISy mobility factor and commuter nondetection at this departure
-        R* fac = reinterpret_cast<R*>(B.risk) + ((int64_t)ws * B.num_nodes + node) * MGPU_MAX_GROUPS * 2;
-        const CVec y{ys, 1};
-        const double t    = rt.t_next;
-        const double nd   = (t >= nm.scalar(MGPU_P_START_COMMUTER_DETECTION) &&
-                           t < nm.scalar(MGPU_P_END_COMMUTER_DETECTION))
-                                ? nm.scalar(MGPU_P_COMMUTER_NONDETECTION)
-                                : 1.0;
-        for (int gr = 0; gr < g.G; ++gr) {
-            fac[2 * gr]     = (R)mobility_isy_factor(nm, y, gr);
-            fac[2 * gr + 1] = (R)nd;
+        // ISy mobility factor (get_mobility_factors, models/ode_secir/model.h:687-715)
+        // and commuter nondetection at this departure
+        const double tnt_c = tnt_w * ys[MGPU_INS];
+        double tnt         = 0.0;
+#pragma unroll
+        for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
+            const double a = __shfl_sync(kFull, tnt_c, q, MGPU_MAX_GROUPS);
+            if (q < G) {
+                tnt += a;
+            }
+        }
+        if (dep && mine) {
+            const double t  = rt.t_next;
+            const double nd = (t >= nm.scalar(MGPU_P_START_COMMUTER_DETECTION) &&
+                               t < nm.scalar(MGPU_P_END_COMMUTER_DETECTION))
+                                  ? nm.scalar(MGPU_P_COMMUTER_NONDETECTION)
+                                  : 1.0;
+            R* fac = reinterpret_cast<R*>(B.risk) + (((int64_t)ws * B.num_nodes + node) * MGPU_MAX_GROUPS + i) * 2;
+            fac[0] = (R)smoother_cosine(tnt, cap, cap * nm.scalar(MGPU_P_TNT_MAX_RISK),
+                                        nm.gp(MGPU_G_RISK_FROM_SYMPTOMATIC, i),
+                                        nm.gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, i));
+            fac[1] = (R)nd;
+        }
+    }
+}
+
+// The same node pass for the mixed solver, in FP32 from the per-(node, group)
+// constants computed at upload (the tables of k_ode_mixed): the auxiliary values
+// and factors are FP32 anyway, and FP64 division and sine would bound the pass.
+__global__ void k_xf_prep(BatchDev B, int64_t n0, int64_t nn)
+{
+    constexpr unsigned kFull = 0xffffffffu;
+    const int64_t tid        = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t seg        = tid / MGPU_MAX_GROUPS;
+    const bool in_range      = seg < nn;
+    const int64_t node       = n0 + (in_range ? seg : nn - 1); // every lane takes part in the shuffles
+    const int lane           = (int)(threadIdx.x % MGPU_MAX_GROUPS);
+    const int gi             = B.node_graph[node];
+    const DevGraph& g        = B.graphs[gi];
+    const GraphRt& rt        = B.rt[gi];
+    const int G              = g.G;
+    const bool mine          = in_range && lane < G;
+    const int i              = lane < G ? lane : 0;
+    const int64_t lv         = node - g.node0;
+    const int64_t so         = g.state_off + lv * g.n + (int64_t)i * kC;
+    const bool ret           = in_range && xb_returning(rt);
+    const bool dep           = in_range && xb_departing(rt);
+    const float* T           = B.tab_f + (node * MGPU_MAX_GROUPS + i) * kTabF;
+    const float a_tnt        = T[TF_A_TNT];
+    if (__any_sync(kFull, ret)) {
+        float pop[kC];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            pop[c] = __fadd_rn(B.v0_hi[so + c], B.v0_lo[so + c]);
+        }
+        float tnt = 0.0f, icu = 0.0f;
+        const float tnt_c = a_tnt * pop[MGPU_INS];
+#pragma unroll
+        for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
+            const float a = __shfl_sync(kFull, tnt_c, q, MGPU_MAX_GROUPS);
+            const float b = __shfl_sync(kFull, pop[MGPU_ICRI], q, MGPU_MAX_GROUPS);
+            if (q < G) {
+                tnt += a;
+                icu += b;
+            }
+        }
+        // this lane as source group: weighted infectious pressure / N
+        const float risk = smoother_cosine(tnt, T[TF_TNT_CAP], T[TF_TNT_CAP2], T[TF_RHO], T[TF_RHO_MAX]);
+        const float Nj   = pop[MGPU_S] + pop[MGPU_E] + pop[MGPU_INS] + pop[MGPU_ISY] + pop[MGPU_ISEV] +
+                         pop[MGPU_ICRI] + pop[MGPU_R];
+        const float divN = (Nj < (float)kZeroTol) ? 0.0f : __frcp_rn(Nj);
+        const float w    = divN * (T[TF_XI] * pop[MGPU_INS] + risk * pop[MGPU_ISY]);
+        // this lane as target group: its contact row at t_dep
+        const NodeModel nm = node_model(B, g, lv);
+        float Crow[MGPU_MAX_GROUPS];
+        if (nm.M == 1) {
+            const long GG   = (long)G * G;
+            const float* Bm = B.contact_f + g.contact_off + lv * 2 * GG + (long)i * G;
+            const float* Lm = Bm + GG;
+            if (nm.K == 0) {
+#pragma unroll
+                for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
+                    Crow[q] = q < G ? Bm[q] : 0.0f;
+                }
+            }
+            else {
+                const int ub    = damping_upper_bound(nm.dtimes, nm.K, rt.t_dep);
+                const double tu = nm.dtimes[ub];
+                const float xl  = (float)((tu - 1.0) - rt.t_dep);
+                const float sc  = (float)(1.0 / (tu - (tu - 1.0)));
+                const float c   = (0.0f <= xl) ? 1.0f : cospif((0.0f - xl) * sc);
+                const float* Dl = B.dvals_f + g.dval_off + lv * g.K * GG + (long)(ub - 1) * GG + (long)i * G;
+                const float* Dr = Dl + GG;
+#pragma unroll
+                for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
+                    if (q < G) {
+                        const float BL = Bm[q] - Lm[q];
+                        const float P  = Bm[q] - (0.5f * (Dl[q] + Dr[q])) * BL;
+                        const float Q  = -(0.5f * (Dl[q] - Dr[q])) * BL;
+                        Crow[q]        = P + Q * c;
+                    }
+                    else {
+                        Crow[q] = 0.0f;
+                    }
+                }
+            }
+        }
+        else {
+            double Cd[MGPU_MAX_GROUPS];
+            contact_row(nm, i, rt.t_dep, Cd);
+#pragma unroll
+            for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
+                Crow[q] = (float)Cd[q];
+            }
+        }
+        float acc = 0.0f;
+#pragma unroll
+        for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
+            const float wq = __shfl_sync(kFull, w, q, MGPU_MAX_GROUPS);
+            if (q < G) {
+                acc += Crow[q] * wq;
+            }
+        }
+        if (ret && mine) {
+            const float sk     = T[TF_SEASON_K];
+            const float season = sk == 0.0f
+                                     ? 1.0f
+                                     : 1.0f + sk * sinpif((float)((nm.scalar(MGPU_P_START_DAY) + rt.t_dep) *
+                                                                      (1.0 / 182.5) +
+                                                                  0.5));
+            float r10 = T[TF_R10L], r12 = T[TF_R12L];
+            if (!(icu <= T[TF_ICU_LO])) {
+                const float crit_adj = smoother_cosine(icu, T[TF_ICU_LO], T[TF_ICU_CAP], T[TF_CPS], 0.0f);
+                r10                  = crit_adj * T[TF_INV_TISEV];
+                r12                  = (T[TF_DPS] + (T[TF_CPS] - crit_adj)) * T[TF_INV_TISEV];
+            }
+            float v[kAux];
+            v[0]  = T[TF_BETA] * season * acc;
+            v[1]  = T[TF_R1];
+            v[2]  = T[TF_R2];
+            v[3]  = T[TF_R3];
+            v[4]  = T[TF_R6];
+            v[5]  = T[TF_R7];
+            v[6]  = r10;
+            v[7]  = T[TF_R11];
+            v[8]  = r12;
+            v[9]  = T[TF_R13];
+            v[10] = T[TF_R14];
+            // can one Euler step of length dt drive a returning compartment negative?
+            // (it cannot when dt times every compartment's total outflow rate is <= 1;
+            // the FP32 test keeps a margin for its own rounding)
+            const float out_rate =
+                fmaxf(fmaxf(v[0], v[1]), fmaxf(fmaxf(v[2] + v[3], v[4] + v[5]), fmaxf(v[6] + v[7] + v[8], v[9] + v[10])));
+            v[11]     = ((float)rt.dt * out_rate > 0.99999f) ? 1.0f : 0.0f;
+            float4* a = reinterpret_cast<float4*>(reinterpret_cast<float*>(B.aux) + (node * MGPU_MAX_GROUPS + i) * kAux);
+            a[0]      = make_float4(v[0], v[1], v[2], v[3]);
+            a[1]      = make_float4(v[4], v[5], v[6], v[7]);
+            a[2]      = make_float4(v[8], v[9], v[10], v[11]);
+        }
+    }
+    if (__any_sync(kFull, dep)) {
+        const int ws = rt.snap_slot ^ 1;
+        float h[kC];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            h[c] = B.st_hi[so + c];
+        }
+        if (dep && mine) {
+            float* yf = B.ysnap_f + (int64_t)ws * B.state_total + so;
+#pragma unroll
+            for (int c = 0; c < kC / 2; ++c) {
+                reinterpret_cast<float2*>(yf)[c] = make_float2(h[2 * c], h[2 * c + 1]); // the FP32 rounding of hi + lo
+            }
+        }
+        // ISy mobility factor (get_mobility_factors, models/ode_secir/model.h:687-715)
+        // and commuter nondetection at this departure
+        const float tnt_c = a_tnt * h[MGPU_INS];
+        float tnt         = 0.0f;
+#pragma unroll
+        for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
+            const float a = __shfl_sync(kFull, tnt_c, q, MGPU_MAX_GROUPS);
+            if (q < G) {
+                tnt += a;
+            }
+        }
+        if (dep && mine) {
+            const double* p = B.params + g.param_off + lv * param_stride(G);
+            const double t  = rt.t_next;
+            const float nd  = (t >= p[MGPU_P_START_COMMUTER_DETECTION] && t < p[MGPU_P_END_COMMUTER_DETECTION])
+                                  ? (float)p[MGPU_P_COMMUTER_NONDETECTION]
+                                  : 1.0f;
+            float2* fac = reinterpret_cast<float2*>(B.risk) + ((int64_t)ws * B.num_nodes + node) * MGPU_MAX_GROUPS + i;
+            *fac        = make_float2(smoother_cosine(tnt, T[TF_TNT_CAP], T[TF_TNT_CAP2], T[TF_RHO], T[TF_RHO_MAX]), nd);
         }
     }
 }
@@ -617,9 +894,7 @@ __global__ void k_xb_return(BatchDev B, int64_t n0, int64_t nn)
         ynew_set(B, so + c, acc[c].get());
         flag = flag || (bound[c] < margin * mag[c]);
     }
-    if (flag) {
-        B.node_flag[node] = 1;
-    }
+    list0_push(B, node * MGPU_MAX_GROUPS + gr, flag);
 }
 
 // ---- FP32 node passes of the mixed solver ------------------------------------
@@ -633,35 +908,91 @@ struct GroupSnap {
     float risk, nd;
 };
 
+// Vector loads of the FP32 tables. Every age-group row of the 10 compartments
+// starts on an 8-byte boundary (state and coefficient offsets are multiples of
+// 10 floats), the 12 auxiliary values of a (node, group) on a 16-byte boundary
+// and the factor pair on an 8-byte boundary. The snapshot, coefficient, factor
+// and auxiliary tables are read-only in the kernels that use them (read-only
+// data path); the node states use plain loads and stores.
+static_assert(kC == 10 && kAux == 12, "vector widths of the FP32 tables");
+__device__ __forceinline__ void ld_row(const float* p, float (&v)[kC])
+{
+    const float2* q = reinterpret_cast<const float2*>(p);
+#pragma unroll
+    for (int i = 0; i < kC / 2; ++i) {
+        const float2 a = __ldg(q + i);
+        v[2 * i]       = a.x;
+        v[2 * i + 1]   = a.y;
+    }
+}
+__device__ __forceinline__ void ld_aux12(const float* p, float (&v)[kAux])
+{
+    const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int i = 0; i < kAux / 4; ++i) {
+        const float4 a = __ldg(q + i);
+        v[4 * i]       = a.x;
+        v[4 * i + 1]   = a.y;
+        v[4 * i + 2]   = a.z;
+        v[4 * i + 3]   = a.w;
+    }
+}
+__device__ __forceinline__ void ld_state(const float* p, float (&v)[kC])
+{
+    const float2* q = reinterpret_cast<const float2*>(p);
+#pragma unroll
+    for (int i = 0; i < kC / 2; ++i) {
+        const float2 a = q[i];
+        v[2 * i]       = a.x;
+        v[2 * i + 1]   = a.y;
+    }
+}
+__device__ __forceinline__ void st_state(float* p, const float (&v)[kC])
+{
+    float2* q = reinterpret_cast<float2*>(p);
+#pragma unroll
+    for (int i = 0; i < kC / 2; ++i) {
+        q[i] = make_float2(v[2 * i], v[2 * i + 1]);
+    }
+}
+
 __device__ __forceinline__ void load_group_snap(const BatchDev& B, const DevGraph& g, int64_t node, int gr, int slot,
                                                 GroupSnap& s)
 {
-    const float* y = B.ysnap_f + (int64_t)slot * B.state_total + g.state_off + (node - g.node0) * g.n + gr * kC;
-#pragma unroll
-    for (int c = 0; c < kC; ++c) {
-        s.y[c] = y[c];
-    }
-    const float* fac = reinterpret_cast<const float*>(B.risk) + (((int64_t)slot * B.num_nodes + node) * MGPU_MAX_GROUPS + gr) * 2;
-    s.risk           = fac[0];
-    s.nd             = fac[1];
+    ld_row(B.ysnap_f + (int64_t)slot * B.state_total + g.state_off + (node - g.node0) * g.n + gr * kC, s.y);
+    const float2 f = __ldg(reinterpret_cast<const float2*>(B.risk) +
+                           ((int64_t)slot * B.num_nodes + node) * MGPU_MAX_GROUPS + gr);
+    s.risk = f.x;
+    s.nd   = f.y;
 }
 
-// m = ((y o c) o f) with the nondetection factor on INS and ISy (same operations as depart_travelers<float>)
-__device__ __forceinline__ void travelers_f(const BatchDev& B, const DevGraph& g, int64_t e, int gr,
-                                            const GroupSnap& s, float (&m)[kC])
+__device__ __forceinline__ void edge_coeff_f(const BatchDev& B, const DevGraph& g, int64_t e, int gr, float (&cf)[kC])
 {
-    const float* cf = B.ecoef_f + g.ecoef_f_off + (e - g.edge0) * g.n + gr * kC;
+    ld_row(B.ecoef_f + g.ecoef_f_off + (e - g.edge0) * g.n + gr * kC, cf);
+}
+
+// m = ((y o c) o f) with the nondetection factor nd on INS and ISy (same operations as depart_travelers<float>)
+__device__ __forceinline__ void travelers_cf(const GroupSnap& s, float nd, const float (&cf)[kC], float (&m)[kC])
+{
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
         float v = __fmul_rn(__fmul_rn(s.y[c], cf[c]), c == MGPU_ISY ? s.risk : 1.0f);
         if (c == MGPU_INS || c == MGPU_ISY) {
-            v = __fmul_rn(v, s.nd);
+            v = __fmul_rn(v, nd);
         }
         m[c] = v;
     }
 }
 
-__device__ __forceinline__ void flows_f(const float* a, float dt, const float (&m)[kC], float (&phi)[kF])
+__device__ __forceinline__ void travelers_f(const BatchDev& B, const DevGraph& g, int64_t e, int gr,
+                                            const GroupSnap& s, float (&m)[kC])
+{
+    float cf[kC];
+    edge_coeff_f(B, g, e, gr, cf);
+    travelers_cf(s, s.nd, cf, m);
+}
+
+__device__ __forceinline__ void flows_f(const float (&a)[kAux], float dt, const float (&m)[kC], float (&phi)[kF])
 {
     const float s[kF] = {m[MGPU_S],    m[MGPU_E],    m[MGPU_INS],  m[MGPU_INS],  m[MGPU_INSC],
                          m[MGPU_INSC], m[MGPU_ISY],  m[MGPU_ISY],  m[MGPU_ISYC], m[MGPU_ISYC],
@@ -691,9 +1022,14 @@ __global__ void k_xf_depart(BatchDev B, int64_t n0, int64_t nn)
     const int64_t lv = node - g.node0;
     const int64_t so = g.state_off + lv * g.n + gr * kC;
     Acc<float> acc[kC];
+    {
+        float h[kC], l[kC];
+        ld_state(B.st_hi + so, h);
+        ld_state(B.st_lo + so, l);
 #pragma unroll
-    for (int c = 0; c < kC; ++c) {
-        acc[c].init_pair(B.st_hi[so + c], B.st_lo[so + c]);
+        for (int c = 0; c < kC; ++c) {
+            acc[c].init_pair(h[c], l[c]);
+        }
     }
     GroupSnap own, src;
     load_group_snap(B, g, node, gr, ws, own);
@@ -721,18 +1057,18 @@ __global__ void k_xf_depart(BatchDev B, int64_t n0, int64_t nn)
         if (!B.edge_static_any[e]) {
             continue;
         }
+        float cf[kC];
+        edge_coeff_f(B, g, e, gr, cf);
         if (detect) {
             // test_commuters: detected commuters move to the confirmed compartments first
-            GroupSnap o = own;
-            o.nd        = 1.0f;
             float mo[kC];
-            travelers_f(B, g, e, gr, o, mo);
+            travelers_cf(own, 1.0f, cf, mo);
             acc[MGPU_INS].add(-__fmul_rn(mo[MGPU_INS], q));
             acc[MGPU_INSC].add(__fmul_rn(mo[MGPU_INS], q));
             acc[MGPU_ISY].add(-__fmul_rn(mo[MGPU_ISY], q));
             acc[MGPU_ISYC].add(__fmul_rn(mo[MGPU_ISY], q));
         }
-        travelers_f(B, g, e, gr, own, m);
+        travelers_cf(own, own.nd, cf, m);
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
             acc[c].add(-m[c]);
@@ -749,12 +1085,15 @@ __global__ void k_xf_depart(BatchDev B, int64_t n0, int64_t nn)
             }
         }
     }
+    float h[kC], l[kC];
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
-        acc[c].store(B.st_hi + so + c, B.st_lo + so + c);
-        B.v0_hi[so + c] = B.st_hi[so + c];
-        B.v0_lo[so + c] = B.st_lo[so + c];
+        acc[c].store(&h[c], &l[c]);
     }
+    st_state(B.st_hi + so, h);
+    st_state(B.st_lo + so, l);
+    st_state(B.v0_hi + so, h);
+    st_state(B.v0_lo + so, l);
 }
 
 __global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
@@ -777,11 +1116,15 @@ __global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
     const int64_t s0 = g.state_off + lv * g.n + gr * kC;
     Acc<float> acc[kC];
     float yf[kC], min_in[kC], phi_in[kF], phi_out[kF];
+    {
+        float l[kC];
+        ld_state(B.st_hi + s0, yf);
+        ld_state(B.st_lo + s0, l);
 #pragma unroll
-    for (int c = 0; c < kC; ++c) {
-        acc[c].init_pair(B.st_hi[s0 + c], B.st_lo[s0 + c]);
-        yf[c]     = acc[c].hi;
-        min_in[c] = 0.0f;
+        for (int c = 0; c < kC; ++c) {
+            acc[c].init_pair(yf[c], l[c]);
+            min_in[c] = 0.0f;
+        }
     }
 #pragma unroll
     for (int f = 0; f < kF; ++f) {
@@ -790,10 +1133,7 @@ __global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
     }
     const float* aux = reinterpret_cast<const float*>(B.aux);
     float a_own[kAux];
-#pragma unroll
-    for (int q = 0; q < kAux; ++q) {
-        a_own[q] = aux[(node * MGPU_MAX_GROUPS + gr) * kAux + q];
-    }
+    ld_aux12(aux + (node * MGPU_MAX_GROUPS + gr) * kAux, a_own);
     GroupSnap own, src;
     load_group_snap(B, g, node, gr, slot, own);
     float m[kC], phi[kF];
@@ -838,7 +1178,8 @@ __global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
         if (!B.edge_static_any[e]) {
             continue;
         }
-        const float* ax = aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux;
+        float ax[kAux];
+        ld_aux12(aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux, ax);
         travelers_f(B, g, e, gr, own, m);
         flows_f(ax, dt, m, phi);
         unsafe = unsafe || ax[11] != 0.0f;
@@ -872,189 +1213,214 @@ __global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
     // least y minus the positive parts of all returning in-edge amounts
     bool flag = lowest < 0.0f || unsafe;
     const int64_t so = g.state_off + lv * g.n + gr * kC;
+    float h[kC], l[kC];
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
-        acc[c].store(B.yn_hi + so + c, B.yn_lo + so + c);
+        acc[c].store(&h[c], &l[c]);
         const float bound = yf[c] - min_in[c];
         const float mag   = fabsf(yf[c]) + min_in[c];
         flag              = flag || (bound < 1e-5f * mag);
     }
-    if (flag) {
-        B.node_flag[node] = 1;
+    st_state(B.yn_hi + so, h);
+    st_state(B.yn_lo + so, l);
+    list0_push(B, node * MGPU_MAX_GROUPS + gr, flag);
+}
+
+// ---- exact underflow path ------------------------------------------------------
+// The reference fixes a negative remainder of compartment c by moving the deficit
+// to the largest compartment of the same age group (:576-596). All of it stays
+// inside one age group, so the exact serial order can be replayed by independent
+// (node, age group) threads. A (node, group) item enters list 0 when its bound
+// fails; a scan of the item fixes its in-edges against its running FP64 state and
+// publishes the fixed travelers per (edge, group) in mfix / fix_cnt; a change
+// marks the edge's (source, group) for a rescan (the source's state contains
+// those travelers). A few passes settle the chains of fixes; a graph with items
+// still marked after the last pass takes the sequential pass.
+
+__global__ void k_list_reset(BatchDev B, int list)
+{
+    B.scan_count[list] = 0;
+}
+
+// Exact fix of one (edge, age group) against the running state y: with
+// rem = y - t, every negative rem[c] is moved, in compartment order, to the
+// first largest remainder (:576-596). Returns the number of fixed compartments.
+__device__ __forceinline__ int fix_group(const double (&y)[kC], double (&t)[kC])
+{
+    double rem[kC];
+    bool neg = false;
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        rem[c] = y[c] - t[c];
+        neg    = neg || rem[c] < 0;
+    }
+    if (!neg) {
+        return 0;
+    }
+    int mx     = 0;
+    double rmx = rem[0];
+#pragma unroll
+    for (int q = 1; q < kC; ++q) {
+        if (rem[q] > rmx) {
+            rmx = rem[q];
+            mx  = q;
+        }
+    }
+    int nfix = 0;
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        if (rem[c] < 0) {
+#pragma unroll
+            for (int q = 0; q < kC; ++q) {
+                if (q == mx) {
+                    t[q] -= rem[c];
+                }
+            }
+            t[c] += rem[c];
+            ++nfix;
+        }
+    }
+    return nfix;
+}
+
+template <class R>
+__global__ void k_xg_scan(BatchDev B, int pass)
+{
+    const int lin    = pass == 0 ? 0 : 1 + ((pass - 1) & 1);
+    const int lout   = 1 + (pass & 1);
+    const int cnt    = B.scan_count[lin];
+    const int64_t NG = B.num_nodes * MGPU_MAX_GROUPS;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && cnt > 0) {
+        atomicAdd(&B.counters[CNT_SCANNED], (unsigned long long)cnt);
+    }
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < cnt;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t item = B.scan_list[lin * NG + idx];
+        B.scan_mark[lin * NG + item] = 0; // consumed
+        const int64_t node = item / MGPU_MAX_GROUPS;
+        const int gr       = (int)(item % MGPU_MAX_GROUPS);
+        const int gi       = B.node_graph[node];
+        const DevGraph& g  = B.graphs[gi];
+        const GraphRt& rt  = B.rt[gi];
+        if (gr >= g.G || !xb_returning(rt)) {
+            continue;
+        }
+        const int64_t so = g.state_off + (node - g.node0) * g.n + gr * kC;
+        double y[kC];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            y[c] = state_get(B, so + c);
+        }
+        auto in_edge = [&](int64_t e) {
+            double t[kC];
+            return_travelers<R>(B, g, rt, e, gr, t);
+            const int nfix = fix_group(y, t);
+            uint8_t* fc    = B.fix_cnt + e * MGPU_MAX_GROUPS + gr;
+            const int prev = *(volatile uint8_t*)fc;
+            bool changed   = false;
+            double* mf     = B.mfix + B.trav_off[e] + gr * kC;
+            if (nfix) {
+                changed = prev == 0;
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    changed = changed || __ldcg(mf + c) != t[c];
+                    __stcg(mf + c, t[c]);
+                }
+                __threadfence();
+                *(volatile uint8_t*)fc = (uint8_t)nfix;
+            }
+            else if (prev) {
+                *(volatile uint8_t*)fc = 0;
+                changed                = true;
+            }
+            if (changed) {
+                list_push(B, lout, B.edge_src[e] * MGPU_MAX_GROUPS + gr);
+            }
+#pragma unroll
+            for (int c = 0; c < kC; ++c) {
+                y[c] -= t[c];
+            }
+        };
+        const int64_t ib = B.in_ptr[node], ie = B.in_ptr[node + 1];
+        int64_t k        = ib;
+        for (; k < ie; ++k) {
+            const int64_t e = B.in_edges[k];
+            if (B.edge_src[e] > node) {
+                break;
+            }
+            if (edge_departed(B, g, e)) {
+                in_edge(e);
+            }
+        }
+        for (int64_t e = B.out_ptr[node]; e < B.out_ptr[node + 1]; ++e) {
+            if (!edge_departed(B, g, e)) {
+                continue;
+            }
+            double t[kC];
+            if (((volatile uint8_t*)B.fix_cnt)[e * MGPU_MAX_GROUPS + gr] != 0) {
+                const double* mf = B.mfix + B.trav_off[e] + gr * kC;
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    t[c] = __ldcg(mf + c);
+                }
+            }
+            else {
+                return_travelers<R>(B, g, rt, e, gr, t);
+            }
+#pragma unroll
+            for (int c = 0; c < kC; ++c) {
+                y[c] += t[c];
+            }
+        }
+        for (; k < ie; ++k) {
+            const int64_t e = B.in_edges[k];
+            if (edge_departed(B, g, e)) {
+                in_edge(e);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            ynew_set(B, so + c, y[c]);
+        }
     }
 }
 
-// Exact serial return order for one flagged or marked node (one warp): FP64
-// state, the underflow fix of each in-edge, fixed travelers published in mfix
-// for the source's rescan. Travelers are the same values as in k_xb_return.
-template <class R>
-__global__ void k_xb_scan(BatchDev B, int64_t n0, int64_t nn, int pass)
+// Nodes still marked after the last pass send their graph to the sequential
+// pass; resets the lists for the next return.
+__global__ void k_xg_scan_done(BatchDev B, int last_list)
 {
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane  = threadIdx.x & 31;
-    if (w >= nn) {
+    const int cnt    = B.scan_count[last_list];
+    const int64_t NG = B.num_nodes * MGPU_MAX_GROUPS;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t item = B.scan_list[last_list * NG + i];
+        B.scan_mark[last_list * NG + item] = 0;
+        GraphRt& rt = B.rt[B.node_graph[item / MGPU_MAX_GROUPS]];
+        if (xb_returning(rt)) {
+            atomicOr(&rt.fallback, 1);
+        }
+    }
+}
+
+// Fix counts of the parallel path; clears the per-(edge, group) fix records.
+__global__ void k_xg_cleanup(BatchDev B, int64_t ne)
+{
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) {
         return;
     }
-    const int64_t node = n0 + w;
-    const int gi       = B.node_graph[node];
-    const DevGraph& g  = B.graphs[gi];
-    const GraphRt& rt  = B.rt[gi];
-    if (!xb_returning(rt)) {
+    const uint2 w = reinterpret_cast<const uint2*>(B.fix_cnt)[e]; // MAX_GROUPS == 8 bytes
+    if ((w.x | w.y) == 0) {
         return;
     }
-    uint8_t* dirty_in  = B.node_dirty + (pass & 1) * B.num_nodes;
-    uint8_t* dirty_out = B.node_dirty + ((pass + 1) & 1) * B.num_nodes;
-    const bool todo    = pass == 0 ? B.node_flag[node] != 0 : dirty_in[node] != 0;
-    if (!todo) {
-        return;
+    unsigned f = 0;
+    for (int q = 0; q < 4; ++q) {
+        f += (w.x >> (8 * q)) & 0xffu;
+        f += (w.y >> (8 * q)) & 0xffu;
     }
-    if (pass > 0 && lane == 0) {
-        dirty_in[node] = 0;
+    if (!B.rt[B.edge_graph[e]].fallback) {
+        atomicAdd(&B.counters[CNT_UNDERFLOW], (unsigned long long)f);
     }
-    __shared__ double sm_m[4][MGPU_MAX_GROUPS * kC];
-    __shared__ double sm_r[4][MGPU_MAX_GROUPS * kC];
-    double* m   = sm_m[(threadIdx.x >> 5) & 3];
-    double* rem = sm_r[(threadIdx.x >> 5) & 3];
-    const int n = g.n;
-    double y[3];
-    const int64_t s0 = g.state_off + (node - g.node0) * n;
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        const int j = lane + 32 * q;
-        y[q]        = j < n ? state_get(B, s0 + j) : 0.0;
-    }
-    // lanes 0..G-1 compute one age group's travelers each into shared memory
-    auto travelers = [&](int64_t e) {
-        if (lane < g.G) {
-            double mt[kC];
-            return_travelers<R>(B, g, rt, e, lane, mt);
-#pragma unroll
-            for (int c = 0; c < kC; ++c) {
-                m[lane * kC + c] = mt[c];
-            }
-        }
-        __syncwarp();
-    };
-    auto in_edge = [&](int64_t e) {
-        travelers(e);
-        bool neg = false;
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            const int j = lane + 32 * q;
-            if (j < n) {
-                rem[j] = y[q] - m[j];
-                neg    = neg || (rem[j] < 0);
-            }
-        }
-        neg = __any_sync(0xffffffffu, neg);
-        __syncwarp();
-        if (neg) {
-            if (lane == 0) {
-                int fixes = 0;
-                for (int j = 0; j < n; ++j) {
-                    if (rem[j] < 0) {
-                        const int group = j / kC;
-                        int max_index   = 0;
-                        for (int c = 1; c < kC; ++c) {
-                            if (rem[group * kC + c] > rem[group * kC + max_index]) {
-                                max_index = c;
-                            }
-                        }
-                        max_index += group * kC;
-                        m[max_index] -= rem[j];
-                        m[j] += rem[j];
-                        ++fixes;
-                    }
-                }
-                rem[0] = (double)fixes;
-            }
-            __syncwarp();
-            const int fixes = (int)rem[0];
-            double* mf      = B.mfix + B.trav_off[e];
-            bool changed    = B.edge_fixed[e] == 0;
-            for (int q = 0; q < 3; ++q) {
-                const int j = lane + 32 * q;
-                if (j < n) {
-                    changed = changed || (__ldcg(mf + j) != m[j]);
-                    __stcg(mf + j, m[j]);
-                }
-            }
-            changed = __any_sync(0xffffffffu, changed);
-            __threadfence();
-            if (lane == 0) {
-                B.edge_fixed[e] = fixes;
-                if (changed) {
-                    dirty_out[B.edge_src[e]] = 1;
-                }
-            }
-        }
-        else if (B.edge_fixed[e] != 0) {
-            if (lane == 0) {
-                B.edge_fixed[e]          = 0;
-                dirty_out[B.edge_src[e]] = 1;
-            }
-        }
-        __syncwarp();
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            const int j = lane + 32 * q;
-            if (j < n) {
-                y[q] -= m[j];
-            }
-        }
-        __syncwarp();
-    };
-    const int64_t ib = B.in_ptr[node], ie = B.in_ptr[node + 1];
-    int64_t k        = ib;
-    for (; k < ie; ++k) {
-        const int64_t e = B.in_edges[k];
-        if (B.edge_src[e] > node) {
-            break;
-        }
-        if (edge_departed(B, g, e)) {
-            in_edge(e);
-        }
-    }
-    for (int64_t e = B.out_ptr[node]; e < B.out_ptr[node + 1]; ++e) {
-        if (!edge_departed(B, g, e)) {
-            continue;
-        }
-        const bool fixed = ((volatile int32_t*)B.edge_fixed)[e] != 0;
-        if (fixed) {
-            const double* src = B.mfix + B.trav_off[e];
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                const int j = lane + 32 * q;
-                if (j < n) {
-                    y[q] += __ldcg(src + j);
-                }
-            }
-        }
-        else {
-            travelers(e);
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                const int j = lane + 32 * q;
-                if (j < n) {
-                    y[q] += m[j];
-                }
-            }
-            __syncwarp();
-        }
-    }
-    for (; k < ie; ++k) {
-        const int64_t e = B.in_edges[k];
-        if (edge_departed(B, g, e)) {
-            in_edge(e);
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        const int j = lane + 32 * q;
-        if (j < n) {
-            ynew_set(B, s0 + j, y[q]);
-        }
-    }
+    reinterpret_cast<uint2*>(B.fix_cnt)[e] = make_uint2(0u, 0u);
 }
 
 // Exact serial return loop of one graph (one warp per graph) for the graphs
@@ -1134,24 +1500,6 @@ __global__ void k_xb_sequential(BatchDev B, int g0, int ng)
     }
 }
 
-// bookkeeping kernels shared with exchange.cu semantics
-__global__ void k_xb_scan_done(BatchDev B, int64_t n0, int64_t nn, int pass_end)
-{
-    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= nn) {
-        return;
-    }
-    const int64_t node = n0 + tid;
-    GraphRt& rt        = B.rt[B.node_graph[node]];
-    uint8_t* dirty     = B.node_dirty + (pass_end & 1) * B.num_nodes;
-    if (xb_returning(rt) && dirty[node]) {
-        atomicOr(&rt.fallback, 1);
-    }
-    dirty[node]                                             = 0;
-    B.node_dirty[((pass_end + 1) & 1) * B.num_nodes + node] = 0;
-    B.node_flag[node]                                       = 0;
-}
-
 __global__ void k_xb_commit(BatchDev B, int64_t n0, int64_t nn, int n_max)
 {
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1176,23 +1524,6 @@ __global__ void k_xb_commit(BatchDev B, int64_t n0, int64_t nn, int n_max)
     }
 }
 
-__global__ void k_xb_cleanup(BatchDev B, int64_t e0, int64_t ne)
-{
-    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= ne) {
-        return;
-    }
-    const int64_t e = e0 + tid;
-    const int f     = B.edge_fixed[e];
-    if (f == 0) {
-        return;
-    }
-    if (!B.rt[B.edge_graph[e]].fallback) {
-        atomicAdd(&B.counters[CNT_UNDERFLOW], (unsigned long long)f);
-    }
-    B.edge_fixed[e] = 0;
-}
-
 inline unsigned blocks_of(int64_t n, int t)
 {
     return (unsigned)((n + t - 1) / t);
@@ -1208,7 +1539,12 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
         return;
     }
     const int T = 128;
-    k_xb_prep<R><<<blocks_of(nn, T), T, 0, s>>>(B, 0, nn);
+    if (std::is_same<R, float>::value) {
+        k_xf_prep<<<blocks_of(nn * MGPU_MAX_GROUPS, T), T, 0, s>>>(B, 0, nn);
+    }
+    else {
+        k_xb_prep<R><<<blocks_of(nn * MGPU_MAX_GROUPS, T), T, 0, s>>>(B, 0, nn);
+    }
     *launches += 1;
     if (ne == 0) {
         return;
@@ -1223,13 +1559,18 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
         k_xb_return<R><<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
         *launches += 1;
     }
+    // exact underflow path over the work lists (list 0 was filled by the return pass)
+    const unsigned scan_blocks = 152 * 8;
     for (int pass = 0; pass < kXbScanPasses; ++pass) {
-        k_xb_scan<R><<<blocks_of(nn * 32, 128), 128, 0, s>>>(B, 0, nn, pass);
+        k_list_reset<<<1, 1, 0, s>>>(B, 1 + (pass & 1));
+        k_xg_scan<R><<<scan_blocks, 128, 0, s>>>(B, pass);
     }
-    k_xb_scan_done<<<blocks_of(nn, 256), 256, 0, s>>>(B, 0, nn, kXbScanPasses);
+    const int last = 1 + ((kXbScanPasses - 1) & 1);
+    k_xg_scan_done<<<scan_blocks, 128, 0, s>>>(B, last);
+    k_list_reset<<<1, 1, 0, s>>>(B, 0);
     k_xb_commit<<<blocks_of(nn * n_max, 256), 256, 0, s>>>(B, 0, nn, (int)n_max);
     k_xb_sequential<R><<<B.num_graphs, 32, 0, s>>>(B, 0, B.num_graphs);
-    k_xb_cleanup<<<blocks_of(ne, 256), 256, 0, s>>>(B, 0, ne);
+    k_xg_cleanup<<<blocks_of(ne, 256), 256, 0, s>>>(B, ne);
     if (any_edge_dampings) {
         k_xb_edge_flags<<<blocks_of(ne, 256), 256, 0, s>>>(B, 0, ne);
         *launches += 1;
@@ -1242,14 +1583,18 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
         k_xb_depart<R><<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
         *launches += 1;
     }
-    *launches += 5 + kXbScanPasses;
+    *launches += 5 + 2 * kXbScanPasses;
 }
 
 } // namespace
 
-int exchange_batched_launches(bool has_edges, bool any_edge_dampings)
+int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings)
 {
-    return has_edges ? 8 + kXbScanPasses + (any_edge_dampings ? 3 : 0) : 1;
+    if (!has_edges) {
+        return 1;
+    }
+    const int extra = !any_edge_dampings ? 0 : (precision == MGPU_PRECISION_MIXED ? 3 : 1);
+    return 8 + 2 * kXbScanPasses + extra;
 }
 
 void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,

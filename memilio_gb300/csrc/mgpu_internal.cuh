@@ -98,6 +98,11 @@ struct BatchDev {
     int32_t* edge_fixed;         // [num_edges] number of fixed compartments (0: mfix unused)
     uint8_t* node_flag;          // [num_nodes] return needs the exact per-node scan
     uint8_t* node_dirty;         // [2][num_nodes] an out-edge changed: rescan (double-buffered)
+    // batched exchange: exact-scan work lists (0: flagged by the bound, 1/2: rescans)
+    int32_t* scan_mark;          // [3][num_nodes * MAX_GROUPS] (node, group) item is in list k
+    int32_t* scan_list;          // [3][num_nodes * MAX_GROUPS] items node * MAX_GROUPS + group
+    int32_t* scan_count;         // [3]
+    uint8_t* fix_cnt;            // [num_edges][MAX_GROUPS] fixed compartments per edge and age group
     const int64_t* trav_off;     // [num_edges] offset of each edge's travelers
     const int64_t* out_ptr;      // [num_nodes+1] CSR (edges sorted by (src, dst))
     const int64_t* in_ptr;       // [num_nodes+1] CSC
@@ -119,7 +124,7 @@ struct BatchDev {
     unsigned long long* counters; // [8]: accepted, rejected, failed, underflow, sequential
 };
 
-enum { CNT_ACCEPTED = 0, CNT_REJECTED, CNT_FAILED, CNT_UNDERFLOW, CNT_SEQUENTIAL, CNT_NUM };
+enum { CNT_ACCEPTED = 0, CNT_REJECTED, CNT_FAILED, CNT_UNDERFLOW, CNT_SEQUENTIAL, CNT_SCANNED, CNT_NUM };
 
 // FP32 per-(node, age group) constants of the mixed solver, computed once from
 // the FP64 parameters (rates as the reference forms them: (1-mu)*(1/T) etc.).
@@ -464,7 +469,7 @@ void launch_exchange(const BatchDev& B, int64_t max_n, cudaStream_t s, int64_t* 
 int exchange_launches(bool has_edges);
 void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,
                              cudaStream_t s, int64_t* launches);
-int exchange_batched_launches(bool has_edges, bool any_edge_dampings);
+int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings);
 void launch_exchange_range(const BatchDev& B, int g0, int ng, int64_t n0, int64_t nn, int64_t e0, int64_t ne,
                            int64_t n_max, cudaStream_t s, int64_t* launches);
 void launch_phase_end(const BatchDev& B, cudaStream_t s);
