@@ -116,6 +116,62 @@ int mgpu_simulate(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, con
                   double* out_y, int32_t* num_points);
 
 /*
+ * Allocation-free variant of mgpu_simulate for callers that must not allocate
+ * device memory inside their loop. No counterpart in the reference: MEmilio
+ * integrates on the host, where this question does not arise.
+ *
+ * Who needs it: every other entry point allocates its device buffers per call
+ * (cudaMalloc) and frees them again (cudaFree), and cudaFree waits for the
+ * whole device. A caller that keeps other work in flight on other streams (a
+ * request loop overlapping solves) would stall on that wait, and a caller whose
+ * device memory is held by another allocator (a framework's caching allocator
+ * that owns the free HBM) may not get the memory at all. This call uses only
+ * memory the caller already owns plus a fixed work space inside the library.
+ *
+ * What it does: integrates `count` isolated nodes from t0 to tmax with initial
+ * step dt0 and the plain FP64 integrator of mgpu_simulate (same kernel
+ * arithmetic, so the same final states), and writes only the final states.
+ * The nodes share num_groups G, num_contact_matrices M and num_damping_points K.
+ * Every array is DEVICE memory owned by the caller:
+ *   params          [count][MGPU_PARAM_STRIDE(G)]
+ *   contact         [count][M][2][G][G]   baseline, then minimum, per matrix
+ *   damping_times   [count][M][K]         (NULL when K == 0; non-decreasing)
+ *   damping_values  [count][M][K][G][G]   (NULL when K == 0)
+ *   y0              [count][10G]
+ *   y_out           [count][10G]          equal to y0 (in place) or not overlapping it
+ *   status          [count]               0 = reached tmax, bit 0 = step cap hit,
+ *                                         bit 1 = non-finite state
+ * The call enqueues one kernel on the context's stream and returns without
+ * waiting; the outputs are valid once that stream has been synchronized.
+ *
+ * Limit: the work space is MGPU_NOALLOC_SCRATCH_BYTES (4 MiB), of which a call
+ * needs 640 * G * count bytes (8 stage vectors of 10G doubles per node), so
+ * count * G <= 6553 (count <= 1092 nodes at G = 6). Larger calls return
+ * MGPU_OUT_OF_RANGE without launching anything.
+ *
+ * Nothing in the work space has to start at zero: every stage vector is
+ * written before it is read, and `status` is written for every node.
+ *
+ * Set-up: the first call on each device looks up the work space's device
+ * address (cudaGetSymbolAddress), which may load the library's device code;
+ * make that first call before any stream capture begins on that device.
+ *
+ * Overlapping calls race: all calls on one device share the one work space, so
+ * a call must not start while another call's kernel may still run (on another
+ * stream or from another thread); two calls on the same stream are ordered.
+ *
+ * Returns MGPU_INVALID_VALUE / MGPU_UNSUPPORTED for bad arguments as
+ * mgpu_simulate does, MGPU_CUDA_ERROR if the launch fails. It does not update
+ * mgpu_last_error (setting the message could allocate host memory).
+ */
+#define MGPU_NOALLOC_SCRATCH_BYTES (4 * 1024 * 1024)
+int mgpu_simulate_final_noalloc(mgpu_context* ctx, int32_t num_groups, int32_t num_contact_matrices,
+                                int32_t num_damping_points, int32_t count, const double* params,
+                                const double* contact, const double* damping_times, const double* damping_values,
+                                const double* y0, double t0, double tmax, double dt0,
+                                const mgpu_integrator_opts* opts, double* y_out, int32_t* status);
+
+/*
  * Upload graphs and create their simulations: for every graph b,
  *   make_mobility_sim(t0, opts->dt_exchange, graph_b)
  * (cpp/memilio/mobility/metapopulation_mobility_instant.h:656-678) with each

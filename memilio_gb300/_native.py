@@ -29,7 +29,7 @@ PRECISION_MIXED = 2
 EXPORTED = ["mgpu_default_solver_opts", "mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_set_memory_budget",
             "mgpu_eval_rhs", "mgpu_simulate", "mgpu_batch_create", "mgpu_batch_advance", "mgpu_batch_get_state",
             "mgpu_batch_get_time", "mgpu_batch_set_state", "mgpu_batch_get_stats", "mgpu_batch_get_timing",
-            "mgpu_batch_device_bytes", "mgpu_batch_reset", "mgpu_batch_destroy"]
+            "mgpu_batch_device_bytes", "mgpu_batch_reset", "mgpu_batch_destroy", "mgpu_simulate_final_noalloc"]
 
 
 class MgpuSolverOpts(ctypes.Structure):
@@ -113,6 +113,10 @@ def lib():
     L.mgpu_batch_get_stats.argtypes = [vp, P(MgpuStats)]
     L.mgpu_batch_get_timing.argtypes = [vp, P(MgpuTiming)]
     L.mgpu_batch_reset.argtypes = [vp, d]
+    i32 = ctypes.c_int32
+    # device pointers are passed as integers (void*)
+    L.mgpu_simulate_final_noalloc.argtypes = [vp, i32, i32, i32, i32, vp, vp, vp, vp, vp, d, d, d,
+                                              P(MgpuIntegratorOpts), vp, vp]
     L.mgpu_batch_device_bytes.argtypes = [vp]
     L.mgpu_batch_device_bytes.restype = ctypes.c_int64
     L.mgpu_batch_destroy.argtypes = [vp]

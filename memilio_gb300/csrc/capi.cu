@@ -25,6 +25,16 @@ struct mgpu_context {
     int64_t allocated    = 0;
 };
 
+int mgpu::context_device_stream(const mgpu_context* ctx, int* device, cudaStream_t* stream)
+{
+    if (!ctx) {
+        return 1;
+    }
+    *device = ctx->device;
+    *stream = ctx->stream;
+    return 0;
+}
+
 namespace
 {
 

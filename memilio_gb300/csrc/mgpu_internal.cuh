@@ -470,6 +470,9 @@ int exchange_launches(bool has_edges);
 void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,
                              cudaStream_t s, int64_t* launches);
 int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings);
+
+// Device and stream of a context (for entry points defined outside capi.cu).
+int context_device_stream(const mgpu_context* ctx, int* device, cudaStream_t* stream);
 void launch_exchange_range(const BatchDev& B, int g0, int ng, int64_t n0, int64_t nn, int64_t e0, int64_t ne,
                            int64_t n_max, cudaStream_t s, int64_t* launches);
 void launch_phase_end(const BatchDev& B, cudaStream_t s);

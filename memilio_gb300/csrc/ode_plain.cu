@@ -10,6 +10,8 @@
 //   RKIntegratorCore::step               memilio/math/adapt_rk.h:217-298 (RKF45)
 #include "mgpu_internal.cuh"
 
+#include <mutex>
+
 namespace mgpu
 {
 namespace
@@ -393,3 +395,145 @@ void launch_eval_rhs(const BatchDev& B, const int32_t* d_nodes, int count, const
 }
 
 } // namespace mgpu
+
+// ---- allocation-free single-node simulate (mgpu_simulate_final_noalloc) ------
+// The stage vectors live in a fixed array of this file instead of a buffer
+// allocated per call; the kernel is k_simulate's integration (same device
+// functions, same compile flags) without the step recording.
+
+namespace mgpu
+{
+namespace
+{
+
+constexpr int64_t kNoallocScratchDoubles = MGPU_NOALLOC_SCRATCH_BYTES / (int64_t)sizeof(double);
+static __device__ __align__(256) double g_noalloc_scratch[kNoallocScratchDoubles];
+
+__global__ void k_simulate_final(BatchDev B, DevGraph g, int count, double t0, double tmax, double dt0,
+                                 double* y_out, int32_t* status)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) {
+        return;
+    }
+    const int n        = g.n;
+    NodeRhs f{node_model(B, g, k)};
+    const double* init = B.state + (int64_t)k * n;
+    double* y          = y_out + (int64_t)k * n;
+    if (y != init) {
+        for (int i = 0; i < n; ++i) {
+            y[i] = init[i];
+        }
+    }
+    Work w    = make_work(B, k, y, n);
+    DevOpts o = B.opts;
+    o.method  = g.method;
+    StepCounts c;
+    double t  = t0;
+    double dt = dt0;
+    int32_t st = 0;
+    if (tmax > t0 && !system_advance(f, w, n, tmax, t, dt, o, c, [](double, const SVec&) {})) {
+        st |= 1;
+    }
+    for (int i = 0; i < n; ++i) {
+        if (!isfinite(y[i])) {
+            st |= 2;
+            break;
+        }
+    }
+    status[k] = st;
+}
+
+// Device address of the work space, looked up once per device.
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_addr[kNoallocMaxDevices] = {};
+
+cudaError_t noalloc_scratch(int device, double** out)
+{
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[device]) {
+        void* p            = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            return e;
+        }
+        g_noalloc_addr[device] = static_cast<double*>(p);
+    }
+    *out = g_noalloc_addr[device];
+    return cudaSuccess;
+}
+
+} // namespace
+} // namespace mgpu
+
+extern "C" int mgpu_simulate_final_noalloc(mgpu_context* ctx, int32_t num_groups, int32_t num_contact_matrices,
+                                           int32_t num_damping_points, int32_t count, const double* params,
+                                           const double* contact, const double* damping_times,
+                                           const double* damping_values, const double* y0, double t0, double tmax,
+                                           double dt0, const mgpu_integrator_opts* opts, double* y_out,
+                                           int32_t* status)
+{
+    using namespace mgpu;
+    if (!ctx || !opts || count < 0 || num_groups < 1 || !(dt0 > 0)) {
+        return MGPU_INVALID_VALUE;
+    }
+    if (num_groups > MGPU_MAX_GROUPS || num_contact_matrices < 1 ||
+        num_contact_matrices > MGPU_MAX_CONTACT_MATRICES ||
+        (opts->method != MGPU_METHOD_CASH_KARP54 && opts->method != MGPU_METHOD_RKF45)) {
+        return MGPU_UNSUPPORTED;
+    }
+    if (num_damping_points < 0 || num_damping_points == 1) {
+        return MGPU_INVALID_VALUE;
+    }
+    if (count == 0) {
+        return MGPU_OK;
+    }
+    if (!params || !contact || !y0 || !y_out || !status ||
+        (num_damping_points > 0 && (!damping_times || !damping_values))) {
+        return MGPU_INVALID_VALUE;
+    }
+    const int n = num_groups * kC;
+    // 8 stage vectors of n doubles per node
+    if ((int64_t)8 * n * count > kNoallocScratchDoubles) {
+        return MGPU_OUT_OF_RANGE;
+    }
+    int device          = 0;
+    cudaStream_t stream = nullptr;
+    if (context_device_stream(ctx, &device, &stream) != 0 || device < 0 || device >= kNoallocMaxDevices) {
+        return MGPU_INVALID_VALUE;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) {
+        return MGPU_CUDA_ERROR;
+    }
+    double* scratch = nullptr;
+    if (noalloc_scratch(device, &scratch) != cudaSuccess) {
+        return MGPU_CUDA_ERROR;
+    }
+    DevGraph g{};
+    g.N      = count;
+    g.G      = num_groups;
+    g.M      = num_contact_matrices;
+    g.K      = num_damping_points;
+    g.n      = n;
+    g.method = opts->method;
+    BatchDev B{};
+    B.params         = params;
+    B.contact        = contact;
+    B.dtimes         = num_damping_points ? damping_times : nullptr;
+    B.dvals          = num_damping_points ? damping_values : nullptr;
+    B.state          = const_cast<double*>(y0); // read only
+    B.scratch        = scratch;
+    B.scratch_stride = count;
+    B.scratch_nmax   = n;
+    B.opts.abs_tol   = opts->abs_tol;
+    B.opts.rel_tol   = opts->rel_tol;
+    B.opts.dt_min    = opts->dt_min;
+    B.opts.dt_max    = opts->dt_max;
+    B.opts.max_steps = 100000;
+    B.opts.method    = opts->method;
+    const int threads = 64;
+    const int blocks  = (count + threads - 1) / threads;
+    k_simulate_final<<<blocks, threads, 0, stream>>>(B, g, count, t0, tmax, dt0, y_out, status);
+    return cudaGetLastError() == cudaSuccess ? MGPU_OK : MGPU_CUDA_ERROR;
+}
