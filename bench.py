@@ -41,6 +41,17 @@ def flops_per_attempt(G: int) -> float:
     return 6.0 * (6 * G * G + 90 * G + 10) + 55.0 * 10 * G
 
 
+def measured_peaks() -> dict:
+    """HBM copy rate measured on the GB300s (MEASURED_PEAKS.json beside
+    this file), else the stated fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            m = json.load(f)
+        return {"hbm_gbs": float(m["hbm_gbs"]), "source": "measured (MEASURED_PEAKS.json: STREAM-style copy)"}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6800.0, "source": "fallback 6.8 TB/s (no MEASURED_PEAKS.json)"}
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -155,12 +166,115 @@ def workload_config(args):
             "l2": "inputs larger than L2 (node parameters and states of the ensemble exceed 129 MB)"}
 
 
-def graph_bytes(g) -> int:
-    arrs = [g.params, g.contact_baseline, g.contact_minimum, g.damping_times, g.damping_values, g.init_state,
-            g.edge_src, g.edge_dst, g.edge_coeff_baseline, g.edge_damping_times, g.edge_damping_values]
-    if g.edge_coeff_minimum is not None:
-        arrs.append(g.edge_coeff_minimum)
-    return int(sum(a.nbytes for a in arrs))
+def uneven_leg(N, ctx, args):
+    """Uneven batch: graphs with log-uniform node counts in [1, 2000], 1-6 age
+    groups, horizons U[30, 180] days, out-degree U{0..50}, mixed precision, all
+    in one batch (one launch per age-group count and interval)."""
+    from memilio_gb300 import workloads as W
+    graphs, horizons = W.uneven_batch(num_graphs=args.uneven, seed=3)
+    nd = W.node_days(graphs, horizons)
+    b = N.Batch(ctx, graphs, 0.0, N.solver_opts(precision=N.PRECISION_MIXED))
+    tune = b.autotune()
+    b.advance(0.0, horizons)  # warm-up
+    ms = []
+    for _ in range(2):
+        b.reset(0.0)
+        b.advance(0.0, horizons)
+        ms.append(b.timing()["advance_ms"])
+    st = b.stats()
+    b.close()
+    return {"value": nd / (min(ms) / 1e3), "unit": UNIT, "graphs": len(graphs),
+            "nodes": int(sum(g.num_nodes for g in graphs)), "node_days": nd, "ms": min(ms),
+            "sequential_exchanges": st["sequential_exchanges"], "autotune": tune,
+            "workload": f"{len(graphs)} graphs, nodes logU[1,2000], groups U{{1..6}}, horizon U[30,180] d, "
+                        "out-degree U{0..50}, mixed precision"}
+
+
+def serving_leg(N, ctx, args):
+    """Serving: requests of the uneven distribution arriving Poisson at each rate
+    for a fixed window; continuous batching (mgpu_server_*); latency from
+    submission to completion; throughput = completed node-days / wall time."""
+    from memilio_gb300 import workloads as W
+    pool, horizons = W.uneven_batch(num_graphs=512, seed=11)
+    rng = np.random.default_rng(13)
+    # the plain per-request FP64 path on a few requests, one after another
+    pk = [i for i in range(len(pool)) if pool[i].num_nodes <= 400][:4]
+    p_ms, p_nd = 0.0, 0.0
+    for i in pk:
+        pb = N.Batch(ctx, [pool[i]], 0.0, N.solver_opts(precision=N.PRECISION_FP64_PLAIN))
+        pb.advance(float(horizons[i]))
+        p_ms += pb.timing()["advance_ms"]
+        p_nd += pool[i].num_nodes * horizons[i]
+        pb.close()
+    out = {"window_s": args.serve_seconds, "plain_fp64_per_request": {"value": p_nd / (p_ms / 1e3), "unit": UNIT,
+                                                                       "sample": f"{len(pk)} requests"},
+           "rates": []}
+    for lam in args.serve_rates:
+        srv = N.Server(ctx_device(ctx), N.server_opts(max_batches=16, phases_per_launch=2))
+        t_start = time.perf_counter()
+        next_t = t_start + rng.exponential(1.0 / lam)
+        submitted, nd_done, lat, k = {}, 0.0, [], 0
+        while True:
+            now = time.perf_counter()
+            while now >= next_t and now - t_start < args.serve_seconds:
+                i = k % len(pool)
+                k += 1
+                submitted[srv.submit(pool[i], 0.0, float(horizons[i]))] = i
+                next_t += rng.exponential(1.0 / lam)
+            srv.step()
+            while True:
+                t = srv.take()
+                if t is None:
+                    break
+                rid, _, l = t
+                i = submitted.pop(rid)
+                nd_done += pool[i].num_nodes * horizons[i]
+                lat.append(l)
+            if now - t_start >= args.serve_seconds and not submitted:
+                break
+            if now - t_start > args.serve_seconds + 120.0:
+                break  # drain limit
+        wall = time.perf_counter() - t_start
+        srv.close()
+        lat_ms = np.array(lat) * 1e3
+        out["rates"].append({"lambda_per_s": lam, "completed": len(lat), "unfinished": len(submitted),
+                             "p50_ms": float(np.percentile(lat_ms, 50)) if len(lat) else None,
+                             "p99_ms": float(np.percentile(lat_ms, 99)) if len(lat) else None,
+                             "node_days_per_s": nd_done / wall, "wall_s": wall})
+    return out
+
+
+def ctx_device(ctx) -> int:
+    import torch
+    return torch.cuda.current_device()
+
+
+def h2d_bytes(graphs) -> int:
+    """Bytes mgpu_batch_create copies to the device: every input array once
+    (arrays shared by several graphs of the batch are uploaded once)."""
+    seen, total = set(), 0
+    for g in graphs:
+        arrs = [g.params, g.contact_baseline, g.contact_minimum, g.damping_times, g.damping_values, g.init_state,
+                g.edge_src, g.edge_dst, g.edge_coeff_baseline, g.edge_damping_times, g.edge_damping_values]
+        if g.edge_coeff_minimum is not None:
+            arrs.append(g.edge_coeff_minimum)
+        for a in arrs:
+            key = (a.__array_interface__["data"][0], a.nbytes)
+            if a.nbytes and key not in seen:
+                seen.add(key)
+                total += a.nbytes
+    return int(total)
+
+
+# Algorithmic bytes per active (node, age group) item and launch of the mixed
+# exchange passes (float-float states: 80 B per state row read or written):
+#   return: state read + next-state write 160, own snapshot 40, factors 8,
+#           return-time rates 48  (snapshot rows of the sources and the
+#           ensemble-shared coefficients are counted once, as the own rows)
+#   depart: state read + write 160, departure state write 80, snapshot 40, factors 8
+#   prep:   departure state read 80, state hi read 40, rates write 48,
+#           snapshot write 40, factors write 8, constant table read 96
+BYTES_PER_ITEM = {"return": 256, "depart": 288, "prep": 312, "exact": 256}
 
 
 def main():
@@ -175,6 +289,10 @@ def main():
     ap.add_argument("--days", type=float, default=90.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--uneven", type=int, default=4096, help="graphs of the uneven-batch leg (0 = skip)")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window per rate (0 = skip)")
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 800.0])
     args = ap.parse_args()
 
     from memilio_gb300 import workloads as W
@@ -240,10 +358,11 @@ def main():
     attempts_step = (st1["accepted_steps"] + st1["rejected_steps"] - st0["accepted_steps"] - st0["rejected_steps"]) \
         / args.steps
 
-    # per-kernel device times (profile mode: events around the node-solve kernels)
+    # per-kernel device times (profile mode: events around the node solves and the exchange passes)
     prof = N.Batch(ctx, graphs, 0.0, N.solver_opts(precision=prec, profile=True))
     prof.advance(args.days)
     tm = prof.timing()
+    dev_bytes = prof.device_bytes()
     prof.close()
     ode_ms_launch = tm["ode_ms"] / max(tm["ode_launches"], 1)
     flops_launch = tm["attempts"] * flops_per_attempt(6) / max(tm["ode_launches"], 1)
@@ -264,24 +383,67 @@ def main():
                 "exchange_ms_per_step": tm["exchange_ms"], "ode_ms_per_step": tm["ode_ms"],
                 "algorithmic_flops_per_launch": flops_launch, "avg_launch_ms": ode_ms_launch}
     roofline["frac"] = roofline["achieved"] / roofline["peak"]
+    parts = {"ode": tm["ode_ms"], "prep": tm["prep_ms"], "return": tm["return_ms"], "exact": tm["exact_ms"],
+             "depart": tm["depart_ms"]}
+    roofline["parts_ms_per_step"] = parts
+    dominant = max(parts, key=parts.get)
+    if prec == N.PRECISION_MIXED and dominant in ("return", "depart", "prep", "exact"):
+        # the exchange pass that dominates the step, against the measured HBM copy rate
+        peaks = measured_peaks()
+        items = sum(g.num_nodes * g.num_groups for g in graphs)
+        launches_active = args.days / 0.5 / (2 if dominant in ("return", "depart", "exact") else 1)
+        if dominant == "exact":
+            items = exchange_stats["scan_items"] / launches_active  # scanned (node, group) items per return
+        bytes_launch = items * BYTES_PER_ITEM[dominant]
+        ms_launch = parts[dominant] / launches_active
+        ach = bytes_launch / (ms_launch / 1e3) / 1e9
+        roofline = dict(roofline, bound="hbm", kernel={"return": "k_xf_return", "depart": "k_xf_depart",
+                                                      "prep": "k_xf_prep", "exact": "k_xf_scan"}[dominant],
+                        achieved=ach, unit="GB/s", peak=peaks["hbm_gbs"], peak_source=peaks["source"],
+                        frac=ach / peaks["hbm_gbs"], algorithmic_bytes_per_launch=bytes_launch,
+                        avg_launch_ms=ms_launch, ode_roofline={"bound": "fp32", "achieved_tflops": achieved,
+                                                               "peak_tflops": fp32_peak,
+                                                               "frac": achieved / fp32_peak})
+    roofline["dominant_part"] = dominant
 
     # end to end through the C ABI from host buffers
     e2e = None
     if not args.no_e2e:
-        h2d = sum(graph_bytes(g) for g in graphs)
+        h2d = h2d_bytes(graphs)
         d2h = batch.total * 8
-        e2e_t = []
+        e2e_t, parts_t = [], []
         for k in range(2):
             t0 = time.perf_counter()
             b2 = N.Batch(ctx, graphs, 0.0, N.solver_opts(precision=prec))
+            t1 = time.perf_counter()
             b2.advance(args.days)
+            t2 = time.perf_counter()
             out = b2.state_flat()
+            t3 = time.perf_counter()
             b2.close()
             e2e_t.append(time.perf_counter() - t0)
+            parts_t.append({"create_s": t1 - t0, "advance_s": t2 - t1, "d2h_s": t3 - t2})
+        best = int(np.argmin(e2e_t))
         e2e = {"value": world * nd_step / min(e2e_t), "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h}
+               "d2h_bytes_per_step": d2h, "parts": parts_t[best]}
         assert np.array_equal(out, final)
     batch.close()
+
+    # the plain per-graph FP64 drop-in on a sample of the same ensemble (graphs
+    # run one after another, so its rate does not depend on the sample size)
+    plain = None
+    if rank == 0 and not args.no_plain and prec != N.PRECISION_FP64_PLAIN:
+        k = min(2, len(graphs))
+        pb = N.Batch(ctx, graphs[:k], 0.0, N.solver_opts(precision=N.PRECISION_FP64_PLAIN))
+        pb.advance(args.days)
+        p_ms = pb.timing()["advance_ms"]
+        pb.close()
+        p_val = k * args.nodes * args.days / (p_ms / 1e3)
+        plain = {"value": p_val, "unit": UNIT, "sample": f"{k} samples x {args.nodes} nodes x {args.days:g} days",
+                 "speedup_of_value": value / world / p_val}
+
+    uneven = uneven_leg(N, ctx, args) if rank == 0 and args.uneven > 0 else None
+    serving = serving_leg(N, ctx, args) if rank == 0 and args.serve_seconds > 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -299,7 +461,8 @@ def main():
             "data": "synthetic (seeded)", "config": workload_config(args), "clocks": clocks,
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
             "attempts_per_node_day": attempts_step / nd_step, "wall_s_timed": t_wall,
-            "exchange_per_step": exchange_stats,
+            "exchange_per_step": exchange_stats, "plain_fp64": plain, "device_bytes": dev_bytes,
+            "uneven_batch": uneven, "serving": serving,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

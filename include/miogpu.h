@@ -66,6 +66,11 @@ typedef struct mgpu_timing {
     double exchange_ms;     /* exchanges incl. interval bookkeeping (profile mode only) */
     int64_t ode_launches;   /* node-solve kernel launches timed in ode_ms */
     int64_t attempts;       /* integrator attempts (accepted + rejected) during the advance */
+    /* parts of exchange_ms, batched solvers in profile mode only: */
+    double prep_ms;         /* per-node pass (snapshots, factors, return-time rates) */
+    double return_ms;       /* return pass with the no-underflow bound */
+    double exact_ms;        /* exact underflow path and commit */
+    double depart_ms;       /* departure pass and interval bookkeeping */
 } mgpu_timing;
 
 typedef struct mgpu_stats {
@@ -114,6 +119,16 @@ int mgpu_eval_rhs(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, con
 int mgpu_simulate(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, const int32_t* nodes, double t0,
                   double tmax, double dt0, const mgpu_integrator_opts* opts, int32_t max_points, double* out_t,
                   double* out_y, int32_t* num_points);
+
+/*
+ * mgpu_simulate with a step size that persists across calls, as
+ * Simulation::advance keeps it (cpp/memilio/compartments/simulation_base.h:86-168,
+ * cpp/memilio/math/integrator.h:184-249): dt [count] holds each node's initial
+ * step on entry and the integrator's next step (Simulation::get_dt) on return.
+ */
+int mgpu_simulate_dt(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, const int32_t* nodes, double t0,
+                     double tmax, double* dt, const mgpu_integrator_opts* opts, int32_t max_points, double* out_t,
+                     double* out_y, int32_t* num_points);
 
 /*
  * Allocation-free variant of mgpu_simulate for callers that must not allocate
@@ -203,12 +218,78 @@ int mgpu_batch_get_time(mgpu_batch* batch, double* out);
 /* Replace the node states (e.g. after a host-side intervention) [sum_b N_b][10 G_b]. */
 int mgpu_batch_set_state(mgpu_batch* batch, const double* state);
 int mgpu_batch_get_stats(mgpu_batch* batch, mgpu_stats* out);
+/*
+ * Asynchronous advance, for request loops that keep several batches in flight
+ * (one context, i.e. one stream, per batch): enqueue at most max_phases exchange
+ * intervals towards tmax (or tmax_per_graph) and return without waiting;
+ * *remaining = intervals still to launch. The horizon is fixed by the first
+ * call after creation or after the previous advance finished. Batched
+ * precisions only (MGPU_UNSUPPORTED for MGPU_PRECISION_FP64_PLAIN).
+ */
+int mgpu_batch_launch(mgpu_batch* batch, double tmax, const double* tmax_per_graph, int32_t max_phases,
+                      int32_t* remaining);
+/* Non-blocking: *done = 1 once the launched intervals have finished on the
+ * device. When no interval remains, this also completes the advance (graph
+ * times updated) and reports device-side errors as its status. */
+int mgpu_batch_query(mgpu_batch* batch, int32_t* done);
+/* Node states of one graph of the batch ([N][10G] doubles), waiting for the stream. */
+int mgpu_batch_get_graph_state(mgpu_batch* batch, int32_t graph, double* out);
+/* Autotuner of the batched solver's schedule: for every age-group count of
+ * the batch, times one exchange interval of the node solves for each candidate
+ * (32, 64 or 128 threads per block; one slot per lane or a persistent grid of
+ * 2, 3, 4 or 6 blocks per SM) on a copy of the current state, restores the state
+ * and keeps the fastest. Reports the choice for the largest instance list. */
+int mgpu_batch_autotune(mgpu_batch* batch, int32_t* instances_per_block, int32_t* grid_blocks);
+/* Upper estimate of the device bytes mgpu_batch_create would allocate for these
+ * graphs (admission control); -1 for invalid arguments. */
+int64_t mgpu_batch_estimate_bytes(const mgpu_graph* graphs, int32_t num_graphs, const mgpu_solver_opts* opts);
+
 /* Event-measured device times of the last advance (no reference counterpart:
  * replaces the reference's wall-clock timers, cpp/memilio/timer/auto_timer.h). */
 int mgpu_batch_get_timing(mgpu_batch* batch, mgpu_timing* out);
 /* Device bytes held by the batch. */
 int64_t mgpu_batch_device_bytes(const mgpu_batch* batch);
 void mgpu_batch_destroy(mgpu_batch* batch);
+
+/*
+ * Serving: a device-resident request loop with continuous batching (no
+ * counterpart in the reference, which runs one simulation per call).
+ *
+ * mgpu_server_submit queues a solve of one graph from t0 to tmax; the graph's
+ * host arrays must stay valid until the request has been taken.
+ * mgpu_server_step runs one scheduling round without waiting for the device:
+ * running batches whose launched exchange intervals have finished get their
+ * next intervals enqueued (each batch on its own stream, so batches admitted
+ * at different times overlap on the device); a request completes as soon as
+ * the intervals up to its own horizon have finished; a batch whose requests
+ * have all completed releases its device memory; then the queued requests
+ * that fit into the memory budget are admitted as a new batch (one batch per
+ * start time). mgpu_server_take hands out one completed request: its id, its
+ * final node states ([N][10G] doubles, N and G of its graph), the time from
+ * submission to completion, and its status as the return value (*request_id = 0
+ * when none is ready). With final_state = NULL it only reports the next ready
+ * request's id and value count and keeps it ready.
+ */
+typedef struct mgpu_server mgpu_server;
+typedef struct mgpu_server_opts {
+    mgpu_solver_opts solver;       /* batched precision; default mixed */
+    int64_t memory_budget;         /* bytes the server may hold; 0 = 90% of the free HBM at creation */
+    int32_t max_batches;           /* batches (streams) in flight, default 16 */
+    int32_t phases_per_launch;     /* exchange intervals enqueued per batch and round, default 2 */
+    int32_t max_graphs_per_batch;  /* default 4096 */
+    int32_t reserved;
+} mgpu_server_opts;
+
+void mgpu_default_server_opts(mgpu_server_opts* opts);
+int mgpu_server_create(int device, const mgpu_server_opts* opts, mgpu_server** out);
+void mgpu_server_destroy(mgpu_server* server);
+int mgpu_server_submit(mgpu_server* server, const mgpu_graph* graph, double t0, double tmax, int64_t* request_id);
+int mgpu_server_step(mgpu_server* server, int32_t* completed, int32_t* running, int32_t* queued);
+int mgpu_server_take(mgpu_server* server, int64_t* request_id, double* final_state, int64_t capacity,
+                     int64_t* count, double* latency_s);
+/* Device bytes held by running batches, and their number. */
+int64_t mgpu_server_memory_in_use(const mgpu_server* server);
+int32_t mgpu_server_num_batches(const mgpu_server* server);
 
 #ifdef __cplusplus
 }

@@ -29,7 +29,10 @@ PRECISION_MIXED = 2
 EXPORTED = ["mgpu_default_solver_opts", "mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_set_memory_budget",
             "mgpu_eval_rhs", "mgpu_simulate", "mgpu_batch_create", "mgpu_batch_advance", "mgpu_batch_get_state",
             "mgpu_batch_get_time", "mgpu_batch_set_state", "mgpu_batch_get_stats", "mgpu_batch_get_timing",
-            "mgpu_batch_device_bytes", "mgpu_batch_reset", "mgpu_batch_destroy", "mgpu_simulate_final_noalloc"]
+            "mgpu_batch_device_bytes", "mgpu_batch_reset", "mgpu_batch_destroy", "mgpu_simulate_final_noalloc",
+            "mgpu_batch_launch", "mgpu_batch_query", "mgpu_batch_autotune", "mgpu_simulate_dt", "mgpu_batch_get_graph_state", "mgpu_batch_estimate_bytes",
+            "mgpu_default_server_opts", "mgpu_server_create", "mgpu_server_destroy", "mgpu_server_submit",
+            "mgpu_server_step", "mgpu_server_take", "mgpu_server_memory_in_use", "mgpu_server_num_batches"]
 
 
 class MgpuSolverOpts(ctypes.Structure):
@@ -45,6 +48,17 @@ class MgpuSolverOpts(ctypes.Structure):
     ]
 
 
+class MgpuServerOpts(ctypes.Structure):
+    _fields_ = [
+        ("solver", MgpuSolverOpts),
+        ("memory_budget", ctypes.c_int64),
+        ("max_batches", ctypes.c_int32),
+        ("phases_per_launch", ctypes.c_int32),
+        ("max_graphs_per_batch", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
 class MgpuTiming(ctypes.Structure):
     _fields_ = [
         ("advance_ms", ctypes.c_double),
@@ -52,6 +66,10 @@ class MgpuTiming(ctypes.Structure):
         ("exchange_ms", ctypes.c_double),
         ("ode_launches", ctypes.c_int64),
         ("attempts", ctypes.c_int64),
+        ("prep_ms", ctypes.c_double),
+        ("return_ms", ctypes.c_double),
+        ("exact_ms", ctypes.c_double),
+        ("depart_ms", ctypes.c_double),
     ]
 
     def as_dict(self):
@@ -105,6 +123,8 @@ def lib():
     L.mgpu_eval_rhs.argtypes = [vp, P(MgpuGraph), ctypes.c_int32, P(ctypes.c_int32), P(d), P(d), P(d), P(d)]
     L.mgpu_simulate.argtypes = [vp, P(MgpuGraph), ctypes.c_int32, P(ctypes.c_int32), d, d, d,
                                 P(MgpuIntegratorOpts), ctypes.c_int32, P(d), P(d), P(ctypes.c_int32)]
+    L.mgpu_simulate_dt.argtypes = [vp, P(MgpuGraph), ctypes.c_int32, P(ctypes.c_int32), d, d, P(d),
+                                P(MgpuIntegratorOpts), ctypes.c_int32, P(d), P(d), P(ctypes.c_int32)]
     L.mgpu_batch_create.argtypes = [vp, P(MgpuGraph), ctypes.c_int32, d, P(MgpuSolverOpts), P(vp)]
     L.mgpu_batch_advance.argtypes = [vp, d, P(d)]
     L.mgpu_batch_get_state.argtypes = [vp, P(d)]
@@ -117,6 +137,24 @@ def lib():
     # device pointers are passed as integers (void*)
     L.mgpu_simulate_final_noalloc.argtypes = [vp, i32, i32, i32, i32, vp, vp, vp, vp, vp, d, d, d,
                                               P(MgpuIntegratorOpts), vp, vp]
+    L.mgpu_batch_launch.argtypes = [vp, d, P(d), i32, P(i32)]
+    L.mgpu_batch_query.argtypes = [vp, P(i32)]
+    L.mgpu_batch_autotune.argtypes = [vp, P(i32), P(i32)]
+    L.mgpu_batch_get_graph_state.argtypes = [vp, i32, P(d)]
+    L.mgpu_batch_estimate_bytes.argtypes = [P(MgpuGraph), i32, P(MgpuSolverOpts)]
+    L.mgpu_batch_estimate_bytes.restype = ctypes.c_int64
+    L.mgpu_default_server_opts.argtypes = [P(MgpuServerOpts)]
+    L.mgpu_default_server_opts.restype = None
+    L.mgpu_server_create.argtypes = [ctypes.c_int, P(MgpuServerOpts), P(vp)]
+    L.mgpu_server_destroy.argtypes = [vp]
+    L.mgpu_server_destroy.restype = None
+    L.mgpu_server_submit.argtypes = [vp, P(MgpuGraph), d, d, P(ctypes.c_int64)]
+    L.mgpu_server_step.argtypes = [vp, P(i32), P(i32), P(i32)]
+    L.mgpu_server_take.argtypes = [vp, P(ctypes.c_int64), P(d), ctypes.c_int64, P(ctypes.c_int64), P(d)]
+    L.mgpu_server_memory_in_use.argtypes = [vp]
+    L.mgpu_server_memory_in_use.restype = ctypes.c_int64
+    L.mgpu_server_num_batches.argtypes = [vp]
+    L.mgpu_server_num_batches.restype = ctypes.c_int32
     L.mgpu_batch_device_bytes.argtypes = [vp]
     L.mgpu_batch_device_bytes.restype = ctypes.c_int64
     L.mgpu_batch_destroy.argtypes = [vp]
@@ -272,6 +310,89 @@ class Batch:
     def close(self):
         if self._h:
             lib().mgpu_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def autotune(self) -> dict:
+        ipb, grid = ctypes.c_int32(), ctypes.c_int32()
+        self.ctx.check(lib().mgpu_batch_autotune(self._h, ctypes.byref(ipb), ctypes.byref(grid)))
+        return {"instances_per_block": ipb.value, "grid_blocks": grid.value}
+
+    def graph_state(self, graph: int) -> np.ndarray:
+        g = self.graphs[graph]
+        out = np.empty(g.num_nodes * g.n)
+        self.ctx.check(lib().mgpu_batch_get_graph_state(self._h, int(graph), _dp(out)))
+        return out.reshape(g.num_nodes, g.n)
+
+
+def server_opts(precision=PRECISION_MIXED, memory_budget=0, max_batches=16, phases_per_launch=2,
+                max_graphs_per_batch=4096, **solver_kw) -> MgpuServerOpts:
+    o = MgpuServerOpts()
+    lib().mgpu_default_server_opts(ctypes.byref(o))
+    o.solver = solver_opts(precision=precision, **solver_kw)
+    o.memory_budget = int(memory_budget)
+    o.max_batches = int(max_batches)
+    o.phases_per_launch = int(phases_per_launch)
+    o.max_graphs_per_batch = int(max_graphs_per_batch)
+    return o
+
+
+class Server:
+    """mgpu_server: device-resident request loop with continuous batching."""
+
+    def __init__(self, device: int = 0, opts: MgpuServerOpts = None):
+        self._h = ctypes.c_void_p()
+        rc = lib().mgpu_server_create(device, ctypes.byref(opts or server_opts()), ctypes.byref(self._h))
+        if rc != OK:
+            raise MgpuError(rc, "mgpu_server_create failed")
+        self._graphs = {}  # request id -> graph (keeps the host arrays alive)
+
+    def submit(self, g: GraphArrays, t0: float, tmax: float) -> int:
+        rid = ctypes.c_int64()
+        rc = lib().mgpu_server_submit(self._h, ctypes.byref(g.as_ctypes()), float(t0), float(tmax),
+                                      ctypes.byref(rid))
+        if rc != OK:
+            raise MgpuError(rc, "mgpu_server_submit failed")
+        self._graphs[rid.value] = g
+        return rid.value
+
+    def step(self):
+        c, r, q = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        rc = lib().mgpu_server_step(self._h, ctypes.byref(c), ctypes.byref(r), ctypes.byref(q))
+        if rc != OK:
+            raise MgpuError(rc, "mgpu_server_step failed")
+        return c.value, r.value, q.value
+
+    def take(self):
+        """(request id, final states [N, 10G], latency s) of one completed request, or None."""
+        rid, cnt, lat = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
+        rc = lib().mgpu_server_take(self._h, ctypes.byref(rid), ctypes.POINTER(ctypes.c_double)(), 0,
+                                    ctypes.byref(cnt), ctypes.byref(lat))
+        if rid.value == 0 and rc == OK:
+            return None
+        g = self._graphs[rid.value] if rid.value in self._graphs else None
+        out = np.empty(max(cnt.value, 1))
+        rc = lib().mgpu_server_take(self._h, ctypes.byref(rid), _dp(out), out.shape[0], ctypes.byref(cnt),
+                                    ctypes.byref(lat))
+        g = self._graphs.pop(rid.value)
+        if rc != OK:
+            raise MgpuError(rc, f"request {rid.value} failed")
+        return rid.value, out[:cnt.value].reshape(g.num_nodes, g.n), lat.value
+
+    def memory_in_use(self) -> int:
+        return int(lib().mgpu_server_memory_in_use(self._h))
+
+    def num_batches(self) -> int:
+        return int(lib().mgpu_server_num_batches(self._h))
+
+    def close(self):
+        if self._h:
+            lib().mgpu_server_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

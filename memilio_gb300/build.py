@@ -19,7 +19,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIB_DIR, "libmiogpu.so")
 
-SOURCES = ["capi.cu", "ode_plain.cu", "ode_batched.cu", "exchange.cu", "exchange_batched.cu"]
+SOURCES = ["capi.cu", "ode_plain.cu", "ode_batched.cu", "exchange.cu", "exchange_batched.cu", "serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "--expt-relaxed-constexpr"]
@@ -90,5 +90,43 @@ def build(verbose: bool = False) -> str:
     return LIB
 
 
+FACADE = os.path.join(HERE, "cpp")
+FACADE_BIN = os.path.join(FACADE, "bin")
+FACADE_PROGRAMS = {"facade_check": "tests/facade_check.cpp", "ode_secir_graph": "examples/ode_secir_graph.cpp"}
+
+
+def build_facade(verbose: bool = False) -> dict:
+    """Compile the C++ facade's test driver and example against libmiogpu.so
+    (host compiler, C++17). Returns {name: path}."""
+    lib = build(verbose)
+    os.makedirs(FACADE_BIN, exist_ok=True)
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "c++"
+    headers = sorted(os.path.join(FACADE, "miogpu", f) for f in os.listdir(os.path.join(FACADE, "miogpu")))
+    out = {}
+
+    def one(item):
+        name, src = item
+        exe = os.path.join(FACADE_BIN, name)
+        deps = [os.path.join(FACADE, src), lib, os.path.join(ROOT, "include", "miogpu.h")] + headers
+        if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(d) for d in deps):
+            return name, exe
+        cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"), "-I", FACADE,
+               os.path.join(FACADE, src), "-o", exe + ".tmp", "-L", os.path.dirname(lib), "-lmiogpu",
+               "-Wl,-rpath," + os.path.dirname(lib)]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"facade build failed on {src}:\n{r.stdout}\n{r.stderr}")
+        os.replace(exe + ".tmp", exe)
+        return name, exe
+
+    with cf.ThreadPoolExecutor(max_workers=len(FACADE_PROGRAMS)) as ex:
+        for name, exe in ex.map(one, FACADE_PROGRAMS.items()):
+            out[name] = exe
+    return out
+
+
 if __name__ == "__main__":
     print(build(verbose=True))
+    print(build_facade(verbose=True))

@@ -1,0 +1,586 @@
+/*
+ * miogpu/mobility.h — the metapopulation graph with the API of MEmilio's
+ * mio::Graph (cpp/memilio/mobility/graph.h:144-303), SimulationNode and
+ * MobilityEdge (metapopulation_mobility_instant.h:39-101,106-290,300-623),
+ * make_mobility_sim / GraphSimulation (:656-678, graph_simulation.h:63-120)
+ * and ParameterStudy (cpp/memilio/compartments/parameter_studies.h:47-374),
+ * computing on the GPU through libmiogpu's batches:
+ *
+ *   GraphSimulation::advance -> mgpu_batch_advance (one batch per graph)
+ *   ParameterStudy::run      -> every sampled graph in one batch
+ *
+ * Node results are recorded at every exchange boundary (every dt of the
+ * graph simulation), not at every accepted integrator step.
+ */
+#ifndef MIOGPU_FACADE_MOBILITY_H
+#define MIOGPU_FACADE_MOBILITY_H
+
+#include "osecir.h"
+
+#include <functional>
+
+namespace miogpu
+{
+
+template <class NodePropertyT>
+struct Node {
+    template <class... Args>
+    Node(int node_id, Args&&... args)
+        : id(node_id)
+        , property(std::forward<Args>(args)...)
+    {
+    }
+    int id;
+    NodePropertyT property;
+};
+
+template <class EdgePropertyT>
+struct Edge {
+    template <class... Args>
+    Edge(size_t start, size_t end, Args&&... args)
+        : start_node_idx(start)
+        , end_node_idx(end)
+        , property(std::forward<Args>(args)...)
+    {
+    }
+    size_t start_node_idx;
+    size_t end_node_idx;
+    EdgePropertyT property;
+};
+
+/* mio::Graph: nodes in insertion order, edges kept sorted by (start, end);
+ * adding an edge that exists replaces its property (graph.h:216-241). */
+template <class NodePropertyT, class EdgePropertyT>
+class Graph
+{
+public:
+    using NodeProperty = NodePropertyT;
+    using EdgeProperty = EdgePropertyT;
+
+    template <class... Args>
+    Node<NodePropertyT>& add_node(int id, Args&&... args)
+    {
+        m_nodes.emplace_back(id, std::forward<Args>(args)...);
+        return m_nodes.back();
+    }
+    template <class... Args>
+    Edge<EdgePropertyT>& add_edge(size_t start, size_t end, Args&&... args)
+    {
+        if (start >= m_nodes.size() || end >= m_nodes.size()) {
+            throw std::out_of_range("edge node index out of range");
+        }
+        Edge<EdgePropertyT> e(start, end, std::forward<Args>(args)...);
+        auto it = std::lower_bound(m_edges.begin(), m_edges.end(), e, [](const auto& a, const auto& b) {
+            return std::make_pair(a.start_node_idx, a.end_node_idx) < std::make_pair(b.start_node_idx, b.end_node_idx);
+        });
+        if (it != m_edges.end() && it->start_node_idx == start && it->end_node_idx == end) {
+            *it = std::move(e);
+            return *it;
+        }
+        return *m_edges.insert(it, std::move(e));
+    }
+    std::vector<Node<NodePropertyT>>& nodes()
+    {
+        return m_nodes;
+    }
+    const std::vector<Node<NodePropertyT>>& nodes() const
+    {
+        return m_nodes;
+    }
+    std::vector<Edge<EdgePropertyT>>& edges()
+    {
+        return m_edges;
+    }
+    const std::vector<Edge<EdgePropertyT>>& edges() const
+    {
+        return m_edges;
+    }
+
+private:
+    std::vector<Node<NodePropertyT>> m_nodes;
+    std::vector<Edge<EdgePropertyT>> m_edges;
+};
+
+/* Mobility coefficients of one edge: a vector over the 10G compartments with
+ * baseline, minimum and dampings (MobilityCoefficientGroup with one matrix). */
+class MobilityCoefficientGroup
+{
+public:
+    MobilityCoefficientGroup(size_t num_matrices = 1, size_t n = 0)
+        : m_coeffs(n, 1)
+    {
+        if (num_matrices != 1) {
+            throw Error(MGPU_UNSUPPORTED, "one mobility coefficient matrix per edge");
+        }
+    }
+    DampingMatrixExpression& operator[](size_t i)
+    {
+        if (i != 0) {
+            throw std::out_of_range("one mobility coefficient matrix per edge");
+        }
+        return m_coeffs;
+    }
+    const DampingMatrixExpression& operator[](size_t i) const
+    {
+        return const_cast<MobilityCoefficientGroup*>(this)->operator[](i);
+    }
+    size_t get_num_matrices() const
+    {
+        return 1;
+    }
+
+private:
+    DampingMatrixExpression m_coeffs;
+};
+
+/* mio::MobilityParameters (:106-290). */
+template <typename FP = double>
+class MobilityParameters
+{
+public:
+    explicit MobilityParameters(const std::vector<FP>& coeffs)
+        : m_coeffs(1, coeffs.size())
+    {
+        std::copy(coeffs.begin(), coeffs.end(), m_coeffs[0].get_baseline().data());
+    }
+    explicit MobilityParameters(const MobilityCoefficientGroup& coeffs)
+        : m_coeffs(coeffs)
+    {
+    }
+    MobilityCoefficientGroup& get_coefficients()
+    {
+        return m_coeffs;
+    }
+    const MobilityCoefficientGroup& get_coefficients() const
+    {
+        return m_coeffs;
+    }
+
+private:
+    MobilityCoefficientGroup m_coeffs;
+};
+
+/* mio::MobilityEdge (:300-623): the edge property of a simulation graph. */
+template <typename FP = double>
+class MobilityEdge
+{
+public:
+    explicit MobilityEdge(const MobilityParameters<FP>& params)
+        : m_params(params)
+    {
+    }
+    explicit MobilityEdge(const std::vector<FP>& coeffs)
+        : m_params(coeffs)
+    {
+    }
+    const MobilityParameters<FP>& get_parameters() const
+    {
+        return m_params;
+    }
+
+private:
+    MobilityParameters<FP> m_params;
+};
+
+/* mio::SimulationNode (:39-101): a node's simulation and its results. */
+template <class Sim>
+class SimulationNode
+{
+public:
+    template <class... Args>
+    SimulationNode(Args&&... args)
+        : m_simulation(std::forward<Args>(args)...)
+        , m_last_state(m_simulation.get_result().get_last_value())
+    {
+    }
+    Sim& get_simulation()
+    {
+        return m_simulation;
+    }
+    const Sim& get_simulation() const
+    {
+        return m_simulation;
+    }
+    decltype(auto) get_result()
+    {
+        return m_simulation.get_result();
+    }
+    decltype(auto) get_result() const
+    {
+        return m_simulation.get_result();
+    }
+    const std::vector<double>& get_last_state() const
+    {
+        return m_last_state;
+    }
+    void set_last_state(const double* v)
+    {
+        m_last_state.assign(v, v + m_last_state.size());
+    }
+
+private:
+    Sim m_simulation;
+    std::vector<double> m_last_state;
+};
+
+namespace detail
+{
+
+/* The arrays of one graph in the layout of include/miogpu_layout.h. */
+struct GraphArrays {
+    int N = 0, G = 0, E = 0, M = 0, K = 0, Ke = 0;
+    std::vector<double> params, contact_baseline, contact_minimum, damping_times, damping_values, state;
+    std::vector<int32_t> src, dst;
+    std::vector<double> coeff_baseline, coeff_minimum, edge_damping_times, edge_damping_values;
+
+    mgpu_graph view() const
+    {
+        mgpu_graph g{};
+        g.num_nodes               = N;
+        g.num_groups              = G;
+        g.num_edges               = E;
+        g.num_contact_matrices    = M;
+        g.num_damping_points      = K;
+        g.num_edge_damping_points = Ke;
+        g.params                  = params.data();
+        g.contact_baseline        = contact_baseline.data();
+        g.contact_minimum         = contact_minimum.data();
+        g.damping_times           = K ? damping_times.data() : nullptr;
+        g.damping_values          = K ? damping_values.data() : nullptr;
+        g.init_state              = state.data();
+        g.edge_src                = E ? src.data() : nullptr;
+        g.edge_dst                = E ? dst.data() : nullptr;
+        g.edge_coeff_baseline     = E ? coeff_baseline.data() : nullptr;
+        g.edge_coeff_minimum      = E ? coeff_minimum.data() : nullptr;
+        g.edge_damping_times      = Ke ? edge_damping_times.data() : nullptr;
+        g.edge_damping_values     = Ke ? edge_damping_values.data() : nullptr;
+        return g;
+    }
+};
+
+/* Packs models (one per node, with its current state) and edge coefficients. */
+template <class ModelT, class EdgeT>
+GraphArrays pack_graph(const std::vector<const ModelT*>& models, const std::vector<const std::vector<double>*>& states,
+                       const std::vector<Edge<EdgeT>>& edges, std::function<const MobilityParameters<double>&(const EdgeT&)> params_of)
+{
+    GraphArrays a;
+    a.N = (int)models.size();
+    if (a.N == 0) {
+        throw Error(MGPU_INVALID_VALUE, "graph without nodes");
+    }
+    a.G = (int)models[0]->num_groups();
+    std::vector<osecir::NodeRecord> recs;
+    int K = 0;
+    for (size_t v = 0; v < models.size(); ++v) {
+        if ((int)models[v]->num_groups() != a.G) {
+            throw Error(MGPU_INVALID_VALUE, "all nodes of a graph need the same number of age groups");
+        }
+        recs.push_back(models[v]->pack(states[v]));
+        K = std::max(K, recs.back().K);
+    }
+    a.M = recs[0].M;
+    a.K = K;
+    const size_t GG = (size_t)a.G * a.G;
+    for (auto& r : recs) {
+        if (r.M != a.M) {
+            throw Error(MGPU_INVALID_VALUE, "all nodes of a graph need the same number of contact matrices");
+        }
+        a.params.insert(a.params.end(), r.params.begin(), r.params.end());
+        a.contact_baseline.insert(a.contact_baseline.end(), r.contact_baseline.begin(), r.contact_baseline.end());
+        a.contact_minimum.insert(a.contact_minimum.end(), r.contact_minimum.begin(), r.contact_minimum.end());
+        a.state.insert(a.state.end(), r.state.begin(), r.state.end());
+        if (K > 0) {
+            // pad every matrix's cache to K points (DBL_MAX times repeating the last matrix)
+            for (int m = 0; m < r.M; ++m) {
+                for (int k = 0; k < K; ++k) {
+                    if (k < r.K) {
+                        a.damping_times.push_back(r.damping_times[(size_t)(m * r.K + k)]);
+                        a.damping_values.insert(a.damping_values.end(),
+                                                r.damping_values.begin() + (long)(((size_t)m * r.K + k) * GG),
+                                                r.damping_values.begin() + (long)(((size_t)m * r.K + k + 1) * GG));
+                    }
+                    else if (r.K == 0) {
+                        // no dampings: a zero cache
+                        a.damping_times.push_back(k == 0 ? std::numeric_limits<double>::lowest()
+                                                         : std::numeric_limits<double>::max());
+                        a.damping_values.insert(a.damping_values.end(), GG, 0.0);
+                    }
+                    else {
+                        a.damping_times.push_back(std::numeric_limits<double>::max());
+                        a.damping_values.insert(a.damping_values.end(),
+                                                r.damping_values.begin() + (long)(((size_t)m * r.K + r.K - 1) * GG),
+                                                r.damping_values.begin() + (long)(((size_t)m * r.K + r.K) * GG));
+                    }
+                }
+            }
+        }
+    }
+    const size_t n = (size_t)a.G * osecir::num_compartments;
+    a.E            = (int)edges.size();
+    std::vector<const DampingMatrixExpression*> ecs;
+    for (auto& e : edges) {
+        const auto& c = params_of(e.property).get_coefficients()[0];
+        if (c.get_baseline().size() != n) {
+            throw Error(MGPU_INVALID_VALUE, "edge coefficients need 10 G entries");
+        }
+        a.src.push_back((int32_t)e.start_node_idx);
+        a.dst.push_back((int32_t)e.end_node_idx);
+        a.coeff_baseline.insert(a.coeff_baseline.end(), c.get_baseline().data(), c.get_baseline().data() + n);
+        a.coeff_minimum.insert(a.coeff_minimum.end(), c.get_minimum().data(), c.get_minimum().data() + n);
+        ecs.push_back(&c);
+    }
+    a.Ke = edges.empty() ? 0 : flatten_damping_caches(ecs, a.edge_damping_times, a.edge_damping_values);
+    return a;
+}
+
+} // namespace detail
+
+/* mio::GraphSimulation over a graph of SimulationNode<Simulation> and
+ * MobilityEdge (graph_simulation.h:63-120). */
+template <class GraphT>
+class GraphSimulation
+{
+public:
+    GraphSimulation(double t0, double dt, GraphT&& graph)
+        : m_t(t0)
+        , m_dt(dt)
+        , m_graph(std::move(graph))
+    {
+    }
+    GraphSimulation(GraphSimulation&&)            = default;
+    GraphSimulation& operator=(GraphSimulation&&) = default;
+    ~GraphSimulation()
+    {
+        if (m_batch) {
+            mgpu_batch_destroy(m_batch);
+        }
+    }
+
+    /* MGPU_PRECISION_FP64 (default: the reference's arithmetic on the batched
+     * solver) or MGPU_PRECISION_MIXED; set before the first advance. */
+    void set_precision(int precision)
+    {
+        m_precision = precision;
+    }
+    /* Record node results at every exchange boundary (default) or only at tmax. */
+    void set_record_boundaries(bool on)
+    {
+        m_record = on;
+    }
+
+    /* Alternates node solves and mobility exchanges up to tmax
+     * (GraphSimulation::advance, graph_simulation.h:101-120). */
+    void advance(double tmax)
+    {
+        ensure_batch();
+        mgpu_context* ctx = Device::context();
+        while (m_t < tmax) {
+            double t_next = m_record ? std::min(m_t + m_dt, tmax) : tmax;
+            if (tmax - t_next < 1e-12 * std::max(1.0, std::abs(tmax))) {
+                t_next = tmax;
+            }
+            check(mgpu_batch_advance(m_batch, t_next, nullptr), ctx, "mgpu_batch_advance");
+            m_t = t_next;
+            record();
+        }
+    }
+    double get_t() const
+    {
+        return m_t;
+    }
+    GraphT& get_graph() &
+    {
+        return m_graph;
+    }
+    const GraphT& get_graph() const&
+    {
+        return m_graph;
+    }
+    GraphT&& get_graph() &&
+    {
+        return std::move(m_graph);
+    }
+    mgpu_batch* batch()
+    {
+        ensure_batch();
+        return m_batch;
+    }
+
+private:
+    void ensure_batch()
+    {
+        if (m_batch) {
+            return;
+        }
+        std::vector<const typename std::decay_t<decltype(m_graph.nodes()[0].property.get_simulation().get_model())>*>
+            models;
+        std::vector<std::vector<double>> states;
+        for (auto& nd : m_graph.nodes()) {
+            models.push_back(&nd.property.get_simulation().get_model());
+            states.push_back(nd.property.get_result().get_last_value());
+        }
+        std::vector<const std::vector<double>*> sp;
+        for (auto& s : states) {
+            sp.push_back(&s);
+        }
+        using EdgeT    = typename GraphT::EdgeProperty;
+        m_arrays       = detail::pack_graph<typename std::decay_t<decltype(*models[0])>, EdgeT>(
+            models, sp, m_graph.edges(), [](const EdgeT& e) -> const MobilityParameters<double>& {
+                return e.get_parameters();
+            });
+        mgpu_graph g     = m_arrays.view();
+        mgpu_solver_opts o;
+        mgpu_default_solver_opts(&o);
+        o.precision   = m_precision;
+        o.dt_exchange = m_dt;
+        if (!m_graph.nodes().empty()) {
+            const auto& sim = m_graph.nodes()[0].property.get_simulation();
+            o.integrator    = sim.get_integrator_core().opts();
+            o.dt0           = sim.get_dt();
+        }
+        mgpu_context* ctx = Device::context();
+        check(mgpu_batch_create(ctx, &g, 1, m_t, &o, &m_batch), ctx, "mgpu_batch_create");
+    }
+    void record()
+    {
+        mgpu_context* ctx = Device::context();
+        const size_t n    = (size_t)m_arrays.G * osecir::num_compartments;
+        std::vector<double> st((size_t)m_arrays.N * n);
+        check(mgpu_batch_get_state(m_batch, st.data()), ctx, "mgpu_batch_get_state");
+        for (size_t v = 0; v < m_graph.nodes().size(); ++v) {
+            auto& nd = m_graph.nodes()[v].property;
+            nd.get_result().add_time_point(m_t, st.data() + v * n);
+            nd.set_last_state(st.data() + v * n);
+        }
+    }
+
+    double m_t, m_dt;
+    GraphT m_graph;
+    int m_precision   = MGPU_PRECISION_FP64;
+    bool m_record     = true;
+    mgpu_batch* m_batch = nullptr;
+    detail::GraphArrays m_arrays;
+};
+
+template <class Sim>
+using MobilitySimGraph = Graph<SimulationNode<Sim>, MobilityEdge<double>>;
+
+/* make_mobility_sim (:656-678). */
+template <class Sim>
+GraphSimulation<MobilitySimGraph<Sim>> make_mobility_sim(double t0, double dt, MobilitySimGraph<Sim>&& graph)
+{
+    return GraphSimulation<MobilitySimGraph<Sim>>(t0, dt, std::move(graph));
+}
+template <class Sim>
+GraphSimulation<MobilitySimGraph<Sim>> make_mobility_sim(double t0, double dt, const MobilitySimGraph<Sim>& graph)
+{
+    MobilitySimGraph<Sim> copy = graph;
+    return GraphSimulation<MobilitySimGraph<Sim>>(t0, dt, std::move(copy));
+}
+
+/* Result of one run of a ParameterStudy: the sampled graph's node states at tmax. */
+struct StudyResult {
+    size_t run_idx = 0;
+    double t       = 0.0;
+    int num_groups = 0;
+    std::vector<std::vector<double>> node_states; // [node][10G]
+};
+
+/* mio::ParameterStudy (parameter_studies.h:47-374) over graphs of models and
+ * mobility parameters: run() samples num_runs graphs on the host and solves
+ * them all in one batch on the GPU. */
+template <class Sim>
+class ParameterStudy
+{
+public:
+    using Model     = typename Sim::Model;
+    using GraphType = Graph<Model, MobilityParameters<double>>;
+
+    ParameterStudy(const GraphType& graph, double t0, double tmax, double dt_graph_sim, size_t num_runs)
+        : m_graph(graph)
+        , m_t0(t0)
+        , m_tmax(tmax)
+        , m_dt(dt_graph_sim)
+        , m_num_runs(num_runs)
+    {
+    }
+    void set_precision(int precision)
+    {
+        m_precision = precision;
+    }
+    void set_integrator_core(const IntegratorCore& core)
+    {
+        m_core = core;
+    }
+
+    /* sample_graph(const GraphType&) -> GraphType; result_processing(StudyResult, run_idx) -> R. */
+    template <class SampleGraphFn, class HandleResultFn>
+    auto run(SampleGraphFn sample_graph, HandleResultFn result_processing)
+        -> std::vector<decltype(result_processing(std::declval<StudyResult>(), size_t(0)))>
+    {
+        std::vector<GraphType> graphs;
+        graphs.reserve(m_num_runs);
+        for (size_t r = 0; r < m_num_runs; ++r) {
+            graphs.push_back(sample_graph(m_graph));
+        }
+        std::vector<detail::GraphArrays> arrays;
+        std::vector<mgpu_graph> views;
+        for (auto& g : graphs) {
+            std::vector<const Model*> models;
+            std::vector<const std::vector<double>*> states;
+            for (auto& nd : g.nodes()) {
+                models.push_back(&nd.property);
+                states.push_back(&nd.property.populations.array());
+            }
+            arrays.push_back(detail::pack_graph<Model, MobilityParameters<double>>(
+                models, states, g.edges(), [](const MobilityParameters<double>& p) -> const MobilityParameters<double>& {
+                    return p;
+                }));
+        }
+        for (auto& a : arrays) {
+            views.push_back(a.view());
+        }
+        mgpu_solver_opts o;
+        mgpu_default_solver_opts(&o);
+        o.precision       = m_precision;
+        o.dt_exchange     = m_dt;
+        o.integrator      = m_core.opts();
+        mgpu_context* ctx = Device::context();
+        mgpu_batch* b     = nullptr;
+        check(mgpu_batch_create(ctx, views.data(), (int32_t)views.size(), m_t0, &o, &b), ctx, "mgpu_batch_create");
+        std::vector<decltype(result_processing(std::declval<StudyResult>(), size_t(0)))> out;
+        try {
+            check(mgpu_batch_advance(b, m_tmax, nullptr), ctx, "mgpu_batch_advance");
+            for (size_t r = 0; r < arrays.size(); ++r) {
+                const size_t n = (size_t)arrays[r].G * osecir::num_compartments;
+                std::vector<double> st((size_t)arrays[r].N * n);
+                check(mgpu_batch_get_graph_state(b, (int32_t)r, st.data()), ctx, "mgpu_batch_get_graph_state");
+                StudyResult res;
+                res.run_idx    = r;
+                res.t          = m_tmax;
+                res.num_groups = arrays[r].G;
+                for (int v = 0; v < arrays[r].N; ++v) {
+                    res.node_states.emplace_back(st.begin() + (long)(v * n), st.begin() + (long)((v + 1) * n));
+                }
+                out.push_back(result_processing(std::move(res), r));
+            }
+        }
+        catch (...) {
+            mgpu_batch_destroy(b);
+            throw;
+        }
+        mgpu_batch_destroy(b);
+        return out;
+    }
+
+private:
+    GraphType m_graph;
+    double m_t0, m_tmax, m_dt;
+    size_t m_num_runs;
+    int m_precision = MGPU_PRECISION_FP64;
+    IntegratorCore m_core;
+};
+
+} // namespace miogpu
+
+#endif // MIOGPU_FACADE_MOBILITY_H

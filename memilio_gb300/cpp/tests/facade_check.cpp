@@ -1,0 +1,332 @@
+// facade_check — drives the C++ facade for the Python tests and prints JSON.
+//
+//   facade_check dampings   host only: damping caches of several damping lists
+//   facade_check pack       host only: the node/edge arrays of a small graph
+//   facade_check simulate   GPU: Simulation::advance in two pieces and in one
+//   facade_check graph      GPU: make_mobility_sim(...).advance, every boundary
+//   facade_check study      GPU: ParameterStudy over 4 sampled graphs
+//
+// The Python side rebuilds the same inputs from the printed arrays and checks
+// the outputs against the FP64 oracle.
+#include "miogpu/mobility.h"
+
+#include <cstdio>
+#include <cstring>
+#include <random>
+
+using namespace miogpu;
+using namespace miogpu::osecir;
+
+namespace
+{
+
+void print_vec(const char* key, const std::vector<double>& v, bool comma = true)
+{
+    std::printf("\"%s\": [", key);
+    for (size_t i = 0; i < v.size(); ++i) {
+        std::printf("%s%.17g", i ? ", " : "", v[i] == std::numeric_limits<double>::max() ? 1.7976931348623157e308
+                                                                                         : v[i]);
+    }
+    std::printf("]%s\n", comma ? "," : "");
+}
+
+Model<double> make_model(int G, unsigned seed)
+{
+    std::mt19937_64 rng(seed);
+    std::uniform_real_distribution<double> u(0.0, 1.0);
+    auto U = [&](double a, double b) {
+        return a + (b - a) * u(rng);
+    };
+    Model<double> m(G);
+    auto& p = m.parameters;
+    p.get<Seasonality<double>>()        = 0.1;
+    p.get<StartDay<double>>()           = 40.0;
+    p.get<TestAndTraceCapacity<double>>() = 60.0;
+    p.get<ICUCapacity<double>>()        = 30.0;
+    for (int i = 0; i < G; ++i) {
+        const AgeGroup g((size_t)i);
+        p.get<TimeExposed<double>>()[g]                       = U(2, 5);
+        p.get<TimeInfectedNoSymptoms<double>>()[g]            = U(2, 5);
+        p.get<TimeInfectedSymptoms<double>>()[g]              = U(4, 8);
+        p.get<TimeInfectedSevere<double>>()[g]                = U(5, 10);
+        p.get<TimeInfectedCritical<double>>()[g]              = U(5, 10);
+        p.get<TransmissionProbabilityOnContact<double>>()[g]  = U(0.05, 0.15);
+        p.get<RelativeTransmissionNoSymptoms<double>>()[g]    = U(0.5, 1.0);
+        p.get<RecoveredPerInfectedNoSymptoms<double>>()[g]    = U(0.1, 0.3);
+        p.get<RiskOfInfectionFromSymptomatic<double>>()[g]    = U(0.1, 0.3);
+        p.get<MaxRiskOfInfectionFromSymptomatic<double>>()[g] = U(0.3, 0.5);
+        p.get<SeverePerInfectedSymptoms<double>>()[g]         = U(0.05, 0.2);
+        p.get<CriticalPerSevere<double>>()[g]                 = U(0.1, 0.3);
+        p.get<DeathsPerCritical<double>>()[g]                 = U(0.1, 0.4);
+        m.populations[{g, InfectionState::Exposed}]            = U(10, 100);
+        m.populations[{g, InfectionState::InfectedNoSymptoms}] = U(10, 100);
+        m.populations[{g, InfectionState::InfectedSymptoms}]   = U(0, 20);
+        m.populations.set_difference_from_group_total<AgeGroup>({g, InfectionState::Susceptible}, U(2e4, 6e4));
+    }
+    auto& c = p.get<ContactPatterns<double>>().get_cont_freq_mat();
+    for (int i = 0; i < G; ++i) {
+        for (int j = 0; j < G; ++j) {
+            c[0].get_baseline()((size_t)i, (size_t)j) = U(1, 6);
+            c[0].get_minimum()((size_t)i, (size_t)j)  = U(0, 0.5);
+        }
+    }
+    c[0].add_damping(0.4, SimulationTime<double>(6.0));
+    c[0].add_damping(Matrix::Constant((size_t)G, (size_t)G, 0.2), DampingLevel(1), DampingType(0),
+                     SimulationTime<double>(9.0));
+    return m;
+}
+
+std::vector<double> commuters(int G, double f)
+{
+    std::vector<double> c(10 * (size_t)G, 0.0);
+    for (int g = 0; g < G; ++g) {
+        for (int k : {0, 1, 2, 4, 8}) {
+            c[(size_t)(10 * g + k)] = f * (1.0 + 0.1 * g);
+        }
+    }
+    return c;
+}
+
+void print_graph_arrays(const detail::GraphArrays& a)
+{
+    std::printf("\"N\": %d, \"G\": %d, \"E\": %d, \"M\": %d, \"K\": %d, \"Ke\": %d,\n", a.N, a.G, a.E, a.M, a.K, a.Ke);
+    print_vec("params", a.params);
+    print_vec("contact_baseline", a.contact_baseline);
+    print_vec("contact_minimum", a.contact_minimum);
+    print_vec("damping_times", a.damping_times);
+    print_vec("damping_values", a.damping_values);
+    print_vec("state", a.state);
+    std::vector<double> s(a.src.begin(), a.src.end()), d(a.dst.begin(), a.dst.end());
+    print_vec("src", s);
+    print_vec("dst", d);
+    print_vec("coeff_baseline", a.coeff_baseline);
+    print_vec("coeff_minimum", a.coeff_minimum);
+}
+
+MobilitySimGraph<Simulation<double>> three_nodes(int G)
+{
+    MobilitySimGraph<Simulation<double>> graph;
+    for (int v = 0; v < 3; ++v) {
+        graph.add_node(100 + v, make_model(G, 7u + (unsigned)v), 0.0, 0.1);
+    }
+    // added out of order on purpose: the graph keeps (start, end) order
+    graph.add_edge(2, 0, commuters(G, 0.02));
+    graph.add_edge(0, 1, commuters(G, 0.03));
+    graph.add_edge(1, 0, commuters(G, 0.01));
+    graph.add_edge(0, 2, commuters(G, 0.02));
+    return graph;
+}
+
+detail::GraphArrays arrays_of(MobilitySimGraph<Simulation<double>>& graph)
+{
+    std::vector<const Model<double>*> models;
+    std::vector<std::vector<double>> st;
+    for (auto& n : graph.nodes()) {
+        models.push_back(&n.property.get_simulation().get_model());
+        st.push_back(n.property.get_result().get_last_value());
+    }
+    std::vector<const std::vector<double>*> sp;
+    for (auto& s : st) {
+        sp.push_back(&s);
+    }
+    return detail::pack_graph<Model<double>, MobilityEdge<double>>(
+        models, sp, graph.edges(), [](const MobilityEdge<double>& e) -> const MobilityParameters<double>& {
+            return e.get_parameters();
+        });
+}
+
+int mode_dampings()
+{
+    // (level, type, time, value) lists; the value fills a 2 x 2 matrix
+    const std::vector<std::vector<std::tuple<int, int, double, double>>> cases = {
+        {},
+        {{0, 0, 20.0, 0.3}},
+        {{0, 0, 5.0, 0.2}, {0, 1, 5.0, 0.1}, {1, 0, 8.0, 0.5}},
+        {{0, 0, 5.0, 0.2}, {0, 0, 9.0, 0.6}, {1, 0, 7.0, 0.4}, {1, 1, 7.0, 0.1}, {0, 0, 12.0, 0.0}},
+        {{2, 0, 3.0, 0.25}, {0, 0, 3.0, 0.5}, {0, 0, 3.0, 0.7}}, // equal key replaces
+    };
+    std::printf("{\"cases\": [\n");
+    for (size_t k = 0; k < cases.size(); ++k) {
+        Dampings d(2, 2);
+        for (auto& c : cases[k]) {
+            d.add(std::get<3>(c), DampingLevel(std::get<0>(c)), DampingType(std::get<1>(c)),
+                  SimulationTime<double>(std::get<2>(c)));
+        }
+        std::vector<double> times;
+        std::vector<Matrix> values;
+        d.cache(times, values);
+        std::vector<double> lv, ty, tm, va, flat;
+        for (auto& x : d.list()) {
+            lv.push_back(x.level.get());
+            ty.push_back(x.type.get());
+            tm.push_back(x.time.get());
+            va.insert(va.end(), x.values.data(), x.values.data() + 4);
+        }
+        for (auto& m : values) {
+            flat.insert(flat.end(), m.data(), m.data() + 4);
+        }
+        std::printf("{");
+        print_vec("levels", lv);
+        print_vec("types", ty);
+        print_vec("times", tm);
+        print_vec("matrices", va);
+        print_vec("cache_times", times);
+        print_vec("cache_values", flat, false);
+        std::printf("}%s\n", k + 1 < cases.size() ? "," : "");
+    }
+    std::printf("]}\n");
+    return 0;
+}
+
+int mode_pack()
+{
+    auto graph = three_nodes(2);
+    auto a     = arrays_of(graph);
+    std::printf("{");
+    print_graph_arrays(a);
+    std::printf("\"ok\": 1}\n");
+    return 0;
+}
+
+int mode_simulate()
+{
+    const Model<double> m = make_model(3, 3u);
+    Simulation<double> pieces(m, 0.0, 0.1);
+    pieces.advance(4.0);
+    const double dt_mid = pieces.get_dt();
+    pieces.advance(12.0);
+    Simulation<double> whole(m, 0.0, 0.1);
+    whole.advance(12.0);
+    std::vector<double> dydt;
+    m.get_derivatives(m.populations.array(), m.populations.array(), 5.0, dydt);
+    auto a = m.pack();
+    std::printf("{\"G\": 3, \"K\": %d, \"M\": %d,\n", a.K, a.M);
+    print_vec("params", a.params);
+    print_vec("contact_baseline", a.contact_baseline);
+    print_vec("contact_minimum", a.contact_minimum);
+    print_vec("damping_times", a.damping_times);
+    print_vec("damping_values", a.damping_values);
+    print_vec("state", a.state);
+    print_vec("dydt_t5", dydt);
+    std::printf("\"dt_mid\": %.17g, \"dt_end\": %.17g, \"points_pieces\": %zu, \"points_whole\": %zu,\n", dt_mid,
+                pieces.get_dt(), pieces.get_result().get_num_time_points(), whole.get_result().get_num_time_points());
+    std::vector<double> tp, tw;
+    for (size_t i = 0; i < pieces.get_result().get_num_time_points(); ++i) {
+        tp.push_back(pieces.get_result().get_time(i));
+    }
+    for (size_t i = 0; i < whole.get_result().get_num_time_points(); ++i) {
+        tw.push_back(whole.get_result().get_time(i));
+    }
+    print_vec("times_pieces", tp);
+    print_vec("times_whole", tw);
+    print_vec("last_pieces", pieces.get_result().get_last_value());
+    print_vec("last_whole", whole.get_result().get_last_value(), false);
+    std::printf("}\n");
+    return 0;
+}
+
+int mode_graph()
+{
+    auto graph = three_nodes(2);
+    auto a     = arrays_of(graph);
+    auto sim   = make_mobility_sim(0.0, 0.5, std::move(graph));
+    sim.advance(6.0);
+    std::printf("{");
+    print_graph_arrays(a);
+    std::vector<double> t, states;
+    auto& nodes = sim.get_graph().nodes();
+    for (size_t i = 0; i < nodes[0].property.get_result().get_num_time_points(); ++i) {
+        t.push_back(nodes[0].property.get_result().get_time(i));
+        for (auto& n : nodes) {
+            const double* v = n.property.get_result().value_ptr(i);
+            states.insert(states.end(), v, v + 20);
+        }
+    }
+    print_vec("t", t);
+    print_vec("states", states);
+    std::printf("\"t_end\": %.17g}\n", sim.get_t());
+    return 0;
+}
+
+int mode_study()
+{
+    using GraphT = ParameterStudy<Simulation<double>>::GraphType;
+    GraphT base;
+    for (int v = 0; v < 3; ++v) {
+        base.add_node(v, make_model(2, 11u + (unsigned)v));
+    }
+    base.add_edge(0, 1, MobilityParameters<double>(commuters(2, 0.02)));
+    base.add_edge(1, 2, MobilityParameters<double>(commuters(2, 0.02)));
+    base.add_edge(2, 0, MobilityParameters<double>(commuters(2, 0.02)));
+    ParameterStudy<Simulation<double>> study(base, 0.0, 5.0, 0.5, 4);
+    std::vector<GraphT> sampled;
+    unsigned run = 0;
+    auto results = study.run(
+        [&](const GraphT& g) {
+            GraphT s = g;
+            const double f = 0.8 + 0.1 * run++;
+            for (auto& n : s.nodes()) {
+                for (size_t i = 0; i < 2; ++i) {
+                    n.property.parameters.get<TransmissionProbabilityOnContact<double>>()[AgeGroup(i)] *= f;
+                }
+            }
+            sampled.push_back(s);
+            return s;
+        },
+        [](StudyResult r, size_t idx) {
+            return std::make_pair(idx, r.node_states);
+        });
+    std::printf("{\"runs\": [\n");
+    for (size_t r = 0; r < results.size(); ++r) {
+        std::vector<const Model<double>*> models;
+        std::vector<const std::vector<double>*> st;
+        for (auto& n : sampled[r].nodes()) {
+            models.push_back(&n.property);
+            st.push_back(&n.property.populations.array());
+        }
+        auto a = detail::pack_graph<Model<double>, MobilityParameters<double>>(
+            models, st, sampled[r].edges(), [](const MobilityParameters<double>& p) -> const MobilityParameters<double>& {
+                return p;
+            });
+        std::vector<double> fin;
+        for (auto& s : results[r].second) {
+            fin.insert(fin.end(), s.begin(), s.end());
+        }
+        std::printf("{");
+        print_graph_arrays(a);
+        print_vec("final", fin, false);
+        std::printf("}%s\n", r + 1 < results.size() ? "," : "");
+    }
+    std::printf("]}\n");
+    return 0;
+}
+
+} // namespace
+
+int main(int argc, char** argv)
+{
+    const char* mode = argc > 1 ? argv[1] : "";
+    try {
+        if (!std::strcmp(mode, "dampings")) {
+            return mode_dampings();
+        }
+        if (!std::strcmp(mode, "pack")) {
+            return mode_pack();
+        }
+        if (!std::strcmp(mode, "simulate")) {
+            return mode_simulate();
+        }
+        if (!std::strcmp(mode, "graph")) {
+            return mode_graph();
+        }
+        if (!std::strcmp(mode, "study")) {
+            return mode_study();
+        }
+    }
+    catch (const Error& e) {
+        std::fprintf(stderr, "miogpu error: %s\n", e.what());
+        return 3;
+    }
+    std::fprintf(stderr, "usage: facade_check dampings|pack|simulate|graph|study\n");
+    return 2;
+}

@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <cstring>
 #include <exception>
+#include <functional>
 #include <map>
 #include <tuple>
 #include <new>
@@ -180,6 +181,8 @@ struct mgpu_batch {
     // batched solver work lists per age-group count
     std::map<int, std::pair<int32_t*, int64_t>> inst_by_G;
     int instances_per_block = 0;
+    // autotuned schedule of the node solves per age-group count: {instances per block, grid blocks}
+    std::map<int, std::pair<int, int>> tuned;
     bool any_edge_dampings  = false;
     int64_t launches        = 0;
     int64_t phases          = 0;
@@ -187,6 +190,11 @@ struct mgpu_batch {
     // CUDA graph of one batched interval
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_failed          = false;
+    // asynchronous advance (mgpu_batch_launch / mgpu_batch_query)
+    bool async_active   = false;
+    int64_t async_left  = 0;
+    std::vector<double> async_t_end;
+    cudaEvent_t ev_async = nullptr;
     // timing
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     std::vector<cudaEvent_t> ev_phase;
@@ -205,6 +213,9 @@ struct mgpu_batch {
         }
         if (ev_stop) {
             cudaEventDestroy(ev_stop);
+        }
+        if (ev_async) {
+            cudaEventDestroy(ev_async);
         }
         pool.release();
     }
@@ -238,6 +249,83 @@ void split_pairs(const double* v, int64_t n, float* hi, float* lo)
         hi[i] = (float)v[i];
         lo[i] = (float)(v[i] - (double)hi[i]);
     }
+}
+
+// FP64 value -> float-float pair on the device (the same roundings as split_pairs)
+__global__ void k_split_pairs(const double* v, int64_t n, float* hi, float* lo, float* hi2, float* lo2)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) {
+        return;
+    }
+    const float h = __double2float_rn(v[i]);
+    const float l = __double2float_rn(v[i] - (double)h);
+    hi[i] = hi2[i] = h;
+    lo[i] = lo2[i] = l;
+}
+
+__global__ void k_to_float(const double* v, int64_t n, float* out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        out[i] = __double2float_rn(v[i]);
+    }
+}
+
+// FP32 per-(node, age group) constants of the mixed solver from the FP64
+// parameters, with the rates formed as the reference forms them.
+__global__ void k_build_tab(BatchDev B, float* tab)
+{
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= B.num_nodes * MGPU_MAX_GROUPS) {
+        return;
+    }
+    const int64_t node = tid / MGPU_MAX_GROUPS;
+    const int gr       = (int)(tid % MGPU_MAX_GROUPS);
+    const DevGraph& d  = B.graphs[B.node_graph[node]];
+    const int G        = d.G;
+    if (gr >= G) {
+        return;
+    }
+    const double* p = B.params + d.param_off + (node - d.node0) * param_stride(G);
+    auto gp         = [&](int w) {
+        return p[MGPU_NUM_SCALAR_PARAMS + w * G + gr];
+    };
+    float* T           = tab + tid * kTabF;
+    const double mu    = gp(MGPU_G_RECOVERED_PER_INS);
+    const double tins  = gp(MGPU_G_TIME_INS);
+    const double sev   = gp(MGPU_G_SEVERE_PER_ISY);
+    const double tisy  = gp(MGPU_G_TIME_ISY);
+    const double tisev = gp(MGPU_G_TIME_ISEV);
+    const double cps   = gp(MGPU_G_CRITICAL_PER_SEVERE);
+    const double dps   = gp(MGPU_G_DEATHS_PER_SEVERE);
+    const double dpc   = gp(MGPU_G_DEATHS_PER_CRITICAL);
+    const double ticri = gp(MGPU_G_TIME_ICRI);
+    T[TF_A_TNT]        = __double2float_rn(__ddiv_rn(1 - mu, tins));
+    T[TF_BETA]         = __double2float_rn(gp(MGPU_G_TRANSMISSION_PROB));
+    T[TF_XI]           = __double2float_rn(gp(MGPU_G_REL_TRANSMISSION_NS));
+    T[TF_RHO]          = __double2float_rn(gp(MGPU_G_RISK_FROM_SYMPTOMATIC));
+    T[TF_RHO_MAX]      = __double2float_rn(gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC));
+    T[TF_R1]           = __double2float_rn(__ddiv_rn(1.0, gp(MGPU_G_TIME_EXPOSED)));
+    T[TF_R2]           = __double2float_rn(__dmul_rn(1 - mu, __ddiv_rn(1.0, tins)));
+    T[TF_R3]           = __double2float_rn(__dmul_rn(mu, __ddiv_rn(1.0, tins)));
+    T[TF_R6]           = __double2float_rn(__ddiv_rn(sev, tisy));
+    T[TF_R7]           = __double2float_rn(__ddiv_rn(1 - sev, tisy));
+    T[TF_R11]          = __double2float_rn(__ddiv_rn(1.0 - cps - dps, tisev));
+    T[TF_R13]          = __double2float_rn(__ddiv_rn(dpc, ticri));
+    T[TF_R14]          = __double2float_rn(__ddiv_rn(1.0 - dpc, ticri));
+    T[TF_R10L]         = __double2float_rn(__ddiv_rn(cps, tisev));
+    T[TF_R12L]         = __double2float_rn(__ddiv_rn(dps + (cps - cps), tisev));
+    T[TF_CPS]          = __double2float_rn(cps);
+    T[TF_DPS]          = __double2float_rn(dps);
+    T[TF_INV_TISEV]    = __double2float_rn(__ddiv_rn(1.0, tisev));
+    const double cap   = p[MGPU_P_TNT_CAPACITY];
+    T[TF_TNT_CAP]      = __double2float_rn(cap);
+    T[TF_TNT_CAP2]     = __double2float_rn(__dmul_rn(cap, p[MGPU_P_TNT_MAX_RISK]));
+    const double icu   = p[MGPU_P_ICU_CAPACITY];
+    T[TF_ICU_LO]       = __double2float_rn(__dmul_rn(0.90, icu));
+    T[TF_ICU_CAP]      = __double2float_rn(icu);
+    T[TF_SEASON_K]     = __double2float_rn(p[MGPU_P_SEASONALITY]);
 }
 
 // Restart: graph clocks and flags, node clocks, states, pending travelers.
@@ -383,6 +471,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     std::vector<uint8_t> h_any(edges);
     std::vector<int64_t> h_trav_off(edges), h_out_ptr(nodes + 1, 0), h_in_ptr(nodes + 1, 0), h_in_edges(edges);
     int64_t trav_pos = 0;
+    std::vector<int32_t> mob_mask(num_graphs, 0);
     for (int i = 0; i < num_graphs; ++i) {
         const mgpu_graph& g = graphs[i];
         const DevGraph& d   = dg[i];
@@ -437,6 +526,9 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
             bool any = false;
             for (int j = 0; j < n; ++j) {
                 any = any || (cb[j] > 0.0);
+                if (cb[j] != 0.0 || (g.edge_coeff_minimum && g.edge_coeff_minimum[(int64_t)e * n + j] != 0.0)) {
+                    mob_mask[i] |= 1 << (j % kC);
+                }
             }
             h_any[ge] = any ? 1 : 0;
             if (d.Ke && own_coeff[i]) {
@@ -468,6 +560,11 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.num_graphs     = num_graphs;
     B.num_nodes      = nodes;
     B.num_edges      = edges;
+    B.mob_union = 0;
+    for (int i = 0; i < num_graphs; ++i) {
+        dg[i].mob_mask = mob_mask[i];
+        B.mob_union |= mob_mask[i];
+    }
     B.graphs         = b->pool.upload(dg);
     std::vector<GraphRt> h_rt(num_graphs);
     for (auto& r : h_rt) {
@@ -488,14 +585,19 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.state    = nullptr;
     B.v0       = nullptr;
     B.ynew     = nullptr;
+    DevPool staging; // released at the end of the upload
+    staging.ctx = ctx;
     if (b->pairs) {
-        // the mixed solver keeps node states as float-float pairs on the device
-        std::vector<float> hi(st), lo(st);
-        split_pairs(h_state.data(), st, hi.data(), lo.data());
-        B.st_hi       = b->pool.upload(hi);
-        B.st_lo       = b->pool.upload(lo);
-        b->init_hi    = b->pool.upload(hi);
-        b->init_lo    = b->pool.upload(lo);
+        // the mixed solver keeps node states as float-float pairs on the device;
+        // the FP64 states are uploaded once and split there
+        double* d_state = staging.upload(h_state);
+        B.st_hi         = b->pool.alloc<float>(st);
+        B.st_lo         = b->pool.alloc<float>(st);
+        b->init_hi      = b->pool.alloc<float>(st);
+        b->init_lo      = b->pool.alloc<float>(st);
+        k_split_pairs<<<(unsigned)std::max<int64_t>((st + 255) / 256, 1), 256, 0, ctx->stream>>>(
+            d_state, st, B.st_hi, B.st_lo, b->init_hi, b->init_lo);
+        ck(cudaGetLastError(), "k_split_pairs");
         B.v0_hi       = b->pool.alloc<float>(st);
         B.v0_lo       = b->pool.alloc<float>(st);
         B.yn_hi       = b->pool.alloc<float>(st);
@@ -523,7 +625,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.trav       = plain ? b->pool.alloc<double>(tr) : nullptr; // the batched exchange recomputes travelers
     B.mfix       = b->pool.alloc<double>(tr);
     B.state_total = st;
-    B.ysnap      = plain ? nullptr : b->pool.alloc<double>(2 * st);
+    B.ysnap      = (plain || b->pairs) ? nullptr : b->pool.alloc<double>(2 * st);
     B.ysnap_f    = plain ? nullptr : b->pool.alloc<float>(2 * st);
     B.risk       = plain ? nullptr : (void*)b->pool.alloc<double>(2 * nodes * MGPU_MAX_GROUPS * 2);
     B.aux        = plain ? nullptr : (void*)b->pool.alloc<double>(nodes * MGPU_MAX_GROUPS * 12);
@@ -533,58 +635,20 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.dvals_f    = nullptr;
     if (b->opts.precision == MGPU_PRECISION_MIXED) {
         // FP32 node constants, contact and damping pools of the mixed solver
-        std::vector<float> tab((size_t)nodes * MGPU_MAX_GROUPS * kTabF, 0.0f);
-        for (int i = 0; i < num_graphs; ++i) {
-            const DevGraph& d = dg[i];
-            const int G       = d.G;
-            for (int64_t v = 0; v < d.N; ++v) {
-                const double* p = h_par.data() + d.param_off + v * param_stride(G);
-                auto gp         = [&](int w, int gr) {
-                    return p[MGPU_NUM_SCALAR_PARAMS + w * G + gr];
-                };
-                for (int gr = 0; gr < G; ++gr) {
-                    float* T           = tab.data() + ((d.node0 + v) * MGPU_MAX_GROUPS + gr) * kTabF;
-                    const double mu    = gp(MGPU_G_RECOVERED_PER_INS, gr);
-                    const double tins  = gp(MGPU_G_TIME_INS, gr);
-                    const double sev   = gp(MGPU_G_SEVERE_PER_ISY, gr);
-                    const double tisy  = gp(MGPU_G_TIME_ISY, gr);
-                    const double tisev = gp(MGPU_G_TIME_ISEV, gr);
-                    const double cps   = gp(MGPU_G_CRITICAL_PER_SEVERE, gr);
-                    const double dps   = gp(MGPU_G_DEATHS_PER_SEVERE, gr);
-                    const double dpc   = gp(MGPU_G_DEATHS_PER_CRITICAL, gr);
-                    const double ticri = gp(MGPU_G_TIME_ICRI, gr);
-                    T[TF_A_TNT]        = (float)((1 - mu) / tins);
-                    T[TF_BETA]         = (float)gp(MGPU_G_TRANSMISSION_PROB, gr);
-                    T[TF_XI]           = (float)gp(MGPU_G_REL_TRANSMISSION_NS, gr);
-                    T[TF_RHO]          = (float)gp(MGPU_G_RISK_FROM_SYMPTOMATIC, gr);
-                    T[TF_RHO_MAX]      = (float)gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, gr);
-                    T[TF_R1]           = (float)(1.0 / gp(MGPU_G_TIME_EXPOSED, gr));
-                    T[TF_R2]           = (float)((1 - mu) * (1 / tins));
-                    T[TF_R3]           = (float)(mu * (1.0 / tins));
-                    T[TF_R6]           = (float)(sev / tisy);
-                    T[TF_R7]           = (float)((1 - sev) / tisy);
-                    T[TF_R11]          = (float)((1.0 - cps - dps) / tisev);
-                    T[TF_R13]          = (float)(dpc / ticri);
-                    T[TF_R14]          = (float)((1.0 - dpc) / ticri);
-                    T[TF_R10L]         = (float)(cps / tisev);
-                    T[TF_R12L]         = (float)((dps + (cps - cps)) / tisev);
-                    T[TF_CPS]          = (float)cps;
-                    T[TF_DPS]          = (float)dps;
-                    T[TF_INV_TISEV]    = (float)(1.0 / tisev);
-                    const double cap   = p[MGPU_P_TNT_CAPACITY];
-                    T[TF_TNT_CAP]      = (float)cap;
-                    T[TF_TNT_CAP2]     = (float)(cap * p[MGPU_P_TNT_MAX_RISK]);
-                    const double icu   = p[MGPU_P_ICU_CAPACITY];
-                    T[TF_ICU_LO]       = (float)(0.90 * icu);
-                    T[TF_ICU_CAP]      = (float)icu;
-                    T[TF_SEASON_K]     = (float)p[MGPU_P_SEASONALITY];
-                }
-            }
-        }
-        B.tab_f = b->pool.upload(tab);
-        std::vector<float> cf(h_con.begin(), h_con.end()), df(h_dtv.begin(), h_dtv.end());
-        B.contact_f = b->pool.upload(cf);
-        B.dvals_f   = b->pool.upload(df);
+        // derived on the device from the uploaded FP64 pools (no second host copy, no second upload)
+        float* tab = b->pool.alloc<float>(nodes * MGPU_MAX_GROUPS * kTabF);
+        float* cf  = b->pool.alloc<float>(con);
+        float* df  = b->pool.alloc<float>(dtv);
+        ck(cudaMemsetAsync(tab, 0, sizeof(float) * std::max<int64_t>(nodes * MGPU_MAX_GROUPS * kTabF, 1), ctx->stream),
+           "memset");
+        k_build_tab<<<(unsigned)std::max<int64_t>((nodes * MGPU_MAX_GROUPS + 255) / 256, 1), 256, 0, ctx->stream>>>(
+            B, tab);
+        k_to_float<<<(unsigned)std::max<int64_t>((con + 255) / 256, 1), 256, 0, ctx->stream>>>(B.contact, con, cf);
+        k_to_float<<<(unsigned)std::max<int64_t>((dtv + 255) / 256, 1), 256, 0, ctx->stream>>>(B.dvals, dtv, df);
+        B.tab_f     = tab;
+        B.contact_f = cf;
+        B.dvals_f   = df;
+        ck(cudaGetLastError(), "table kernels");
     }
     b->any_edge_dampings = false;
     for (int i = 0; i < num_graphs; ++i) {
@@ -635,7 +699,13 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     for (auto& kv : lists) {
         b->inst_by_G[kv.first] = {b->pool.upload(kv.second), (int64_t)kv.second.size()};
     }
+    for (int G = 0; G <= MGPU_MAX_GROUPS; ++G) {
+        auto it     = b->inst_by_G.find(G);
+        B.glist[G]  = it != b->inst_by_G.end() ? it->second.first : nullptr;
+        B.gcount[G] = it != b->inst_by_G.end() ? it->second.second : 0;
+    }
     ck(cudaStreamSynchronize(ctx->stream), "upload sync");
+    staging.release();
 }
 
 int check_device_error(mgpu_batch* b)
@@ -664,17 +734,19 @@ void enqueue_batched_phase(mgpu_batch* b, cudaStream_t s, cudaEvent_t* ev = null
         ck(cudaEventRecord(ev[0], s), "cudaEventRecord");
     }
     for (auto& kv : b->inst_by_G) {
-        launch_ode_batched(B, kv.first, b->opts.precision, kv.second.first, kv.second.second,
-                           b->instances_per_block, 0, s);
+        auto it       = b->tuned.find(kv.first);
+        const int ipb = it != b->tuned.end() ? it->second.first : b->instances_per_block;
+        const int grd = it != b->tuned.end() ? it->second.second : 0;
+        launch_ode_batched(B, kv.first, b->opts.precision, kv.second.first, kv.second.second, ipb, grd, s);
     }
     if (ev) {
         ck(cudaEventRecord(ev[1], s), "cudaEventRecord");
     }
     int64_t l = 0;
-    launch_exchange_batched(B, b->opts.precision, b->n_max, b->any_edge_dampings, s, &l);
+    launch_exchange_batched(B, b->opts.precision, b->n_max, b->any_edge_dampings, s, &l, ev ? ev + 2 : nullptr);
     launch_phase_end(B, s);
     if (ev) {
-        ck(cudaEventRecord(ev[2], s), "cudaEventRecord");
+        ck(cudaEventRecord(ev[5], s), "cudaEventRecord");
     }
 }
 
@@ -854,9 +926,13 @@ int mgpu_eval_rhs(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, con
     });
 }
 
-int mgpu_simulate(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, const int32_t* nodes, double t0,
-                  double tmax, double dt0, const mgpu_integrator_opts* opts, int32_t max_points, double* out_t,
-                  double* out_y, int32_t* num_points)
+namespace
+{
+// mgpu_simulate and mgpu_simulate_dt; dt_io (host, may be null) holds the
+// per-node step size in and out
+int simulate_impl(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, const int32_t* nodes, double t0,
+                  double tmax, double dt0, double* dt_io, const mgpu_integrator_opts* opts, int32_t max_points,
+                  double* out_t, double* out_y, int32_t* num_points)
 {
     return guarded(ctx, [&]() -> int {
         if (!graph || !opts || count < 0 || max_points < 1 ||
@@ -865,6 +941,11 @@ int mgpu_simulate(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, con
         }
         if (!(dt0 > 0)) {
             fail(MGPU_INVALID_VALUE, "dt0 must be > 0");
+        }
+        for (int k = 0; dt_io && k < count; ++k) {
+            if (!(dt_io[k] > 0)) {
+                fail(MGPU_INVALID_VALUE, "dt must be > 0");
+            }
         }
         if (count == 0) {
             return MGPU_OK;
@@ -892,10 +973,17 @@ int mgpu_simulate(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, con
             double* d_t      = io.alloc<double>((int64_t)count * max_points);
             double* d_y      = io.alloc<double>((int64_t)count * max_points * n);
             int32_t* d_np    = io.alloc<int32_t>(count);
+            double* d_dt     = dt_io ? io.alloc<double>(count) : nullptr;
             cudaStream_t s   = ctx->stream;
             ck(cudaMemcpyAsync(d_nodes, nodes, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s), "h2d");
-            launch_simulate(b.dev, d_nodes, count, t0, tmax, dt0, max_points, d_t, d_y, d_np, s);
+            if (d_dt) {
+                ck(cudaMemcpyAsync(d_dt, dt_io, sizeof(double) * count, cudaMemcpyHostToDevice, s), "h2d");
+            }
+            launch_simulate(b.dev, d_nodes, count, t0, tmax, dt0, max_points, d_t, d_y, d_np, s, d_dt);
             ck(cudaGetLastError(), "k_simulate");
+            if (d_dt) {
+                ck(cudaMemcpyAsync(dt_io, d_dt, sizeof(double) * count, cudaMemcpyDeviceToHost, s), "d2h");
+            }
             ck(cudaMemcpyAsync(num_points, d_np, sizeof(int32_t) * count, cudaMemcpyDeviceToHost, s), "d2h");
             ck(cudaMemcpyAsync(out_t, d_t, sizeof(double) * count * max_points, cudaMemcpyDeviceToHost, s), "d2h");
             ck(cudaMemcpyAsync(out_y, d_y, sizeof(double) * count * max_points * n, cudaMemcpyDeviceToHost, s),
@@ -919,6 +1007,26 @@ int mgpu_simulate(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, con
         }
         return rc;
     });
+}
+} // namespace
+
+int mgpu_simulate(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, const int32_t* nodes, double t0,
+                  double tmax, double dt0, const mgpu_integrator_opts* opts, int32_t max_points, double* out_t,
+                  double* out_y, int32_t* num_points)
+{
+    return simulate_impl(ctx, graph, count, nodes, t0, tmax, dt0, nullptr, opts, max_points, out_t, out_y,
+                         num_points);
+}
+
+int mgpu_simulate_dt(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, const int32_t* nodes, double t0,
+                     double tmax, double* dt, const mgpu_integrator_opts* opts, int32_t max_points, double* out_t,
+                     double* out_y, int32_t* num_points)
+{
+    if (count > 0 && !dt) {
+        return MGPU_INVALID_VALUE;
+    }
+    return simulate_impl(ctx, graph, count, nodes, t0, tmax, count > 0 ? dt[0] : 1.0, dt, opts, max_points, out_t,
+                         out_y, num_points);
 }
 
 int mgpu_batch_create(mgpu_context* ctx, const mgpu_graph* graphs, int32_t num_graphs, double t0,
@@ -991,6 +1099,7 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
         const int64_t attempts0 = (int64_t)(c0[CNT_ACCEPTED] + c0[CNT_REJECTED]);
         std::vector<size_t> ev_base;
         size_t nev           = 0;
+        bool six_events      = false; // batched phases: start, ODE, prep, return, exact path, end
         int64_t ode_launches = 0;
         ck(cudaEventRecord(b->ev_start, s), "cudaEventRecord");
         k_set_tmax<<<(b->num_graphs + 127) / 128, 128, 0, s>>>(b->dev.rt, b->d_tmax, b->num_graphs);
@@ -1051,14 +1160,15 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
         }
         else if (b->opts.profile) {
             for (int64_t p = 0; p < P; ++p) {
-                b->phase_event(nev + 2);
+                b->phase_event(nev + 5);
                 ev_base.push_back(nev);
                 enqueue_batched_phase(b, s, &b->ev_phase[nev]);
-                nev += 3;
+                nev += 6;
+                six_events = true;
                 ode_launches += (int64_t)b->inst_by_G.size();
             }
             b->launches +=
-                P * (2 + (int64_t)b->inst_by_G.size() + exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings));
+                P * (2 + (int64_t)b->inst_by_G.size() + exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size()));
             b->phases += P;
         }
         else {
@@ -1079,7 +1189,7 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
                 }
             }
             const int64_t per_phase = 2 + (int64_t)b->inst_by_G.size() +
-                                      exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings);
+                                      exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size());
             for (int64_t p = 0; p < P; ++p) {
                 if (b->graph_exec) {
                     ck(cudaGraphLaunch(b->graph_exec, s), "cudaGraphLaunch");
@@ -1098,21 +1208,336 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
         float ms = 0.0f;
         ck(cudaEventElapsedTime(&ms, b->ev_start, b->ev_stop), "cudaEventElapsedTime");
         b->timing.advance_ms = ms;
-        double ode = 0.0, exch = 0.0;
+        double ode = 0.0, exch = 0.0, part[4] = {0.0, 0.0, 0.0, 0.0};
+        const int last = six_events ? 5 : 2;
         for (size_t k : ev_base) {
             float a = 0.0f, c = 0.0f;
             ck(cudaEventElapsedTime(&a, b->ev_phase[k], b->ev_phase[k + 1]), "cudaEventElapsedTime");
-            ck(cudaEventElapsedTime(&c, b->ev_phase[k + 1], b->ev_phase[k + 2]), "cudaEventElapsedTime");
+            ck(cudaEventElapsedTime(&c, b->ev_phase[k + 1], b->ev_phase[k + last]), "cudaEventElapsedTime");
             ode += a;
             exch += c;
+            if (six_events) {
+                for (int q = 0; q < 4; ++q) {
+                    float x = 0.0f;
+                    ck(cudaEventElapsedTime(&x, b->ev_phase[k + 1 + q], b->ev_phase[k + 2 + q]),
+                       "cudaEventElapsedTime");
+                    part[q] += x;
+                }
+            }
         }
         b->timing.ode_ms       = ode;
         b->timing.exchange_ms  = exch;
+        b->timing.prep_ms      = part[0];
+        b->timing.return_ms    = part[1];
+        b->timing.exact_ms     = part[2];
+        b->timing.depart_ms    = part[3];
         b->timing.ode_launches = ode_launches;
         unsigned long long c1[CNT_NUM];
         ck(cudaMemcpy(c1, b->dev.counters, sizeof(c1), cudaMemcpyDeviceToHost), "d2h counters");
         b->timing.attempts = (int64_t)(c1[CNT_ACCEPTED] + c1[CNT_REJECTED]) - attempts0;
         return rc;
+    });
+}
+
+int mgpu_batch_launch(mgpu_batch* b, double tmax, const double* tmax_per_graph, int32_t max_phases,
+                      int32_t* remaining)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (max_phases < 1 || !remaining) {
+            fail(MGPU_INVALID_VALUE, "max_phases must be >= 1 and remaining non-null");
+        }
+        if (b->opts.precision == MGPU_PRECISION_FP64_PLAIN) {
+            fail(MGPU_UNSUPPORTED, "asynchronous advance needs a batched precision");
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        cudaStream_t s = b->ctx->stream;
+        if (!b->async_active) {
+            for (int i = 0; i < b->num_graphs; ++i) {
+                b->tmax_host[i] = tmax_per_graph ? tmax_per_graph[i] : tmax;
+            }
+            ck(cudaMemcpyAsync(b->d_tmax, b->tmax_host.data(), sizeof(double) * b->num_graphs,
+                               cudaMemcpyHostToDevice, s),
+               "h2d tmax");
+            k_set_tmax<<<(b->num_graphs + 127) / 128, 128, 0, s>>>(b->dev.rt, b->d_tmax, b->num_graphs);
+            ++b->launches;
+            b->async_t_end  = b->t_host;
+            b->async_left   = phases_needed(b, b->async_t_end);
+            b->async_active = true;
+            if (!b->ev_async) {
+                ck(cudaEventCreateWithFlags(&b->ev_async, cudaEventDisableTiming), "cudaEventCreate");
+            }
+        }
+        const int64_t n = std::min<int64_t>(max_phases, b->async_left);
+        const bool use_graph = b->opts.use_cuda_graph && !b->graph_failed;
+        if (use_graph && !b->graph_exec && n > 0) {
+            cudaGraph_t graph = nullptr;
+            ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+            enqueue_batched_phase(b, s);
+            cudaError_t e = cudaStreamEndCapture(s, &graph);
+            if (e == cudaSuccess) {
+                e = cudaGraphInstantiate(&b->graph_exec, graph, 0);
+                cudaGraphDestroy(graph);
+            }
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                b->graph_failed = true;
+                b->graph_exec   = nullptr;
+            }
+        }
+        for (int64_t p = 0; p < n; ++p) {
+            if (b->graph_exec) {
+                ck(cudaGraphLaunch(b->graph_exec, s), "cudaGraphLaunch");
+            }
+            else {
+                enqueue_batched_phase(b, s);
+            }
+        }
+        ck(cudaGetLastError(), "launch");
+        b->launches += n * (2 + (int64_t)b->inst_by_G.size() +
+                            exchange_batched_launches(b->opts.precision, b->dev.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size()));
+        b->phases += n;
+        b->async_left -= n;
+        ck(cudaEventRecord(b->ev_async, s), "cudaEventRecord");
+        *remaining = (int32_t)b->async_left;
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_query(mgpu_batch* b, int32_t* done)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!done) {
+            fail(MGPU_INVALID_VALUE, "null output");
+        }
+        *done = 1;
+        if (!b->async_active) {
+            return MGPU_OK;
+        }
+        const cudaError_t e = cudaEventQuery(b->ev_async);
+        if (e == cudaErrorNotReady) {
+            *done = 0;
+            return MGPU_OK;
+        }
+        ck(e, "cudaEventQuery");
+        if (b->async_left > 0) {
+            return MGPU_OK; // the launched intervals are done; more remain
+        }
+        b->async_active = false;
+        b->t_host       = b->async_t_end;
+        return check_device_error(b);
+    });
+}
+
+int mgpu_batch_get_graph_state(mgpu_batch* b, int32_t graph, double* out)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!out || graph < 0 || graph >= b->num_graphs) {
+            fail(MGPU_INVALID_VALUE, "null output or graph index out of range");
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        const int64_t off = b->state_off[graph];
+        const int64_t cnt = (int64_t)b->N[graph] * b->n[graph];
+        if (cnt == 0) {
+            return MGPU_OK;
+        }
+        cudaStream_t s = b->ctx->stream;
+        if (b->pairs) {
+            std::vector<float> hi(cnt), lo(cnt);
+            ck(cudaMemcpyAsync(hi.data(), b->dev.st_hi + off, sizeof(float) * cnt, cudaMemcpyDeviceToHost, s), "d2h");
+            ck(cudaMemcpyAsync(lo.data(), b->dev.st_lo + off, sizeof(float) * cnt, cudaMemcpyDeviceToHost, s), "d2h");
+            ck(cudaStreamSynchronize(s), "sync");
+            for (int64_t k = 0; k < cnt; ++k) {
+                out[k] = (double)hi[k] + (double)lo[k];
+            }
+        }
+        else {
+            ck(cudaMemcpyAsync(out, b->dev.state + off, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s), "d2h");
+            ck(cudaStreamSynchronize(s), "sync");
+        }
+        return MGPU_OK;
+    });
+}
+
+int64_t mgpu_batch_estimate_bytes(const mgpu_graph* graphs, int32_t num_graphs, const mgpu_solver_opts* opts)
+{
+    if (!graphs || num_graphs < 1) {
+        return -1;
+    }
+    mgpu_solver_opts o;
+    if (opts) {
+        o = *opts;
+    }
+    else {
+        mgpu_default_solver_opts(&o);
+    }
+    const bool plain = o.precision == MGPU_PRECISION_FP64_PLAIN;
+    const bool mixed = o.precision == MGPU_PRECISION_MIXED;
+    int64_t nodes = 0, edges = 0, st = 0, tr = 0, par = 0, con = 0, dtv = 0, dtt = 0, ec = 0, edv = 0, edt = 0,
+            nmax = 0;
+    for (int i = 0; i < num_graphs; ++i) {
+        const mgpu_graph& g = graphs[i];
+        const int64_t G = g.num_groups, n = 10 * G, N = g.num_nodes, E = g.num_edges, M = g.num_contact_matrices,
+                      K = g.num_damping_points, Ke = g.num_edge_damping_points;
+        nodes += N;
+        edges += E;
+        st += N * n;
+        tr += E * n;
+        par += N * MGPU_PARAM_STRIDE(G);
+        con += N * M * 2 * G * G;
+        dtt += N * M * K;
+        dtv += N * M * K * G * G;
+        ec += E * 2 * n;
+        edt += E * Ke;
+        edv += E * Ke * n;
+        nmax = std::max<int64_t>(nmax, N);
+    }
+    int64_t b = 8 * (par + con + dtt + dtv + ec + edt + edv) + 4 * tr; // inputs and FP32 coefficients
+    b += mixed ? 4 * st * 8 + 4 * nodes * MGPU_MAX_GROUPS * kTabF + 4 * (con + dtv) : 8 * st * 4;
+    b += plain ? 8 * st + 8 * tr + 8 * 8 * nmax * 60 : 8 * st * (mixed ? 0 : 2) + 4 * st * 2 +
+                                                            8 * nodes * MGPU_MAX_GROUPS * (4 + 12);
+    b += 8 * tr;                                             // fixed travelers
+    b += 16 * nodes + 4 * 2 * 3 * nodes * MGPU_MAX_GROUPS + 4 * nodes + 3 * nodes + 16 * (nodes + 1);
+    b += edges * (4 + 4 + 4 + 1 + 1 + 4 + 8 + 8 + MGPU_MAX_GROUPS);
+    b += num_graphs * (int64_t)(sizeof(DevGraph) + sizeof(GraphRt) + 8) + 64 * 1024;
+    return b + b / 10;
+}
+
+int mgpu_batch_autotune(mgpu_batch* b, int32_t* instances_per_block, int32_t* grid_blocks)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (b->opts.precision == MGPU_PRECISION_FP64_PLAIN) {
+            fail(MGPU_UNSUPPORTED, "the autotuner schedules the batched solvers");
+        }
+        if (b->async_active) {
+            fail(MGPU_INVALID_VALUE, "an asynchronous advance is in progress");
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        cudaStream_t s   = b->ctx->stream;
+        const BatchDev& B = b->dev;
+        // snapshot of everything one interval of node solves changes
+        struct Saved {
+            void* dst;
+            void* copy;
+            size_t bytes;
+        };
+        std::vector<Saved> saved;
+        DevPool tmp;
+        tmp.ctx  = b->ctx;
+        auto keep = [&](void* p, size_t bytes) {
+            if (p && bytes) {
+                void* c = tmp.alloc<char>((int64_t)bytes);
+                ck(cudaMemcpyAsync(c, p, bytes, cudaMemcpyDeviceToDevice, s), "d2d");
+                saved.push_back({p, c, bytes});
+            }
+        };
+        int best_ipb = 0, best_grid = 0;
+        std::function<void()> restore_all;
+        try {
+            const size_t st = (size_t)b->state_total;
+            if (b->pairs) {
+                keep(B.st_hi, st * sizeof(float));
+                keep(B.st_lo, st * sizeof(float));
+            }
+            else {
+                keep(B.state, st * sizeof(double));
+            }
+            keep(B.node_t, sizeof(double) * (size_t)B.num_nodes);
+            keep(B.node_dt, sizeof(double) * (size_t)B.num_nodes);
+            keep(B.rt, sizeof(GraphRt) * (size_t)b->num_graphs);
+            keep(B.counters, sizeof(unsigned long long) * CNT_NUM);
+            keep(B.err, sizeof(int32_t));
+            keep(b->d_tmax, sizeof(double) * (size_t)b->num_graphs);
+            restore_all = [&]() {
+                for (auto& x : saved) {
+                    ck(cudaMemcpyAsync(x.dst, x.copy, x.bytes, cudaMemcpyDeviceToDevice, s), "d2d");
+                }
+            };
+            auto& restore = restore_all;
+            // one interval for every graph: horizon t + dt_exchange
+            std::vector<double> h(b->num_graphs);
+            for (int i = 0; i < b->num_graphs; ++i) {
+                h[i] = b->t_host[i] + b->opts.dt_exchange;
+            }
+            ck(cudaMemcpyAsync(b->d_tmax, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, s), "h2d");
+            cudaEvent_t e0, e1;
+            ck(cudaEventCreate(&e0), "cudaEventCreate");
+            ck(cudaEventCreate(&e1), "cudaEventCreate");
+            // the node-solve kernels take at most 128 threads per block (their launch bounds)
+            const int warps_c[3] = {1, 2, 4};
+            const int grid_c[5]  = {0, 152 * 2, 152 * 3, 152 * 4, 152 * 6};
+            size_t most = 0;
+            for (auto& kv : b->inst_by_G) {
+                const int G   = kv.first;
+                const int ipw = 32 / G;
+                float best    = 1e30f;
+                std::pair<int, int> pick{4 * ipw, 0};
+                for (int w : warps_c) {
+                    for (int gr : grid_c) {
+                        k_set_tmax<<<(b->num_graphs + 127) / 128, 128, 0, s>>>(B.rt, b->d_tmax, b->num_graphs);
+                        launch_phase_begin(B, b->opts.dt_exchange, s);
+                        ck(cudaEventRecord(e0, s), "cudaEventRecord");
+                        launch_ode_batched(B, G, b->opts.precision, kv.second.first, kv.second.second, w * ipw, gr, s);
+                        ck(cudaEventRecord(e1, s), "cudaEventRecord");
+                        ck(cudaGetLastError(), "autotune launch");
+                        restore();
+                        ck(cudaStreamSynchronize(s), "sync");
+                        float ms = 0.0f;
+                        ck(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+                        if (ms < best) {
+                            best = ms;
+                            pick = {w * ipw, gr};
+                        }
+                    }
+                }
+                b->tuned[G] = pick;
+                if ((size_t)kv.second.second > most) {
+                    most      = (size_t)kv.second.second;
+                    best_ipb  = pick.first;
+                    best_grid = pick.second;
+                }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            if (b->graph_exec) {
+                cudaGraphExecDestroy(b->graph_exec); // recaptured with the tuned schedule
+                b->graph_exec = nullptr;
+            }
+        }
+        catch (...) {
+            // put the batch back as it was before the failed candidate
+            cudaGetLastError();
+            if (restore_all) {
+                try {
+                    restore_all();
+                    cudaStreamSynchronize(s);
+                }
+                catch (...) {
+                }
+            }
+            b->tuned.clear();
+            tmp.release();
+            throw;
+        }
+        tmp.release();
+        if (instances_per_block) {
+            *instances_per_block = best_ipb;
+        }
+        if (grid_blocks) {
+            *grid_blocks = best_grid;
+        }
+        return MGPU_OK;
     });
 }
 

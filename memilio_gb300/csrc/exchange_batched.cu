@@ -25,8 +25,9 @@
 //
 // Underflow fixes: a conservative per-node bound flags the nodes whose serial
 // return order might meet a negative remainder; those run the exact
-// (node, age group) scan of exchange.cu semantics in FP64 (k_xg_scan), then the
-// per-graph sequential pass handles what the scan passes leave unresolved.
+// (node, age group) scan of exchange.cu semantics (k_xg_scan in FP64, k_xf_scan
+// in float-float for the mixed solver), then the per-graph sequential pass
+// handles what the scan passes leave unresolved.
 #include "mgpu_internal.cuh"
 
 #include <type_traits>
@@ -971,11 +972,39 @@ __device__ __forceinline__ void edge_coeff_f(const BatchDev& B, const DevGraph& 
     ld_row(B.ecoef_f + g.ecoef_f_off + (e - g.edge0) * g.n + gr * kC, cf);
 }
 
+// Compartment masks of the FP32 passes: MASK holds the compartments whose
+// travelers can be nonzero (a nonzero coefficient on some edge of every graph
+// of the batch); the other compartments' travelers and the flows out of them
+// are exactly zero, so their arithmetic is compiled out. kMaskAll is the
+// general case; kMaskSEIYR the usual commuter pattern (S, E, INS, ISy, R).
+constexpr int kMaskAll   = (1 << kC) - 1;
+constexpr int kMaskSEIYR = (1 << MGPU_S) | (1 << MGPU_E) | (1 << MGPU_INS) | (1 << MGPU_ISY) | (1 << MGPU_R);
+__host__ __device__ constexpr bool in_mask(int mask, int c)
+{
+    return ((mask >> c) & 1) != 0;
+}
+// compartments a return can change: the mobile ones and the targets of their flows
+__host__ __device__ constexpr int touched_mask(int mask)
+{
+    int t = mask;
+    for (int k = 0; k < kF; ++k) {
+        if (in_mask(mask, kFlowSrcI(k))) {
+            t |= 1 << kFlowDstI(k);
+        }
+    }
+    return t;
+}
+
 // m = ((y o c) o f) with the nondetection factor nd on INS and ISy (same operations as depart_travelers<float>)
+template <int MASK = kMaskAll>
 __device__ __forceinline__ void travelers_cf(const GroupSnap& s, float nd, const float (&cf)[kC], float (&m)[kC])
 {
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
+        if (!in_mask(MASK, c)) {
+            m[c] = 0.0f;
+            continue;
+        }
         float v = __fmul_rn(__fmul_rn(s.y[c], cf[c]), c == MGPU_ISY ? s.risk : 1.0f);
         if (c == MGPU_INS || c == MGPU_ISY) {
             v = __fmul_rn(v, nd);
@@ -984,38 +1013,90 @@ __device__ __forceinline__ void travelers_cf(const GroupSnap& s, float nd, const
     }
 }
 
+template <int MASK = kMaskAll>
 __device__ __forceinline__ void travelers_f(const BatchDev& B, const DevGraph& g, int64_t e, int gr,
                                             const GroupSnap& s, float (&m)[kC])
 {
     float cf[kC];
     edge_coeff_f(B, g, e, gr, cf);
-    travelers_cf(s, s.nd, cf, m);
+    travelers_cf<MASK>(s, s.nd, cf, m);
 }
 
+template <int MASK = kMaskAll>
 __device__ __forceinline__ void flows_f(const float (&a)[kAux], float dt, const float (&m)[kC], float (&phi)[kF])
 {
-    const float s[kF] = {m[MGPU_S],    m[MGPU_E],    m[MGPU_INS],  m[MGPU_INS],  m[MGPU_INSC],
-                         m[MGPU_INSC], m[MGPU_ISY],  m[MGPU_ISY],  m[MGPU_ISYC], m[MGPU_ISYC],
-                         m[MGPU_ISEV], m[MGPU_ISEV], m[MGPU_ISEV], m[MGPU_ICRI], m[MGPU_ICRI]};
     const int ai[kF] = {0, 1, 2, 3, 2, 3, 4, 5, 4, 5, 6, 7, 8, 9, 10};
 #pragma unroll
     for (int k = 0; k < kF; ++k) {
-        phi[k] = __fmul_rn(dt, __fmul_rn(a[ai[k]], s[k]));
+        phi[k] = in_mask(MASK, kFlowSrcI(k)) ? __fmul_rn(dt, __fmul_rn(a[ai[k]], m[kFlowSrcI(k)])) : 0.0f;
     }
 }
 
-__global__ void k_xf_depart(BatchDev B, int64_t n0, int64_t nn)
+// The incident edges of `node` in the serial return order of the reference
+// (edges sorted by (src, dst)): in-edges from lower nodes, the out-edges, then
+// in-edges from higher nodes. next() yields each edge once with its kind and
+// reports the switch from the first in-edge run to the out-edges.
+struct ReturnOrder {
+    const BatchDev& B;
+    int64_t node, k, ie, o, oe;
+    int phase; // 0: in-edges with src < node, 1: out-edges, 2: in-edges with src > node
+    __device__ ReturnOrder(const BatchDev& b, int64_t v)
+        : B(b)
+        , node(v)
+        , k(b.in_ptr[v])
+        , ie(b.in_ptr[v + 1])
+        , o(b.out_ptr[v])
+        , oe(b.out_ptr[v + 1])
+        , phase(0)
+    {
+    }
+    // e: the edge; returns 0 at the end, 1 for an in-edge, 2 for an out-edge;
+    // *switched is set on the first edge after the lower in-edges
+    __device__ __forceinline__ int next(int64_t& e, bool& switched)
+    {
+        switched = false;
+        if (phase == 0) {
+            if (k < ie) {
+                const int64_t x = B.in_edges[k];
+                if (B.edge_src[x] < node) {
+                    ++k;
+                    e = x;
+                    return 1;
+                }
+            }
+            phase    = 1;
+            switched = true;
+        }
+        if (phase == 1) {
+            if (o < oe) {
+                e = o++;
+                return 2;
+            }
+            phase = 2;
+        }
+        if (k < ie) {
+            e = B.in_edges[k++];
+            return 1;
+        }
+        return 0;
+    }
+};
+
+// Dense (node, group) mapping as k_xf_return.
+template <int MASK>
+__global__ void k_xf_depart(BatchDev B, const int32_t* inst, int64_t count, int G)
 {
-    const int64_t tid  = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t node = n0 + tid / MGPU_MAX_GROUPS;
-    const int gr       = (int)(tid % MGPU_MAX_GROUPS);
-    if (tid >= nn * MGPU_MAX_GROUPS) {
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= count * G) {
         return;
     }
-    const int gi      = B.node_graph[node];
-    const DevGraph& g = B.graphs[gi];
-    const GraphRt& rt = B.rt[gi];
-    if (gr >= g.G || !xb_departing(rt) || g.Ke != 0) {
+    const int64_t qi   = tid / G;
+    const int64_t node = inst[qi];
+    const int gr       = (int)(tid - qi * G);
+    const int gi       = B.node_graph[node];
+    const DevGraph& g  = B.graphs[gi];
+    const GraphRt& rt  = B.rt[gi];
+    if (!xb_departing(rt) || g.Ke != 0) {
         return;
     }
     const int ws     = rt.snap_slot ^ 1;
@@ -1034,27 +1115,25 @@ __global__ void k_xf_depart(BatchDev B, int64_t n0, int64_t nn)
     GroupSnap own, src;
     load_group_snap(B, g, node, gr, ws, own);
     float m[kC];
-    const int64_t ib = B.in_ptr[node], ie = B.in_ptr[node + 1];
-    int64_t k        = ib;
-    for (; k < ie; ++k) {
-        const int64_t e = B.in_edges[k];
-        const int64_t u = B.edge_src[e];
-        if (u > node) {
-            break;
-        }
-        if (B.edge_static_any[e]) {
-            load_group_snap(B, g, u, gr, ws, src);
-            travelers_f(B, g, e, gr, src, m);
-#pragma unroll
-            for (int c = 0; c < kC; ++c) {
-                acc[c].add(m[c]);
-            }
-        }
-    }
     const bool detect = own.nd != 1.0f;
     const float q     = 1.0f - own.nd;
-    for (int64_t e = B.out_ptr[node]; e < B.out_ptr[node + 1]; ++e) {
+    ReturnOrder order(B, node);
+    int64_t e;
+    bool switched;
+    for (int kind = order.next(e, switched); kind != 0; kind = order.next(e, switched)) {
         if (!B.edge_static_any[e]) {
+            continue;
+        }
+        if (kind == 1) {
+            // travelers arriving from the edge's source
+            load_group_snap(B, g, B.edge_src[e], gr, ws, src);
+            travelers_f<MASK>(B, g, e, gr, src, m);
+#pragma unroll
+            for (int c = 0; c < kC; ++c) {
+                if (in_mask(MASK, c)) {
+                    acc[c].add(m[c]);
+                }
+            }
             continue;
         }
         float cf[kC];
@@ -1062,26 +1141,21 @@ __global__ void k_xf_depart(BatchDev B, int64_t n0, int64_t nn)
         if (detect) {
             // test_commuters: detected commuters move to the confirmed compartments first
             float mo[kC];
-            travelers_cf(own, 1.0f, cf, mo);
-            acc[MGPU_INS].add(-__fmul_rn(mo[MGPU_INS], q));
-            acc[MGPU_INSC].add(__fmul_rn(mo[MGPU_INS], q));
-            acc[MGPU_ISY].add(-__fmul_rn(mo[MGPU_ISY], q));
-            acc[MGPU_ISYC].add(__fmul_rn(mo[MGPU_ISY], q));
+            travelers_cf<MASK>(own, 1.0f, cf, mo);
+            if (in_mask(MASK, MGPU_INS)) {
+                acc[MGPU_INS].add(-__fmul_rn(mo[MGPU_INS], q));
+                acc[MGPU_INSC].add(__fmul_rn(mo[MGPU_INS], q));
+            }
+            if (in_mask(MASK, MGPU_ISY)) {
+                acc[MGPU_ISY].add(-__fmul_rn(mo[MGPU_ISY], q));
+                acc[MGPU_ISYC].add(__fmul_rn(mo[MGPU_ISY], q));
+            }
         }
-        travelers_cf(own, own.nd, cf, m);
+        travelers_cf<MASK>(own, own.nd, cf, m);
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
-            acc[c].add(-m[c]);
-        }
-    }
-    for (; k < ie; ++k) {
-        const int64_t e = B.in_edges[k];
-        if (B.edge_static_any[e]) {
-            load_group_snap(B, g, B.edge_src[e], gr, ws, src);
-            travelers_f(B, g, e, gr, src, m);
-#pragma unroll
-            for (int c = 0; c < kC; ++c) {
-                acc[c].add(m[c]);
+            if (in_mask(MASK, c)) {
+                acc[c].add(-m[c]);
             }
         }
     }
@@ -1096,18 +1170,22 @@ __global__ void k_xf_depart(BatchDev B, int64_t n0, int64_t nn)
     st_state(B.v0_lo + so, l);
 }
 
-__global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
+// One thread per (node, group) of the nodes with G age groups (dense: node
+// = inst[tid / G], group = tid % G, so no lane idles on unused groups).
+template <int MASK>
+__global__ void __launch_bounds__(128, 4) k_xf_return(BatchDev B, const int32_t* inst, int64_t count, int G)
 {
-    const int64_t tid  = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t node = n0 + tid / MGPU_MAX_GROUPS;
-    const int gr       = (int)(tid % MGPU_MAX_GROUPS);
-    if (tid >= nn * MGPU_MAX_GROUPS) {
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= count * G) {
         return;
     }
-    const int gi      = B.node_graph[node];
-    const DevGraph& g = B.graphs[gi];
-    const GraphRt& rt = B.rt[gi];
-    if (gr >= g.G || !xb_returning(rt) || g.Ke != 0) {
+    const int64_t q    = tid / G;
+    const int64_t node = inst[q];
+    const int gr       = (int)(tid - q * G);
+    const int gi       = B.node_graph[node];
+    const DevGraph& g  = B.graphs[gi];
+    const GraphRt& rt  = B.rt[gi];
+    if (!xb_returning(rt) || g.Ke != 0) {
         return;
     }
     const int slot   = rt.snap_slot;
@@ -1115,111 +1193,108 @@ __global__ void k_xf_return(BatchDev B, int64_t n0, int64_t nn)
     const int64_t lv = node - g.node0;
     const int64_t s0 = g.state_off + lv * g.n + gr * kC;
     Acc<float> acc[kC];
-    float yf[kC], min_in[kC], phi_in[kF], phi_out[kF];
+    // lower bound of the running state along the serial order, and its magnitude
+    float run[kC], mag[kC], phi_net[kF];
     {
-        float l[kC];
-        ld_state(B.st_hi + s0, yf);
+        float h[kC], l[kC];
+        ld_state(B.st_hi + s0, h);
         ld_state(B.st_lo + s0, l);
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
-            acc[c].init_pair(yf[c], l[c]);
-            min_in[c] = 0.0f;
+            acc[c].init_pair(h[c], l[c]);
+            run[c] = h[c];
+            mag[c] = fabsf(h[c]);
         }
     }
 #pragma unroll
     for (int f = 0; f < kF; ++f) {
-        phi_in[f]  = 0.0f;
-        phi_out[f] = 0.0f;
+        phi_net[f] = 0.0f;
     }
     const float* aux = reinterpret_cast<const float*>(B.aux);
     float a_own[kAux];
     ld_aux12(aux + (node * MGPU_MAX_GROUPS + gr) * kAux, a_own);
     GroupSnap own, src;
     load_group_snap(B, g, node, gr, slot, own);
-    float m[kC], phi[kF];
-    float lowest = 0.0f; // a negative traveler voids the bound
-    bool unsafe  = false; // a destination whose Euler step may drive travelers negative
-    auto in_edge = [&](int64_t e, int64_t u) {
-        load_group_snap(B, g, u, gr, slot, src);
-        travelers_f(B, g, e, gr, src, m);
-        flows_f(a_own, dt, m, phi);
-        // returning amounts t_c = m_c + inflows - outflows (for the bound only)
-        float t[kC];
+    // run[c] is a lower bound of the exact running state of the serial order:
+    // in-edges take max(t, 0) away, out-edges add t (negative amounts included),
+    // so within each run of in-edges it only decreases, and the underflow test of
+    // the reference (rem = running - t < 0 at in-edges) can only fail if run
+    // drops below zero at the end of a run of in-edges. Those two points are
+    // checked with a margin of 1e-5 of the magnitudes, above the FP32 rounding of
+    // the running sums.
+    bool flag = false;
+    ReturnOrder order(B, node);
+    int64_t e;
+    bool switched;
+    for (int kind = order.next(e, switched);; kind = order.next(e, switched)) {
+        if (switched) {
 #pragma unroll
-        for (int c = 0; c < kC; ++c) {
-            acc[c].add(-m[c]);
-            t[c]   = m[c];
-            lowest = fminf(lowest, m[c]);
+            for (int c = 0; c < kC; ++c) {
+                flag = flag || run[c] < 1e-5f * mag[c];
+            }
         }
-#pragma unroll
-        for (int f = 0; f < kF; ++f) {
-            phi_in[f] += phi[f];
-            t[kFlowSrcI(f)] -= phi[f];
-            t[kFlowDstI(f)] += phi[f];
-        }
-#pragma unroll
-        for (int c = 0; c < kC; ++c) {
-            min_in[c] += fmaxf(t[c], 0.0f);
-        }
-    };
-    const int64_t ib = B.in_ptr[node], ie = B.in_ptr[node + 1];
-    int64_t k        = ib;
-    for (; k < ie; ++k) {
-        const int64_t e = B.in_edges[k];
-        const int64_t u = B.edge_src[e];
-        if (u > node) {
+        if (kind == 0) {
             break;
         }
-        if (B.edge_static_any[e]) {
-            in_edge(e, u);
-        }
-    }
-    for (int64_t e = B.out_ptr[node]; e < B.out_ptr[node + 1]; ++e) {
         if (!B.edge_static_any[e]) {
             continue;
         }
         float ax[kAux];
-        ld_aux12(aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux, ax);
-        travelers_f(B, g, e, gr, own, m);
-        flows_f(ax, dt, m, phi);
-        unsafe = unsafe || ax[11] != 0.0f;
+        const float* a;
+        float m[kC], phi[kF];
+        if (kind == 1) {
+            load_group_snap(B, g, B.edge_src[e], gr, slot, src);
+            travelers_f<MASK>(B, g, e, gr, src, m);
+            a = a_own;
+        }
+        else {
+            ld_aux12(aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux, ax);
+            travelers_f<MASK>(B, g, e, gr, own, m);
+            a = ax;
+        }
+        flows_f<MASK>(*reinterpret_cast<const float(*)[kAux]>(a), dt, m, phi);
+        // returning amounts t_c = m_c + inflows - outflows (for the bound only)
+        float t[kC];
+        const float sgn = kind == 1 ? -1.0f : 1.0f;
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
-            acc[c].add(m[c]);
-            lowest = fminf(lowest, m[c]);
+            if (in_mask(MASK, c)) {
+                acc[c].add(sgn * m[c]);
+            }
+            t[c] = m[c];
         }
 #pragma unroll
         for (int f = 0; f < kF; ++f) {
-            phi_out[f] += phi[f];
+            if (in_mask(MASK, kFlowSrcI(f))) {
+                phi_net[f] += sgn * phi[f];
+                t[kFlowSrcI(f)] -= phi[f];
+                t[kFlowDstI(f)] += phi[f];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            // in-edges take max(t, 0) away; out-edges bring t home (a negative t counts against)
+            if (in_mask(touched_mask(MASK), c)) {
+                run[c] += kind == 1 ? -fmaxf(t[c], 0.0f) : t[c];
+                mag[c] += fabsf(t[c]);
+            }
         }
     }
-    for (; k < ie; ++k) {
-        const int64_t e = B.in_edges[k];
-        if (B.edge_static_any[e]) {
-            in_edge(e, B.edge_src[e]);
-        }
-    }
-    // flow increments: in-edges take travelers away (their increments count
-    // with the opposite sign), out-edges bring them home
+    // flow increments: in-edges take travelers away (their increments count with
+    // the opposite sign), out-edges bring them home
 #pragma unroll
     for (int f = 0; f < kF; ++f) {
-        acc[kFlowSrcI(f)].add(phi_in[f]);
-        acc[kFlowDstI(f)].add(-phi_in[f]);
-        acc[kFlowSrcI(f)].add(-phi_out[f]);
-        acc[kFlowDstI(f)].add(phi_out[f]);
+        if (in_mask(MASK, kFlowSrcI(f))) {
+            acc[kFlowSrcI(f)].add(-phi_net[f]);
+            acc[kFlowDstI(f)].add(phi_net[f]);
+        }
     }
-    // conservative no-underflow bound: with nonnegative travelers whose Euler
-    // step stays nonnegative, every partial state of the serial order is at
-    // least y minus the positive parts of all returning in-edge amounts
-    bool flag = lowest < 0.0f || unsafe;
     const int64_t so = g.state_off + lv * g.n + gr * kC;
     float h[kC], l[kC];
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
         acc[c].store(&h[c], &l[c]);
-        const float bound = yf[c] - min_in[c];
-        const float mag   = fabsf(yf[c]) + min_in[c];
-        flag              = flag || (bound < 1e-5f * mag);
+        flag = flag || run[c] < 1e-5f * mag[c];
     }
     st_state(B.yn_hi + so, h);
     st_state(B.yn_lo + so, l);
@@ -1385,6 +1460,200 @@ __global__ void k_xg_scan(BatchDev B, int pass)
     }
 }
 
+// ---- the exact path of the mixed solver in float-float arithmetic -------------
+// GB300 runs FP64 at a small fraction of its FP32 rate, so the mixed solver
+// replays the serial return order with float-float values (hi + lo, ~48 bits):
+// the same decisions as FP64 except where a remainder is within ~1e-14 of zero,
+// and node totals conserved to the same order. Fixed travelers are published as
+// the exact pair (two floats in the 8-byte record).
+
+struct FF {
+    float h, l;
+};
+__device__ __forceinline__ FF ff_two_sum(float a, float b)
+{
+    const float s  = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e  = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+__device__ __forceinline__ FF ff_norm(float s, float e)
+{
+    const float h = __fadd_rn(s, e);
+    return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b)
+{
+    const FF s = ff_two_sum(a.h, b.h);
+    const FF t = ff_two_sum(a.l, b.l);
+    FF r       = ff_norm(s.h, __fadd_rn(s.l, t.h));
+    return ff_norm(r.h, __fadd_rn(r.l, t.l));
+}
+__device__ __forceinline__ FF ff_neg(FF a)
+{
+    return {-a.h, -a.l};
+}
+__device__ __forceinline__ FF ff_add_f(FF a, float b)
+{
+    const FF s = ff_two_sum(a.h, b);
+    return ff_norm(s.h, __fadd_rn(s.l, a.l));
+}
+__device__ __forceinline__ bool ff_neg_p(FF a)
+{
+    return a.h < 0.0f || (a.h == 0.0f && a.l < 0.0f);
+}
+__device__ __forceinline__ bool ff_gt(FF a, FF b)
+{
+    return a.h > b.h || (a.h == b.h && a.l > b.l);
+}
+
+// Returning travelers of group gr on edge e as float-float values: the FP32
+// travelers plus the Euler flow increments (return_travelers in pairs).
+__device__ __forceinline__ void return_travelers_ff(const BatchDev& B, const DevGraph& g, const GraphRt& rt,
+                                                    int64_t e, int gr, FF (&t)[kC])
+{
+    float m[kC], phi[kF];
+    return_flows<float>(B, g, rt, e, gr, m, phi);
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        t[c] = {m[c], 0.0f};
+    }
+#pragma unroll
+    for (int k = 0; k < kF; ++k) {
+        t[kFlowSrcI(k)] = ff_add_f(t[kFlowSrcI(k)], -phi[k]);
+        t[kFlowDstI(k)] = ff_add_f(t[kFlowDstI(k)], phi[k]);
+    }
+}
+
+// fix_group in pairs
+__device__ __forceinline__ int fix_group_ff(const FF (&y)[kC], FF (&t)[kC])
+{
+    FF rem[kC];
+    bool neg = false;
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        rem[c] = ff_add(y[c], ff_neg(t[c]));
+        neg    = neg || ff_neg_p(rem[c]);
+    }
+    if (!neg) {
+        return 0;
+    }
+    int mx = 0;
+    FF rmx = rem[0];
+#pragma unroll
+    for (int q = 1; q < kC; ++q) {
+        if (ff_gt(rem[q], rmx)) {
+            rmx = rem[q];
+            mx  = q;
+        }
+    }
+    int nfix = 0;
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        if (ff_neg_p(rem[c])) {
+#pragma unroll
+            for (int q = 0; q < kC; ++q) {
+                if (q == mx) {
+                    t[q] = ff_add(t[q], ff_neg(rem[c]));
+                }
+            }
+            t[c] = ff_add(t[c], rem[c]);
+            ++nfix;
+        }
+    }
+    return nfix;
+}
+
+__global__ void k_xf_scan(BatchDev B, int pass)
+{
+    const int lin    = pass == 0 ? 0 : 1 + ((pass - 1) & 1);
+    const int lout   = 1 + (pass & 1);
+    const int cnt    = B.scan_count[lin];
+    const int64_t NG = B.num_nodes * MGPU_MAX_GROUPS;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && cnt > 0) {
+        atomicAdd(&B.counters[CNT_SCANNED], (unsigned long long)cnt);
+    }
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < cnt;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t item = B.scan_list[lin * NG + idx];
+        B.scan_mark[lin * NG + item] = 0; // consumed
+        const int64_t node = item / MGPU_MAX_GROUPS;
+        const int gr       = (int)(item % MGPU_MAX_GROUPS);
+        const int gi       = B.node_graph[node];
+        const DevGraph& g  = B.graphs[gi];
+        const GraphRt& rt  = B.rt[gi];
+        if (gr >= g.G || !xb_returning(rt)) {
+            continue;
+        }
+        const int64_t so = g.state_off + (node - g.node0) * g.n + gr * kC;
+        FF y[kC];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            y[c] = {B.st_hi[so + c], B.st_lo[so + c]};
+        }
+        ReturnOrder order(B, node);
+        int64_t e;
+        bool switched;
+        for (int kind = order.next(e, switched); kind != 0; kind = order.next(e, switched)) {
+            if (!edge_departed(B, g, e)) {
+                continue;
+            }
+            uint8_t* fc    = B.fix_cnt + e * MGPU_MAX_GROUPS + gr;
+            float2* mf     = reinterpret_cast<float2*>(B.mfix + B.trav_off[e] + gr * kC);
+            const int prev = *(volatile uint8_t*)fc;
+            FF t[kC];
+            if (kind == 2 && prev != 0) {
+                // fixed by the destination's scan: the published pair
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    const float2 v = __ldcg(mf + c);
+                    t[c]           = {v.x, v.y};
+                }
+            }
+            else {
+                return_travelers_ff(B, g, rt, e, gr, t);
+            }
+            if (kind == 2) {
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    y[c] = ff_add(y[c], t[c]);
+                }
+                continue;
+            }
+            const int nfix = fix_group_ff(y, t);
+            bool changed   = false;
+            if (nfix) {
+                changed = prev == 0;
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    const float2 old = __ldcg(mf + c);
+                    changed          = changed || old.x != t[c].h || old.y != t[c].l;
+                    __stcg(mf + c, make_float2(t[c].h, t[c].l));
+                }
+                __threadfence();
+                *(volatile uint8_t*)fc = (uint8_t)nfix;
+            }
+            else if (prev) {
+                *(volatile uint8_t*)fc = 0;
+                changed                = true;
+            }
+            if (changed) {
+                list_push(B, lout, B.edge_src[e] * MGPU_MAX_GROUPS + gr);
+            }
+#pragma unroll
+            for (int c = 0; c < kC; ++c) {
+                y[c] = ff_add(y[c], ff_neg(t[c]));
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            const FF v      = ff_norm(y[c].h, y[c].l);
+            B.yn_hi[so + c] = v.h;
+            B.yn_lo[so + c] = v.l;
+        }
+    }
+}
+
 // Nodes still marked after the last pass send their graph to the sequential
 // pass; resets the lists for the next return.
 __global__ void k_xg_scan_done(BatchDev B, int last_list)
@@ -1531,9 +1800,17 @@ inline unsigned blocks_of(int64_t n, int t)
 
 constexpr int kXbScanPasses = 4;
 
+// ev (profiling, may be null): recorded after the node pass, after the return
+// pass, and after the exact path with the commit.
 template <class R>
-void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStream_t s, int64_t* launches)
+void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStream_t s, int64_t* launches,
+               cudaEvent_t* ev)
 {
+    auto mark = [&](int k) {
+        if (ev) {
+            cudaEventRecord(ev[k], s);
+        }
+    };
     const int64_t nn = B.num_nodes, ne = B.num_edges;
     if (nn == 0) {
         return;
@@ -1546,24 +1823,42 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
         k_xb_prep<R><<<blocks_of(nn * MGPU_MAX_GROUPS, T), T, 0, s>>>(B, 0, nn);
     }
     *launches += 1;
+    mark(0);
     if (ne == 0) {
+        mark(1);
+        mark(2);
         return;
     }
     const int64_t ng  = nn * MGPU_MAX_GROUPS;
     const bool mixed  = std::is_same<R, float>::value;
     if (mixed) {
-        k_xf_return<<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
-        *launches += 1;
+        for (int G = 1; G <= MGPU_MAX_GROUPS; ++G) {
+            if (B.gcount[G] > 0) {
+                if ((B.mob_union & ~kMaskSEIYR) == 0) {
+                    k_xf_return<kMaskSEIYR><<<blocks_of(B.gcount[G] * G, T), T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                }
+                else {
+                    k_xf_return<kMaskAll><<<blocks_of(B.gcount[G] * G, T), T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                }
+                *launches += 1;
+            }
+        }
     }
     if (!mixed || any_edge_dampings) {
         k_xb_return<R><<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
         *launches += 1;
     }
+    mark(1);
     // exact underflow path over the work lists (list 0 was filled by the return pass)
     const unsigned scan_blocks = 152 * 8;
     for (int pass = 0; pass < kXbScanPasses; ++pass) {
         k_list_reset<<<1, 1, 0, s>>>(B, 1 + (pass & 1));
-        k_xg_scan<R><<<scan_blocks, 128, 0, s>>>(B, pass);
+        if (std::is_same<R, float>::value) {
+            k_xf_scan<<<scan_blocks, 128, 0, s>>>(B, pass);
+        }
+        else {
+            k_xg_scan<R><<<scan_blocks, 128, 0, s>>>(B, pass);
+        }
     }
     const int last = 1 + ((kXbScanPasses - 1) & 1);
     k_xg_scan_done<<<scan_blocks, 128, 0, s>>>(B, last);
@@ -1571,13 +1866,23 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
     k_xb_commit<<<blocks_of(nn * n_max, 256), 256, 0, s>>>(B, 0, nn, (int)n_max);
     k_xb_sequential<R><<<B.num_graphs, 32, 0, s>>>(B, 0, B.num_graphs);
     k_xg_cleanup<<<blocks_of(ne, 256), 256, 0, s>>>(B, ne);
+    mark(2);
     if (any_edge_dampings) {
         k_xb_edge_flags<<<blocks_of(ne, 256), 256, 0, s>>>(B, 0, ne);
         *launches += 1;
     }
     if (mixed) {
-        k_xf_depart<<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
-        *launches += 1;
+        for (int G = 1; G <= MGPU_MAX_GROUPS; ++G) {
+            if (B.gcount[G] > 0) {
+                if ((B.mob_union & ~kMaskSEIYR) == 0) {
+                    k_xf_depart<kMaskSEIYR><<<blocks_of(B.gcount[G] * G, T), T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                }
+                else {
+                    k_xf_depart<kMaskAll><<<blocks_of(B.gcount[G] * G, T), T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                }
+                *launches += 1;
+            }
+        }
     }
     if (!mixed || any_edge_dampings) {
         k_xb_depart<R><<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
@@ -1588,23 +1893,25 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
 
 } // namespace
 
-int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings)
+int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings, int group_lists)
 {
     if (!has_edges) {
         return 1;
     }
-    const int extra = !any_edge_dampings ? 0 : (precision == MGPU_PRECISION_MIXED ? 3 : 1);
-    return 8 + 2 * kXbScanPasses + extra;
+    const bool mixed = precision == MGPU_PRECISION_MIXED;
+    const int extra  = !any_edge_dampings ? 0 : (mixed ? 3 : 1);
+    // prep, return and departure passes (one per age-group count when mixed), the exact path
+    return 6 + (mixed ? 2 * group_lists : 2) + 2 * kXbScanPasses + extra;
 }
 
 void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,
-                             cudaStream_t s, int64_t* launches)
+                             cudaStream_t s, int64_t* launches, cudaEvent_t* ev)
 {
     if (precision == MGPU_PRECISION_MIXED) {
-        launch_xb<float>(B, n_max, any_edge_dampings, s, launches);
+        launch_xb<float>(B, n_max, any_edge_dampings, s, launches, ev);
     }
     else {
-        launch_xb<double>(B, n_max, any_edge_dampings, s, launches);
+        launch_xb<double>(B, n_max, any_edge_dampings, s, launches, ev);
     }
 }
 

@@ -39,6 +39,7 @@ struct DevGraph {
     int64_t edt_off;     // doubles, [E][Ke]
     int64_t edv_off;     // doubles, [E][Ke][n]
     int64_t ecoef_f_off; // floats, [E][n] coefficients (Ke == 0) for the mixed exchange
+    int32_t mob_mask;    // compartments c with a nonzero coefficient on some edge and age group
 };
 
 // Mutable per-graph state (GraphSimulation::m_t and the edges' shared return flag).
@@ -99,6 +100,10 @@ struct BatchDev {
     uint8_t* node_flag;          // [num_nodes] return needs the exact per-node scan
     uint8_t* node_dirty;         // [2][num_nodes] an out-edge changed: rescan (double-buffered)
     // batched exchange: exact-scan work lists (0: flagged by the bound, 1/2: rescans)
+    // node instances per age-group count (dense (node, group) mappings): glist[G], gcount[G]
+    int32_t mob_union;           // OR of the graphs' mob_mask
+    const int32_t* glist[MGPU_MAX_GROUPS + 1];
+    int64_t gcount[MGPU_MAX_GROUPS + 1];
     int32_t* scan_mark;          // [3][num_nodes * MAX_GROUPS] (node, group) item is in list k
     int32_t* scan_list;          // [3][num_nodes * MAX_GROUPS] items node * MAX_GROUPS + group
     int32_t* scan_count;         // [3]
@@ -459,7 +464,8 @@ __device__ inline double edge_coeff_at(const BatchDev& B, const DevGraph& g, int
 // Launchers (defined in the .cu files).
 void launch_ode_plain(const BatchDev& B, int64_t node_begin, int64_t node_end, cudaStream_t s);
 void launch_simulate(const BatchDev& B, const int32_t* d_nodes, int count, double t0, double tmax, double dt0,
-                     int max_points, double* d_out_t, double* d_out_y, int32_t* d_num_points, cudaStream_t s);
+                     int max_points, double* d_out_t, double* d_out_y, int32_t* d_num_points, cudaStream_t s,
+                     double* d_dt_io = nullptr);
 void launch_eval_rhs(const BatchDev& B, const int32_t* d_nodes, int count, const double* d_pop, const double* d_y,
                      const double* d_t, double* d_dydt, cudaStream_t s);
 int launch_ode_batched(const BatchDev& B, int G, int precision, const int32_t* d_instances, int64_t count,
@@ -468,8 +474,9 @@ void launch_phase_begin(const BatchDev& B, double dt_exchange, cudaStream_t s);
 void launch_exchange(const BatchDev& B, int64_t max_n, cudaStream_t s, int64_t* launches);
 int exchange_launches(bool has_edges);
 void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,
-                             cudaStream_t s, int64_t* launches);
-int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings);
+                             cudaStream_t s, int64_t* launches,
+                             cudaEvent_t* ev = nullptr);
+int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings, int group_lists);
 
 // Device and stream of a context (for entry points defined outside capi.cu).
 int context_device_stream(const mgpu_context* ctx, int* device, cudaStream_t* stream);

@@ -561,6 +561,7 @@ struct SegF {
     float P[G], Q[G];
     float t_lo, t_hi, xl, scale; // damping segment and ramp, relative to t_base
     double t_base;
+    float t_base_f;
     const float* cm_f; // the node's contact matrix (baseline, minimum) in FP32
     const float* dv_f; // the node's damping cache values in FP32
 };
@@ -584,11 +585,17 @@ __device__ void segf_load_contact(SegF<G>& X, float tau_rel)
         X.scale = 0.0f;
         return;
     }
-    const double tau = X.t_base + (double)tau_rel;
+    // FP32 on the interval-relative clock: the FP64 pipe of GB300 is a small
+    // fraction of the FP32 one, and relative times within an interval need no
+    // more than FP32 (the cache times are converted once per lookup)
     const double* T  = nm.dtimes;
-    const int ub     = damping_upper_bound(T, nm.K, tau);
-    const float* Dl  = X.dv_f + (long)(ub - 1) * GG + (long)X.gi * G;
-    const float* Dr  = Dl + GG;
+    int ub           = 0;
+    while (ub < nm.K && !(tau_rel < (float)T[ub] - X.t_base_f)) {
+        ++ub;
+    }
+    ub              = ub < nm.K ? ub : nm.K - 1;
+    const float* Dl = X.dv_f + (long)(ub - 1) * GG + (long)X.gi * G;
+    const float* Dr = Dl + GG;
 #pragma unroll
     for (int j = 0; j < G; ++j) {
         const float BL = Bm[j] - Lm[j];
@@ -596,10 +603,11 @@ __device__ void segf_load_contact(SegF<G>& X, float tau_rel)
         X.Q[j]         = -(0.5f * (Dl[j] - Dr[j])) * BL;
     }
     // times relative to the interval start; far sentinels saturate to +-inf
-    X.t_lo  = (float)(T[ub - 1] - X.t_base);
-    X.t_hi  = (float)(T[ub] - X.t_base);
-    X.xl    = (float)((T[ub] - 1.0) - X.t_base);
-    X.scale = (float)(1.0 / (T[ub] - (T[ub] - 1.0)));
+    const float tu = (float)T[ub];
+    X.t_lo         = (float)T[ub - 1] - X.t_base_f;
+    X.t_hi         = tu - X.t_base_f;
+    X.xl           = (tu - 1.0f) - X.t_base_f;
+    X.scale        = __frcp_rn(tu - (tu - 1.0f));
 }
 
 template <int G>
@@ -613,6 +621,7 @@ __device__ void segf_load(SegF<G>& X, const BatchDev& B, const DevGraph& g, int6
     // per-(node, group) constants precomputed in FP32 at upload (no FP64 division here)
     const float* T = B.tab_f + ((g.node0 + local) * MGPU_MAX_GROUPS + X.gi) * kTabF;
     X.t_base       = t_base;
+    X.t_base_f     = (float)t_base;
     X.a_tnt        = T[TF_A_TNT];
     X.beta         = T[TF_BETA];
     X.xi           = T[TF_XI];
@@ -947,7 +956,7 @@ int launch_g(const BatchDev& B, int precision, const int32_t* inst, int64_t coun
 {
     constexpr int IPW  = 32 / G;
     const int warps    = ipb > 0 ? (ipb + IPW - 1) / IPW : 4;
-    const int threads  = 32 * (warps < 1 ? 1 : (warps > 32 ? 32 : warps));
+    const int threads  = 32 * (warps < 1 ? 1 : (warps > 4 ? 4 : warps)); // launch bounds: 128 threads
     const int64_t per  = (int64_t)(threads / 32) * IPW;
     int64_t blocks     = (count + per - 1) / per;
     if (grid > 0 && blocks > grid) {

@@ -302,8 +302,11 @@ __global__ void k_ode_plain(BatchDev B, int64_t node_begin, int64_t node_end, in
 }
 
 // Single-node simulate() with every accepted step recorded.
+// dt_io (may be null): per-node initial step on entry, the integrator's next
+// step on exit (Simulation::get_dt), instead of dt0.
 __global__ void k_simulate(BatchDev B, const int32_t* nodes, int count, double t0, double tmax, double dt0,
-                           int max_points, double* out_t, double* out_y, int32_t* num_points, int n_max)
+                           int max_points, double* out_t, double* out_y, int32_t* num_points, int n_max,
+                           double* dt_io)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count) {
@@ -329,7 +332,7 @@ __global__ void k_simulate(BatchDev B, const int32_t* nodes, int count, double t
     o.method   = g.method;
     StepCounts c;
     double t  = t0;
-    double dt = dt0;
+    double dt = dt_io ? dt_io[k] : dt0;
     const int n = g.n;
     auto rec  = [&](double tt, const SVec& v) {
         if (np >= max_points) {
@@ -348,6 +351,9 @@ __global__ void k_simulate(BatchDev B, const int32_t* nodes, int count, double t
         }
     }
     num_points[k] = full ? -np : np;
+    if (dt_io) {
+        dt_io[k] = dt;
+    }
     add_counts(B, c);
 }
 
@@ -378,12 +384,13 @@ void launch_ode_plain(const BatchDev& B, int64_t node_begin, int64_t node_end, c
 }
 
 void launch_simulate(const BatchDev& B, const int32_t* d_nodes, int count, double t0, double tmax, double dt0,
-                     int max_points, double* d_out_t, double* d_out_y, int32_t* d_num_points, cudaStream_t s)
+                     int max_points, double* d_out_t, double* d_out_y, int32_t* d_num_points, cudaStream_t s,
+                     double* d_dt_io)
 {
     const int threads = 64;
     const int blocks  = (count + threads - 1) / threads;
     k_simulate<<<blocks, threads, 0, s>>>(B, d_nodes, count, t0, tmax, dt0, max_points, d_out_t, d_out_y,
-                                          d_num_points, B.scratch_nmax);
+                                          d_num_points, B.scratch_nmax, d_dt_io);
 }
 
 void launch_eval_rhs(const BatchDev& B, const int32_t* d_nodes, int count, const double* d_pop, const double* d_y,

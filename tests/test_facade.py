@@ -1,0 +1,126 @@
+"""The C++ facade (memilio_gb300/cpp/miogpu): MEmilio's C++ API over libmiogpu.
+
+Host-only checks (no GPU): the facade's damping cache equals the oracle's
+restatement of Dampings::update_cache, and a graph packs into a valid layout
+(edges sorted by (src, dst) although added out of order, padded damping
+caches, the reference's parameter defaults). GPU checks compare the facade's
+Simulation, GraphSimulation and ParameterStudy with the FP64 oracle.
+"""
+import json
+import subprocess
+
+import numpy as np
+import pytest
+
+from memilio_gb300 import build as B
+from memilio_gb300 import layout as L
+from oracle import oracle as O
+
+FP64_TOL = 1e-10  # batched FP64 solver vs oracle, relative to the age group's population
+ODE_TOL = 1e-5    # two accurate solutions with different step sequences (the integrator's rel tol)
+
+
+@pytest.fixture(scope="module")
+def programs():
+    return B.build_facade()
+
+
+def run(programs, mode):
+    r = subprocess.run([programs["facade_check"], mode], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    return json.loads(r.stdout)
+
+
+def graph_of(d):
+    G, N, M, K = d["G"], d["N"], d["M"], d["K"]
+    E = d["E"]
+    return L.GraphArrays(G, np.array(d["params"]), np.array(d["contact_baseline"]).reshape(N, M, G, G),
+                         np.array(d["contact_minimum"]).reshape(N, M, G, G),
+                         np.array(d["damping_times"]).reshape(N, M, K),
+                         np.array(d["damping_values"]).reshape(N, M, K, G, G),
+                         np.array(d["state"]).reshape(N, 10 * G), np.array(d["src"], np.int32),
+                         np.array(d["dst"], np.int32), np.array(d["coeff_baseline"]).reshape(E, 10 * G),
+                         np.array(d["coeff_minimum"]).reshape(E, 10 * G))
+
+
+def scaled(a, b, G):
+    a = np.asarray(a).reshape(-1, G, 10)
+    b = np.asarray(b).reshape(-1, G, 10)
+    return float(np.max(np.abs(a - b) / np.maximum(b.sum(axis=2, keepdims=True), 1.0)))
+
+
+def test_damping_cache_matches_oracle(programs):
+    cases = run(programs, "dampings")["cases"]
+    assert len(cases) == 5
+    for c in cases:
+        n = len(c["times"])
+        t = np.array(c["cache_times"])
+        v = np.array(c["cache_values"]).reshape(-1, 2, 2)
+        if n == 0:
+            assert t.shape[0] == 2 and np.all(v == 0)
+            continue
+        ot, ov = O.damping_cache(2, 2, c["times"], np.array(c["levels"], np.int32), np.array(c["types"], np.int32),
+                                 np.array(c["matrices"]).reshape(n, 2, 2))
+        np.testing.assert_array_equal(t, ot)
+        np.testing.assert_allclose(v, ov, rtol=0, atol=1e-15)
+    # an equal (time, type, level) key replaces the damping
+    assert cases[4]["times"] == [3.0, 3.0] and cases[4]["matrices"][0] == 0.7
+
+
+def test_graph_packs_into_layout(programs):
+    d = run(programs, "pack")
+    g = graph_of(d)  # validates shapes and (src, dst) order
+    assert list(zip(d["src"], d["dst"])) == [(0, 1), (0, 2), (1, 0), (2, 0)]
+    assert g.num_damping_points == d["K"] >= 3
+    assert np.all(g.damping_times[:, :, 0] == np.finfo(np.float64).min)
+    assert np.all(g.damping_times[:, :, -1] == np.finfo(np.float64).max)
+    p = g.params[0]
+    assert p[L.P_TNT_MAX_RISK] == 5.0  # the reference's default
+    assert np.all(g.init_state >= 0)
+
+
+@pytest.mark.gpu
+def test_simulation_matches_oracle(programs):
+    d = run(programs, "simulate")
+    G, K, M = d["G"], d["K"], d["M"]
+    g = L.GraphArrays(G, np.array(d["params"]), np.array(d["contact_baseline"]).reshape(1, M, G, G),
+                      np.array(d["contact_minimum"]).reshape(1, M, G, G), np.array(d["damping_times"]).reshape(1, M, K),
+                      np.array(d["damping_values"]).reshape(1, M, K, G, G), np.array(d["state"]).reshape(1, 10 * G),
+                      np.zeros(0, np.int32), np.zeros(0, np.int32), np.zeros((0, 10 * G)))
+    t, y, _ = O.simulate(g, 0, 0.0, 12.0, 0.1)
+    np.testing.assert_allclose(d["times_whole"], t, rtol=0, atol=1e-6)
+    assert scaled(d["last_whole"], y[-1], G) < 1e-8
+    # two advance() calls keep the step size: the grid contains the first horizon
+    assert 4.0 in d["times_pieces"] and d["dt_mid"] > 0
+    assert scaled(d["last_pieces"], y[-1], G) < ODE_TOL
+    ref = O.eval_rhs(g, 0, g.init_state[0], g.init_state[0], 5.0)
+    np.testing.assert_allclose(d["dydt_t5"], ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+
+
+@pytest.mark.gpu
+def test_graph_simulation_matches_oracle(programs):
+    d = run(programs, "graph")
+    g = graph_of(d)
+    rec, fin, _ = O.graph_run(g, 0.0, 6.0, record=True)
+    assert d["t_end"] == 6.0
+    t = np.array(d["t"])
+    np.testing.assert_allclose(t, np.arange(0.0, 6.01, 0.5), rtol=0, atol=1e-12)
+    states = np.array(d["states"]).reshape(len(t), g.num_nodes, g.n)
+    assert scaled(states[0], g.init_state, g.num_groups) == 0.0
+    for b in range(1, len(t)):
+        assert scaled(states[b], rec[b - 1], g.num_groups) < FP64_TOL, b
+
+
+@pytest.mark.gpu
+def test_parameter_study_matches_oracle(programs):
+    runs = run(programs, "study")["runs"]
+    assert len(runs) == 4
+    finals = []
+    for r in runs:
+        g = graph_of(r)
+        _, fin, _ = O.graph_run(g, 0.0, 5.0, record=False)
+        got = np.array(r["final"]).reshape(g.num_nodes, g.n)
+        assert scaled(got, fin, g.num_groups) < FP64_TOL
+        finals.append(got)
+    # the sampled transmission factors differ, so do the results
+    assert not np.allclose(finals[0], finals[3])

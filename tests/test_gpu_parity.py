@@ -115,6 +115,22 @@ def test_graph_matches_oracle_every_boundary(ctx, precision):
 
 
 @pytest.mark.parametrize("precision", PRECISIONS)
+def test_graph_all_compartments_mobile(ctx, precision):
+    # coefficients on every compartment (not only S, E, INS, ISy, R): the exchange
+    # kernels' general compartment mask
+    g0 = W.mobility_graph(seed=23, N=30, out_degree=6)
+    rng = np.random.default_rng(5)
+    coeff = g0.edge_coeff_baseline.copy()
+    coeff[coeff == 0.0] = rng.uniform(0.001, 0.02, int((coeff == 0.0).sum()))
+    g = L.GraphArrays(g0.num_groups, g0.params, g0.contact_baseline, g0.contact_minimum, g0.damping_times,
+                      g0.damping_values, g0.init_state, g0.edge_src, g0.edge_dst, coeff)
+    rec_ref, _, _ = O.graph_run(g, 0.0, 6.0)
+    rec, _, _ = run_graph(ctx, g, precision, 6.0)
+    err = max(group_scaled_error(rec[b], rec_ref[b], g.num_groups) for b in range(rec.shape[0]))
+    assert err < TOL[precision], err
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
 def test_graph_with_underflow_fixes(ctx, precision):
     # stress variant (finite test-and-trace / ICU capacities): the reference's
     # return underflow fix fires; the sequential exact pass must reproduce it
