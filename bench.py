@@ -275,6 +275,11 @@ def h2d_bytes(graphs) -> int:
 #   prep:   departure state read 80, state hi read 40, rates write 48,
 #           snapshot write 40, factors write 8, constant table read 96
 BYTES_PER_ITEM = {"return": 256, "depart": 288, "prep": 312, "exact": 256}
+# DRAM bytes (read + write) per (node, group) item of one launch, from one ncu
+# capture of a 256-sample x 400-node ensemble (profiles/ncu_k_xf_return_256x400.md,
+# profiles/ncu_k_xf_depart_256x400.md): 212.9 MB and 179.7 MB for 614,400 items.
+# The traffic grows in proportion to the items, so it scales to the full launch.
+NCU_BYTES_PER_ITEM = {"return": (177.251072e6 + 35.664384e6) / 614400, "depart": (125.641728e6 + 54.061312e6) / 614400}
 
 
 def main():
@@ -401,6 +406,9 @@ def main():
                                                       "prep": "k_xf_prep", "exact": "k_xf_scan"}[dominant],
                         achieved=ach, unit="GB/s", peak=peaks["hbm_gbs"], peak_source=peaks["source"],
                         frac=ach / peaks["hbm_gbs"], algorithmic_bytes_per_launch=bytes_launch,
+                        traffic=(items * NCU_BYTES_PER_ITEM[dominant] if dominant in NCU_BYTES_PER_ITEM else None),
+                        traffic_source=("ncu dram__bytes_read.sum + dram__bytes_write.sum per item of a "
+                                        "256-sample capture, times the items of this launch"),
                         avg_launch_ms=ms_launch, ode_roofline={"bound": "fp32", "achieved_tflops": achieved,
                                                                "peak_tflops": fp32_peak,
                                                                "frac": achieved / fp32_peak})

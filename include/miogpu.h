@@ -121,6 +121,20 @@ int mgpu_simulate(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, con
                   double* out_y, int32_t* num_points);
 
 /*
+ * Flow simulations: for k < count, simulate_flows (cpp/memilio/compartments/
+ * flow_simulation.h:104-121) of node nodes[k] of `graph` (edges ignored): the
+ * integrator's state is the accumulated flows (starting at zero) and the
+ * population is the initial population plus the flows scattered to their
+ * compartments. Every accepted step is recorded: out_t [count][max_points],
+ * out_flows [count][max_points][15G] (flat index g*15 + k as the Flows
+ * typelist), out_y [count][max_points][10G] (compute_population_results).
+ * FP64, one thread per node.
+ */
+int mgpu_simulate_flows(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, const int32_t* nodes, double t0,
+                        double tmax, double dt0, const mgpu_integrator_opts* opts, int32_t max_points, double* out_t,
+                        double* out_flows, double* out_y, int32_t* num_points);
+
+/*
  * mgpu_simulate with a step size that persists across calls, as
  * Simulation::advance keeps it (cpp/memilio/compartments/simulation_base.h:86-168,
  * cpp/memilio/math/integrator.h:184-249): dt [count] holds each node's initial
@@ -234,6 +248,17 @@ int mgpu_batch_launch(mgpu_batch* batch, double tmax, const double* tmax_per_gra
 int mgpu_batch_query(mgpu_batch* batch, int32_t* done);
 /* Node states of one graph of the batch ([N][10G] doubles), waiting for the stream. */
 int mgpu_batch_get_graph_state(mgpu_batch* batch, int32_t graph, double* out);
+/*
+ * Ensemble statistics of the current node states over the graphs of a batch
+ * (all graphs of one node count and age-group count, at most 4096):
+ * ensemble_mean and ensemble_percentile (cpp/memilio/data/analyze_result.h:
+ * 289-338) on the device. mean [N][10G]; out_percentiles [num_percentiles][N][10G]
+ * with the value at sorted index floor(runs * p), p in (0, 1). Call after each
+ * advance for a time series.
+ */
+int mgpu_batch_ensemble_stats(mgpu_batch* batch, const double* percentiles, int32_t num_percentiles, double* mean,
+                              double* out_percentiles);
+
 /* Autotuner of the batched solver's schedule: for every age-group count of
  * the batch, times one exchange interval of the node solves for each candidate
  * (32, 64 or 128 threads per block; one slot per lane or a persistent grid of

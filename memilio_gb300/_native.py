@@ -30,7 +30,7 @@ EXPORTED = ["mgpu_default_solver_opts", "mgpu_create", "mgpu_destroy", "mgpu_las
             "mgpu_eval_rhs", "mgpu_simulate", "mgpu_batch_create", "mgpu_batch_advance", "mgpu_batch_get_state",
             "mgpu_batch_get_time", "mgpu_batch_set_state", "mgpu_batch_get_stats", "mgpu_batch_get_timing",
             "mgpu_batch_device_bytes", "mgpu_batch_reset", "mgpu_batch_destroy", "mgpu_simulate_final_noalloc",
-            "mgpu_batch_launch", "mgpu_batch_query", "mgpu_batch_autotune", "mgpu_simulate_dt", "mgpu_batch_get_graph_state", "mgpu_batch_estimate_bytes",
+            "mgpu_batch_launch", "mgpu_batch_query", "mgpu_batch_autotune", "mgpu_simulate_dt", "mgpu_simulate_flows", "mgpu_batch_ensemble_stats", "mgpu_batch_get_graph_state", "mgpu_batch_estimate_bytes",
             "mgpu_default_server_opts", "mgpu_server_create", "mgpu_server_destroy", "mgpu_server_submit",
             "mgpu_server_step", "mgpu_server_take", "mgpu_server_memory_in_use", "mgpu_server_num_batches"]
 
@@ -125,6 +125,8 @@ def lib():
                                 P(MgpuIntegratorOpts), ctypes.c_int32, P(d), P(d), P(ctypes.c_int32)]
     L.mgpu_simulate_dt.argtypes = [vp, P(MgpuGraph), ctypes.c_int32, P(ctypes.c_int32), d, d, P(d),
                                 P(MgpuIntegratorOpts), ctypes.c_int32, P(d), P(d), P(ctypes.c_int32)]
+    L.mgpu_simulate_flows.argtypes = [vp, P(MgpuGraph), ctypes.c_int32, P(ctypes.c_int32), d, d, d,
+                                      P(MgpuIntegratorOpts), ctypes.c_int32, P(d), P(d), P(d), P(ctypes.c_int32)]
     L.mgpu_batch_create.argtypes = [vp, P(MgpuGraph), ctypes.c_int32, d, P(MgpuSolverOpts), P(vp)]
     L.mgpu_batch_advance.argtypes = [vp, d, P(d)]
     L.mgpu_batch_get_state.argtypes = [vp, P(d)]
@@ -140,6 +142,7 @@ def lib():
     L.mgpu_batch_launch.argtypes = [vp, d, P(d), i32, P(i32)]
     L.mgpu_batch_query.argtypes = [vp, P(i32)]
     L.mgpu_batch_autotune.argtypes = [vp, P(i32), P(i32)]
+    L.mgpu_batch_ensemble_stats.argtypes = [vp, P(d), i32, P(d), P(d)]
     L.mgpu_batch_get_graph_state.argtypes = [vp, i32, P(d)]
     L.mgpu_batch_estimate_bytes.argtypes = [P(MgpuGraph), i32, P(MgpuSolverOpts)]
     L.mgpu_batch_estimate_bytes.restype = ctypes.c_int64
@@ -231,6 +234,24 @@ class Context:
                                        _dp(out)))
         return out
 
+    def simulate_flows(self, g: GraphArrays, nodes, t0: float, tmax: float, dt0: float, opts=None,
+                       max_points=4096):
+        """Per node: (times [P], flows [P, 15G], populations [P, 10G]) of every accepted step."""
+        opts = opts or integrator_opts()
+        nodes = np.ascontiguousarray(nodes, np.int32)
+        cnt = nodes.shape[0]
+        nf = 15 * g.num_groups
+        out_t = np.zeros((cnt, max_points))
+        out_f = np.zeros((cnt, max_points, nf))
+        out_y = np.zeros((cnt, max_points, g.n))
+        npts = np.zeros(cnt, np.int32)
+        cg = g.as_ctypes()
+        self.check(lib().mgpu_simulate_flows(self._h, ctypes.byref(cg), cnt, _ip(nodes), t0, tmax, dt0,
+                                             ctypes.byref(opts), max_points, _dp(out_t), _dp(out_f), _dp(out_y),
+                                             _ip(npts)))
+        return [(out_t[k, :npts[k]].copy(), out_f[k, :npts[k]].copy(), out_y[k, :npts[k]].copy())
+                for k in range(cnt)]
+
     def simulate(self, g: GraphArrays, nodes, t0: float, tmax: float, dt0: float, opts=None, max_points=4096):
         """Per node: (times [P], values [P, 10G]) of every accepted step."""
         opts = opts or integrator_opts()
@@ -317,6 +338,15 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+    def ensemble_stats(self, percentiles=(0.05, 0.5, 0.95)):
+        """(mean [N, 10G], percentiles [P, N, 10G]) of the current states over the batch's graphs."""
+        g = self.graphs[0]
+        p = np.ascontiguousarray(percentiles, np.float64)
+        mean = np.empty((g.num_nodes, g.n))
+        pct = np.empty((p.shape[0], g.num_nodes, g.n))
+        self.ctx.check(lib().mgpu_batch_ensemble_stats(self._h, _dp(p), p.shape[0], _dp(mean), _dp(pct)))
+        return mean, pct
 
     def autotune(self) -> dict:
         ipb, grid = ctypes.c_int32(), ctypes.c_int32()

@@ -520,6 +520,110 @@ private:
     IntegratorCore m_core;
 };
 
+/* mio::FlowSimulation (compartments/flow_simulation.h:36-102): the integrator's
+ * state is the accumulated flows; get_result() holds the populations and
+ * get_flows() the flows (15G per time point, flat index g*15 + k) of every
+ * accepted step. A later advance continues from the last time point with the
+ * flows accumulated so far (the step size restarts from dt). */
+template <typename FP = double>
+class FlowSimulation
+{
+public:
+    using Model = osecir::Model<FP>;
+
+    explicit FlowSimulation(const Model& model, FP t0 = 0., FP dt = 0.1)
+        : m_model(model)
+        , m_result(model.populations.get_num_compartments())
+        , m_flows(model.num_groups() * (size_t)MGPU_NUM_FLOWS)
+        , m_dt(dt)
+    {
+        m_result.add_time_point(t0, model.get_initial_values());
+        m_flows.add_time_point(t0, std::vector<FP>(m_flows.get_num_elements(), 0.0));
+    }
+
+    std::vector<FP> advance(FP tmax)
+    {
+        const FP t0 = m_result.get_last_time();
+        if (!(tmax > t0)) {
+            return m_result.get_last_value();
+        }
+        const std::vector<FP> y0 = m_result.get_last_value();
+        const std::vector<FP> f0 = m_flows.get_last_value();
+        const NodeRecord r       = m_model.pack(&y0);
+        mgpu_graph g             = Model::graph_of(r);
+        const mgpu_integrator_opts o = m_core.opts();
+        mgpu_context* ctx        = Device::context();
+        const int32_t node       = 0;
+        const size_t n = y0.size(), nf = f0.size();
+        for (int32_t cap = 1024;; cap *= 4) {
+            std::vector<double> t(cap), f((size_t)cap * nf), y((size_t)cap * n);
+            int32_t np   = 0;
+            const int rc = mgpu_simulate_flows(ctx, &g, 1, &node, t0, tmax, m_dt, &o, cap, t.data(), f.data(),
+                                               y.data(), &np);
+            if (rc == MGPU_OUT_OF_RANGE && cap < (1 << 22)) {
+                continue;
+            }
+            check(rc, ctx, "mgpu_simulate_flows");
+            std::vector<FP> acc(nf);
+            for (int32_t k = 1; k < np; ++k) {
+                for (size_t q = 0; q < nf; ++q) {
+                    acc[q] = f0[q] + f[(size_t)k * nf + q];
+                }
+                m_flows.add_time_point(t[(size_t)k], acc);
+                m_result.add_time_point(t[(size_t)k], y.data() + (size_t)k * n);
+            }
+            break;
+        }
+        return m_result.get_last_value();
+    }
+
+    TimeSeries<FP>& get_result()
+    {
+        return m_result;
+    }
+    const TimeSeries<FP>& get_result() const
+    {
+        return m_result;
+    }
+    TimeSeries<FP>& get_flows()
+    {
+        return m_flows;
+    }
+    const TimeSeries<FP>& get_flows() const
+    {
+        return m_flows;
+    }
+    Model& get_model()
+    {
+        return m_model;
+    }
+    FP& get_dt()
+    {
+        return m_dt;
+    }
+    void set_integrator_core(const IntegratorCore& core)
+    {
+        m_core = core;
+    }
+
+private:
+    Model m_model;
+    TimeSeries<FP> m_result, m_flows;
+    FP m_dt;
+    IntegratorCore m_core;
+};
+
+/* mio::simulate_flows (flow_simulation.h:104-121): {populations, flows}. */
+template <typename FP = double>
+std::vector<TimeSeries<FP>> simulate_flows(FP t0, FP tmax, FP dt, const Model<FP>& model,
+                                           const IntegratorCore& core = ControlledStepperWrapper())
+{
+    FlowSimulation<FP> sim(model, t0, dt);
+    sim.set_integrator_core(core);
+    sim.advance(tmax);
+    return {sim.get_result(), sim.get_flows()};
+}
+
 /* mio::simulate / osecir::simulate (simulation.h:99-110, model.h:385-390). */
 template <typename FP = double>
 TimeSeries<FP> simulate(FP t0, FP tmax, FP dt, const Model<FP>& model,

@@ -3,6 +3,7 @@
 //   facade_check dampings   host only: damping caches of several damping lists
 //   facade_check pack       host only: the node/edge arrays of a small graph
 //   facade_check simulate   GPU: Simulation::advance in two pieces and in one
+//   facade_check flows      GPU: simulate_flows (FlowSimulation)
 //   facade_check graph      GPU: make_mobility_sim(...).advance, every boundary
 //   facade_check study      GPU: ParameterStudy over 4 sampled graphs
 //
@@ -225,6 +226,29 @@ int mode_simulate()
     return 0;
 }
 
+int mode_flows()
+{
+    const Model<double> m = make_model(2, 5u);
+    auto res              = simulate_flows(0.0, 10.0, 0.1, m);
+    auto a                = m.pack();
+    std::printf("{\"G\": 2, \"K\": %d, \"M\": %d,\n", a.K, a.M);
+    print_vec("params", a.params);
+    print_vec("contact_baseline", a.contact_baseline);
+    print_vec("contact_minimum", a.contact_minimum);
+    print_vec("damping_times", a.damping_times);
+    print_vec("damping_values", a.damping_values);
+    print_vec("state", a.state);
+    std::vector<double> t;
+    for (size_t i = 0; i < res[0].get_num_time_points(); ++i) {
+        t.push_back(res[0].get_time(i));
+    }
+    print_vec("t", t);
+    print_vec("last_pop", res[0].get_last_value());
+    print_vec("last_flows", res[1].get_last_value(), false);
+    std::printf("}\n");
+    return 0;
+}
+
 int mode_graph()
 {
     auto graph = three_nodes(2);
@@ -315,6 +339,9 @@ int main(int argc, char** argv)
         }
         if (!std::strcmp(mode, "simulate")) {
             return mode_simulate();
+        }
+        if (!std::strcmp(mode, "flows")) {
+            return mode_flows();
         }
         if (!std::strcmp(mode, "graph")) {
             return mode_graph();

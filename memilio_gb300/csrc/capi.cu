@@ -373,6 +373,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     using Key = std::tuple<const void*, const void*, const void*, const void*, int64_t, int64_t, int64_t>;
     std::map<Key, int> contact_first, damping_first, coeff_first;
     std::vector<char> own_contact(num_graphs, 1), own_damping(num_graphs, 1), own_coeff(num_graphs, 1);
+    std::vector<int> coeff_src(num_graphs, -1); // graph whose edge coefficients this one shares
     b->N.resize(num_graphs);
     b->G.resize(num_graphs);
     b->n.resize(num_graphs);
@@ -439,6 +440,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
             d.edv_off     = dg[ite->second].edv_off;
             d.ecoef_f_off = dg[ite->second].ecoef_f_off;
             own_coeff[i]  = 0;
+            coeff_src[i]  = ite->second;
         }
         else {
             coeff_first[ke] = i;
@@ -523,14 +525,20 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
                     h_ecf[d.ecoef_f_off + (int64_t)e * n + j] = (float)cb[j];
                 }
             }
-            bool any = false;
-            for (int j = 0; j < n; ++j) {
-                any = any || (cb[j] > 0.0);
-                if (cb[j] != 0.0 || (g.edge_coeff_minimum && g.edge_coeff_minimum[(int64_t)e * n + j] != 0.0)) {
-                    mob_mask[i] |= 1 << (j % kC);
+            if (own_coeff[i]) {
+                bool any = false;
+                for (int j = 0; j < n; ++j) {
+                    any = any || (cb[j] > 0.0);
+                    if (cb[j] != 0.0 || (g.edge_coeff_minimum && g.edge_coeff_minimum[(int64_t)e * n + j] != 0.0)) {
+                        mob_mask[i] |= 1 << (j % kC);
+                    }
                 }
+                h_any[ge] = any ? 1 : 0;
             }
-            h_any[ge] = any ? 1 : 0;
+            else {
+                // the same coefficient arrays as an earlier graph: its flags
+                h_any[ge] = h_any[dg[coeff_src[i]].edge0 + e];
+            }
             if (d.Ke && own_coeff[i]) {
                 std::memcpy(h_edt.data() + d.edt_off + (int64_t)e * d.Ke, g.edge_damping_times + (int64_t)e * d.Ke,
                             sizeof(double) * d.Ke);
@@ -539,6 +547,9 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
             }
             h_trav_off[ge] = trav_pos;
             trav_pos += n;
+        }
+        if (!own_coeff[i]) {
+            mob_mask[i] = mob_mask[coeff_src[i]];
         }
         for (int v = 0; v < g.num_nodes; ++v) {
             indeg[v + 1] += indeg[v];
@@ -1016,6 +1027,82 @@ int mgpu_simulate(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, con
 {
     return simulate_impl(ctx, graph, count, nodes, t0, tmax, dt0, nullptr, opts, max_points, out_t, out_y,
                          num_points);
+}
+
+int mgpu_simulate_flows(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, const int32_t* nodes, double t0,
+                        double tmax, double dt0, const mgpu_integrator_opts* opts, int32_t max_points, double* out_t,
+                        double* out_flows, double* out_y, int32_t* num_points)
+{
+    return guarded(ctx, [&]() -> int {
+        if (!graph || !opts || count < 0 || max_points < 1 ||
+            (count > 0 && (!nodes || !out_t || !out_flows || !out_y || !num_points))) {
+            fail(MGPU_INVALID_VALUE, "null argument");
+        }
+        if (!(dt0 > 0)) {
+            fail(MGPU_INVALID_VALUE, "dt0 must be > 0");
+        }
+        if (count == 0) {
+            return MGPU_OK;
+        }
+        ck(cudaSetDevice(ctx->device), "cudaSetDevice");
+        mgpu_graph g = *graph;
+        g.num_edges  = 0;
+        for (int k = 0; k < count; ++k) {
+            if (nodes[k] < 0 || nodes[k] >= g.num_nodes) {
+                fail(MGPU_OUT_OF_RANGE, "node index out of range");
+            }
+        }
+        mgpu_batch b;
+        b.ctx = ctx;
+        mgpu_default_solver_opts(&b.opts);
+        b.opts.precision  = MGPU_PRECISION_FP64_PLAIN;
+        b.opts.integrator = *opts;
+        build_batch(&b, &g, 1, t0, dt0, false, 0);
+        const int n  = g.num_groups * kC;
+        const int nf = g.num_groups * kF;
+        DevPool io;
+        io.ctx = ctx;
+        int rc = MGPU_OK;
+        try {
+            int32_t* d_nodes = io.alloc<int32_t>(count);
+            double* d_t      = io.alloc<double>((int64_t)count * max_points);
+            double* d_f      = io.alloc<double>((int64_t)count * max_points * nf);
+            double* d_y      = io.alloc<double>((int64_t)count * max_points * n);
+            int32_t* d_np    = io.alloc<int32_t>(count);
+            double* d_rows   = io.alloc<double>((int64_t)count * nf);
+            BatchDev B       = b.dev;
+            B.scratch        = io.alloc<double>((int64_t)8 * nf * count);
+            B.scratch_stride = count;
+            B.scratch_nmax   = nf;
+            cudaStream_t s   = ctx->stream;
+            ck(cudaMemcpyAsync(d_nodes, nodes, sizeof(int32_t) * count, cudaMemcpyHostToDevice, s), "h2d");
+            launch_simulate_flows(B, d_nodes, count, t0, tmax, dt0, max_points, d_t, d_f, d_y, d_np, nf, d_rows, s);
+            ck(cudaGetLastError(), "k_simulate_flows");
+            ck(cudaMemcpyAsync(num_points, d_np, sizeof(int32_t) * count, cudaMemcpyDeviceToHost, s), "d2h");
+            ck(cudaMemcpyAsync(out_t, d_t, sizeof(double) * count * max_points, cudaMemcpyDeviceToHost, s), "d2h");
+            ck(cudaMemcpyAsync(out_flows, d_f, sizeof(double) * count * max_points * nf, cudaMemcpyDeviceToHost, s),
+               "d2h");
+            ck(cudaMemcpyAsync(out_y, d_y, sizeof(double) * count * max_points * n, cudaMemcpyDeviceToHost, s),
+               "d2h");
+            ck(cudaStreamSynchronize(s), "sync");
+            for (int k = 0; k < count; ++k) {
+                if (num_points[k] < 0) {
+                    num_points[k] = max_points;
+                    rc            = MGPU_OUT_OF_RANGE;
+                }
+            }
+            check_device_error(&b);
+        }
+        catch (...) {
+            io.release();
+            throw;
+        }
+        io.release();
+        if (rc != MGPU_OK) {
+            ctx->error = "trajectory longer than max_points";
+        }
+        return rc;
+    });
 }
 
 int mgpu_simulate_dt(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, const int32_t* nodes, double t0,
@@ -1537,6 +1624,116 @@ int mgpu_batch_autotune(mgpu_batch* b, int32_t* instances_per_block, int32_t* gr
         if (grid_blocks) {
             *grid_blocks = best_grid;
         }
+        return MGPU_OK;
+    });
+}
+
+namespace
+{
+// ensemble_mean / ensemble_percentile (cpp/memilio/data/analyze_result.h:289-338) of
+// one (node, compartment) column over the graphs of a batch: one block per
+// column, the values sorted in shared memory (bitonic, padded with +inf to a
+// power of two); mean = sum over runs of x / runs, in run order.
+__global__ void k_ensemble_stats(BatchDev B, const int64_t* state_off, int runs, int pow2, int64_t n_col,
+                                 const double* p, int num_p, double* mean, double* pct)
+{
+    extern __shared__ double vals[];
+    const int64_t col = blockIdx.x;
+    if (col >= n_col) {
+        return;
+    }
+    for (int r = threadIdx.x; r < pow2; r += blockDim.x) {
+        vals[r] = r < runs ? state_get(B, state_off[r] + col) : INFINITY;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int r = 0; r < runs; ++r) {
+            m += vals[r] / runs;
+        }
+        mean[col] = m;
+    }
+    __syncthreads();
+    for (int k = 2; k <= pow2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < pow2; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const bool up = (i & k) == 0;
+                    const double a = vals[i], b = vals[l];
+                    if ((a > b) == up) {
+                        vals[i] = b;
+                        vals[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int q = threadIdx.x; q < num_p; q += blockDim.x) {
+        pct[(int64_t)q * n_col + col] = vals[(int)((double)runs * p[q])];
+    }
+}
+} // namespace
+
+int mgpu_batch_ensemble_stats(mgpu_batch* b, const double* percentiles, int32_t num_percentiles, double* mean,
+                              double* out_percentiles)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!mean || num_percentiles < 0 || (num_percentiles > 0 && (!percentiles || !out_percentiles))) {
+            fail(MGPU_INVALID_VALUE, "null argument");
+        }
+        for (int q = 0; q < num_percentiles; ++q) {
+            if (!(percentiles[q] > 0.0 && percentiles[q] < 1.0)) {
+                fail(MGPU_INVALID_VALUE, "percentiles must lie in (0, 1)");
+            }
+        }
+        const int runs = b->num_graphs;
+        for (int i = 1; i < runs; ++i) {
+            if (b->N[i] != b->N[0] || b->G[i] != b->G[0]) {
+                fail(MGPU_INVALID_VALUE, "ensemble statistics need graphs of one shape");
+            }
+        }
+        if (runs > 4096) {
+            fail(MGPU_UNSUPPORTED, "ensemble statistics over at most 4096 graphs per batch");
+        }
+        int pow2 = 1;
+        while (pow2 < runs) {
+            pow2 <<= 1;
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        const int64_t n_col = (int64_t)b->N[0] * b->n[0];
+        cudaStream_t s      = b->ctx->stream;
+        DevPool io;
+        io.ctx = b->ctx;
+        try {
+            int64_t* d_off = io.upload(b->state_off);
+            double* d_p    = io.alloc<double>(std::max(num_percentiles, 1));
+            double* d_mean = io.alloc<double>(n_col);
+            double* d_pct  = io.alloc<double>(std::max<int64_t>(n_col * num_percentiles, 1));
+            if (num_percentiles > 0) {
+                ck(cudaMemcpyAsync(d_p, percentiles, sizeof(double) * num_percentiles, cudaMemcpyHostToDevice, s),
+                   "h2d");
+            }
+            k_ensemble_stats<<<(unsigned)n_col, 256, sizeof(double) * pow2, s>>>(b->dev, d_off, runs, pow2, n_col, d_p,
+                                                                                num_percentiles, d_mean, d_pct);
+            ck(cudaGetLastError(), "k_ensemble_stats");
+            ck(cudaMemcpyAsync(mean, d_mean, sizeof(double) * n_col, cudaMemcpyDeviceToHost, s), "d2h");
+            if (num_percentiles > 0) {
+                ck(cudaMemcpyAsync(out_percentiles, d_pct, sizeof(double) * n_col * num_percentiles,
+                                   cudaMemcpyDeviceToHost, s),
+                   "d2h");
+            }
+            ck(cudaStreamSynchronize(s), "sync");
+        }
+        catch (...) {
+            io.release();
+            throw;
+        }
+        io.release();
         return MGPU_OK;
     });
 }

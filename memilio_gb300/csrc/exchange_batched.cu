@@ -1082,9 +1082,16 @@ struct ReturnOrder {
     }
 };
 
+#ifndef MGPU_XF_RETURN_MIN_BLOCKS
+#define MGPU_XF_RETURN_MIN_BLOCKS 4 // resident 128-thread blocks per SM the register budget must allow
+#endif
+#ifndef MGPU_XF_DEPART_MIN_BLOCKS
+#define MGPU_XF_DEPART_MIN_BLOCKS 6
+#endif
 // Dense (node, group) mapping as k_xf_return.
 template <int MASK>
-__global__ void k_xf_depart(BatchDev B, const int32_t* inst, int64_t count, int G)
+__global__ void __launch_bounds__(128, MGPU_XF_DEPART_MIN_BLOCKS)
+    k_xf_depart(BatchDev B, const int32_t* inst, int64_t count, int G)
 {
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= count * G) {
@@ -1173,7 +1180,8 @@ __global__ void k_xf_depart(BatchDev B, const int32_t* inst, int64_t count, int 
 // One thread per (node, group) of the nodes with G age groups (dense: node
 // = inst[tid / G], group = tid % G, so no lane idles on unused groups).
 template <int MASK>
-__global__ void __launch_bounds__(128, 4) k_xf_return(BatchDev B, const int32_t* inst, int64_t count, int G)
+__global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
+    k_xf_return(BatchDev B, const int32_t* inst, int64_t count, int G)
 {
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= count * G) {

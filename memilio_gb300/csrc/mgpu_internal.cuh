@@ -357,8 +357,9 @@ __device__ inline void contact_matrix_at(const NodeModel& nm, double t, double* 
 // compartments/flow_model.h:112-144) for one node, FP64, one thread. The
 // contact matrix, seasonality and risk smoother are evaluated once per call
 // (they depend on t and pop only) instead of once per (i, j).
-template <class PopV, class YV, class OutV>
-__device__ void secir_rhs(const NodeModel& nm, const PopV& pop, const YV& y, double t, const OutV& dydt)
+// The 15 flows of every age group, handed to sink(i, f) group by group.
+template <class PopV, class YV, class Sink>
+__device__ void secir_flows_core(const NodeModel& nm, const PopV& pop, const YV& y, double t, Sink&& sink)
 {
     const int G = nm.G;
     double C[MGPU_MAX_GROUPS * MGPU_MAX_GROUPS];
@@ -384,9 +385,6 @@ __device__ void secir_rhs(const NodeModel& nm, const PopV& pop, const YV& y, dou
         const double risk = ramp_apply(rrisk, nm.gp(MGPU_G_RISK_FROM_SYMPTOMATIC, j),
                                        nm.gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, j));
         press[j] = nm.gp(MGPU_G_REL_TRANSMISSION_NS, j) * pop[o + MGPU_INS] + risk * pop[o + MGPU_ISY];
-    }
-    for (int k = 0; k < G * kC; ++k) {
-        dydt[k] = 0.0;
     }
     for (int i = 0; i < G; ++i) {
         const int o       = i * kC;
@@ -422,12 +420,37 @@ __device__ void secir_rhs(const NodeModel& nm, const PopV& pop, const YV& y, dou
         f[12] = (dps + death_adj) / tisev * y[o + MGPU_ISEV];
         f[13] = dpc / ticri * y[o + MGPU_ICRI];
         f[14] = (1.0 - dpc) / ticri * y[o + MGPU_ICRI];
+        sink(i, f);
+    }
+}
+
+// dydt = f(pop, y, t): the flows scattered to their compartments (FlowModel::get_derivatives).
+template <class PopV, class YV, class OutV>
+__device__ void secir_rhs(const NodeModel& nm, const PopV& pop, const YV& y, double t, const OutV& dydt)
+{
+    for (int k = 0; k < nm.G * kC; ++k) {
+        dydt[k] = 0.0;
+    }
+    secir_flows_core(nm, pop, y, t, [&](int i, const double (&f)[kF]) {
+        const int o = i * kC;
 #pragma unroll
         for (int k = 0; k < kF; ++k) {
             dydt[o + kFlowSrc[k]] -= f[k];
             dydt[o + kFlowDst[k]] += f[k];
         }
-    }
+    });
+}
+
+// The flows themselves, flat index i*15 + k (osecir::Model::get_flows).
+template <class PopV, class YV, class OutV>
+__device__ void secir_flows(const NodeModel& nm, const PopV& pop, const YV& y, double t, const OutV& flows)
+{
+    secir_flows_core(nm, pop, y, t, [&](int i, const double (&f)[kF]) {
+#pragma unroll
+        for (int k = 0; k < kF; ++k) {
+            flows[i * kF + k] = f[k];
+        }
+    });
 }
 
 // Mobility risk factor of the ISy compartments (get_mobility_factors,
@@ -466,6 +489,9 @@ void launch_ode_plain(const BatchDev& B, int64_t node_begin, int64_t node_end, c
 void launch_simulate(const BatchDev& B, const int32_t* d_nodes, int count, double t0, double tmax, double dt0,
                      int max_points, double* d_out_t, double* d_out_y, int32_t* d_num_points, cudaStream_t s,
                      double* d_dt_io = nullptr);
+void launch_simulate_flows(const BatchDev& B, const int32_t* d_nodes, int count, double t0, double tmax, double dt0,
+                           int max_points, double* d_out_t, double* d_out_f, double* d_out_y, int32_t* d_num_points,
+                           int nf_max, double* d_flow_rows, cudaStream_t s);
 void launch_eval_rhs(const BatchDev& B, const int32_t* d_nodes, int count, const double* d_pop, const double* d_y,
                      const double* d_t, double* d_dydt, cudaStream_t s);
 int launch_ode_batched(const BatchDev& B, int G, int precision, const int32_t* d_instances, int64_t count,

@@ -63,8 +63,40 @@ struct NodeRhs {
     }
 };
 
+// FlowSimulation's right-hand side (compartments/flow_simulation.h:56-79): the
+// state is the accumulated flows; the population is the initial population
+// plus the flows scattered to their compartments (FlowModel::get_derivatives),
+// and the derivative is get_flows(pop, pop, t).
+struct FlowRhs {
+    NodeModel nm;
+    const double* pop0; // initial population [10G]
+    __device__ void operator()(const SVec& x, double t, const SVec& out) const
+    {
+        double pop[MGPU_MAX_GROUPS * kC];
+        const int G = nm.G;
+        for (int j = 0; j < G * kC; ++j) {
+            pop[j] = 0.0;
+        }
+        for (int i = 0; i < G; ++i) {
+#pragma unroll
+            for (int k = 0; k < kF; ++k) {
+                const double f = x[i * kF + k];
+                pop[i * kC + kFlowSrc[k]] -= f;
+                pop[i * kC + kFlowDst[k]] += f;
+            }
+        }
+        for (int j = 0; j < G * kC; ++j) {
+            pop[j] += pop0[j];
+        }
+        const CVec p{pop, 1};
+        secir_flows(nm, p, p, t, out);
+    }
+};
+
 // One Cash-Karp attempt; returns Odeint's error measure (writes the 5th-order result into w.yn).
-__device__ double ck_attempt(const NodeRhs& f, Work& w, int n, double t, double dt, const DevOpts& o)
+// F: the right-hand side, f(x, t, out) (NodeRhs; FlowRhs for flow simulations).
+template <class F>
+__device__ double ck_attempt(const F& f, Work& w, int n, double t, double dt, const DevOpts& o)
 {
     f(w.y, t, w.k[0]);
     for (int s = 1; s < 6; ++s) {
@@ -95,7 +127,8 @@ __device__ double ck_attempt(const NodeRhs& f, Work& w, int n, double t, double 
 }
 
 // ControlledStepperWrapper::step. On return w.yn holds y(t').
-__device__ bool ck_step(const NodeRhs& f, Work& w, int n, double& t, double& dt, double dt_min, const DevOpts& o,
+template <class F>
+__device__ bool ck_step(const F& f, Work& w, int n, double& t, double& dt, double dt_min, const DevOpts& o,
                         StepCounts& c)
 {
     bool success     = false;
@@ -141,7 +174,8 @@ __device__ bool ck_step(const NodeRhs& f, Work& w, int n, double& t, double& dt,
 }
 
 // RKIntegratorCore::step (RKF45, lower order propagated).
-__device__ bool rkf_step(const NodeRhs& f, Work& w, int n, double& t, double& dt, double dt_min, const DevOpts& o,
+template <class F>
+__device__ bool rkf_step(const F& f, Work& w, int n, double& t, double& dt, double dt_min, const DevOpts& o,
                          StepCounts& c)
 {
     dt                 = fmin(dt, o.dt_max);
@@ -204,9 +238,9 @@ __device__ bool rkf_step(const NodeRhs& f, Work& w, int n, double& t, double& dt
 
 // SystemIntegrator::advance for one node; y advanced in place. `rec` is
 // called after every step with (t, y). Returns false when the step cap hit.
-template <class Rec>
-__device__ bool system_advance(const NodeRhs& f, Work& w, int n, double tmax, double& t, double& dt,
-                               const DevOpts& o, StepCounts& c, Rec rec)
+template <class F, class Rec>
+__device__ bool system_advance(const F& f, Work& w, int n, double tmax, double& t, double& dt, const DevOpts& o,
+                               StepCounts& c, Rec rec)
 {
     const double t0       = t;
     double dt_restore     = 0.0;
@@ -357,6 +391,72 @@ __global__ void k_simulate(BatchDev B, const int32_t* nodes, int count, double t
     add_counts(B, c);
 }
 
+// simulate_flows (flow_simulation.h:104-121): FlowSimulation::advance from zero
+// flows with every accepted step recorded; the populations of every time point
+// are the initial population plus the scattered flows
+// (compute_population_results, flow_simulation_base.h:90-103).
+__global__ void k_simulate_flows(BatchDev B, const int32_t* nodes, int count, double t0, double tmax, double dt0,
+                                 int max_points, double* out_t, double* out_f, double* out_y, int32_t* num_points,
+                                 int nf_max, double* flow_rows)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) {
+        return;
+    }
+    const DevGraph& g   = B.graphs[0];
+    const int64_t local = nodes[k];
+    const int n         = g.n;
+    const int nf        = g.G * kF;
+    const double* pop0  = B.state + g.state_off + local * n;
+    FlowRhs f{node_model(B, g, local), pop0};
+    double* x = flow_rows + (int64_t)k * nf;
+    for (int i = 0; i < nf; ++i) {
+        x[i] = 0.0;
+    }
+    double* ts = out_t + (int64_t)k * max_points;
+    double* fs = out_f + (int64_t)k * max_points * nf;
+    double* ys = out_y + (int64_t)k * max_points * n;
+    int np     = 0;
+    bool full  = false;
+    auto rec   = [&](double tt, const SVec& v) {
+        if (np >= max_points) {
+            full = true;
+            return;
+        }
+        ts[np] = tt;
+        double* yrow = ys + (int64_t)np * n;
+        for (int j = 0; j < n; ++j) {
+            yrow[j] = 0.0;
+        }
+        for (int i = 0; i < g.G; ++i) {
+            for (int q = 0; q < kF; ++q) {
+                const double fl = v[i * kF + q];
+                fs[(int64_t)np * nf + i * kF + q] = fl;
+                yrow[i * kC + kFlowSrc[q]] -= fl;
+                yrow[i * kC + kFlowDst[q]] += fl;
+            }
+        }
+        for (int j = 0; j < n; ++j) {
+            yrow[j] += pop0[j];
+        }
+        ++np;
+    };
+    Work w    = make_work(B, k, x, nf_max);
+    DevOpts o = B.opts;
+    o.method  = g.method;
+    StepCounts c;
+    double t  = t0;
+    double dt = dt0;
+    rec(t, SVec{x, 1});
+    if (tmax > t0) {
+        if (!system_advance(f, w, nf, tmax, t, dt, o, c, rec)) {
+            atomicOr(B.err, ERR_STEP_CAP);
+        }
+    }
+    num_points[k] = full ? -np : np;
+    add_counts(B, c);
+}
+
 __global__ void k_eval_rhs(BatchDev B, const int32_t* nodes, int count, const double* pop, const double* y,
                            const double* t, double* dydt)
 {
@@ -391,6 +491,16 @@ void launch_simulate(const BatchDev& B, const int32_t* d_nodes, int count, doubl
     const int blocks  = (count + threads - 1) / threads;
     k_simulate<<<blocks, threads, 0, s>>>(B, d_nodes, count, t0, tmax, dt0, max_points, d_out_t, d_out_y,
                                           d_num_points, B.scratch_nmax, d_dt_io);
+}
+
+void launch_simulate_flows(const BatchDev& B, const int32_t* d_nodes, int count, double t0, double tmax, double dt0,
+                           int max_points, double* d_out_t, double* d_out_f, double* d_out_y, int32_t* d_num_points,
+                           int nf_max, double* d_flow_rows, cudaStream_t s)
+{
+    const int threads = 64;
+    const int blocks  = (count + threads - 1) / threads;
+    k_simulate_flows<<<blocks, threads, 0, s>>>(B, d_nodes, count, t0, tmax, dt0, max_points, d_out_t, d_out_f,
+                                                d_out_y, d_num_points, nf_max, d_flow_rows);
 }
 
 void launch_eval_rhs(const BatchDev& B, const int32_t* d_nodes, int count, const double* d_pop, const double* d_y,

@@ -51,6 +51,8 @@ def lib():
         L.orc_eval_flows.argtypes = [P(MgpuGraph), ctypes.c_int, P(d), P(d), d, P(d)]
         L.orc_simulate.argtypes = [P(MgpuGraph), ctypes.c_int, d, d, d, P(MgpuIntegratorOpts), ctypes.c_int,
                                    P(d), P(d), P(ctypes.c_int), P(OrcStats)]
+        L.orc_simulate_flows.argtypes = [P(MgpuGraph), ctypes.c_int, d, d, d, P(MgpuIntegratorOpts), ctypes.c_int,
+                                         P(d), P(d), P(d), P(ctypes.c_int), P(OrcStats)]
         L.orc_graph_run.argtypes = [P(MgpuGraph), d, d, d, d, P(MgpuIntegratorOpts), P(d), P(d), P(OrcStats)]
         L.orc_ensemble_run.argtypes = [P(MgpuGraph), ctypes.c_int, d, d, d, d, P(MgpuIntegratorOpts), ctypes.c_int,
                                        P(d), P(d), P(OrcStats)]
@@ -95,6 +97,25 @@ def simulate(g: GraphArrays, node: int, t0: float, tmax: float, dt: float, opts=
     if rc != 0:
         raise RuntimeError("orc_simulate failed (max_points too small?)")
     return out_t[:npts.value].copy(), out_y[:npts.value].copy(), st.as_dict()
+
+
+def simulate_flows(g: GraphArrays, node: int, t0: float, tmax: float, dt: float, opts=None,
+                   max_points: int = 200000):
+    """simulate_flows(): returns (times [P], flows [P, 15G], populations [P, 10G], stats)."""
+    opts = opts or integrator_opts()
+    nf = 15 * g.num_groups
+    out_t = np.zeros(max_points)
+    out_f = np.zeros((max_points, nf))
+    out_y = np.zeros((max_points, g.n))
+    npts = ctypes.c_int(0)
+    st = OrcStats()
+    cg = g.as_ctypes()
+    rc = lib().orc_simulate_flows(ctypes.byref(cg), node, t0, tmax, dt, ctypes.byref(opts), max_points, _p(out_t),
+                                  _p(out_f), _p(out_y), ctypes.byref(npts), ctypes.byref(st))
+    if rc != 0:
+        raise RuntimeError("orc_simulate_flows failed (max_points too small?)")
+    k = npts.value
+    return out_t[:k].copy(), out_f[:k].copy(), out_y[:k].copy(), st.as_dict()
 
 
 def num_boundaries(t0: float, tmax: float, dt_exchange: float) -> int:

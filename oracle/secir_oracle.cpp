@@ -735,6 +735,75 @@ int orc_eval_rhs(const mgpu_graph* g, int node, const double* pop, const double*
     return 0;
 }
 
+// FlowSimulation::advance (flow_simulation.h:56-79): f(flows) = get_flows(pop, pop, t)
+// with pop = y0 + get_derivatives(flows) (groups outer, flows inner, as
+// FlowModel::get_derivatives, flow_model.h:112-125); populations of the
+// recorded points by compute_population_results (flow_simulation_base.h:90-103).
+int orc_simulate_flows(const mgpu_graph* g, int node, double t0, double tmax, double dt,
+                       const mgpu_integrator_opts* opts, int max_points, double* out_t, double* out_f,
+                       double* out_y, int* num_points, orc_stats* stats)
+{
+    if (!graph_ok(g) || node < 0 || node >= g->num_nodes || !opts || max_points < 1) {
+        return -1;
+    }
+    const int G  = g->num_groups;
+    const int n  = G * kC;
+    const int nf = G * kF;
+    const NodeView nv = node_view(g, node);
+    const double* y0  = g->init_state + (long)node * n;
+    auto scatter = [&](const double* flows, double* dydt) {
+        std::fill(dydt, dydt + n, 0.0);
+        for (int i = 0; i < G; ++i) {
+            for (int k = 0; k < kF; ++k) {
+                const double fv = flows[i * kF + k];
+                dydt[i * kC + kFlowSrc[k]] -= fv;
+                dydt[i * kC + kFlowDst[k]] += fv;
+            }
+        }
+    };
+    std::vector<double> pop(n);
+    long evals = 0;
+    auto f = [&](const double*, const double* flows, double t, double* dflows) {
+        scatter(flows, pop.data());
+        for (int j = 0; j < n; ++j) {
+            pop[j] += y0[j];
+        }
+        std::fill(dflows, dflows + nf, 0.0);
+        get_flows(nv, pop.data(), pop.data(), t, dflows);
+        ++evals;
+    };
+    Counters cnt;
+    Core core(*opts, nf, &cnt);
+    std::vector<double> x(nf, 0.0);
+    int np    = 0;
+    bool full = false;
+    auto rec  = [&](double t, const std::vector<double>& v) {
+        if (np >= max_points) {
+            full = true;
+            return;
+        }
+        out_t[np] = t;
+        std::memcpy(out_f + (long)np * nf, v.data(), nf * sizeof(double));
+        double* yrow = out_y + (long)np * n;
+        scatter(v.data(), yrow);
+        for (int j = 0; j < n; ++j) {
+            yrow[j] += y0[j];
+        }
+        ++np;
+    };
+    double t = t0;
+    rec(t, x);
+    system_advance(core, f, tmax, t, dt, x, rec);
+    *num_points = np;
+    if (stats) {
+        stats->accepted_steps += cnt.accepted;
+        stats->rejected_steps += cnt.rejected;
+        stats->failed_steps += cnt.failed;
+        stats->rhs_evals += evals;
+    }
+    return full ? -1 : 0;
+}
+
 int orc_simulate(const mgpu_graph* g, int node, double t0, double tmax, double dt, const mgpu_integrator_opts* opts,
                  int max_points, double* out_t, double* out_y, int* num_points, orc_stats* stats)
 {

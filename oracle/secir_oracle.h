@@ -50,6 +50,15 @@ int orc_simulate(const mgpu_graph* g, int node, double t0, double tmax, double d
                  const mgpu_integrator_opts* opts, int max_points, double* out_t, double* out_y,
                  int* num_points, orc_stats* stats);
 
+/* simulate_flows(t0, tmax, dt, model, core) (compartments/flow_simulation.h:36-121,
+ * flow_simulation_base.h:90-103): the integrator's state is the accumulated flows
+ * (from zero); every accepted step is recorded with its flows out_f
+ * [max_points][15G] and populations out_y [max_points][10G]. Returns 0, or -1
+ * when max_points is too small. */
+int orc_simulate_flows(const mgpu_graph* g, int node, double t0, double tmax, double dt,
+                       const mgpu_integrator_opts* opts, int max_points, double* out_t, double* out_f,
+                       double* out_y, int* num_points, orc_stats* stats);
+
 /* make_mobility_sim(t0, dt_exchange, graph).advance(tmax). Writes the node
  * states after every exchange boundary into out_states
  * [num_boundaries][N][10G] when out_states != NULL (num_boundaries =

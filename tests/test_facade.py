@@ -124,3 +124,17 @@ def test_parameter_study_matches_oracle(programs):
         finals.append(got)
     # the sampled transmission factors differ, so do the results
     assert not np.allclose(finals[0], finals[3])
+
+
+@pytest.mark.gpu
+def test_flow_simulation_matches_oracle(programs):
+    d = run(programs, "flows")
+    G, K, M = d["G"], d["K"], d["M"]
+    g = L.GraphArrays(G, np.array(d["params"]), np.array(d["contact_baseline"]).reshape(1, M, G, G),
+                      np.array(d["contact_minimum"]).reshape(1, M, G, G), np.array(d["damping_times"]).reshape(1, M, K),
+                      np.array(d["damping_values"]).reshape(1, M, K, G, G), np.array(d["state"]).reshape(1, 10 * G),
+                      np.zeros(0, np.int32), np.zeros(0, np.int32), np.zeros((0, 10 * G)))
+    t, f, y, _ = O.simulate_flows(g, 0, 0.0, 10.0, 0.1)
+    np.testing.assert_allclose(d["t"], t, rtol=0, atol=1e-6)
+    assert scaled(d["last_pop"], y[-1], G) < 1e-8
+    np.testing.assert_allclose(d["last_flows"], f[-1], rtol=1e-8, atol=1e-8 * np.abs(f[-1]).max())
