@@ -76,6 +76,14 @@ def build(verbose: bool = False) -> str:
     os.makedirs(LIB_DIR, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
+    # drop objects of earlier source versions (the cache keeps only the current set)
+    keep = {os.path.basename(o) for o in objs}
+    for f in os.listdir(OBJ):
+        if f.endswith(".o") and f not in keep:
+            try:
+                os.remove(os.path.join(OBJ, f))
+            except OSError:
+                pass
     stamp = hashlib.sha1("".join(objs).encode()).hexdigest()[:16]
     stamp_file = LIB + ".stamp"
     if os.path.exists(LIB) and os.path.exists(stamp_file) and open(stamp_file).read() == stamp:

@@ -1083,10 +1083,10 @@ struct ReturnOrder {
 };
 
 #ifndef MGPU_XF_RETURN_MIN_BLOCKS
-#define MGPU_XF_RETURN_MIN_BLOCKS 4 // resident 128-thread blocks per SM the register budget must allow
+#define MGPU_XF_RETURN_MIN_BLOCKS 6 // resident 128-thread blocks per SM the register budget must allow (measured best)
 #endif
 #ifndef MGPU_XF_DEPART_MIN_BLOCKS
-#define MGPU_XF_DEPART_MIN_BLOCKS 6
+#define MGPU_XF_DEPART_MIN_BLOCKS 8
 #endif
 // Dense (node, group) mapping as k_xf_return.
 template <int MASK>

@@ -728,6 +728,8 @@ __device__ __forceinline__ void segf_rhs(SegF<G>& X, const float (&u)[kC], float
     kc[D_]    = fl[12] + fl[13];
 }
 
+// shared memory per lane of the mixed solver: 5 stage derivative vectors and the flow increments
+constexpr int kOdeSmemPerLane = 5 * kC + kF;
 template <int G>
 #ifndef MGPU_MIXED_MIN_BLOCKS
 #define MGPU_MIXED_MIN_BLOCKS 3 // resident 128-thread blocks per SM the register budget must allow
@@ -753,8 +755,10 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
     const float o_dt_max = (float)o.dt_max; // DBL_MAX becomes +inf
     // stage derivatives k_0..k_4: [warp][stage*10 + c][lane] (conflict-free columns)
     extern __shared__ float ode_smem[];
-    float* skw = ode_smem + (threadIdx.x >> 5) * (5 * kC * 32);
+    float* skw = ode_smem + (threadIdx.x >> 5) * (kOdeSmemPerLane * 32);
 #define SK(s, c) skw[((s) * kC + (c)) * 32 + lane]
+    // the 5th-order flow increments of the attempt, after the stage derivatives
+#define SP(f) skw[(5 * kC + (f)) * 32 + lane]
     unsigned long long n_acc = 0, n_rej = 0, n_fail = 0;
     bool cap_hit = false, nonfinite = false;
 
@@ -807,7 +811,6 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
             // ControlledStepperWrapper::step
             bool success     = false;
             bool is_dt_valid = true;
-            float phi[kF];
             const float dt_try0 = dt;
             while (!success && is_dt_valid) {
                 if (dt < dt_min) {
@@ -821,16 +824,15 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
                 }
                 const float dtf  = dt;
                 const float trel = tr;
-                float kc[kC], fl[kF], xe[kC];
+                float kc[kC], fl[kF];
                 segf_rhs(X, hi, trel, fl, kc);
 #pragma unroll
                 for (int c = 0; c < kC; ++c) {
                     SK(0, c) = kc[c];
-                    xe[c]    = (fk_db[0] * dtf) * kc[c];
                 }
 #pragma unroll
                 for (int f = 0; f < kF; ++f) {
-                    phi[f] = (fk_b5[0] * dtf) * fl[f];
+                    SP(f) = (fk_b5[0] * dtf) * fl[f];
                 }
                 // stages 2..6: one copy of the right-hand side in the code, stage
                 // derivatives in this lane's shared-memory column
@@ -850,11 +852,6 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
                         }
                     }
                     segf_rhs(X, u, trel + fk_c[s] * dtf, fl, kc);
-                    const float db = fk_db[s] * dtf;
-#pragma unroll
-                    for (int c = 0; c < kC; ++c) {
-                        xe[c] = xe[c] + db * kc[c];
-                    }
                     if (s < 5) {
 #pragma unroll
                         for (int c = 0; c < kC; ++c) {
@@ -865,8 +862,30 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
                     if (b5 != 0.0f) {
 #pragma unroll
                         for (int f = 0; f < kF; ++f) {
-                            phi[f] = phi[f] + b5 * fl[f];
+                            SP(f) = SP(f) + b5 * fl[f];
                         }
+                    }
+                }
+                // embedded error: the stage derivatives weighted in stage order
+                // (k_0..k_4 from shared memory, k_5 still in registers)
+                float xe[kC];
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    xe[c] = (fk_db[0] * dtf) * SK(0, c);
+                }
+#pragma unroll 1
+                for (int s = 1; s < 5; ++s) {
+                    const float db = fk_db[s] * dtf;
+#pragma unroll
+                    for (int c = 0; c < kC; ++c) {
+                        xe[c] = xe[c] + db * SK(s, c);
+                    }
+                }
+                {
+                    const float db = fk_db[5] * dtf;
+#pragma unroll
+                    for (int c = 0; c < kC; ++c) {
+                        xe[c] = xe[c] + db * kc[c];
                     }
                 }
                 // Odeint error measure, max over the instance
@@ -912,8 +931,9 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
             // flow-space update of the (last) attempt: exact TwoSum on both ends of each flow
 #pragma unroll
             for (int f = 0; f < kF; ++f) {
-                df_add(hi[kFlowSrcI(f)], lo[kFlowSrcI(f)], -phi[f]);
-                df_add(hi[kFlowDstI(f)], lo[kFlowDstI(f)], phi[f]);
+                const float ph = SP(f);
+                df_add(hi[kFlowSrcI(f)], lo[kFlowSrcI(f)], -ph);
+                df_add(hi[kFlowDstI(f)], lo[kFlowDstI(f)], ph);
             }
 #pragma unroll
             for (int c = 0; c < kC; ++c) {
@@ -966,7 +986,7 @@ int launch_g(const BatchDev& B, int precision, const int32_t* inst, int64_t coun
         blocks = 1;
     }
     if (precision == MGPU_PRECISION_MIXED) {
-        const size_t smem = (size_t)(threads / 32) * 5 * kC * 32 * sizeof(float);
+        const size_t smem = (size_t)(threads / 32) * kOdeSmemPerLane * 32 * sizeof(float);
         k_ode_mixed<G><<<(unsigned)blocks, threads, smem, s>>>(B, inst, count);
     }
     else {
