@@ -521,8 +521,15 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
                 else {
                     std::fill(dc + n, dc + 2 * n, 0.0);
                 }
+                // an edge with no positive coefficient carries nobody (apply_mobility,
+                // metapopulation_mobility_instant.h:606): its FP32 row is zero, so the
+                // FP32 passes, which do not test the edge, add exact zeros for it
+                bool pos = false;
                 for (int j = 0; j < n; ++j) {
-                    h_ecf[d.ecoef_f_off + (int64_t)e * n + j] = (float)cb[j];
+                    pos = pos || cb[j] > 0.0;
+                }
+                for (int j = 0; j < n; ++j) {
+                    h_ecf[d.ecoef_f_off + (int64_t)e * n + j] = pos ? (float)cb[j] : 0.0f;
                 }
             }
             if (own_coeff[i]) {
@@ -683,6 +690,13 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.out_ptr  = b->pool.upload(h_out_ptr);
     B.in_ptr   = b->pool.upload(h_in_ptr);
     B.in_edges = b->pool.upload(h_in_edges);
+    {
+        std::vector<int32_t> h_in_src(edges);
+        for (int64_t k = 0; k < edges; ++k) {
+            h_in_src[k] = h_src[h_in_edges[k]];
+        }
+        B.in_src = b->pool.upload(h_in_src);
+    }
     B.scratch_stride = std::max<int64_t>(scratch_slots, 1);
     B.scratch_nmax   = (int32_t)b->n_max;
     B.scratch        = scratch_slots > 0 ? b->pool.alloc<double>(8 * b->n_max * B.scratch_stride) : nullptr;

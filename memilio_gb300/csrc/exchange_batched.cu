@@ -1050,17 +1050,22 @@ struct ReturnOrder {
         , phase(0)
     {
     }
-    // e: the edge; returns 0 at the end, 1 for an in-edge, 2 for an out-edge;
-    // *switched is set on the first edge after the lower in-edges
+    // e: the edge; returns 0 at the end, 1 for an in-edge (u: its source), 2 for
+    // an out-edge; switched is set on the first edge after the lower in-edges
     __device__ __forceinline__ int next(int64_t& e, bool& switched)
+    {
+        int64_t u;
+        return next(e, u, switched);
+    }
+    __device__ __forceinline__ int next(int64_t& e, int64_t& u, bool& switched)
     {
         switched = false;
         if (phase == 0) {
             if (k < ie) {
-                const int64_t x = B.in_edges[k];
-                if (B.edge_src[x] < node) {
-                    ++k;
-                    e = x;
+                const int32_t src = B.in_src[k];
+                if (src < node) {
+                    e = B.in_edges[k++];
+                    u = src;
                     return 1;
                 }
             }
@@ -1075,6 +1080,7 @@ struct ReturnOrder {
             phase = 2;
         }
         if (k < ie) {
+            u = B.in_src[k];
             e = B.in_edges[k++];
             return 1;
         }
@@ -1125,15 +1131,13 @@ __global__ void __launch_bounds__(128, MGPU_XF_DEPART_MIN_BLOCKS)
     const bool detect = own.nd != 1.0f;
     const float q     = 1.0f - own.nd;
     ReturnOrder order(B, node);
-    int64_t e;
+    int64_t e, u;
     bool switched;
-    for (int kind = order.next(e, switched); kind != 0; kind = order.next(e, switched)) {
-        if (!B.edge_static_any[e]) {
-            continue;
-        }
+    for (int kind = order.next(e, u, switched); kind != 0; kind = order.next(e, u, switched)) {
+        // (an edge without travelers has zero coefficients and adds exact zeros)
         if (kind == 1) {
             // travelers arriving from the edge's source
-            load_group_snap(B, g, B.edge_src[e], gr, ws, src);
+            load_group_snap(B, g, u, gr, ws, src);
             travelers_f<MASK>(B, g, e, gr, src, m);
 #pragma unroll
             for (int c = 0; c < kC; ++c) {
@@ -1204,9 +1208,13 @@ __global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
     // lower bound of the running state along the serial order, and its magnitude
     float run[kC], mag[kC], phi_net[kF];
     {
+        // the return is applied in place; the state before it goes to yn for the
+        // exact path (rescans and the sequential fallback start from it)
         float h[kC], l[kC];
         ld_state(B.st_hi + s0, h);
         ld_state(B.st_lo + s0, l);
+        st_state(B.yn_hi + s0, h);
+        st_state(B.yn_lo + s0, l);
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
             acc[c].init_pair(h[c], l[c]);
@@ -1232,9 +1240,9 @@ __global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
     // the running sums.
     bool flag = false;
     ReturnOrder order(B, node);
-    int64_t e;
+    int64_t e, u;
     bool switched;
-    for (int kind = order.next(e, switched);; kind = order.next(e, switched)) {
+    for (int kind = order.next(e, u, switched);; kind = order.next(e, u, switched)) {
         if (switched) {
 #pragma unroll
             for (int c = 0; c < kC; ++c) {
@@ -1244,14 +1252,12 @@ __global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
         if (kind == 0) {
             break;
         }
-        if (!B.edge_static_any[e]) {
-            continue;
-        }
+        // (an edge without travelers has zero coefficients and adds exact zeros)
         float ax[kAux];
         const float* a;
         float m[kC], phi[kF];
         if (kind == 1) {
-            load_group_snap(B, g, B.edge_src[e], gr, slot, src);
+            load_group_snap(B, g, u, gr, slot, src);
             travelers_f<MASK>(B, g, e, gr, src, m);
             a = a_own;
         }
@@ -1304,8 +1310,8 @@ __global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
         acc[c].store(&h[c], &l[c]);
         flag = flag || run[c] < 1e-5f * mag[c];
     }
-    st_state(B.yn_hi + so, h);
-    st_state(B.yn_lo + so, l);
+    st_state(B.st_hi + so, h);
+    st_state(B.st_lo + so, l);
     list0_push(B, node * MGPU_MAX_GROUPS + gr, flag);
 }
 
@@ -1594,10 +1600,15 @@ __global__ void k_xf_scan(BatchDev B, int pass)
             continue;
         }
         const int64_t so = g.state_off + (node - g.node0) * g.n + gr * kC;
+        // static graphs: the return pass ran in place and left the state before
+        // the return in yn; graphs with edge dampings: the state is still in st
+        const bool inplace = g.Ke == 0;
+        const float* src_hi = inplace ? B.yn_hi : B.st_hi;
+        const float* src_lo = inplace ? B.yn_lo : B.st_lo;
         FF y[kC];
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
-            y[c] = {B.st_hi[so + c], B.st_lo[so + c]};
+            y[c] = {src_hi[so + c], src_lo[so + c]};
         }
         ReturnOrder order(B, node);
         int64_t e;
@@ -1653,11 +1664,13 @@ __global__ void k_xf_scan(BatchDev B, int pass)
                 y[c] = ff_add(y[c], ff_neg(t[c]));
             }
         }
+        float* dst_hi = inplace ? B.st_hi : B.yn_hi;
+        float* dst_lo = inplace ? B.st_lo : B.yn_lo;
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
-            const FF v      = ff_norm(y[c].h, y[c].l);
-            B.yn_hi[so + c] = v.h;
-            B.yn_lo[so + c] = v.l;
+            const FF v     = ff_norm(y[c].h, y[c].l);
+            dst_hi[so + c] = v.h;
+            dst_lo[so + c] = v.l;
         }
     }
 }
@@ -1718,6 +1731,14 @@ __global__ void k_xb_sequential(BatchDev B, int g0, int ng)
     __shared__ double rem[MGPU_MAX_GROUPS * kC];
     const int lane = threadIdx.x;
     const int n    = g.n;
+    if (B.st_hi && g.Ke == 0) {
+        // the in-place return pass left the state before the return in yn
+        for (int64_t j = lane; j < (int64_t)g.N * n; j += 32) {
+            B.st_hi[g.state_off + j] = B.yn_hi[g.state_off + j];
+            B.st_lo[g.state_off + j] = B.yn_lo[g.state_off + j];
+        }
+        __syncwarp();
+    }
     int64_t fixes  = 0;
     for (int64_t e = g.edge0; e < g.edge0 + g.E; ++e) {
         if (!edge_departed(B, g, e)) {
@@ -1788,8 +1809,8 @@ __global__ void k_xb_commit(BatchDev B, int64_t n0, int64_t nn, int n_max)
     const int gi       = B.node_graph[node];
     const DevGraph& g  = B.graphs[gi];
     const GraphRt& rt  = B.rt[gi];
-    if (j >= g.n || !xb_returning(rt) || rt.fallback) {
-        return;
+    if (j >= g.n || !xb_returning(rt) || rt.fallback || (B.st_hi && g.Ke == 0)) {
+        return; // the mixed return of static graphs runs in place
     }
     const int64_t o = g.state_off + (node - g.node0) * g.n + j;
     if (B.st_hi) {

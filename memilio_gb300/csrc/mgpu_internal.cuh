@@ -112,6 +112,7 @@ struct BatchDev {
     const int64_t* out_ptr;      // [num_nodes+1] CSR (edges sorted by (src, dst))
     const int64_t* in_ptr;       // [num_nodes+1] CSC
     const int64_t* in_edges;     // [num_edges] edge ids sorted by (dst, src)
+    const int32_t* in_src;       // [num_edges] the source node of in_edges[k]
     int64_t state_total;         // doubles in a state pool
     double* ysnap;               // [2][state_total] departure snapshots (batched exchange)
     float* ysnap_f;              // [2][state_total] the same in FP32
