@@ -300,12 +300,14 @@ def main():
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 800.0])
     args = ap.parse_args()
 
+    from memilio_gb300 import replicas as R
     from memilio_gb300 import workloads as W
 
     base = W.mobility_graph(seed=1, N=args.nodes)
 
     def graphs_builder(count):
-        return W.ensemble(num_samples=count, base=base)
+        # every rank its own samples (rank 0: the single-GPU ensemble)
+        return R.ensemble_for_rank(count, dist_info()[0], base=base)
 
     if args.impl == "reference":
         run_reference(args, graphs_builder)
@@ -352,13 +354,8 @@ def main():
     launches = (st1["kernel_launches"] - st0["kernel_launches"])
     exchange_stats = {k: (st1[k] - st0[k]) // args.steps for k in ("underflow_fixes", "sequential_exchanges", "scan_items")}
     ms_step = float(np.sum(dev_ms)) / args.steps
-    ms_max = ms_step
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_max = float(tt.item())
-    value = world * nd_step / (ms_max / 1e3)
+    ms_max = R.max_over_ranks(ms_step, device="cuda")
+    value = R.job_throughput(nd_step, ms_max / 1e3, world)
     final = batch.state_flat()
     attempts_step = (st1["accepted_steps"] + st1["rejected_steps"] - st0["accepted_steps"] - st0["rejected_steps"]) \
         / args.steps

@@ -55,7 +55,8 @@ class MgpuServerOpts(ctypes.Structure):
         ("max_batches", ctypes.c_int32),
         ("phases_per_launch", ctypes.c_int32),
         ("max_graphs_per_batch", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("min_batch_graphs", ctypes.c_int32),
+        ("max_wait_ms", ctypes.c_double),
     ]
 
 
@@ -361,7 +362,7 @@ class Batch:
 
 
 def server_opts(precision=PRECISION_MIXED, memory_budget=0, max_batches=16, phases_per_launch=2,
-                max_graphs_per_batch=4096, **solver_kw) -> MgpuServerOpts:
+                max_graphs_per_batch=4096, min_batch_graphs=64, max_wait_ms=20.0, **solver_kw) -> MgpuServerOpts:
     o = MgpuServerOpts()
     lib().mgpu_default_server_opts(ctypes.byref(o))
     o.solver = solver_opts(precision=precision, **solver_kw)
@@ -369,6 +370,8 @@ def server_opts(precision=PRECISION_MIXED, memory_budget=0, max_batches=16, phas
     o.max_batches = int(max_batches)
     o.phases_per_launch = int(phases_per_launch)
     o.max_graphs_per_batch = int(max_graphs_per_batch)
+    o.min_batch_graphs = int(min_batch_graphs)
+    o.max_wait_ms = float(max_wait_ms)
     return o
 
 

@@ -1809,8 +1809,8 @@ __global__ void k_xb_commit(BatchDev B, int64_t n0, int64_t nn, int n_max)
     const int gi       = B.node_graph[node];
     const DevGraph& g  = B.graphs[gi];
     const GraphRt& rt  = B.rt[gi];
-    if (j >= g.n || !xb_returning(rt) || rt.fallback || (B.st_hi && g.Ke == 0)) {
-        return; // the mixed return of static graphs runs in place
+    if (j >= g.n || !xb_returning(rt) || rt.fallback || (B.st_hi && (g.Ke == 0 || g.E == 0))) {
+        return; // the mixed return of static graphs runs in place; without edges nothing returns
     }
     const int64_t o = g.state_off + (node - g.node0) * g.n + j;
     if (B.st_hi) {
@@ -1892,7 +1892,10 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
     const int last = 1 + ((kXbScanPasses - 1) & 1);
     k_xg_scan_done<<<scan_blocks, 128, 0, s>>>(B, last);
     k_list_reset<<<1, 1, 0, s>>>(B, 0);
-    k_xb_commit<<<blocks_of(nn * n_max, 256), 256, 0, s>>>(B, 0, nn, (int)n_max);
+    if (!mixed || any_edge_dampings) {
+        // (mixed batches without edge dampings return in place)
+        k_xb_commit<<<blocks_of(nn * n_max, 256), 256, 0, s>>>(B, 0, nn, (int)n_max);
+    }
     k_xb_sequential<R><<<B.num_graphs, 32, 0, s>>>(B, 0, B.num_graphs);
     k_xg_cleanup<<<blocks_of(ne, 256), 256, 0, s>>>(B, ne);
     mark(2);
@@ -1917,7 +1920,7 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
         k_xb_depart<R><<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
         *launches += 1;
     }
-    *launches += 5 + 2 * kXbScanPasses;
+    *launches += 4 + 2 * kXbScanPasses + ((!mixed || any_edge_dampings) ? 1 : 0);
 }
 
 } // namespace
@@ -1929,8 +1932,10 @@ int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampi
     }
     const bool mixed = precision == MGPU_PRECISION_MIXED;
     const int extra  = !any_edge_dampings ? 0 : (mixed ? 3 : 1);
-    // prep, return and departure passes (one per age-group count when mixed), the exact path
-    return 6 + (mixed ? 2 * group_lists : 2) + 2 * kXbScanPasses + extra;
+    const int commit = (!mixed || any_edge_dampings) ? 1 : 0;
+    // prep; return and departure passes (one per age-group count when mixed); the
+    // exact path: scan passes with their list resets, done, reset, sequential, cleanup
+    return 5 + (mixed ? 2 * group_lists : 2) + 2 * kXbScanPasses + commit + extra;
 }
 
 void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,

@@ -142,6 +142,8 @@ void mgpu_default_server_opts(mgpu_server_opts* o)
     o->max_batches         = 16;
     o->phases_per_launch   = 2;
     o->max_graphs_per_batch = 4096;
+    o->min_batch_graphs     = 64;
+    o->max_wait_ms          = 20.0;
 }
 
 int mgpu_server_create(int device, const mgpu_server_opts* opts, mgpu_server** out)
@@ -160,7 +162,8 @@ int mgpu_server_create(int device, const mgpu_server_opts* opts, mgpu_server** o
     if (o.solver.precision == MGPU_PRECISION_FP64_PLAIN) {
         return MGPU_UNSUPPORTED;
     }
-    if (o.max_batches < 1 || o.phases_per_launch < 1 || o.max_graphs_per_batch < 1 || o.memory_budget < 0) {
+    if (o.max_batches < 1 || o.phases_per_launch < 1 || o.max_graphs_per_batch < 1 || o.memory_budget < 0 ||
+        o.min_batch_graphs < 1 || !(o.max_wait_ms >= 0.0)) {
         return MGPU_INVALID_VALUE;
     }
     if (cudaSetDevice(device) != cudaSuccess) {
@@ -264,8 +267,15 @@ int mgpu_server_step(mgpu_server* s, int32_t* completed, int32_t* running, int32
         s->in_use -= r.bytes;
         s->running.erase(s->running.begin() + (long)k);
     }
-    // 2. admission: the queued requests that fit, as one new batch per start time
-    while (!s->queue.empty() && (int32_t)s->running.size() < s->opts.max_batches) {
+    // 2. admission: the queued requests that fit, as one new batch per start time.
+    // While batches run, requests wait until enough of them queue up or the
+    // oldest has waited max_wait_ms, so that batches are large enough to fill
+    // the device (one small batch per arrival would leave it launch-bound).
+    const bool busy  = !s->running.empty();
+    const bool ready = !s->queue.empty() &&
+                       (!busy || (int32_t)s->queue.size() >= s->opts.min_batch_graphs ||
+                        (now_s() - s->queue.front().t_submit) * 1e3 >= s->opts.max_wait_ms);
+    while (ready && !s->queue.empty() && (int32_t)s->running.size() < s->opts.max_batches) {
         const double t0 = s->queue.front().t0;
         std::vector<Request> take;
         std::vector<mgpu_graph> graphs;

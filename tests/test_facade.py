@@ -138,3 +138,14 @@ def test_flow_simulation_matches_oracle(programs):
     np.testing.assert_allclose(d["t"], t, rtol=0, atol=1e-6)
     assert scaled(d["last_pop"], y[-1], G) < 1e-8
     np.testing.assert_allclose(d["last_flows"], f[-1], rtol=1e-8, atol=1e-8 * np.abs(f[-1]).max())
+
+
+@pytest.mark.gpu
+def test_example_program_runs():
+    # memilio_gb300/cpp/examples/ode_secir_graph.cpp: two counties, 30 days
+    r = subprocess.run([B.build_facade()["ode_secir_graph"]], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = [l for l in r.stdout.splitlines() if l.startswith("node ")]
+    assert len(lines) == 2 and all("t=30.0" in l for l in lines)
+    totals = [float(l.split("(total ")[1].split(",")[0]) for l in lines]
+    assert abs(sum(totals) - 30000.0) < 1e-6  # 20000 + 10000 residents, conserved by the exchange

@@ -74,7 +74,8 @@ def test_async_launch_matches_advance(ctx):
 
 def test_server_results_equal_alone_and_overlap(ctx):
     graphs, horizons = requests(24)
-    srv = N.Server(0, N.server_opts(max_batches=8, phases_per_launch=2))
+    # immediate admission, so that every wave becomes its own batch
+    srv = N.Server(0, N.server_opts(max_batches=8, phases_per_launch=2, min_batch_graphs=1, max_wait_ms=0.0))
     ids, results, max_batches = {}, {}, 0
     # three waves: later requests arrive while earlier ones are on the device
     waves = [range(0, 8), range(8, 16), range(16, 24)]
@@ -149,3 +150,28 @@ def test_autotuned_schedule_gives_identical_results(ctx):
     assert np.array_equal(a.state_flat(), b.state_flat())
     a.close()
     b.close()
+
+
+def test_server_waits_to_batch_requests_while_busy(ctx):
+    # with a batch running, later requests wait for min_batch_graphs or max_wait_ms
+    graphs, horizons = requests(10, seed=57)
+    srv = N.Server(0, N.server_opts(min_batch_graphs=4, max_wait_ms=1e6))
+    srv.submit(graphs[0], 0.0, 60.0)  # a long first request keeps the device busy
+    srv.step()
+    assert srv.num_batches() == 1
+    for i in range(1, 4):
+        srv.submit(graphs[i], 0.0, horizons[i])
+        srv.step()
+        assert srv.num_batches() == 1  # fewer than 4 waiting: no new batch yet
+    srv.submit(graphs[4], 0.0, horizons[4])
+    srv.step()
+    assert srv.num_batches() == 2  # 4 waiting: admitted together
+    done = 0
+    for _ in range(500000):
+        srv.step()
+        while srv.take() is not None:
+            done += 1
+        if done == 5:
+            break
+    assert done == 5
+    srv.close()
