@@ -303,8 +303,8 @@ typedef struct mgpu_server_opts {
     int32_t phases_per_launch;     /* exchange intervals enqueued per batch and round, default 2 */
     int32_t max_graphs_per_batch;  /* default 4096 */
     int32_t min_batch_graphs;      /* while batches run, admit once this many requests wait ... */
-    double max_wait_ms;            /* ... or the oldest has waited this long (default 64, 20 ms);
-                                      with nothing running, queued requests are admitted at once */
+    double max_wait_ms;            /* ... or the oldest has waited this long (default 1 and 0:
+                                      at once); with nothing running, requests are admitted at once */
 } mgpu_server_opts;
 
 void mgpu_default_server_opts(mgpu_server_opts* opts);

@@ -362,7 +362,7 @@ class Batch:
 
 
 def server_opts(precision=PRECISION_MIXED, memory_budget=0, max_batches=16, phases_per_launch=2,
-                max_graphs_per_batch=4096, min_batch_graphs=64, max_wait_ms=20.0, **solver_kw) -> MgpuServerOpts:
+                max_graphs_per_batch=4096, min_batch_graphs=1, max_wait_ms=0.0, **solver_kw) -> MgpuServerOpts:
     o = MgpuServerOpts()
     lib().mgpu_default_server_opts(ctypes.byref(o))
     o.solver = solver_opts(precision=precision, **solver_kw)

@@ -547,16 +547,31 @@ __device__ __forceinline__ void df_renorm(float& hi, float& lo)
     hi            = s;
 }
 
+#ifndef MGPU_ODE_TAB_LOADS
+#define MGPU_ODE_TAB_LOADS 0
+#endif
 template <int G>
 struct SegF {
     int base;
     unsigned mask;
     int gi;
     NodeModel nm;
-    float a_tnt, beta, xi, rho, rho_max;
-    float r1, r2, r3, r6, r7, r11, r13, r14, r10l, r12l, cps, dps, inv_tisev;
-    float tnt_cap, tnt_cap2, icu_lo, icu_cap;
-    float season_k, season_s0;
+    // per-(node, group) constants (TF_* of the FP32 table): in registers, or
+    // read through L1 at every use with MGPU_ODE_TAB_LOADS (fewer registers)
+#if MGPU_ODE_TAB_LOADS
+    const float* tab;
+    __device__ __forceinline__ float tc(int i) const
+    {
+        return __ldg(tab + i);
+    }
+#else
+    float tabv[kTabF];
+    __device__ __forceinline__ float tc(int i) const
+    {
+        return tabv[i];
+    }
+#endif
+    float season_s0;
     bool fast;
     float P[G], Q[G];
     float t_lo, t_hi, xl, scale; // damping segment and ramp, relative to t_base
@@ -622,29 +637,14 @@ __device__ void segf_load(SegF<G>& X, const BatchDev& B, const DevGraph& g, int6
     const float* T = B.tab_f + ((g.node0 + local) * MGPU_MAX_GROUPS + X.gi) * kTabF;
     X.t_base       = t_base;
     X.t_base_f     = (float)t_base;
-    X.a_tnt        = T[TF_A_TNT];
-    X.beta         = T[TF_BETA];
-    X.xi           = T[TF_XI];
-    X.rho          = T[TF_RHO];
-    X.rho_max      = T[TF_RHO_MAX];
-    X.r1           = T[TF_R1];
-    X.r2           = T[TF_R2];
-    X.r3           = T[TF_R3];
-    X.r6           = T[TF_R6];
-    X.r7           = T[TF_R7];
-    X.r11          = T[TF_R11];
-    X.r13          = T[TF_R13];
-    X.r14          = T[TF_R14];
-    X.r10l         = T[TF_R10L];
-    X.r12l         = T[TF_R12L];
-    X.cps          = T[TF_CPS];
-    X.dps          = T[TF_DPS];
-    X.inv_tisev    = T[TF_INV_TISEV];
-    X.tnt_cap      = T[TF_TNT_CAP];
-    X.tnt_cap2     = T[TF_TNT_CAP2];
-    X.icu_lo       = T[TF_ICU_LO];
-    X.icu_cap      = T[TF_ICU_CAP];
-    X.season_k     = T[TF_SEASON_K];
+#if MGPU_ODE_TAB_LOADS
+    X.tab = T;
+#else
+#pragma unroll
+    for (int q = 0; q < kTabF; ++q) {
+        X.tabv[q] = T[q];
+    }
+#endif
     X.season_s0    = (float)((nm.scalar(MGPU_P_START_DAY) + t_base) * (1.0 / 182.5) + 0.5);
     X.fast         = nm.M == 1;
     if (X.fast) {
@@ -668,14 +668,14 @@ template <int G>
 __device__ __forceinline__ void segf_rhs(SegF<G>& X, const float (&u)[kC], float tau_rel, float (&fl)[kF],
                                          float (&kc)[kC])
 {
-    const float tnt   = segf_sum(X, X.a_tnt * u[INS_]);
+    const float tnt   = segf_sum(X, X.tc(TF_A_TNT) * u[INS_]);
     const float icu   = segf_sum(X, u[ICRI_]);
-    const float risk  = smoother_cosine(tnt, X.tnt_cap, X.tnt_cap2, X.rho, X.rho_max);
+    const float risk  = smoother_cosine(tnt, X.tc(TF_TNT_CAP), X.tc(TF_TNT_CAP2), X.tc(TF_RHO), X.tc(TF_RHO_MAX));
     const float Nj    = u[S_] + u[E_] + u[INS_] + u[ISY_] + u[ISEV_] + u[ICRI_] + u[R_];
     const float divN  = (Nj < (float)kZeroTol) ? 0.0f : __frcp_rn(Nj);
-    const float w     = divN * (X.xi * u[INS_] + risk * u[ISY_]);
+    const float w     = divN * (X.tc(TF_XI) * u[INS_] + risk * u[ISY_]);
     const float season =
-        X.season_k == 0.0f ? 1.0f : 1.0f + X.season_k * sinpif(X.season_s0 + tau_rel * (float)(1.0 / 182.5));
+        X.tc(TF_SEASON_K) == 0.0f ? 1.0f : 1.0f + X.tc(TF_SEASON_K) * sinpif(X.season_s0 + tau_rel * (float)(1.0 / 182.5));
     float acc = 0.0f;
     if (X.fast) {
         if (!(tau_rel >= X.t_lo && tau_rel < X.t_hi)) {
@@ -695,27 +695,27 @@ __device__ __forceinline__ void segf_rhs(SegF<G>& X, const float (&u)[kC], float
             acc += (float)C[j] * __shfl_sync(X.mask, w, X.base + j);
         }
     }
-    float r10 = X.r10l, r12 = X.r12l;
-    if (!(icu <= X.icu_lo)) {
-        const float crit_adj = smoother_cosine(icu, X.icu_lo, X.icu_cap, X.cps, 0.0f);
-        r10                  = crit_adj * X.inv_tisev;
-        r12                  = (X.dps + (X.cps - crit_adj)) * X.inv_tisev;
+    float r10 = X.tc(TF_R10L), r12 = X.tc(TF_R12L);
+    if (!(icu <= X.tc(TF_ICU_LO))) {
+        const float crit_adj = smoother_cosine(icu, X.tc(TF_ICU_LO), X.tc(TF_ICU_CAP), X.tc(TF_CPS), 0.0f);
+        r10                  = crit_adj * X.tc(TF_INV_TISEV);
+        r12                  = (X.tc(TF_DPS) + (X.tc(TF_CPS) - crit_adj)) * X.tc(TF_INV_TISEV);
     }
-    fl[0]  = u[S_] * X.beta * season * acc;
-    fl[1]  = X.r1 * u[E_];
-    fl[2]  = X.r2 * u[INS_];
-    fl[3]  = X.r3 * u[INS_];
-    fl[4]  = X.r2 * u[INSC_];
-    fl[5]  = X.r3 * u[INSC_];
-    fl[6]  = X.r6 * u[ISY_];
-    fl[7]  = X.r7 * u[ISY_];
-    fl[8]  = X.r6 * u[ISYC_];
-    fl[9]  = X.r7 * u[ISYC_];
+    fl[0]  = u[S_] * X.tc(TF_BETA) * season * acc;
+    fl[1]  = X.tc(TF_R1) * u[E_];
+    fl[2]  = X.tc(TF_R2) * u[INS_];
+    fl[3]  = X.tc(TF_R3) * u[INS_];
+    fl[4]  = X.tc(TF_R2) * u[INSC_];
+    fl[5]  = X.tc(TF_R3) * u[INSC_];
+    fl[6]  = X.tc(TF_R6) * u[ISY_];
+    fl[7]  = X.tc(TF_R7) * u[ISY_];
+    fl[8]  = X.tc(TF_R6) * u[ISYC_];
+    fl[9]  = X.tc(TF_R7) * u[ISYC_];
     fl[10] = r10 * u[ISEV_];
-    fl[11] = X.r11 * u[ISEV_];
+    fl[11] = X.tc(TF_R11) * u[ISEV_];
     fl[12] = r12 * u[ISEV_];
-    fl[13] = X.r13 * u[ICRI_];
-    fl[14] = X.r14 * u[ICRI_];
+    fl[13] = X.tc(TF_R13) * u[ICRI_];
+    fl[14] = X.tc(TF_R14) * u[ICRI_];
     kc[S_]    = -fl[0];
     kc[E_]    = fl[0] - fl[1];
     kc[INS_]  = (fl[1] - fl[2]) - fl[3];

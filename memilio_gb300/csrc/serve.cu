@@ -142,8 +142,8 @@ void mgpu_default_server_opts(mgpu_server_opts* o)
     o->max_batches         = 16;
     o->phases_per_launch   = 2;
     o->max_graphs_per_batch = 4096;
-    o->min_batch_graphs     = 64;
-    o->max_wait_ms          = 20.0;
+    o->min_batch_graphs     = 1; // admit at once (measured: waiting to batch did not raise throughput)
+    o->max_wait_ms          = 0.0;
 }
 
 int mgpu_server_create(int device, const mgpu_server_opts* opts, mgpu_server** out)

@@ -172,6 +172,25 @@ def test_ensemble_matches_oracle(ctx, precision):
         assert group_scaled_error(gs, rs, 6) < TOL[precision]
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_edge_cases_in_one_batch(ctx, precision):
+    # the largest age-group count, a single node without edges, a graph without
+    # edges and a stressed graph (finite capacities) side by side in one batch
+    graphs = [W.mobility_graph(seed=61, N=12, G=8, out_degree=3),
+              W.single_node(seed=62, G=2, count=1),
+              W.single_node(seed=63, G=5, count=4),
+              W.mobility_graph(seed=64, N=9, G=3, out_degree=8, stress=True)]
+    horizons = np.array([7.0, 3.0, 4.5, 6.0])
+    b = N.Batch(ctx, graphs, 0.0, N.solver_opts(precision=precision))
+    b.advance(0.0, horizons)
+    np.testing.assert_allclose(b.times(), horizons, rtol=0, atol=1e-12)
+    got = b.states()
+    for g, h, gs in zip(graphs, horizons, got):
+        _, fin, _ = O.graph_run(g, 0.0, float(h), record=False)
+        assert group_scaled_error(gs, fin, g.num_groups) < TOL[precision]
+    b.close()
+
+
 @pytest.mark.parametrize("precision", [N.PRECISION_FP64, N.PRECISION_MIXED])
 def test_uneven_batch_matches_oracle(ctx, precision):
     graphs, horizons = W.uneven_batch(num_graphs=24, seed=5, max_nodes=60, max_degree=10, horizon=(2.0, 12.0))
