@@ -995,6 +995,55 @@ __host__ __device__ constexpr int touched_mask(int mask)
     return t;
 }
 
+// Row loads that skip the float pairs holding no compartment of MASK (those
+// values are never used), and the auxiliary values the flows out of MASK need.
+template <int MASK>
+__device__ __forceinline__ void ld_row_m(const float* p, float (&v)[kC])
+{
+    const float2* q = reinterpret_cast<const float2*>(p);
+#pragma unroll
+    for (int i = 0; i < kC / 2; ++i) {
+        if (in_mask(MASK, 2 * i) || in_mask(MASK, 2 * i + 1)) {
+            const float2 a = __ldg(q + i);
+            v[2 * i]       = a.x;
+            v[2 * i + 1]   = a.y;
+        }
+        else {
+            v[2 * i] = v[2 * i + 1] = 0.0f;
+        }
+    }
+}
+__host__ __device__ constexpr int aux_of_flow(int k)
+{
+    // the rate index of flow k in the auxiliary values (see flows_f)
+    return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 2 : k == 3 ? 3 : k == 4 ? 2 : k == 5 ? 3 : k == 6 ? 4 : k == 7 ? 5
+         : k == 8 ? 4 : k == 9 ? 5 : k == 10 ? 6 : k == 11 ? 7 : k == 12 ? 8 : k == 13 ? 9 : 10;
+}
+template <int MASK>
+__device__ __forceinline__ void ld_aux_m(const float* p, float (&v)[kAux])
+{
+    const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int i = 0; i < kAux / 4; ++i) {
+        bool need = false;
+#pragma unroll
+        for (int k = 0; k < kF; ++k) {
+            const int a = aux_of_flow(k);
+            need        = need || (in_mask(MASK, kFlowSrcI(k)) && a >= 4 * i && a < 4 * i + 4);
+        }
+        if (need) {
+            const float4 x = __ldg(q + i);
+            v[4 * i]       = x.x;
+            v[4 * i + 1]   = x.y;
+            v[4 * i + 2]   = x.z;
+            v[4 * i + 3]   = x.w;
+        }
+        else {
+            v[4 * i] = v[4 * i + 1] = v[4 * i + 2] = v[4 * i + 3] = 0.0f;
+        }
+    }
+}
+
 // m = ((y o c) o f) with the nondetection factor nd on INS and ISy (same operations as depart_travelers<float>)
 template <int MASK = kMaskAll>
 __device__ __forceinline__ void travelers_cf(const GroupSnap& s, float nd, const float (&cf)[kC], float (&m)[kC])
@@ -1018,8 +1067,19 @@ __device__ __forceinline__ void travelers_f(const BatchDev& B, const DevGraph& g
                                             const GroupSnap& s, float (&m)[kC])
 {
     float cf[kC];
-    edge_coeff_f(B, g, e, gr, cf);
+    ld_row_m<MASK>(B.ecoef_f + g.ecoef_f_off + (e - g.edge0) * g.n + gr * kC, cf);
     travelers_cf<MASK>(s, s.nd, cf, m);
+}
+
+template <int MASK>
+__device__ __forceinline__ void load_group_snap_m(const BatchDev& B, const DevGraph& g, int64_t node, int gr,
+                                                  int slot, GroupSnap& s)
+{
+    ld_row_m<MASK>(B.ysnap_f + (int64_t)slot * B.state_total + g.state_off + (node - g.node0) * g.n + gr * kC, s.y);
+    const float2 f = __ldg(reinterpret_cast<const float2*>(B.risk) +
+                           ((int64_t)slot * B.num_nodes + node) * MGPU_MAX_GROUPS + gr);
+    s.risk = f.x;
+    s.nd   = f.y;
 }
 
 template <int MASK = kMaskAll>
@@ -1126,7 +1186,7 @@ __global__ void __launch_bounds__(128, MGPU_XF_DEPART_MIN_BLOCKS)
         }
     }
     GroupSnap own, src;
-    load_group_snap(B, g, node, gr, ws, own);
+    load_group_snap_m<MASK>(B, g, node, gr, ws, own);
     float m[kC];
     const bool detect = own.nd != 1.0f;
     const float q     = 1.0f - own.nd;
@@ -1137,7 +1197,7 @@ __global__ void __launch_bounds__(128, MGPU_XF_DEPART_MIN_BLOCKS)
         // (an edge without travelers has zero coefficients and adds exact zeros)
         if (kind == 1) {
             // travelers arriving from the edge's source
-            load_group_snap(B, g, u, gr, ws, src);
+            load_group_snap_m<MASK>(B, g, u, gr, ws, src);
             travelers_f<MASK>(B, g, e, gr, src, m);
 #pragma unroll
             for (int c = 0; c < kC; ++c) {
@@ -1148,7 +1208,7 @@ __global__ void __launch_bounds__(128, MGPU_XF_DEPART_MIN_BLOCKS)
             continue;
         }
         float cf[kC];
-        edge_coeff_f(B, g, e, gr, cf);
+        ld_row_m<MASK>(B.ecoef_f + g.ecoef_f_off + (e - g.edge0) * g.n + gr * kC, cf);
         if (detect) {
             // test_commuters: detected commuters move to the confirmed compartments first
             float mo[kC];
@@ -1228,9 +1288,9 @@ __global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
     }
     const float* aux = reinterpret_cast<const float*>(B.aux);
     float a_own[kAux];
-    ld_aux12(aux + (node * MGPU_MAX_GROUPS + gr) * kAux, a_own);
+    ld_aux_m<MASK>(aux + (node * MGPU_MAX_GROUPS + gr) * kAux, a_own);
     GroupSnap own, src;
-    load_group_snap(B, g, node, gr, slot, own);
+    load_group_snap_m<MASK>(B, g, node, gr, slot, own);
     // run[c] is a lower bound of the exact running state of the serial order:
     // in-edges take max(t, 0) away, out-edges add t (negative amounts included),
     // so within each run of in-edges it only decreases, and the underflow test of
@@ -1257,12 +1317,12 @@ __global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
         const float* a;
         float m[kC], phi[kF];
         if (kind == 1) {
-            load_group_snap(B, g, u, gr, slot, src);
+            load_group_snap_m<MASK>(B, g, u, gr, slot, src);
             travelers_f<MASK>(B, g, e, gr, src, m);
             a = a_own;
         }
         else {
-            ld_aux12(aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux, ax);
+            ld_aux_m<MASK>(aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux, ax);
             travelers_f<MASK>(B, g, e, gr, own, m);
             a = ax;
         }
