@@ -916,28 +916,6 @@ struct GroupSnap {
 // and auxiliary tables are read-only in the kernels that use them (read-only
 // data path); the node states use plain loads and stores.
 static_assert(kC == 10 && kAux == 12, "vector widths of the FP32 tables");
-__device__ __forceinline__ void ld_row(const float* p, float (&v)[kC])
-{
-    const float2* q = reinterpret_cast<const float2*>(p);
-#pragma unroll
-    for (int i = 0; i < kC / 2; ++i) {
-        const float2 a = __ldg(q + i);
-        v[2 * i]       = a.x;
-        v[2 * i + 1]   = a.y;
-    }
-}
-__device__ __forceinline__ void ld_aux12(const float* p, float (&v)[kAux])
-{
-    const float4* q = reinterpret_cast<const float4*>(p);
-#pragma unroll
-    for (int i = 0; i < kAux / 4; ++i) {
-        const float4 a = __ldg(q + i);
-        v[4 * i]       = a.x;
-        v[4 * i + 1]   = a.y;
-        v[4 * i + 2]   = a.z;
-        v[4 * i + 3]   = a.w;
-    }
-}
 __device__ __forceinline__ void ld_state(const float* p, float (&v)[kC])
 {
     const float2* q = reinterpret_cast<const float2*>(p);
@@ -957,20 +935,7 @@ __device__ __forceinline__ void st_state(float* p, const float (&v)[kC])
     }
 }
 
-__device__ __forceinline__ void load_group_snap(const BatchDev& B, const DevGraph& g, int64_t node, int gr, int slot,
-                                                GroupSnap& s)
-{
-    ld_row(B.ysnap_f + (int64_t)slot * B.state_total + g.state_off + (node - g.node0) * g.n + gr * kC, s.y);
-    const float2 f = __ldg(reinterpret_cast<const float2*>(B.risk) +
-                           ((int64_t)slot * B.num_nodes + node) * MGPU_MAX_GROUPS + gr);
-    s.risk = f.x;
-    s.nd   = f.y;
-}
 
-__device__ __forceinline__ void edge_coeff_f(const BatchDev& B, const DevGraph& g, int64_t e, int gr, float (&cf)[kC])
-{
-    ld_row(B.ecoef_f + g.ecoef_f_off + (e - g.edge0) * g.n + gr * kC, cf);
-}
 
 // Compartment masks of the FP32 passes: MASK holds the compartments whose
 // travelers can be nonzero (a nonzero coefficient on some edge of every graph
@@ -1112,11 +1077,6 @@ struct ReturnOrder {
     }
     // e: the edge; returns 0 at the end, 1 for an in-edge (u: its source), 2 for
     // an out-edge; switched is set on the first edge after the lower in-edges
-    __device__ __forceinline__ int next(int64_t& e, bool& switched)
-    {
-        int64_t u;
-        return next(e, u, switched);
-    }
     __device__ __forceinline__ int next(int64_t& e, int64_t& u, bool& switched)
     {
         switched = false;
@@ -1638,31 +1598,41 @@ __device__ __forceinline__ int fix_group_ff(const FF (&y)[kC], FF (&t)[kC])
     return nfix;
 }
 
+// One warp per item: the lanes compute the returning travelers of 32 incident
+// edges at a time in parallel (the gathers), then replay the serial order over
+// them together: every lane holds the same running state, the travelers of
+// edge j come from lane j by shuffles, and lane j publishes edge j's fix.
 __global__ void k_xf_scan(BatchDev B, int pass)
 {
+    constexpr unsigned kFull = 0xffffffffu;
     const int lin    = pass == 0 ? 0 : 1 + ((pass - 1) & 1);
     const int lout   = 1 + (pass & 1);
     const int cnt    = B.scan_count[lin];
     const int64_t NG = B.num_nodes * MGPU_MAX_GROUPS;
+    const int lane   = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     if (blockIdx.x == 0 && threadIdx.x == 0 && cnt > 0) {
         atomicAdd(&B.counters[CNT_SCANNED], (unsigned long long)cnt);
     }
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < cnt;
-         idx += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t idx = w0; idx < cnt; idx += nw) {
         const int64_t item = B.scan_list[lin * NG + idx];
-        B.scan_mark[lin * NG + item] = 0; // consumed
         const int64_t node = item / MGPU_MAX_GROUPS;
         const int gr       = (int)(item % MGPU_MAX_GROUPS);
-        const int gi       = B.node_graph[node];
-        const DevGraph& g  = B.graphs[gi];
-        const GraphRt& rt  = B.rt[gi];
+        __syncwarp();
+        if (lane == 0) {
+            B.scan_mark[lin * NG + item] = 0; // consumed
+        }
+        const int gi      = B.node_graph[node];
+        const DevGraph& g = B.graphs[gi];
+        const GraphRt& rt = B.rt[gi];
         if (gr >= g.G || !xb_returning(rt)) {
-            continue;
+            continue; // the whole warp
         }
         const int64_t so = g.state_off + (node - g.node0) * g.n + gr * kC;
         // static graphs: the return pass ran in place and left the state before
         // the return in yn; graphs with edge dampings: the state is still in st
-        const bool inplace = g.Ke == 0;
+        const bool inplace  = g.Ke == 0;
         const float* src_hi = inplace ? B.yn_hi : B.st_hi;
         const float* src_lo = inplace ? B.yn_lo : B.st_lo;
         FF y[kC];
@@ -1670,67 +1640,121 @@ __global__ void k_xf_scan(BatchDev B, int pass)
         for (int c = 0; c < kC; ++c) {
             y[c] = {src_hi[so + c], src_lo[so + c]};
         }
-        ReturnOrder order(B, node);
-        int64_t e;
-        bool switched;
-        for (int kind = order.next(e, switched); kind != 0; kind = order.next(e, switched)) {
-            if (!edge_departed(B, g, e)) {
-                continue;
+        const int64_t ib = B.in_ptr[node], ie = B.in_ptr[node + 1];
+        const int64_t ob = B.out_ptr[node], oe = B.out_ptr[node + 1];
+        // in-edges from lower nodes come first (in_src ascends within the node)
+        int nlow = 0;
+        for (int64_t base = ib; base < ie; base += 32) {
+            const int64_t k = base + lane;
+            nlow += __popc(__ballot_sync(kFull, k < ie && B.in_src[k] < node));
+        }
+        const int nout = (int)(oe - ob);
+        const int deg  = (int)(ie - ib) + nout;
+        for (int base = 0; base < deg; base += 32) {
+            // this lane's edge of the chunk, in the serial order
+            const int i    = base + lane;
+            int kind       = 0;
+            int64_t e      = 0, u = 0;
+            if (i < deg) {
+                if (i < nlow) {
+                    kind = 1;
+                    e    = B.in_edges[ib + i];
+                    u    = B.in_src[ib + i];
+                }
+                else if (i < nlow + nout) {
+                    kind = 2;
+                    e    = ob + (i - nlow);
+                }
+                else {
+                    kind = 1;
+                    e    = B.in_edges[ib + i - nout];
+                    u    = B.in_src[ib + i - nout];
+                }
+                if (!edge_departed(B, g, e)) {
+                    kind = 0;
+                }
             }
-            uint8_t* fc    = B.fix_cnt + e * MGPU_MAX_GROUPS + gr;
-            float2* mf     = reinterpret_cast<float2*>(B.mfix + B.trav_off[e] + gr * kC);
-            const int prev = *(volatile uint8_t*)fc;
             FF t[kC];
-            if (kind == 2 && prev != 0) {
-                // fixed by the destination's scan: the published pair
+            int prev = 0;
+            if (kind != 0) {
+                prev = *(volatile uint8_t*)(B.fix_cnt + e * MGPU_MAX_GROUPS + gr);
+                if (kind == 2 && prev != 0) {
+                    // fixed by the destination's scan: the published pair
+                    const float2* mf = reinterpret_cast<const float2*>(B.mfix + B.trav_off[e] + gr * kC);
 #pragma unroll
-                for (int c = 0; c < kC; ++c) {
-                    const float2 v = __ldcg(mf + c);
-                    t[c]           = {v.x, v.y};
+                    for (int c = 0; c < kC; ++c) {
+                        const float2 v = __ldcg(mf + c);
+                        t[c]           = {v.x, v.y};
+                    }
+                }
+                else {
+                    return_travelers_ff(B, g, rt, e, gr, t);
                 }
             }
             else {
-                return_travelers_ff(B, g, rt, e, gr, t);
-            }
-            if (kind == 2) {
 #pragma unroll
                 for (int c = 0; c < kC; ++c) {
-                    y[c] = ff_add(y[c], t[c]);
+                    t[c] = {0.0f, 0.0f};
                 }
-                continue;
             }
-            const int nfix = fix_group_ff(y, t);
-            bool changed   = false;
-            if (nfix) {
-                changed = prev == 0;
+            const int nchunk = deg - base < 32 ? deg - base : 32;
+            for (int j = 0; j < nchunk; ++j) {
+                const int kj = __shfl_sync(kFull, kind, j);
+                FF tj[kC];
 #pragma unroll
                 for (int c = 0; c < kC; ++c) {
-                    const float2 old = __ldcg(mf + c);
-                    changed          = changed || old.x != t[c].h || old.y != t[c].l;
-                    __stcg(mf + c, make_float2(t[c].h, t[c].l));
+                    tj[c].h = __shfl_sync(kFull, t[c].h, j);
+                    tj[c].l = __shfl_sync(kFull, t[c].l, j);
                 }
-                __threadfence();
-                *(volatile uint8_t*)fc = (uint8_t)nfix;
-            }
-            else if (prev) {
-                *(volatile uint8_t*)fc = 0;
-                changed                = true;
-            }
-            if (changed) {
-                list_push(B, lout, B.edge_src[e] * MGPU_MAX_GROUPS + gr);
-            }
+                if (kj == 0) {
+                    continue;
+                }
+                if (kj == 2) {
 #pragma unroll
-            for (int c = 0; c < kC; ++c) {
-                y[c] = ff_add(y[c], ff_neg(t[c]));
+                    for (int c = 0; c < kC; ++c) {
+                        y[c] = ff_add(y[c], tj[c]);
+                    }
+                    continue;
+                }
+                const int nfix = fix_group_ff(y, tj);
+                if (lane == j) {
+                    uint8_t* fc  = B.fix_cnt + e * MGPU_MAX_GROUPS + gr;
+                    float2* mf   = reinterpret_cast<float2*>(B.mfix + B.trav_off[e] + gr * kC);
+                    bool changed = false;
+                    if (nfix) {
+                        changed = prev == 0;
+#pragma unroll
+                        for (int c = 0; c < kC; ++c) {
+                            const float2 old = __ldcg(mf + c);
+                            changed          = changed || old.x != tj[c].h || old.y != tj[c].l;
+                            __stcg(mf + c, make_float2(tj[c].h, tj[c].l));
+                        }
+                        __threadfence();
+                        *(volatile uint8_t*)fc = (uint8_t)nfix;
+                    }
+                    else if (prev) {
+                        *(volatile uint8_t*)fc = 0;
+                        changed                = true;
+                    }
+                    if (changed) {
+                        list_push(B, lout, u * MGPU_MAX_GROUPS + gr);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    y[c] = ff_add(y[c], ff_neg(tj[c]));
+                }
             }
         }
-        float* dst_hi = inplace ? B.st_hi : B.yn_hi;
-        float* dst_lo = inplace ? B.st_lo : B.yn_lo;
+        if (lane == 0) {
+            float* dst_hi = inplace ? B.st_hi : B.yn_hi;
+            float* dst_lo = inplace ? B.st_lo : B.yn_lo;
 #pragma unroll
-        for (int c = 0; c < kC; ++c) {
-            const FF v     = ff_norm(y[c].h, y[c].l);
-            dst_hi[so + c] = v.h;
-            dst_lo[so + c] = v.l;
+            for (int c = 0; c < kC; ++c) {
+                const FF v     = ff_norm(y[c].h, y[c].l);
+                dst_hi[so + c] = v.h;
+                dst_lo[so + c] = v.l;
+            }
         }
     }
 }
