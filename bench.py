@@ -272,9 +272,9 @@ def h2d_bytes(graphs) -> int:
 #           return-time rates 48  (snapshot rows of the sources and the
 #           ensemble-shared coefficients are counted once, as the own rows)
 #   depart: state read + write 160, departure state write 80, snapshot 40, factors 8
-#   prep:   departure state read 80, state hi read 40, rates write 48,
-#           snapshot write 40, factors write 8, constant table read 96
-BYTES_PER_ITEM = {"return": 256, "depart": 288, "prep": 312, "exact": 256}
+#   (the node pass, return-time rates and departure snapshot, runs inside the
+#   mixed node kernel)
+BYTES_PER_ITEM = {"return": 256, "depart": 288, "exact": 256}
 # DRAM bytes (read + write) per (node, group) item of one launch, from one ncu
 # capture of a 256-sample x 400-node ensemble (profiles/ncu_k_xf_return_256x400.md,
 # profiles/ncu_k_xf_depart_256x400.md): 212.9 MB and 179.7 MB for 614,400 items.
@@ -389,18 +389,18 @@ def main():
              "depart": tm["depart_ms"]}
     roofline["parts_ms_per_step"] = parts
     dominant = max(parts, key=parts.get)
-    if prec == N.PRECISION_MIXED and dominant in ("return", "depart", "prep", "exact"):
+    if prec == N.PRECISION_MIXED and dominant in ("return", "depart", "exact"):
         # the exchange pass that dominates the step, against the measured HBM copy rate
         peaks = measured_peaks()
         items = sum(g.num_nodes * g.num_groups for g in graphs)
-        launches_active = args.days / 0.5 / (2 if dominant in ("return", "depart", "exact") else 1)
+        launches_active = args.days / 0.5 / 2  # one return and one departure per day
         if dominant == "exact":
             items = exchange_stats["scan_items"] / launches_active  # scanned (node, group) items per return
         bytes_launch = items * BYTES_PER_ITEM[dominant]
         ms_launch = parts[dominant] / launches_active
         ach = bytes_launch / (ms_launch / 1e3) / 1e9
         roofline = dict(roofline, bound="hbm", kernel={"return": "k_xf_return", "depart": "k_xf_depart",
-                                                      "prep": "k_xf_prep", "exact": "k_xf_scan"}[dominant],
+                                                      "exact": "k_xf_scan"}[dominant],
                         achieved=ach, unit="GB/s", peak=peaks["hbm_gbs"], peak_source=peaks["source"],
                         frac=ach / peaks["hbm_gbs"], algorithmic_bytes_per_launch=bytes_launch,
                         traffic=(items * NCU_BYTES_PER_ITEM[dominant] if dominant in NCU_BYTES_PER_ITEM else None),

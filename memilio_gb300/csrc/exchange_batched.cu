@@ -37,8 +37,6 @@ namespace mgpu
 namespace
 {
 
-constexpr int kAux = 12; // per destination and age group: lambda, r1, r2, r3, r6, r7, r10, r11, r12, r13, r14
-
 __device__ __forceinline__ bool xb_departing(const GraphRt& rt)
 {
     return rt.active && rt.do_depart;
@@ -512,177 +510,6 @@ __global__ void k_xb_prep(BatchDev B, int64_t n0, int64_t nn)
                                         nm.gp(MGPU_G_RISK_FROM_SYMPTOMATIC, i),
                                         nm.gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, i));
             fac[1] = (R)nd;
-        }
-    }
-}
-
-// The same node pass for the mixed solver, in FP32 from the per-(node, group)
-// constants computed at upload (the tables of k_ode_mixed): the auxiliary values
-// and factors are FP32 anyway, and FP64 division and sine would bound the pass.
-__global__ void k_xf_prep(BatchDev B, int64_t n0, int64_t nn)
-{
-    constexpr unsigned kFull = 0xffffffffu;
-    const int64_t tid        = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t seg        = tid / MGPU_MAX_GROUPS;
-    const bool in_range      = seg < nn;
-    const int64_t node       = n0 + (in_range ? seg : nn - 1); // every lane takes part in the shuffles
-    const int lane           = (int)(threadIdx.x % MGPU_MAX_GROUPS);
-    const int gi             = B.node_graph[node];
-    const DevGraph& g        = B.graphs[gi];
-    const GraphRt& rt        = B.rt[gi];
-    const int G              = g.G;
-    const bool mine          = in_range && lane < G;
-    const int i              = lane < G ? lane : 0;
-    const int64_t lv         = node - g.node0;
-    const int64_t so         = g.state_off + lv * g.n + (int64_t)i * kC;
-    const bool ret           = in_range && xb_returning(rt);
-    const bool dep           = in_range && xb_departing(rt);
-    const float* T           = B.tab_f + (node * MGPU_MAX_GROUPS + i) * kTabF;
-    const float a_tnt        = T[TF_A_TNT];
-    if (__any_sync(kFull, ret)) {
-        float pop[kC];
-#pragma unroll
-        for (int c = 0; c < kC; ++c) {
-            pop[c] = __fadd_rn(B.v0_hi[so + c], B.v0_lo[so + c]);
-        }
-        float tnt = 0.0f, icu = 0.0f;
-        const float tnt_c = a_tnt * pop[MGPU_INS];
-#pragma unroll
-        for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
-            const float a = __shfl_sync(kFull, tnt_c, q, MGPU_MAX_GROUPS);
-            const float b = __shfl_sync(kFull, pop[MGPU_ICRI], q, MGPU_MAX_GROUPS);
-            if (q < G) {
-                tnt += a;
-                icu += b;
-            }
-        }
-        // this lane as source group: weighted infectious pressure / N
-        const float risk = smoother_cosine(tnt, T[TF_TNT_CAP], T[TF_TNT_CAP2], T[TF_RHO], T[TF_RHO_MAX]);
-        const float Nj   = pop[MGPU_S] + pop[MGPU_E] + pop[MGPU_INS] + pop[MGPU_ISY] + pop[MGPU_ISEV] +
-                         pop[MGPU_ICRI] + pop[MGPU_R];
-        const float divN = (Nj < (float)kZeroTol) ? 0.0f : __frcp_rn(Nj);
-        const float w    = divN * (T[TF_XI] * pop[MGPU_INS] + risk * pop[MGPU_ISY]);
-        // this lane as target group: its contact row at t_dep
-        const NodeModel nm = node_model(B, g, lv);
-        float Crow[MGPU_MAX_GROUPS];
-        if (nm.M == 1) {
-            const long GG   = (long)G * G;
-            const float* Bm = B.contact_f + g.contact_off + lv * 2 * GG + (long)i * G;
-            const float* Lm = Bm + GG;
-            if (nm.K == 0) {
-#pragma unroll
-                for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
-                    Crow[q] = q < G ? Bm[q] : 0.0f;
-                }
-            }
-            else {
-                const int ub    = damping_upper_bound(nm.dtimes, nm.K, rt.t_dep);
-                const double tu = nm.dtimes[ub];
-                const float xl  = (float)((tu - 1.0) - rt.t_dep);
-                const float sc  = (float)(1.0 / (tu - (tu - 1.0)));
-                const float c   = (0.0f <= xl) ? 1.0f : cospif((0.0f - xl) * sc);
-                const float* Dl = B.dvals_f + g.dval_off + lv * g.K * GG + (long)(ub - 1) * GG + (long)i * G;
-                const float* Dr = Dl + GG;
-#pragma unroll
-                for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
-                    if (q < G) {
-                        const float BL = Bm[q] - Lm[q];
-                        const float P  = Bm[q] - (0.5f * (Dl[q] + Dr[q])) * BL;
-                        const float Q  = -(0.5f * (Dl[q] - Dr[q])) * BL;
-                        Crow[q]        = P + Q * c;
-                    }
-                    else {
-                        Crow[q] = 0.0f;
-                    }
-                }
-            }
-        }
-        else {
-            double Cd[MGPU_MAX_GROUPS];
-            contact_row(nm, i, rt.t_dep, Cd);
-#pragma unroll
-            for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
-                Crow[q] = (float)Cd[q];
-            }
-        }
-        float acc = 0.0f;
-#pragma unroll
-        for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
-            const float wq = __shfl_sync(kFull, w, q, MGPU_MAX_GROUPS);
-            if (q < G) {
-                acc += Crow[q] * wq;
-            }
-        }
-        if (ret && mine) {
-            const float sk     = T[TF_SEASON_K];
-            const float season = sk == 0.0f
-                                     ? 1.0f
-                                     : 1.0f + sk * sinpif((float)((nm.scalar(MGPU_P_START_DAY) + rt.t_dep) *
-                                                                      (1.0 / 182.5) +
-                                                                  0.5));
-            float r10 = T[TF_R10L], r12 = T[TF_R12L];
-            if (!(icu <= T[TF_ICU_LO])) {
-                const float crit_adj = smoother_cosine(icu, T[TF_ICU_LO], T[TF_ICU_CAP], T[TF_CPS], 0.0f);
-                r10                  = crit_adj * T[TF_INV_TISEV];
-                r12                  = (T[TF_DPS] + (T[TF_CPS] - crit_adj)) * T[TF_INV_TISEV];
-            }
-            float v[kAux];
-            v[0]  = T[TF_BETA] * season * acc;
-            v[1]  = T[TF_R1];
-            v[2]  = T[TF_R2];
-            v[3]  = T[TF_R3];
-            v[4]  = T[TF_R6];
-            v[5]  = T[TF_R7];
-            v[6]  = r10;
-            v[7]  = T[TF_R11];
-            v[8]  = r12;
-            v[9]  = T[TF_R13];
-            v[10] = T[TF_R14];
-            // can one Euler step of length dt drive a returning compartment negative?
-            // (it cannot when dt times every compartment's total outflow rate is <= 1;
-            // the FP32 test keeps a margin for its own rounding)
-            const float out_rate =
-                fmaxf(fmaxf(v[0], v[1]), fmaxf(fmaxf(v[2] + v[3], v[4] + v[5]), fmaxf(v[6] + v[7] + v[8], v[9] + v[10])));
-            v[11]     = ((float)rt.dt * out_rate > 0.99999f) ? 1.0f : 0.0f;
-            float4* a = reinterpret_cast<float4*>(reinterpret_cast<float*>(B.aux) + (node * MGPU_MAX_GROUPS + i) * kAux);
-            a[0]      = make_float4(v[0], v[1], v[2], v[3]);
-            a[1]      = make_float4(v[4], v[5], v[6], v[7]);
-            a[2]      = make_float4(v[8], v[9], v[10], v[11]);
-        }
-    }
-    if (__any_sync(kFull, dep)) {
-        const int ws = rt.snap_slot ^ 1;
-        float h[kC];
-#pragma unroll
-        for (int c = 0; c < kC; ++c) {
-            h[c] = B.st_hi[so + c];
-        }
-        if (dep && mine) {
-            float* yf = B.ysnap_f + (int64_t)ws * B.state_total + so;
-#pragma unroll
-            for (int c = 0; c < kC / 2; ++c) {
-                reinterpret_cast<float2*>(yf)[c] = make_float2(h[2 * c], h[2 * c + 1]); // the FP32 rounding of hi + lo
-            }
-        }
-        // ISy mobility factor (get_mobility_factors, models/ode_secir/model.h:687-715)
-        // and commuter nondetection at this departure
-        const float tnt_c = a_tnt * h[MGPU_INS];
-        float tnt         = 0.0f;
-#pragma unroll
-        for (int q = 0; q < MGPU_MAX_GROUPS; ++q) {
-            const float a = __shfl_sync(kFull, tnt_c, q, MGPU_MAX_GROUPS);
-            if (q < G) {
-                tnt += a;
-            }
-        }
-        if (dep && mine) {
-            const double* p = B.params + g.param_off + lv * param_stride(G);
-            const double t  = rt.t_next;
-            const float nd  = (t >= p[MGPU_P_START_COMMUTER_DETECTION] && t < p[MGPU_P_END_COMMUTER_DETECTION])
-                                  ? (float)p[MGPU_P_COMMUTER_NONDETECTION]
-                                  : 1.0f;
-            float2* fac = reinterpret_cast<float2*>(B.risk) + ((int64_t)ws * B.num_nodes + node) * MGPU_MAX_GROUPS + i;
-            *fac        = make_float2(smoother_cosine(tnt, T[TF_TNT_CAP], T[TF_TNT_CAP2], T[TF_RHO], T[TF_RHO_MAX]), nd);
         }
     }
 }
@@ -1929,13 +1756,11 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
         return;
     }
     const int T = 128;
-    if (std::is_same<R, float>::value) {
-        k_xf_prep<<<blocks_of(nn * MGPU_MAX_GROUPS, T), T, 0, s>>>(B, 0, nn);
-    }
-    else {
+    // (the mixed solver's node kernel does the node pass itself)
+    if (!std::is_same<R, float>::value) {
         k_xb_prep<R><<<blocks_of(nn * MGPU_MAX_GROUPS, T), T, 0, s>>>(B, 0, nn);
+        *launches += 1;
     }
-    *launches += 1;
     mark(0);
     if (ne == 0) {
         mark(1);
@@ -2011,15 +1836,16 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
 
 int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings, int group_lists)
 {
-    if (!has_edges) {
-        return 1;
-    }
     const bool mixed = precision == MGPU_PRECISION_MIXED;
+    const int prep   = mixed ? 0 : 1; // the node pass (inside the node kernel when mixed)
+    if (!has_edges) {
+        return prep;
+    }
     const int extra  = !any_edge_dampings ? 0 : (mixed ? 3 : 1);
     const int commit = (!mixed || any_edge_dampings) ? 1 : 0;
-    // prep; return and departure passes (one per age-group count when mixed); the
-    // exact path: scan passes with their list resets, done, reset, sequential, cleanup
-    return 5 + (mixed ? 2 * group_lists : 2) + 2 * kXbScanPasses + commit + extra;
+    // return and departure passes (one per age-group count when mixed); the exact
+    // path: scan passes with their list resets, done, reset, sequential, cleanup
+    return prep + 4 + (mixed ? 2 * group_lists : 2) + 2 * kXbScanPasses + commit + extra;
 }
 
 void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,

@@ -140,6 +140,11 @@ enum {
     kTabF = 24
 };
 
+// Return-side values per (node, age group) at the pending departure, written
+// before each return: lambda, r1, r2, r3, r6, r7, r10, r11, r12, r13, r14 and a
+// flag (1: one Euler step of the interval's length may drive a compartment negative).
+constexpr int kAux = 12;
+
 __host__ __device__ inline int param_stride(int G)
 {
     return MGPU_NUM_SCALAR_PARAMS + MGPU_NUM_GROUP_PARAMS * G;

@@ -663,10 +663,12 @@ __device__ __forceinline__ float segf_sum(const SegF<G>& X, float v)
     return s;
 }
 
-// Flows and derivative of the lane's age group in FP32 (same model as seg_rhs).
+// Rates of the lane's age group at state u: the force-of-infection factors
+// (season and the contact-weighted pressure acc, so lambda = beta * season * acc)
+// and the ICU-adjusted ISev -> ICri and ISev -> D rates.
 template <int G>
-__device__ __forceinline__ void segf_rhs(SegF<G>& X, const float (&u)[kC], float tau_rel, float (&fl)[kF],
-                                         float (&kc)[kC])
+__device__ __forceinline__ void segf_rates(SegF<G>& X, const float (&u)[kC], float tau_rel, float& season,
+                                           float& acc, float& r10, float& r12)
 {
     const float tnt   = segf_sum(X, X.tc(TF_A_TNT) * u[INS_]);
     const float icu   = segf_sum(X, u[ICRI_]);
@@ -674,9 +676,9 @@ __device__ __forceinline__ void segf_rhs(SegF<G>& X, const float (&u)[kC], float
     const float Nj    = u[S_] + u[E_] + u[INS_] + u[ISY_] + u[ISEV_] + u[ICRI_] + u[R_];
     const float divN  = (Nj < (float)kZeroTol) ? 0.0f : __frcp_rn(Nj);
     const float w     = divN * (X.tc(TF_XI) * u[INS_] + risk * u[ISY_]);
-    const float season =
+    season =
         X.tc(TF_SEASON_K) == 0.0f ? 1.0f : 1.0f + X.tc(TF_SEASON_K) * sinpif(X.season_s0 + tau_rel * (float)(1.0 / 182.5));
-    float acc = 0.0f;
+    acc = 0.0f;
     if (X.fast) {
         if (!(tau_rel >= X.t_lo && tau_rel < X.t_hi)) {
             segf_load_contact(X, tau_rel);
@@ -695,12 +697,22 @@ __device__ __forceinline__ void segf_rhs(SegF<G>& X, const float (&u)[kC], float
             acc += (float)C[j] * __shfl_sync(X.mask, w, X.base + j);
         }
     }
-    float r10 = X.tc(TF_R10L), r12 = X.tc(TF_R12L);
+    r10 = X.tc(TF_R10L);
+    r12 = X.tc(TF_R12L);
     if (!(icu <= X.tc(TF_ICU_LO))) {
         const float crit_adj = smoother_cosine(icu, X.tc(TF_ICU_LO), X.tc(TF_ICU_CAP), X.tc(TF_CPS), 0.0f);
         r10                  = crit_adj * X.tc(TF_INV_TISEV);
         r12                  = (X.tc(TF_DPS) + (X.tc(TF_CPS) - crit_adj)) * X.tc(TF_INV_TISEV);
     }
+}
+
+// Flows and derivative of the lane's age group in FP32 (same model as seg_rhs).
+template <int G>
+__device__ __forceinline__ void segf_rhs(SegF<G>& X, const float (&u)[kC], float tau_rel, float (&fl)[kF],
+                                         float (&kc)[kC])
+{
+    float season, acc, r10, r12;
+    segf_rates(X, u, tau_rel, season, acc, r10, r12);
     fl[0]  = u[S_] * X.tc(TF_BETA) * season * acc;
     fl[1]  = X.tc(TF_R1) * u[E_];
     fl[2]  = X.tc(TF_R2) * u[INS_];
@@ -783,6 +795,50 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
         const double t_start = B.node_t[node];
         const double tmax    = rt.t_next;
         segf_load(X, B, g, local, t_start);
+        // Return-side values of the pending departure (the exchange's node pass,
+        // done here): lambda and the transition rates at the state the travelers
+        // left, i.e. at t_dep. That state is this interval's start state unless a
+        // horizon split the interval; then it is read back from v0.
+        if (rt.do_return && g.E > 0) {
+            const bool at_dep = t_start == rt.t_dep;
+            float pop[kC];
+            if (at_dep) {
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    pop[c] = __fadd_rn(hi[c], lo[c]);
+                }
+            }
+            else {
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    pop[c] = __fadd_rn(B.v0_hi[so + c], B.v0_lo[so + c]);
+                }
+            }
+            float season, acc, r10, r12;
+            segf_rates(X, pop, at_dep ? 0.0f : (float)(rt.t_dep - t_start), season, acc, r10, r12);
+            float v[kAux];
+            v[0]  = X.tc(TF_BETA) * season * acc;
+            v[1]  = X.tc(TF_R1);
+            v[2]  = X.tc(TF_R2);
+            v[3]  = X.tc(TF_R3);
+            v[4]  = X.tc(TF_R6);
+            v[5]  = X.tc(TF_R7);
+            v[6]  = r10;
+            v[7]  = X.tc(TF_R11);
+            v[8]  = r12;
+            v[9]  = X.tc(TF_R13);
+            v[10] = X.tc(TF_R14);
+            // can one Euler step of length dt drive a returning compartment negative?
+            // (it cannot when dt times every compartment's total outflow rate is <= 1;
+            // the FP32 test keeps a margin for its own rounding)
+            const float out_rate =
+                fmaxf(fmaxf(v[0], v[1]), fmaxf(fmaxf(v[2] + v[3], v[4] + v[5]), fmaxf(v[6] + v[7] + v[8], v[9] + v[10])));
+            v[11]     = ((float)rt.dt * out_rate > 0.99999f) ? 1.0f : 0.0f;
+            float4* a = reinterpret_cast<float4*>(reinterpret_cast<float*>(B.aux) + (node * MGPU_MAX_GROUPS + X.gi) * kAux);
+            a[0]      = make_float4(v[0], v[1], v[2], v[3]);
+            a[1]      = make_float4(v[4], v[5], v[6], v[7]);
+            a[2]      = make_float4(v[8], v[9], v[10], v[11]);
+        }
 
         // SystemIntegrator::advance on an interval-relative FP32 clock: tr runs
         // from 0 to span (0.5 days is exact in FP32); a step clipped to the
@@ -950,6 +1006,27 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
         if (X.gi == 0) {
             B.node_t[node]  = (tr >= span) ? tmax : t_start + (double)tr;
             B.node_dt[node] = (double)dt;
+        }
+        // Departure at the interval's end (the exchange's node pass, done here):
+        // the snapshot (the FP32 rounding of hi + lo) and the ISy mobility factor
+        // with the commuter nondetection (get_mobility_factors,
+        // models/ode_secir/model.h:687-715) into the free snapshot slot.
+        if (rt.do_depart && g.E > 0) {
+            const int ws = rt.snap_slot ^ 1;
+            float2* yf   = reinterpret_cast<float2*>(B.ysnap_f + (int64_t)ws * B.state_total + so);
+#pragma unroll
+            for (int c = 0; c < kC / 2; ++c) {
+                yf[c] = make_float2(hi[2 * c], hi[2 * c + 1]);
+            }
+            const float tnt = segf_sum(X, X.tc(TF_A_TNT) * hi[INS_]);
+            const double t  = rt.t_next;
+            const float nd  = (t >= X.nm.scalar(MGPU_P_START_COMMUTER_DETECTION) &&
+                              t < X.nm.scalar(MGPU_P_END_COMMUTER_DETECTION))
+                                  ? (float)X.nm.scalar(MGPU_P_COMMUTER_NONDETECTION)
+                                  : 1.0f;
+            float2* fac = reinterpret_cast<float2*>(B.risk) + ((int64_t)ws * B.num_nodes + node) * MGPU_MAX_GROUPS + X.gi;
+            *fac = make_float2(smoother_cosine(tnt, X.tc(TF_TNT_CAP), X.tc(TF_TNT_CAP2), X.tc(TF_RHO), X.tc(TF_RHO_MAX)),
+                               nd);
         }
     }
     if (cap_hit) {
