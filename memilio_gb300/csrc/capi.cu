@@ -696,6 +696,16 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
             h_in_src[k] = h_src[h_in_edges[k]];
         }
         B.in_src = b->pool.upload(h_in_src);
+        // the serial return order splits each node's in-edges at the node itself
+        std::vector<int64_t> h_in_mid(nodes);
+        for (int64_t v = 0; v < nodes; ++v) {
+            int64_t k = h_in_ptr[v];
+            while (k < h_in_ptr[v + 1] && h_in_src[k] < v) {
+                ++k;
+            }
+            h_in_mid[v] = k;
+        }
+        B.in_mid = b->pool.upload(h_in_mid);
     }
     B.scratch_stride = std::max<int64_t>(scratch_slots, 1);
     B.scratch_nmax   = (int32_t)b->n_max;
@@ -1506,7 +1516,7 @@ int64_t mgpu_batch_estimate_bytes(const mgpu_graph* graphs, int32_t num_graphs, 
     b += plain ? 8 * st + 8 * tr + 8 * 8 * nmax * 60 : 8 * st * (mixed ? 0 : 2) + 4 * st * 2 +
                                                             8 * nodes * MGPU_MAX_GROUPS * (4 + 12);
     b += 8 * tr;                                             // fixed travelers
-    b += 16 * nodes + 4 * 2 * 3 * nodes * MGPU_MAX_GROUPS + 4 * nodes + 3 * nodes + 16 * (nodes + 1);
+    b += 24 * nodes + 4 * 2 * 3 * nodes * MGPU_MAX_GROUPS + 4 * nodes + 3 * nodes + 16 * (nodes + 1);
     b += edges * (4 + 4 + 4 + 1 + 1 + 4 + 8 + 8 + MGPU_MAX_GROUPS);
     b += num_graphs * (int64_t)(sizeof(DevGraph) + sizeof(GraphRt) + 8) + 64 * 1024;
     return b + b / 10;

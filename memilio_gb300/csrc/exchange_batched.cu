@@ -885,61 +885,31 @@ __device__ __forceinline__ void flows_f(const float (&a)[kAux], float dt, const 
 }
 
 // The incident edges of `node` in the serial return order of the reference
-// (edges sorted by (src, dst)): in-edges from lower nodes, the out-edges, then
-// in-edges from higher nodes. next() yields each edge once with its kind and
-// reports the switch from the first in-edge run to the out-edges.
-struct ReturnOrder {
-    const BatchDev& B;
-    int64_t node, k, ie, o, oe;
-    int phase; // 0: in-edges with src < node, 1: out-edges, 2: in-edges with src > node
-    __device__ ReturnOrder(const BatchDev& b, int64_t v)
-        : B(b)
-        , node(v)
-        , k(b.in_ptr[v])
-        , ie(b.in_ptr[v + 1])
-        , o(b.out_ptr[v])
-        , oe(b.out_ptr[v + 1])
-        , phase(0)
+// (edges sorted by (src, dst)): in-edges from lower nodes [k0, km), the
+// out-edges [o0, o1), then in-edges from higher nodes [km, k1). Three counted
+// loops (instead of one loop over a merged sequence) let the compiler issue the
+// gathers of the next edges ahead of the arithmetic of the current one.
+struct EdgeRanges {
+    int64_t k0, km, k1, o0, o1;
+    __device__ EdgeRanges(const BatchDev& B, int64_t v)
+        : k0(B.in_ptr[v])
+        , km(B.in_mid[v])
+        , k1(B.in_ptr[v + 1])
+        , o0(B.out_ptr[v])
+        , o1(B.out_ptr[v + 1])
     {
-    }
-    // e: the edge; returns 0 at the end, 1 for an in-edge (u: its source), 2 for
-    // an out-edge; switched is set on the first edge after the lower in-edges
-    __device__ __forceinline__ int next(int64_t& e, int64_t& u, bool& switched)
-    {
-        switched = false;
-        if (phase == 0) {
-            if (k < ie) {
-                const int32_t src = B.in_src[k];
-                if (src < node) {
-                    e = B.in_edges[k++];
-                    u = src;
-                    return 1;
-                }
-            }
-            phase    = 1;
-            switched = true;
-        }
-        if (phase == 1) {
-            if (o < oe) {
-                e = o++;
-                return 2;
-            }
-            phase = 2;
-        }
-        if (k < ie) {
-            u = B.in_src[k];
-            e = B.in_edges[k++];
-            return 1;
-        }
-        return 0;
     }
 };
 
+#ifndef MGPU_XF_UNROLL
+#define MGPU_XF_UNROLL 2 // edges per iteration of the return and departure loops
+#endif
+constexpr int kXfUnroll = MGPU_XF_UNROLL;
 #ifndef MGPU_XF_RETURN_MIN_BLOCKS
-#define MGPU_XF_RETURN_MIN_BLOCKS 6 // resident 128-thread blocks per SM the register budget must allow (measured best)
+#define MGPU_XF_RETURN_MIN_BLOCKS 4 // resident 128-thread blocks per SM the register budget must allow
 #endif
 #ifndef MGPU_XF_DEPART_MIN_BLOCKS
-#define MGPU_XF_DEPART_MIN_BLOCKS 8
+#define MGPU_XF_DEPART_MIN_BLOCKS 6
 #endif
 // Dense (node, group) mapping as k_xf_return.
 template <int MASK>
@@ -972,29 +942,32 @@ __global__ void __launch_bounds__(128, MGPU_XF_DEPART_MIN_BLOCKS)
             acc[c].init_pair(h[c], l[c]);
         }
     }
-    GroupSnap own, src;
+    GroupSnap own;
     load_group_snap_m<MASK>(B, g, node, gr, ws, own);
-    float m[kC];
     const bool detect = own.nd != 1.0f;
     const float q     = 1.0f - own.nd;
-    ReturnOrder order(B, node);
-    int64_t e, u;
-    bool switched;
-    for (int kind = order.next(e, u, switched); kind != 0; kind = order.next(e, u, switched)) {
-        // (an edge without travelers has zero coefficients and adds exact zeros)
-        if (kind == 1) {
-            // travelers arriving from the edge's source
-            load_group_snap_m<MASK>(B, g, u, gr, ws, src);
-            travelers_f<MASK>(B, g, e, gr, src, m);
+    // travelers arriving from the source of in-edge k
+    // (an edge without travelers has zero coefficients and adds exact zeros)
+    auto arrive = [&](int64_t k) {
+        GroupSnap src;
+        float m[kC];
+        load_group_snap_m<MASK>(B, g, B.in_src[k], gr, ws, src);
+        travelers_f<MASK>(B, g, B.in_edges[k], gr, src, m);
 #pragma unroll
-            for (int c = 0; c < kC; ++c) {
-                if (in_mask(MASK, c)) {
-                    acc[c].add(m[c]);
-                }
+        for (int c = 0; c < kC; ++c) {
+            if (in_mask(MASK, c)) {
+                acc[c].add(m[c]);
             }
-            continue;
         }
-        float cf[kC];
+    };
+    const EdgeRanges r(B, node);
+#pragma unroll kXfUnroll
+    for (int64_t k = r.k0; k < r.km; ++k) {
+        arrive(k);
+    }
+#pragma unroll kXfUnroll
+    for (int64_t e = r.o0; e < r.o1; ++e) {
+        float cf[kC], m[kC];
         ld_row_m<MASK>(B.ecoef_f + g.ecoef_f_off + (e - g.edge0) * g.n + gr * kC, cf);
         if (detect) {
             // test_commuters: detected commuters move to the confirmed compartments first
@@ -1016,6 +989,10 @@ __global__ void __launch_bounds__(128, MGPU_XF_DEPART_MIN_BLOCKS)
                 acc[c].add(-m[c]);
             }
         }
+    }
+#pragma unroll kXfUnroll
+    for (int64_t k = r.km; k < r.k1; ++k) {
+        arrive(k);
     }
     float h[kC], l[kC];
 #pragma unroll
@@ -1076,7 +1053,7 @@ __global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
     const float* aux = reinterpret_cast<const float*>(B.aux);
     float a_own[kAux];
     ld_aux_m<MASK>(aux + (node * MGPU_MAX_GROUPS + gr) * kAux, a_own);
-    GroupSnap own, src;
+    GroupSnap own;
     load_group_snap_m<MASK>(B, g, node, gr, slot, own);
     // run[c] is a lower bound of the exact running state of the serial order:
     // in-edges take max(t, 0) away, out-edges add t (negative amounts included),
@@ -1086,37 +1063,14 @@ __global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
     // checked with a margin of 1e-5 of the magnitudes, above the FP32 rounding of
     // the running sums.
     bool flag = false;
-    ReturnOrder order(B, node);
-    int64_t e, u;
-    bool switched;
-    for (int kind = order.next(e, u, switched);; kind = order.next(e, u, switched)) {
-        if (switched) {
-#pragma unroll
-            for (int c = 0; c < kC; ++c) {
-                flag = flag || run[c] < 1e-5f * mag[c];
-            }
-        }
-        if (kind == 0) {
-            break;
-        }
-        // (an edge without travelers has zero coefficients and adds exact zeros)
-        float ax[kAux];
-        const float* a;
-        float m[kC], phi[kF];
-        if (kind == 1) {
-            load_group_snap_m<MASK>(B, g, u, gr, slot, src);
-            travelers_f<MASK>(B, g, e, gr, src, m);
-            a = a_own;
-        }
-        else {
-            ld_aux_m<MASK>(aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux, ax);
-            travelers_f<MASK>(B, g, e, gr, own, m);
-            a = ax;
-        }
-        flows_f<MASK>(*reinterpret_cast<const float(*)[kAux]>(a), dt, m, phi);
+    // one returning edge: travelers m, their Euler flows phi at the destination's
+    // rates a; sgn = -1 for in-edges (travelers leave), +1 for out-edges
+    // (an edge without travelers has zero coefficients and adds exact zeros)
+    auto apply = [&](const float (&a)[kAux], const float (&m)[kC], float sgn) {
+        float phi[kF];
+        flows_f<MASK>(a, dt, m, phi);
         // returning amounts t_c = m_c + inflows - outflows (for the bound only)
         float t[kC];
-        const float sgn = kind == 1 ? -1.0f : 1.0f;
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
             if (in_mask(MASK, c)) {
@@ -1136,10 +1090,37 @@ __global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
         for (int c = 0; c < kC; ++c) {
             // in-edges take max(t, 0) away; out-edges bring t home (a negative t counts against)
             if (in_mask(touched_mask(MASK), c)) {
-                run[c] += kind == 1 ? -fmaxf(t[c], 0.0f) : t[c];
+                run[c] += sgn < 0.0f ? -fmaxf(t[c], 0.0f) : t[c];
                 mag[c] += fabsf(t[c]);
             }
         }
+    };
+    auto leave = [&](int64_t k) {
+        GroupSnap src;
+        float m[kC];
+        load_group_snap_m<MASK>(B, g, B.in_src[k], gr, slot, src);
+        travelers_f<MASK>(B, g, B.in_edges[k], gr, src, m);
+        apply(a_own, m, -1.0f);
+    };
+    const EdgeRanges r(B, node);
+#pragma unroll kXfUnroll
+    for (int64_t k = r.k0; k < r.km; ++k) {
+        leave(k);
+    }
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        flag = flag || run[c] < 1e-5f * mag[c];
+    }
+#pragma unroll kXfUnroll
+    for (int64_t e = r.o0; e < r.o1; ++e) {
+        float ax[kAux], m[kC];
+        ld_aux_m<MASK>(aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux, ax);
+        travelers_f<MASK>(B, g, e, gr, own, m);
+        apply(ax, m, 1.0f);
+    }
+#pragma unroll kXfUnroll
+    for (int64_t k = r.km; k < r.k1; ++k) {
+        leave(k);
     }
     // flow increments: in-edges take travelers away (their increments count with
     // the opposite sign), out-edges bring them home

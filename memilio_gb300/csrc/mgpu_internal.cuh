@@ -113,6 +113,7 @@ struct BatchDev {
     const int64_t* in_ptr;       // [num_nodes+1] CSC
     const int64_t* in_edges;     // [num_edges] edge ids sorted by (dst, src)
     const int32_t* in_src;       // [num_edges] the source node of in_edges[k]
+    const int64_t* in_mid;       // [num_nodes] first k of the node's in-edges with a higher source
     int64_t state_total;         // doubles in a state pool
     double* ysnap;               // [2][state_total] departure snapshots (batched exchange)
     float* ysnap_f;              // [2][state_total] the same in FP32
