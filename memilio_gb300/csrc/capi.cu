@@ -738,7 +738,12 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         auto it     = b->inst_by_G.find(G);
         B.glist[G]  = it != b->inst_by_G.end() ? it->second.first : nullptr;
         B.gcount[G] = it != b->inst_by_G.end() ? it->second.second : 0;
+        B.gorder[G] = (b->opts.precision == MGPU_PRECISION_MIXED && B.gcount[G] > 0)
+                          ? b->pool.alloc<int32_t>(B.gcount[G])
+                          : nullptr;
     }
+    B.order_cnt = b->pool.alloc<int32_t>(2 * (MGPU_MAX_GROUPS + 1));
+    ck(cudaMemsetAsync(B.order_cnt, 0, sizeof(int32_t) * 2 * (MGPU_MAX_GROUPS + 1), ctx->stream), "memset");
     ck(cudaStreamSynchronize(ctx->stream), "upload sync");
     staging.release();
 }
@@ -756,6 +761,12 @@ int check_device_error(mgpu_batch* b)
         fail(MGPU_UNKNOWN_ERROR, "device error word " + std::to_string(err));
     }
     return MGPU_OK;
+}
+
+// node-solve launches per interval: one per age-group count (mixed: with its ordering pass)
+int64_t node_kernel_launches(const mgpu_batch* b)
+{
+    return (int64_t)b->inst_by_G.size() * (b->opts.precision == MGPU_PRECISION_MIXED ? 2 : 1);
 }
 
 // One batched interval: interval bookkeeping, node solves per G, exchange.
@@ -1276,10 +1287,10 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
                 enqueue_batched_phase(b, s, &b->ev_phase[nev]);
                 nev += 6;
                 six_events = true;
-                ode_launches += (int64_t)b->inst_by_G.size();
+                ode_launches += (int64_t)b->inst_by_G.size(); // node-solve kernels (their ordering passes excluded)
             }
             b->launches +=
-                P * (2 + (int64_t)b->inst_by_G.size() + exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size()));
+                P * (2 + node_kernel_launches(b) + exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size()));
             b->phases += P;
         }
         else {
@@ -1299,7 +1310,7 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
                     b->graph_exec   = nullptr;
                 }
             }
-            const int64_t per_phase = 2 + (int64_t)b->inst_by_G.size() +
+            const int64_t per_phase = 2 + node_kernel_launches(b) +
                                       exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size());
             for (int64_t p = 0; p < P; ++p) {
                 if (b->graph_exec) {
@@ -1407,7 +1418,7 @@ int mgpu_batch_launch(mgpu_batch* b, double tmax, const double* tmax_per_graph, 
             }
         }
         ck(cudaGetLastError(), "launch");
-        b->launches += n * (2 + (int64_t)b->inst_by_G.size() +
+        b->launches += n * (2 + node_kernel_launches(b) +
                             exchange_batched_launches(b->opts.precision, b->dev.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size()));
         b->phases += n;
         b->async_left -= n;

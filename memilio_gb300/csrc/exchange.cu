@@ -40,6 +40,11 @@ __global__ void k_phase_begin(BatchDev B, double dt_exchange)
     if (gi >= B.num_graphs) {
         return;
     }
+    if (gi == 0 && B.order_cnt) {
+        for (int k = 0; k < 2 * (MGPU_MAX_GROUPS + 1); ++k) {
+            B.order_cnt[k] = 0;
+        }
+    }
     GraphRt& rt = B.rt[gi];
     rt.fallback = 0;
     if (rt.t < rt.tmax) {

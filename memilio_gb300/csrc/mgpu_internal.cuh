@@ -104,6 +104,11 @@ struct BatchDev {
     int32_t mob_union;           // OR of the graphs' mob_mask
     const int32_t* glist[MGPU_MAX_GROUPS + 1];
     int64_t gcount[MGPU_MAX_GROUPS + 1];
+    // the mixed node kernel's order of the same instances for the current interval
+    // (nodes expected to need one step first, the others last) and its two fill
+    // counters per age-group count, zeroed at each interval start
+    int32_t* gorder[MGPU_MAX_GROUPS + 1];
+    int32_t* order_cnt; // [2 * (MAX_GROUPS + 1)]
     int32_t* scan_mark;          // [3][num_nodes * MAX_GROUPS] (node, group) item is in list k
     int32_t* scan_list;          // [3][num_nodes * MAX_GROUPS] items node * MAX_GROUPS + group
     int32_t* scan_count;         // [3]

@@ -1048,6 +1048,43 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
     }
 }
 
+// Order of the instances with G age groups for the mixed node kernel in this
+// interval: a node whose proposed step size covers the whole interval is likely
+// done in one step and goes to the front, the others to the back. The segments
+// of a warp move in lockstep until the last of them finishes its interval, so
+// warps of nodes with similar step counts idle less. (Only the order changes:
+// every node is solved by the same code wherever it lands.)
+__global__ void k_ode_order(BatchDev B, int G)
+{
+    const int64_t i   = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n   = B.gcount[G];
+    const bool valid  = i < n;
+    int32_t node      = 0;
+    bool front        = false;
+    if (valid) {
+        node             = B.glist[G][i];
+        const GraphRt rt = B.rt[B.node_graph[node]];
+        front            = !rt.active || B.node_dt[node] >= rt.t_next - B.node_t[node];
+    }
+    const unsigned lanes = __ballot_sync(0xffffffffu, valid);
+    const unsigned fm    = __ballot_sync(0xffffffffu, valid && front);
+    const unsigned bm    = lanes & ~fm;
+    const int lane       = threadIdx.x & 31;
+    const int leader     = __ffs(lanes) - 1;
+    int fb = 0, bb = 0;
+    if (lane == leader) {
+        fb = fm ? atomicAdd(B.order_cnt + 2 * G, __popc(fm)) : 0;
+        bb = bm ? atomicAdd(B.order_cnt + 2 * G + 1, __popc(bm)) : 0;
+    }
+    fb                 = __shfl_sync(0xffffffffu, fb, leader < 0 ? 0 : leader);
+    bb                 = __shfl_sync(0xffffffffu, bb, leader < 0 ? 0 : leader);
+    const unsigned below = (1u << lane) - 1u;
+    if (valid) {
+        const int64_t pos = front ? (int64_t)fb + __popc(fm & below) : n - 1 - ((int64_t)bb + __popc(bm & below));
+        B.gorder[G][pos]  = node;
+    }
+}
+
 template <int G>
 int launch_g(const BatchDev& B, int precision, const int32_t* inst, int64_t count, int ipb, int grid, cudaStream_t s)
 {
@@ -1064,6 +1101,10 @@ int launch_g(const BatchDev& B, int precision, const int32_t* inst, int64_t coun
     }
     if (precision == MGPU_PRECISION_MIXED) {
         const size_t smem = (size_t)(threads / 32) * kOdeSmemPerLane * 32 * sizeof(float);
+        if (B.gorder[G] && inst == B.glist[G] && count == B.gcount[G]) {
+            k_ode_order<<<(unsigned)((count + 127) / 128), 128, 0, s>>>(B, G);
+            inst = B.gorder[G];
+        }
         k_ode_mixed<G><<<(unsigned)blocks, threads, smem, s>>>(B, inst, count);
     }
     else {
