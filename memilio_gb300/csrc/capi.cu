@@ -468,7 +468,8 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     // host staging
     std::vector<double> h_par(par), h_con(con), h_dtt(dtt), h_dtv(dtv), h_state(st), h_ec(ec), h_edt(edt),
         h_edv(edv);
-    std::vector<float> h_ecf(ecf);
+    // FP32 coefficient records (rec_vec layout) of the mixed exchange
+    std::vector<float> h_ecr(b->opts.precision == MGPU_PRECISION_MIXED ? ecf / kC * kRec : 0, 0.0f);
     std::vector<int32_t> h_node_graph(nodes), h_edge_graph(edges), h_src(edges), h_dst(edges);
     std::vector<uint8_t> h_any(edges);
     std::vector<int64_t> h_trav_off(edges), h_out_ptr(nodes + 1, 0), h_in_ptr(nodes + 1, 0), h_in_edges(edges);
@@ -528,8 +529,11 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
                 for (int j = 0; j < n; ++j) {
                     pos = pos || cb[j] > 0.0;
                 }
-                for (int j = 0; j < n; ++j) {
-                    h_ecf[d.ecoef_f_off + (int64_t)e * n + j] = pos ? (float)cb[j] : 0.0f;
+                if (!h_ecr.empty()) {
+                    for (int j = 0; j < n; ++j) {
+                        h_ecr[rec_elem(d.ecoef_f_off / kC + (int64_t)e * G, G, j / kC, rec_pos(j % kC))] =
+                            pos ? (float)cb[j] : 0.0f;
+                    }
                 }
             }
             if (own_coeff[i]) {
@@ -644,10 +648,10 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.mfix       = b->pool.alloc<double>(tr);
     B.state_total = st;
     B.ysnap      = (plain || b->pairs) ? nullptr : b->pool.alloc<double>(2 * st);
-    B.ysnap_f    = plain ? nullptr : b->pool.alloc<float>(2 * st);
-    B.risk       = plain ? nullptr : (void*)b->pool.alloc<double>(2 * nodes * MGPU_MAX_GROUPS * 2);
+    B.gsnap      = b->pairs ? b->pool.alloc<float>(2 * (st / kC) * kRec) : nullptr;
+    B.risk       = (plain || b->pairs) ? nullptr : (void*)b->pool.alloc<double>(2 * nodes * MGPU_MAX_GROUPS * 2);
     B.aux        = plain ? nullptr : (void*)b->pool.alloc<double>(nodes * MGPU_MAX_GROUPS * 12);
-    B.ecoef_f    = b->pool.upload(h_ecf);
+    B.ecoef_r    = b->pairs ? b->pool.upload(h_ecr) : nullptr;
     B.tab_f      = nullptr;
     B.contact_f  = nullptr;
     B.dvals_f    = nullptr;
@@ -1522,10 +1526,12 @@ int64_t mgpu_batch_estimate_bytes(const mgpu_graph* graphs, int32_t num_graphs, 
         edv += E * Ke * n;
         nmax = std::max<int64_t>(nmax, N);
     }
-    int64_t b = 8 * (par + con + dtt + dtv + ec + edt + edv) + 4 * tr; // inputs and FP32 coefficients
+    int64_t b = 8 * (par + con + dtt + dtv + ec + edt + edv) + (mixed ? 4 * (tr / kC) * kRec : 0); // inputs, FP32 coefficients
     b += mixed ? 4 * st * 8 + 4 * nodes * MGPU_MAX_GROUPS * kTabF + 4 * (con + dtv) : 8 * st * 4;
-    b += plain ? 8 * st + 8 * tr + 8 * 8 * nmax * 60 : 8 * st * (mixed ? 0 : 2) + 4 * st * 2 +
-                                                            8 * nodes * MGPU_MAX_GROUPS * (4 + 12);
+    // snapshots (mixed: two slots of records), factors, auxiliary values
+    b += plain ? 8 * st + 8 * tr + 8 * 8 * nmax * 60
+               : (mixed ? 4 * 2 * (st / kC) * kRec : 8 * st * 2 + 8 * nodes * MGPU_MAX_GROUPS * 4) +
+                     8 * nodes * MGPU_MAX_GROUPS * 12;
     b += 8 * tr;                                             // fixed travelers
     b += 24 * nodes + 4 * 2 * 3 * nodes * MGPU_MAX_GROUPS + 4 * nodes + 3 * nodes + 16 * (nodes + 1);
     b += edges * (4 + 4 + 4 + 1 + 1 + 4 + 8 + 8 + MGPU_MAX_GROUPS);

@@ -175,7 +175,7 @@ __device__ __forceinline__ R xb_coeff(const BatchDev& B, const DevGraph& g, int6
 {
     if (g.Ke == 0) {
         if constexpr (std::is_same<R, float>::value) {
-            return B.ecoef_f[g.ecoef_f_off + le * g.n + j];
+            return B.ecoef_r[rec_elem(g.ecoef_f_off / kC + le * g.G, g.G, j / kC, rec_pos(j % kC))];
         }
         else {
             return B.ecoef[g.ecoef_off + le * 2 * g.n + j] -
@@ -185,16 +185,6 @@ __device__ __forceinline__ R xb_coeff(const BatchDev& B, const DevGraph& g, int6
     return (R)edge_coeff_at(B, g, le, j, t);
 }
 
-template <class R>
-__device__ __forceinline__ const R* snap_ptr(const BatchDev& B, int slot)
-{
-    if constexpr (std::is_same<R, float>::value) {
-        return B.ysnap_f + (int64_t)slot * B.state_total;
-    }
-    else {
-        return B.ysnap + (int64_t)slot * B.state_total;
-    }
-}
 
 template <class R>
 __device__ __forceinline__ R* aux_ptr(const BatchDev& B)
@@ -212,10 +202,31 @@ __device__ __forceinline__ void depart_travelers(const BatchDev& B, const DevGra
     const int64_t u  = B.edge_src[e];
     const int64_t lu = u - g.node0;
     const int64_t le = e - g.edge0;
-    const R* y       = snap_ptr<R>(B, slot) + g.state_off + lu * g.n + gr * kC;
-    const R* fac     = reinterpret_cast<const R*>(B.risk) + (((int64_t)slot * B.num_nodes + u) * MGPU_MAX_GROUPS + gr) * 2;
-    const R risk     = fac[0];
-    const R nd       = orig ? (R)1 : fac[1];
+    R y[kC], risk, nd;
+    if constexpr (std::is_same<R, float>::value) {
+        // the source's snapshot record (mixed)
+        const float* rec = B.gsnap + (int64_t)slot * (B.state_total / kC) * kRec;
+        const int64_t r0 = (g.state_off + lu * g.n) / kC;
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            y[c] = rec[rec_elem(r0, g.G, gr, rec_pos(c))];
+        }
+        risk = rec[rec_elem(r0, g.G, gr, REC_RISK)];
+        nd   = rec[rec_elem(r0, g.G, gr, REC_ND)];
+    }
+    else {
+        const R* ys  = B.ysnap + (int64_t)slot * B.state_total + g.state_off + lu * g.n + gr * kC;
+        const R* fac = reinterpret_cast<const R*>(B.risk) + (((int64_t)slot * B.num_nodes + u) * MGPU_MAX_GROUPS + gr) * 2;
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            y[c] = ys[c];
+        }
+        risk = fac[0];
+        nd   = fac[1];
+    }
+    if (orig) {
+        nd = (R)1;
+    }
     (void)t;
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
@@ -361,10 +372,12 @@ __device__ __forceinline__ void contact_row(const NodeModel& nm, int i, double t
 // Per node, one 8-lane segment with a lane per age group: the departure snapshot
 // and mobility factors; the force of infection and flow rates at the departure
 // time for the return's Euler step. Sums over age groups run in group order
-// (shuffles from lanes 0..G-1), as in the serial right-hand side.
+// (shuffles from lanes 0..G-1), as in the serial right-hand side. FP64 batches
+// only: the mixed node kernel does this pass itself.
 template <class R>
 __global__ void k_xb_prep(BatchDev B, int64_t n0, int64_t nn)
 {
+    static_assert(std::is_same<R, double>::value, "the FP64 node pass");
     constexpr unsigned kFull = 0xffffffffu;
     const int64_t tid        = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t seg        = tid / MGPU_MAX_GROUPS;
@@ -468,24 +481,11 @@ __global__ void k_xb_prep(BatchDev B, int64_t n0, int64_t nn)
     if (__any_sync(kFull, dep)) {
         const int ws = rt.snap_slot ^ 1;
         double ys[kC];
-        if (B.st_hi) {
 #pragma unroll
-            for (int c = 0; c < kC; ++c) {
-                const float h = B.st_hi[so + c];
-                ys[c]         = (double)h + (double)B.st_lo[so + c];
-                if (dep && mine) {
-                    B.ysnap_f[(int64_t)ws * B.state_total + so + c] = h; // the FP32 rounding of hi + lo
-                }
-            }
-        }
-        else {
-#pragma unroll
-            for (int c = 0; c < kC; ++c) {
-                ys[c] = B.state[so + c];
-                if (dep && mine) {
-                    B.ysnap[(int64_t)ws * B.state_total + so + c]   = ys[c];
-                    B.ysnap_f[(int64_t)ws * B.state_total + so + c] = (float)ys[c];
-                }
+        for (int c = 0; c < kC; ++c) {
+            ys[c] = B.state[so + c];
+            if (dep && mine) {
+                B.ysnap[(int64_t)ws * B.state_total + so + c] = ys[c];
             }
         }
         // ISy mobility factor (get_mobility_factors, models/ode_secir/model.h:687-715)
@@ -726,8 +726,9 @@ __global__ void k_xb_return(BatchDev B, int64_t n0, int64_t nn)
 }
 
 // ---- FP32 node passes of the mixed solver ------------------------------------
-// Per edge: 22 loads (source snapshot, source factors, coefficients), the
-// traveler products, and 10 exact TwoSum updates; everything about the node
+// Per edge: the float4 vectors of the source's snapshot record and of the edge's
+// coefficient record that hold mobile compartments (two each for S, E, INS, ISy,
+// R), the traveler products, and exact TwoSum updates; everything about the node
 // itself (its snapshot and factors for out-edges, its force of infection and
 // rates for in-edges) is loaded once.
 
@@ -736,12 +737,12 @@ struct GroupSnap {
     float risk, nd;
 };
 
-// Vector loads of the FP32 tables. Every age-group row of the 10 compartments
-// starts on an 8-byte boundary (state and coefficient offsets are multiples of
-// 10 floats), the 12 auxiliary values of a (node, group) on a 16-byte boundary
-// and the factor pair on an 8-byte boundary. The snapshot, coefficient, factor
-// and auxiliary tables are read-only in the kernels that use them (read-only
-// data path); the node states use plain loads and stores.
+// Vector loads of the FP32 tables. Every age-group state row of the 10
+// compartments starts on an 8-byte boundary (state offsets are multiples of 10
+// floats); the 12 auxiliary values of a (node, group) and every vector of the
+// snapshot and coefficient records start on a 16-byte boundary. The snapshot,
+// coefficient and auxiliary tables are read-only in the kernels that use them
+// (read-only data path); the node states use plain loads and stores.
 static_assert(kC == 10 && kAux == 12, "vector widths of the FP32 tables");
 __device__ __forceinline__ void ld_state(const float* p, float (&v)[kC])
 {
@@ -787,24 +788,7 @@ __host__ __device__ constexpr int touched_mask(int mask)
     return t;
 }
 
-// Row loads that skip the float pairs holding no compartment of MASK (those
-// values are never used), and the auxiliary values the flows out of MASK need.
-template <int MASK>
-__device__ __forceinline__ void ld_row_m(const float* p, float (&v)[kC])
-{
-    const float2* q = reinterpret_cast<const float2*>(p);
-#pragma unroll
-    for (int i = 0; i < kC / 2; ++i) {
-        if (in_mask(MASK, 2 * i) || in_mask(MASK, 2 * i + 1)) {
-            const float2 a = __ldg(q + i);
-            v[2 * i]       = a.x;
-            v[2 * i + 1]   = a.y;
-        }
-        else {
-            v[2 * i] = v[2 * i + 1] = 0.0f;
-        }
-    }
-}
+// The auxiliary values the flows out of MASK need (the others are never used).
 __host__ __device__ constexpr int aux_of_flow(int k)
 {
     // the rate index of flow k in the auxiliary values (see flows_f)
@@ -854,12 +838,56 @@ __device__ __forceinline__ void travelers_cf(const GroupSnap& s, float nd, const
     }
 }
 
+// does MASK need vector v of a record (with the factor slots when `factors`)?
+__host__ __device__ constexpr bool rec_need(int mask, int v, bool factors)
+{
+    bool need = factors && v == REC_RISK / 4 && (in_mask(mask, MGPU_INS) || in_mask(mask, MGPU_ISY));
+    for (int c = 0; c < kC; ++c) {
+        need = need || (in_mask(mask, c) && rec_pos(c) / 4 == v);
+    }
+    return need;
+}
+// Record loads of the vectors MASK needs (the other compartments read as zero).
+template <int MASK, bool FACTORS>
+__device__ __forceinline__ void ld_rec_m(const float* base, int64_t r0, int G, int gr, float (&y)[kC], float& risk,
+                                         float& nd)
+{
+    float r[kRec];
+#pragma unroll
+    for (int v = 0; v < kRec / 4; ++v) {
+        if (rec_need(MASK, v, FACTORS)) {
+            const float4 x = __ldg(reinterpret_cast<const float4*>(base + rec_vec(r0, G, gr, v)));
+            r[4 * v]       = x.x;
+            r[4 * v + 1]   = x.y;
+            r[4 * v + 2]   = x.z;
+            r[4 * v + 3]   = x.w;
+        }
+        else {
+            r[4 * v] = r[4 * v + 1] = r[4 * v + 2] = r[4 * v + 3] = 0.0f;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        y[c] = in_mask(MASK, c) ? r[rec_pos(c)] : 0.0f;
+    }
+    risk = r[REC_RISK];
+    nd   = r[REC_ND];
+}
+
+// the coefficients of edge e for age group gr (its record)
+template <int MASK>
+__device__ __forceinline__ void ld_coef_m(const BatchDev& B, const DevGraph& g, int64_t e, int gr, float (&cf)[kC])
+{
+    float unused0, unused1;
+    ld_rec_m<MASK, false>(B.ecoef_r, g.ecoef_f_off / kC + (e - g.edge0) * g.G, g.G, gr, cf, unused0, unused1);
+}
+
 template <int MASK = kMaskAll>
 __device__ __forceinline__ void travelers_f(const BatchDev& B, const DevGraph& g, int64_t e, int gr,
                                             const GroupSnap& s, float (&m)[kC])
 {
     float cf[kC];
-    ld_row_m<MASK>(B.ecoef_f + g.ecoef_f_off + (e - g.edge0) * g.n + gr * kC, cf);
+    ld_coef_m<MASK>(B, g, e, gr, cf);
     travelers_cf<MASK>(s, s.nd, cf, m);
 }
 
@@ -867,11 +895,8 @@ template <int MASK>
 __device__ __forceinline__ void load_group_snap_m(const BatchDev& B, const DevGraph& g, int64_t node, int gr,
                                                   int slot, GroupSnap& s)
 {
-    ld_row_m<MASK>(B.ysnap_f + (int64_t)slot * B.state_total + g.state_off + (node - g.node0) * g.n + gr * kC, s.y);
-    const float2 f = __ldg(reinterpret_cast<const float2*>(B.risk) +
-                           ((int64_t)slot * B.num_nodes + node) * MGPU_MAX_GROUPS + gr);
-    s.risk = f.x;
-    s.nd   = f.y;
+    ld_rec_m<MASK, true>(B.gsnap + (int64_t)slot * (B.state_total / kC) * kRec,
+                         (g.state_off + (node - g.node0) * g.n) / kC, g.G, gr, s.y, s.risk, s.nd);
 }
 
 template <int MASK = kMaskAll>
@@ -909,7 +934,7 @@ constexpr int kXfUnroll = MGPU_XF_UNROLL;
 #define MGPU_XF_RETURN_MIN_BLOCKS 4 // resident 128-thread blocks per SM the register budget must allow
 #endif
 #ifndef MGPU_XF_DEPART_MIN_BLOCKS
-#define MGPU_XF_DEPART_MIN_BLOCKS 6
+#define MGPU_XF_DEPART_MIN_BLOCKS 5
 #endif
 // Dense (node, group) mapping as k_xf_return.
 template <int MASK>
@@ -968,7 +993,7 @@ __global__ void __launch_bounds__(128, MGPU_XF_DEPART_MIN_BLOCKS)
 #pragma unroll kXfUnroll
     for (int64_t e = r.o0; e < r.o1; ++e) {
         float cf[kC], m[kC];
-        ld_row_m<MASK>(B.ecoef_f + g.ecoef_f_off + (e - g.edge0) * g.n + gr * kC, cf);
+        ld_coef_m<MASK>(B, g, e, gr, cf);
         if (detect) {
             // test_commuters: detected commuters move to the confirmed compartments first
             float mo[kC];
@@ -1738,7 +1763,7 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
     }
     const int T = 128;
     // (the mixed solver's node kernel does the node pass itself)
-    if (!std::is_same<R, float>::value) {
+    if constexpr (!std::is_same<R, float>::value) {
         k_xb_prep<R><<<blocks_of(nn * MGPU_MAX_GROUPS, T), T, 0, s>>>(B, 0, nn);
         *launches += 1;
     }

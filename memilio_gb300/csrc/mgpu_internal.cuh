@@ -38,7 +38,7 @@ struct DevGraph {
     int64_t ecoef_off;   // doubles, [E][2][n] (baseline, minimum)
     int64_t edt_off;     // doubles, [E][Ke]
     int64_t edv_off;     // doubles, [E][Ke][n]
-    int64_t ecoef_f_off; // floats, [E][n] coefficients (Ke == 0) for the mixed exchange
+    int64_t ecoef_f_off; // [E][n] floats before the records: the edges' first row * 10 (Ke == 0, mixed)
     int32_t mob_mask;    // compartments c with a nonzero coefficient on some edge and age group
 };
 
@@ -121,10 +121,10 @@ struct BatchDev {
     const int64_t* in_mid;       // [num_nodes] first k of the node's in-edges with a higher source
     int64_t state_total;         // doubles in a state pool
     double* ysnap;               // [2][state_total] departure snapshots (batched exchange)
-    float* ysnap_f;              // [2][state_total] the same in FP32
+    float* gsnap;                // [2][state_total / 10][kRec] FP32 snapshot records (mixed), see rec_vec
     void* risk;                  // [2][num_nodes][MAX_GROUPS] ISy mobility factor at departure (R)
     void* aux;                   // [num_nodes][MAX_GROUPS][12] return-time force of infection and rates (R)
-    const float* ecoef_f;        // FP32 coefficients of edges without dampings
+    const float* ecoef_r;        // FP32 coefficient records of edges without dampings (mixed), see rec_vec
     const float* tab_f;          // [num_nodes][MAX_GROUPS][kTabF] FP32 node constants (mixed solver)
     const float* contact_f;      // FP32 copy of the contact pool
     const float* dvals_f;        // FP32 copy of the damping-value pool
@@ -145,6 +145,33 @@ enum {
     TF_R10L, TF_R12L, TF_CPS, TF_DPS, TF_INV_TISEV, TF_TNT_CAP, TF_TNT_CAP2, TF_ICU_LO, TF_ICU_CAP, TF_SEASON_K,
     kTabF = 24
 };
+
+// FP32 group records of the mixed exchange: the departure snapshot of a
+// (node, age group) with its two mobility factors, and the coefficients of an
+// (edge, age group), 12 floats each in three float4 vectors. Within a node (an
+// edge) the records are vector-major, [vector][group][4], so that the age
+// groups of one node read one contiguous block per vector. Vector 0 holds S, E,
+// INS, ISy (the usual commuter compartments), vector 1 R, the ISy mobility
+// factor, the commuter nondetection factor and INSC, vector 2 ISyC, ISev, ICri,
+// D. Coefficient records keep the two factor slots zero. Rows are dense
+// (node, group) or (edge, group) ordinals: a node's first row is its state
+// offset / 10, an edge's is ecoef_f_off / 10 + (local edge) * G.
+constexpr int kRec = 12;
+enum { REC_RISK = 5, REC_ND = 6 };
+__host__ __device__ constexpr int rec_pos(int c)
+{
+    return c == MGPU_S ? 0 : c == MGPU_E ? 1 : c == MGPU_INS ? 2 : c == MGPU_ISY ? 3 : c == MGPU_R ? 4
+         : c == MGPU_INSC ? 7 : c == MGPU_ISYC ? 8 : c == MGPU_ISEV ? 9 : c == MGPU_ICRI ? 10 : 11;
+}
+// float offset of vector v of group gr's record, the node's (edge's) rows starting at row r0
+__host__ __device__ inline int64_t rec_vec(int64_t r0, int G, int gr, int v)
+{
+    return r0 * kRec + (int64_t)v * G * 4 + (int64_t)gr * 4;
+}
+__host__ __device__ inline int64_t rec_elem(int64_t r0, int G, int gr, int p)
+{
+    return rec_vec(r0, G, gr, p / 4) + p % 4;
+}
 
 // Return-side values per (node, age group) at the pending departure, written
 // before each return: lambda, r1, r2, r3, r6, r7, r10, r11, r12, r13, r14 and a

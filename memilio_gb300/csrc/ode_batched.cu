@@ -1008,25 +1008,30 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
             B.node_dt[node] = (double)dt;
         }
         // Departure at the interval's end (the exchange's node pass, done here):
-        // the snapshot (the FP32 rounding of hi + lo) and the ISy mobility factor
-        // with the commuter nondetection (get_mobility_factors,
-        // models/ode_secir/model.h:687-715) into the free snapshot slot.
+        // the snapshot record, i.e. the FP32 rounding of hi + lo, the ISy mobility
+        // factor and the commuter nondetection (get_mobility_factors,
+        // models/ode_secir/model.h:687-715), into the free snapshot slot.
         if (rt.do_depart && g.E > 0) {
-            const int ws = rt.snap_slot ^ 1;
-            float2* yf   = reinterpret_cast<float2*>(B.ysnap_f + (int64_t)ws * B.state_total + so);
-#pragma unroll
-            for (int c = 0; c < kC / 2; ++c) {
-                yf[c] = make_float2(hi[2 * c], hi[2 * c + 1]);
-            }
+            const int ws    = rt.snap_slot ^ 1;
             const float tnt = segf_sum(X, X.tc(TF_A_TNT) * hi[INS_]);
             const double t  = rt.t_next;
-            const float nd  = (t >= X.nm.scalar(MGPU_P_START_COMMUTER_DETECTION) &&
-                              t < X.nm.scalar(MGPU_P_END_COMMUTER_DETECTION))
-                                  ? (float)X.nm.scalar(MGPU_P_COMMUTER_NONDETECTION)
-                                  : 1.0f;
-            float2* fac = reinterpret_cast<float2*>(B.risk) + ((int64_t)ws * B.num_nodes + node) * MGPU_MAX_GROUPS + X.gi;
-            *fac = make_float2(smoother_cosine(tnt, X.tc(TF_TNT_CAP), X.tc(TF_TNT_CAP2), X.tc(TF_RHO), X.tc(TF_RHO_MAX)),
-                               nd);
+            float r[kRec];
+#pragma unroll
+            for (int c = 0; c < kC; ++c) {
+                r[rec_pos(c)] = hi[c];
+            }
+            r[REC_RISK] = smoother_cosine(tnt, X.tc(TF_TNT_CAP), X.tc(TF_TNT_CAP2), X.tc(TF_RHO), X.tc(TF_RHO_MAX));
+            r[REC_ND]   = (t >= X.nm.scalar(MGPU_P_START_COMMUTER_DETECTION) &&
+                         t < X.nm.scalar(MGPU_P_END_COMMUTER_DETECTION))
+                              ? (float)X.nm.scalar(MGPU_P_COMMUTER_NONDETECTION)
+                              : 1.0f;
+            float* base      = B.gsnap + (int64_t)ws * (B.state_total / kC) * kRec;
+            const int64_t r0 = (g.state_off + local * g.n) / kC;
+#pragma unroll
+            for (int v = 0; v < kRec / 4; ++v) {
+                *reinterpret_cast<float4*>(base + rec_vec(r0, G, X.gi, v)) =
+                    make_float4(r[4 * v], r[4 * v + 1], r[4 * v + 2], r[4 * v + 3]);
+            }
         }
     }
     if (cap_hit) {
