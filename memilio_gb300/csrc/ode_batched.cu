@@ -550,6 +550,7 @@ __device__ __forceinline__ void df_renorm(float& hi, float& lo)
 #ifndef MGPU_ODE_TAB_LOADS
 #define MGPU_ODE_TAB_LOADS 0
 #endif
+
 template <int G>
 struct SegF {
     int base;
@@ -674,8 +675,10 @@ __device__ __forceinline__ void segf_rates(SegF<G>& X, const float (&u)[kC], flo
     const float icu   = segf_sum(X, u[ICRI_]);
     const float risk  = smoother_cosine(tnt, X.tc(TF_TNT_CAP), X.tc(TF_TNT_CAP2), X.tc(TF_RHO), X.tc(TF_RHO_MAX));
     const float Nj    = u[S_] + u[E_] + u[INS_] + u[ISY_] + u[ISEV_] + u[ICRI_] + u[R_];
-    const float divN  = (Nj < (float)kZeroTol) ? 0.0f : __frcp_rn(Nj);
-    const float w     = divN * (X.tc(TF_XI) * u[INS_] + risk * u[ISY_]);
+    // the weighted infectious share of the group: an approximate quotient (a
+    // correctly rounded reciprocal costs several times more, for no accuracy
+    // the FP32 right-hand side keeps)
+    const float w = (Nj < (float)kZeroTol) ? 0.0f : __fdividef(X.tc(TF_XI) * u[INS_] + risk * u[ISY_], Nj);
     season =
         X.tc(TF_SEASON_K) == 0.0f ? 1.0f : 1.0f + X.tc(TF_SEASON_K) * sinpif(X.season_s0 + tau_rel * (float)(1.0 / 182.5));
     acc = 0.0f;
@@ -743,10 +746,13 @@ __device__ __forceinline__ void segf_rhs(SegF<G>& X, const float (&u)[kC], float
 // shared memory per lane of the mixed solver: 5 stage derivative vectors and the flow increments
 constexpr int kOdeSmemPerLane = 5 * kC + kF;
 template <int G>
-#ifndef MGPU_MIXED_MIN_BLOCKS
-#define MGPU_MIXED_MIN_BLOCKS 3 // resident 128-thread blocks per SM the register budget must allow
+#ifndef MGPU_MIXED_THREADS
+#define MGPU_MIXED_THREADS 128 // largest block of the mixed node kernel
 #endif
-__global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchDev B, const int32_t* inst,
+#ifndef MGPU_MIXED_MIN_BLOCKS
+#define MGPU_MIXED_MIN_BLOCKS 3 // resident blocks per SM the register budget must allow
+#endif
+__global__ void __launch_bounds__(MGPU_MIXED_THREADS, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchDev B, const int32_t* inst,
                                                                          int64_t count)
 {
     constexpr int IPW = 32 / G;
@@ -949,7 +955,8 @@ __global__ void __launch_bounds__(128, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchD
 #pragma unroll
                 for (int c = 0; c < kC; ++c) {
                     const float den = abs_f + rel_f * (fabsf(hi[c]) + dtf * fabsf(SK(0, c)));
-                    el              = fmaxf(el, fabsf(xe[c]) * __frcp_rn(den));
+                    // (an approximate quotient: the controller needs no correctly rounded ratios)
+                    el = fmaxf(el, __fdividef(fabsf(xe[c]), den));
                 }
 #pragma unroll
                 for (int q = 0; q < G; ++q) {
