@@ -4,6 +4,7 @@
 #include "mgpu_internal.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -14,6 +15,7 @@
 #include <tuple>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 using namespace mgpu;
@@ -78,10 +80,11 @@ struct DevPool {
         ctx->allocated += nb;
         return static_cast<T*>(p);
     }
-    template <class T>
-    T* upload(const std::vector<T>& v)
+    template <class V>
+    typename V::value_type* upload(const V& v)
     {
-        T* d = alloc<T>((int64_t)v.size());
+        using T = typename V::value_type;
+        T* d    = alloc<T>((int64_t)v.size());
         if (!v.empty()) {
             ck(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream), "upload");
         }
@@ -98,7 +101,83 @@ struct DevPool {
     }
 };
 
-void validate_graph(const mgpu_graph& g, bool need_edges_sorted = true)
+// Host staging buffers whose elements are all written before use: no zero fill.
+template <class T>
+struct NoInit : std::allocator<T> {
+    using value_type = T;
+    template <class U>
+    struct rebind {
+        using other = NoInit<U>;
+    };
+    NoInit() = default;
+    template <class U>
+    NoInit(const NoInit<U>&)
+    {
+    }
+    template <class U>
+    void construct(U* p) noexcept
+    {
+        ::new ((void*)p) U;
+    }
+    template <class U, class... A>
+    void construct(U* p, A&&... a)
+    {
+        ::new ((void*)p) U(std::forward<A>(a)...);
+    }
+};
+template <class T>
+using HostBuf = std::vector<T, NoInit<T>>;
+
+// f(i) for i in [0, n) on the host's cores (chunks handed out in order); the
+// first exception of any worker is rethrown here.
+template <class F>
+void parallel_for(int64_t n, F&& f)
+{
+    const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
+    const int64_t T  = std::min<int64_t>(hw, n);
+    if (T <= 1) {
+        for (int64_t i = 0; i < n; ++i) {
+            f(i);
+        }
+        return;
+    }
+    const int64_t chunk = std::max<int64_t>(1, n / (T * 8));
+    std::atomic<int64_t> next{0};
+    std::vector<std::exception_ptr> err(T);
+    std::vector<std::thread> th;
+    th.reserve(T);
+    for (int64_t t = 0; t < T; ++t) {
+        th.emplace_back([&, t]() {
+            try {
+                for (;;) {
+                    const int64_t a = next.fetch_add(chunk);
+                    if (a >= n) {
+                        break;
+                    }
+                    const int64_t b = std::min(n, a + chunk);
+                    for (int64_t i = a; i < b; ++i) {
+                        f(i);
+                    }
+                }
+            }
+            catch (...) {
+                err[t] = std::current_exception();
+                next.store(n);
+            }
+        });
+    }
+    for (auto& x : th) {
+        x.join();
+    }
+    for (auto& e : err) {
+        if (e) {
+            std::rethrow_exception(e);
+        }
+    }
+}
+
+// Counts and pointers of a graph (O(1)); the arrays are checked by validate_graph_arrays.
+void validate_graph_header(const mgpu_graph& g)
 {
     if (g.num_nodes < 0 || g.num_edges < 0) {
         fail(MGPU_INVALID_VALUE, "negative node or edge count");
@@ -128,7 +207,12 @@ void validate_graph(const mgpu_graph& g, bool need_edges_sorted = true)
     if (g.num_edge_damping_points > 0 && (!g.edge_damping_times || !g.edge_damping_values)) {
         fail(MGPU_INVALID_VALUE, "edge damping times/values required when num_edge_damping_points > 0");
     }
-    for (int e = 0; e < g.num_edges; ++e) {
+}
+
+// Edge indices (range, no self-loops, sorted by (src, dst)) and damping cache times.
+void validate_graph_arrays(const mgpu_graph& g, bool edges, bool dampings, bool need_edges_sorted)
+{
+    for (int e = 0; edges && e < g.num_edges; ++e) {
         const int s = g.edge_src[e], d = g.edge_dst[e];
         if (s < 0 || s >= g.num_nodes || d < 0 || d >= g.num_nodes) {
             fail(MGPU_OUT_OF_RANGE, "edge node index out of range");
@@ -144,7 +228,7 @@ void validate_graph(const mgpu_graph& g, bool need_edges_sorted = true)
         }
     }
     const int K = g.num_damping_points;
-    if (K > 0) {
+    if (dampings && K > 0) {
         const long GG = (long)g.num_groups * g.num_groups;
         for (long v = 0; v < (long)g.num_nodes * g.num_contact_matrices; ++v) {
             const double* T = g.damping_times + v * K;
@@ -381,9 +465,21 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     b->edge0.resize(num_graphs);
     b->state_off.resize(num_graphs);
     b->n_max = 0;
+    std::vector<int64_t> trav0(num_graphs);
+    // arrays to check: each (edge index arrays, damping times) once, however many graphs share it
+    using AKey = std::tuple<const void*, const void*, int64_t, int64_t>;
+    std::map<AKey, int> edges_seen, times_seen;
+    std::vector<char> check_edges(num_graphs, 0), check_times(num_graphs, 0);
     for (int i = 0; i < num_graphs; ++i) {
         const mgpu_graph& g = graphs[i];
-        validate_graph(g);
+        validate_graph_header(g);
+        check_edges[i] = edges_seen.emplace(AKey{g.edge_src, g.edge_dst, g.num_edges, g.num_nodes}, i).second;
+        check_times[i] = times_seen
+                             .emplace(AKey{g.damping_times, nullptr, (int64_t)g.num_nodes * g.num_contact_matrices,
+                                           g.num_damping_points},
+                                      i)
+                             .second;
+
         DevGraph& d   = dg[i];
         const int G   = g.num_groups;
         const int n   = G * kC;
@@ -405,6 +501,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         edges += E;
         par += (int64_t)g.num_nodes * param_stride(G);
         st += (int64_t)g.num_nodes * n;
+        trav0[i] = tr;
         tr += (int64_t)E * n;
         const Key kc{g.contact_baseline, g.contact_minimum, nullptr, nullptr, g.num_nodes, d.M, G};
         auto itc = contact_first.find(kc);
@@ -465,17 +562,27 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     if (nodes * MGPU_MAX_GROUPS > INT32_MAX) {
         fail(MGPU_INVALID_VALUE, "batch too large: more than 2^28 nodes in one batch");
     }
-    // host staging
-    std::vector<double> h_par(par), h_con(con), h_dtt(dtt), h_dtv(dtv), h_state(st), h_ec(ec), h_edt(edt),
-        h_edv(edv);
-    // FP32 coefficient records (rec_vec layout) of the mixed exchange
+    if (edges > INT32_MAX) {
+        fail(MGPU_INVALID_VALUE, "batch too large: more than 2^31 - 1 edges in one batch");
+    }
+    // edge index arrays and damping times, each distinct array once, on the host's cores
+    parallel_for(num_graphs, [&](int64_t i) {
+        validate_graph_arrays(graphs[i], with_edges && check_edges[i], check_times[i], true);
+    });
+    // host staging (every element is written below, so no zero fill)
+    HostBuf<double> h_par(par), h_con(con), h_dtt(dtt), h_dtv(dtv), h_state(st), h_ec(ec), h_edt(edt), h_edv(edv);
+    // FP32 coefficient records (rec_vec layout) of the mixed exchange; the factor slots stay zero
     std::vector<float> h_ecr(b->opts.precision == MGPU_PRECISION_MIXED ? ecf / kC * kRec : 0, 0.0f);
-    std::vector<int32_t> h_node_graph(nodes), h_edge_graph(edges), h_src(edges), h_dst(edges);
-    std::vector<uint8_t> h_any(edges);
-    std::vector<int64_t> h_trav_off(edges), h_out_ptr(nodes + 1, 0), h_in_ptr(nodes + 1, 0), h_in_edges(edges);
-    int64_t trav_pos = 0;
+    HostBuf<int32_t> h_node_graph(nodes), h_edge_graph(edges), h_src(edges), h_dst(edges);
+    HostBuf<uint8_t> h_any(edges);
+    HostBuf<int64_t> h_trav_off(edges), h_in_ptr(nodes + 1), h_in_edges(edges);
+    std::vector<int64_t> h_out_ptr(nodes + 1, 0);
     std::vector<int32_t> mob_mask(num_graphs, 0);
-    for (int i = 0; i < num_graphs; ++i) {
+    // Graphs pack into disjoint ranges of the staging buffers, on the host's
+    // cores; a graph that shares the coefficient arrays of an earlier one copies
+    // that graph's flags afterwards.
+    parallel_for(num_graphs, [&](int64_t gi) {
+        const int i         = (int)gi;
         const mgpu_graph& g = graphs[i];
         const DevGraph& d   = dg[i];
         const int G = d.G, n = d.n;
@@ -505,6 +612,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         }
         // edges: CSR by source (already sorted), CSC by destination (sorted by source within)
         std::vector<int64_t> indeg(g.num_nodes + 1, 0);
+        int64_t trav_pos = trav0[i];
         for (int e = 0; e < d.E; ++e) {
             const int64_t ge = d.edge0 + e;
             h_edge_graph[ge] = i;
@@ -525,18 +633,6 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
                 // an edge with no positive coefficient carries nobody (apply_mobility,
                 // metapopulation_mobility_instant.h:606): its FP32 row is zero, so the
                 // FP32 passes, which do not test the edge, add exact zeros for it
-                bool pos = false;
-                for (int j = 0; j < n; ++j) {
-                    pos = pos || cb[j] > 0.0;
-                }
-                if (!h_ecr.empty()) {
-                    for (int j = 0; j < n; ++j) {
-                        h_ecr[rec_elem(d.ecoef_f_off / kC + (int64_t)e * G, G, j / kC, rec_pos(j % kC))] =
-                            pos ? (float)cb[j] : 0.0f;
-                    }
-                }
-            }
-            if (own_coeff[i]) {
                 bool any = false;
                 for (int j = 0; j < n; ++j) {
                     any = any || (cb[j] > 0.0);
@@ -544,34 +640,44 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
                         mob_mask[i] |= 1 << (j % kC);
                     }
                 }
+                if (!h_ecr.empty()) {
+                    for (int j = 0; j < n; ++j) {
+                        h_ecr[rec_elem(d.ecoef_f_off / kC + (int64_t)e * G, G, j / kC, rec_pos(j % kC))] =
+                            any ? (float)cb[j] : 0.0f;
+                    }
+                }
                 h_any[ge] = any ? 1 : 0;
-            }
-            else {
-                // the same coefficient arrays as an earlier graph: its flags
-                h_any[ge] = h_any[dg[coeff_src[i]].edge0 + e];
-            }
-            if (d.Ke && own_coeff[i]) {
-                std::memcpy(h_edt.data() + d.edt_off + (int64_t)e * d.Ke, g.edge_damping_times + (int64_t)e * d.Ke,
-                            sizeof(double) * d.Ke);
-                std::memcpy(h_edv.data() + d.edv_off + (int64_t)e * d.Ke * n,
-                            g.edge_damping_values + (int64_t)e * d.Ke * n, sizeof(double) * d.Ke * n);
+                if (d.Ke) {
+                    std::memcpy(h_edt.data() + d.edt_off + (int64_t)e * d.Ke,
+                                g.edge_damping_times + (int64_t)e * d.Ke, sizeof(double) * d.Ke);
+                    std::memcpy(h_edv.data() + d.edv_off + (int64_t)e * d.Ke * n,
+                                g.edge_damping_values + (int64_t)e * d.Ke * n, sizeof(double) * d.Ke * n);
+                }
             }
             h_trav_off[ge] = trav_pos;
             trav_pos += n;
-        }
-        if (!own_coeff[i]) {
-            mob_mask[i] = mob_mask[coeff_src[i]];
         }
         for (int v = 0; v < g.num_nodes; ++v) {
             indeg[v + 1] += indeg[v];
         }
         std::vector<int64_t> fillp(indeg.begin(), indeg.end() - 1);
         for (int e = 0; e < d.E; ++e) { // edges visited in (src, dst) order -> CSC sorted by src
-            const int v                                       = g.edge_dst[e];
-            h_in_edges[d.edge0 + indeg[0] + fillp[v]++ - 0]   = d.edge0 + e;
+            const int v                          = g.edge_dst[e];
+            h_in_edges[d.edge0 + fillp[v]++]     = d.edge0 + e;
         }
-        for (int v = 0; v <= g.num_nodes; ++v) {
+        for (int v = 0; v < g.num_nodes; ++v) {
             h_in_ptr[d.node0 + v] = d.edge0 + indeg[v];
+        }
+    });
+    h_in_ptr[nodes] = edges;
+    for (int i = 0; i < num_graphs; ++i) {
+        if (!own_coeff[i]) {
+            // the same coefficient arrays as an earlier graph: its flags
+            const DevGraph& d = dg[i];
+            if (d.E) {
+                std::memcpy(h_any.data() + d.edge0, h_any.data() + dg[coeff_src[i]].edge0, (size_t)d.E);
+            }
+            mob_mask[i] = mob_mask[coeff_src[i]];
         }
     }
     for (int64_t v = 0; v < nodes; ++v) {
@@ -695,20 +801,23 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.in_ptr   = b->pool.upload(h_in_ptr);
     B.in_edges = b->pool.upload(h_in_edges);
     {
-        std::vector<int32_t> h_in_src(edges);
-        for (int64_t k = 0; k < edges; ++k) {
-            h_in_src[k] = h_src[h_in_edges[k]];
-        }
-        B.in_src = b->pool.upload(h_in_src);
-        // the serial return order splits each node's in-edges at the node itself
-        std::vector<int64_t> h_in_mid(nodes);
-        for (int64_t v = 0; v < nodes; ++v) {
-            int64_t k = h_in_ptr[v];
-            while (k < h_in_ptr[v + 1] && h_in_src[k] < v) {
-                ++k;
+        HostBuf<int2> h_in_se(edges);
+        HostBuf<int64_t> h_in_mid(nodes);
+        parallel_for(num_graphs, [&](int64_t i) {
+            const DevGraph& d = dg[i];
+            for (int64_t k = d.edge0; k < d.edge0 + d.E; ++k) {
+                h_in_se[k] = make_int2(h_src[h_in_edges[k]], (int32_t)h_in_edges[k]);
             }
-            h_in_mid[v] = k;
-        }
+            // the serial return order splits each node's in-edges at the node itself
+            for (int64_t v = d.node0; v < d.node0 + d.N; ++v) {
+                int64_t k = h_in_ptr[v];
+                while (k < h_in_ptr[v + 1] && h_in_se[k].x < v) {
+                    ++k;
+                }
+                h_in_mid[v] = k;
+            }
+        });
+        B.in_se  = b->pool.upload(h_in_se);
         B.in_mid = b->pool.upload(h_in_mid);
     }
     B.scratch_stride = std::max<int64_t>(scratch_slots, 1);
@@ -1534,7 +1643,7 @@ int64_t mgpu_batch_estimate_bytes(const mgpu_graph* graphs, int32_t num_graphs, 
                      8 * nodes * MGPU_MAX_GROUPS * 12;
     b += 8 * tr;                                             // fixed travelers
     b += 24 * nodes + 4 * 2 * 3 * nodes * MGPU_MAX_GROUPS + 4 * nodes + 3 * nodes + 16 * (nodes + 1);
-    b += edges * (4 + 4 + 4 + 1 + 1 + 4 + 8 + 8 + MGPU_MAX_GROUPS);
+    b += edges * (4 + 4 + 8 + 1 + 1 + 4 + 8 + 8 + MGPU_MAX_GROUPS);
     b += num_graphs * (int64_t)(sizeof(DevGraph) + sizeof(GraphRt) + 8) + 64 * 1024;
     return b + b / 10;
 }

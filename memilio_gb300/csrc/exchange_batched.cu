@@ -874,29 +874,43 @@ __device__ __forceinline__ void ld_rec_m(const float* base, int64_t r0, int G, i
     nd   = r[REC_ND];
 }
 
+// Record addressing of one graph for the FP32 passes, computed once per thread:
+// the snapshot slot, and the record rows of node 0 and edge 0 (a node's first row
+// is srow0 + node * G, an edge's crow0 + edge * G, with global node and edge ids).
+struct RecCtx {
+    const float* snap;
+    int64_t srow0, crow0;
+    int G;
+    __device__ RecCtx(const BatchDev& B, const DevGraph& g, int slot)
+        : snap(B.gsnap + (int64_t)slot * (B.state_total / kC) * kRec)
+        , srow0(g.state_off / kC - g.node0 * g.G)
+        , crow0(g.ecoef_f_off / kC - g.edge0 * g.G)
+        , G(g.G)
+    {
+    }
+};
+
 // the coefficients of edge e for age group gr (its record)
 template <int MASK>
-__device__ __forceinline__ void ld_coef_m(const BatchDev& B, const DevGraph& g, int64_t e, int gr, float (&cf)[kC])
+__device__ __forceinline__ void ld_coef_m(const BatchDev& B, const RecCtx& x, int64_t e, int gr, float (&cf)[kC])
 {
     float unused0, unused1;
-    ld_rec_m<MASK, false>(B.ecoef_r, g.ecoef_f_off / kC + (e - g.edge0) * g.G, g.G, gr, cf, unused0, unused1);
+    ld_rec_m<MASK, false>(B.ecoef_r, x.crow0 + e * x.G, x.G, gr, cf, unused0, unused1);
 }
 
 template <int MASK = kMaskAll>
-__device__ __forceinline__ void travelers_f(const BatchDev& B, const DevGraph& g, int64_t e, int gr,
+__device__ __forceinline__ void travelers_f(const BatchDev& B, const RecCtx& x, int64_t e, int gr,
                                             const GroupSnap& s, float (&m)[kC])
 {
     float cf[kC];
-    ld_coef_m<MASK>(B, g, e, gr, cf);
+    ld_coef_m<MASK>(B, x, e, gr, cf);
     travelers_cf<MASK>(s, s.nd, cf, m);
 }
 
 template <int MASK>
-__device__ __forceinline__ void load_group_snap_m(const BatchDev& B, const DevGraph& g, int64_t node, int gr,
-                                                  int slot, GroupSnap& s)
+__device__ __forceinline__ void load_group_snap_m(const RecCtx& x, int64_t node, int gr, GroupSnap& s)
 {
-    ld_rec_m<MASK, true>(B.gsnap + (int64_t)slot * (B.state_total / kC) * kRec,
-                         (g.state_off + (node - g.node0) * g.n) / kC, g.G, gr, s.y, s.risk, s.nd);
+    ld_rec_m<MASK, true>(x.snap, x.srow0 + node * x.G, x.G, gr, s.y, s.risk, s.nd);
 }
 
 template <int MASK = kMaskAll>
@@ -930,15 +944,23 @@ struct EdgeRanges {
 #define MGPU_XF_UNROLL 2 // edges per iteration of the return and departure loops
 #endif
 constexpr int kXfUnroll = MGPU_XF_UNROLL;
+// resident 128-thread blocks per SM the register budget must allow, for the
+// usual commuter mask and for all compartments mobile (measured)
 #ifndef MGPU_XF_RETURN_MIN_BLOCKS
-#define MGPU_XF_RETURN_MIN_BLOCKS 4 // resident 128-thread blocks per SM the register budget must allow
+#define MGPU_XF_RETURN_MIN_BLOCKS 5
+#endif
+#ifndef MGPU_XF_RETURN_MIN_BLOCKS_ALL
+#define MGPU_XF_RETURN_MIN_BLOCKS_ALL 3
 #endif
 #ifndef MGPU_XF_DEPART_MIN_BLOCKS
 #define MGPU_XF_DEPART_MIN_BLOCKS 5
 #endif
+#ifndef MGPU_XF_DEPART_MIN_BLOCKS_ALL
+#define MGPU_XF_DEPART_MIN_BLOCKS_ALL 4
+#endif
 // Dense (node, group) mapping as k_xf_return.
 template <int MASK>
-__global__ void __launch_bounds__(128, MGPU_XF_DEPART_MIN_BLOCKS)
+__global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_DEPART_MIN_BLOCKS_ALL : MGPU_XF_DEPART_MIN_BLOCKS)
     k_xf_depart(BatchDev B, const int32_t* inst, int64_t count, int G)
 {
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -967,8 +989,9 @@ __global__ void __launch_bounds__(128, MGPU_XF_DEPART_MIN_BLOCKS)
             acc[c].init_pair(h[c], l[c]);
         }
     }
+    const RecCtx x(B, g, ws);
     GroupSnap own;
-    load_group_snap_m<MASK>(B, g, node, gr, ws, own);
+    load_group_snap_m<MASK>(x, node, gr, own);
     const bool detect = own.nd != 1.0f;
     const float q     = 1.0f - own.nd;
     // travelers arriving from the source of in-edge k
@@ -976,8 +999,9 @@ __global__ void __launch_bounds__(128, MGPU_XF_DEPART_MIN_BLOCKS)
     auto arrive = [&](int64_t k) {
         GroupSnap src;
         float m[kC];
-        load_group_snap_m<MASK>(B, g, B.in_src[k], gr, ws, src);
-        travelers_f<MASK>(B, g, B.in_edges[k], gr, src, m);
+        const int2 se = B.in_se[k];
+        load_group_snap_m<MASK>(x, se.x, gr, src);
+        travelers_f<MASK>(B, x, se.y, gr, src, m);
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
             if (in_mask(MASK, c)) {
@@ -993,7 +1017,7 @@ __global__ void __launch_bounds__(128, MGPU_XF_DEPART_MIN_BLOCKS)
 #pragma unroll kXfUnroll
     for (int64_t e = r.o0; e < r.o1; ++e) {
         float cf[kC], m[kC];
-        ld_coef_m<MASK>(B, g, e, gr, cf);
+        ld_coef_m<MASK>(B, x, e, gr, cf);
         if (detect) {
             // test_commuters: detected commuters move to the confirmed compartments first
             float mo[kC];
@@ -1033,7 +1057,7 @@ __global__ void __launch_bounds__(128, MGPU_XF_DEPART_MIN_BLOCKS)
 // One thread per (node, group) of the nodes with G age groups (dense: node
 // = inst[tid / G], group = tid % G, so no lane idles on unused groups).
 template <int MASK>
-__global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
+__global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_RETURN_MIN_BLOCKS_ALL : MGPU_XF_RETURN_MIN_BLOCKS)
     k_xf_return(BatchDev B, const int32_t* inst, int64_t count, int G)
 {
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1078,8 +1102,9 @@ __global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
     const float* aux = reinterpret_cast<const float*>(B.aux);
     float a_own[kAux];
     ld_aux_m<MASK>(aux + (node * MGPU_MAX_GROUPS + gr) * kAux, a_own);
+    const RecCtx x(B, g, slot);
     GroupSnap own;
-    load_group_snap_m<MASK>(B, g, node, gr, slot, own);
+    load_group_snap_m<MASK>(x, node, gr, own);
     // run[c] is a lower bound of the exact running state of the serial order:
     // in-edges take max(t, 0) away, out-edges add t (negative amounts included),
     // so within each run of in-edges it only decreases, and the underflow test of
@@ -1123,8 +1148,9 @@ __global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
     auto leave = [&](int64_t k) {
         GroupSnap src;
         float m[kC];
-        load_group_snap_m<MASK>(B, g, B.in_src[k], gr, slot, src);
-        travelers_f<MASK>(B, g, B.in_edges[k], gr, src, m);
+        const int2 se = B.in_se[k];
+        load_group_snap_m<MASK>(x, se.x, gr, src);
+        travelers_f<MASK>(B, x, se.y, gr, src, m);
         apply(a_own, m, -1.0f);
     };
     const EdgeRanges r(B, node);
@@ -1140,7 +1166,7 @@ __global__ void __launch_bounds__(128, MGPU_XF_RETURN_MIN_BLOCKS)
     for (int64_t e = r.o0; e < r.o1; ++e) {
         float ax[kAux], m[kC];
         ld_aux_m<MASK>(aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux, ax);
-        travelers_f<MASK>(B, g, e, gr, own, m);
+        travelers_f<MASK>(B, x, e, gr, own, m);
         apply(ax, m, 1.0f);
     }
 #pragma unroll kXfUnroll
@@ -1475,11 +1501,11 @@ __global__ void k_xf_scan(BatchDev B, int pass)
         }
         const int64_t ib = B.in_ptr[node], ie = B.in_ptr[node + 1];
         const int64_t ob = B.out_ptr[node], oe = B.out_ptr[node + 1];
-        // in-edges from lower nodes come first (in_src ascends within the node)
+        // in-edges from lower nodes come first (the sources ascend within the node)
         int nlow = 0;
         for (int64_t base = ib; base < ie; base += 32) {
             const int64_t k = base + lane;
-            nlow += __popc(__ballot_sync(kFull, k < ie && B.in_src[k] < node));
+            nlow += __popc(__ballot_sync(kFull, k < ie && B.in_se[k].x < node));
         }
         const int nout = (int)(oe - ob);
         const int deg  = (int)(ie - ib) + nout;
@@ -1491,8 +1517,8 @@ __global__ void k_xf_scan(BatchDev B, int pass)
             if (i < deg) {
                 if (i < nlow) {
                     kind = 1;
-                    e    = B.in_edges[ib + i];
-                    u    = B.in_src[ib + i];
+                    e    = B.in_se[ib + i].y;
+                    u    = B.in_se[ib + i].x;
                 }
                 else if (i < nlow + nout) {
                     kind = 2;
@@ -1500,8 +1526,8 @@ __global__ void k_xf_scan(BatchDev B, int pass)
                 }
                 else {
                     kind = 1;
-                    e    = B.in_edges[ib + i - nout];
-                    u    = B.in_src[ib + i - nout];
+                    e    = B.in_se[ib + i - nout].y;
+                    u    = B.in_se[ib + i - nout].x;
                 }
                 if (!edge_departed(B, g, e)) {
                     kind = 0;

@@ -117,7 +117,7 @@ struct BatchDev {
     const int64_t* out_ptr;      // [num_nodes+1] CSR (edges sorted by (src, dst))
     const int64_t* in_ptr;       // [num_nodes+1] CSC
     const int64_t* in_edges;     // [num_edges] edge ids sorted by (dst, src)
-    const int32_t* in_src;       // [num_edges] the source node of in_edges[k]
+    const int2* in_se;           // [num_edges] (source node, edge id) of in_edges[k]
     const int64_t* in_mid;       // [num_nodes] first k of the node's in-edges with a higher source
     int64_t state_total;         // doubles in a state pool
     double* ysnap;               // [2][state_total] departure snapshots (batched exchange)
