@@ -887,19 +887,10 @@ __global__ void __launch_bounds__(MGPU_MIXED_THREADS, MGPU_MIXED_MIN_BLOCKS) k_o
                 const float dtf  = dt;
                 const float trel = tr;
                 float kc[kC], fl[kF];
-                segf_rhs(X, hi, trel, fl, kc);
-#pragma unroll
-                for (int c = 0; c < kC; ++c) {
-                    SK(0, c) = kc[c];
-                }
-#pragma unroll
-                for (int f = 0; f < kF; ++f) {
-                    SP(f) = (fk_b5[0] * dtf) * fl[f];
-                }
-                // stages 2..6: one copy of the right-hand side in the code, stage
-                // derivatives in this lane's shared-memory column
+                // the six stages: one copy of the right-hand side in the code,
+                // stage derivatives in this lane's shared-memory column
 #pragma unroll 1
-                for (int s = 1; s < 6; ++s) {
+                for (int s = 0; s < 6; ++s) {
                     float u[kC];
 #pragma unroll
                     for (int c = 0; c < kC; ++c) {
@@ -921,7 +912,13 @@ __global__ void __launch_bounds__(MGPU_MIXED_THREADS, MGPU_MIXED_MIN_BLOCKS) k_o
                         }
                     }
                     const float b5 = fk_b5[s] * dtf;
-                    if (b5 != 0.0f) {
+                    if (s == 0) {
+#pragma unroll
+                        for (int f = 0; f < kF; ++f) {
+                            SP(f) = b5 * fl[f];
+                        }
+                    }
+                    else if (b5 != 0.0f) {
 #pragma unroll
                         for (int f = 0; f < kF; ++f) {
                             SP(f) = SP(f) + b5 * fl[f];
