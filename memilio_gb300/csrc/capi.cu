@@ -787,6 +787,10 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.scan_list  = b->pool.alloc<int32_t>(3 * nodes * MGPU_MAX_GROUPS);
     B.scan_count = b->pool.alloc<int32_t>(3);
     B.fix_cnt    = b->pool.alloc<uint8_t>(edges * MGPU_MAX_GROUPS);
+    B.fix_cap    = std::min<int64_t>(std::max<int64_t>(edges, 1), 1 << 22);
+    B.fix_edges  = b->pool.alloc<int32_t>(B.fix_cap);
+    B.fix_meta   = b->pool.alloc<int32_t>(2);
+    ck(cudaMemsetAsync(B.fix_meta, 0, sizeof(int32_t) * 2, ctx->stream), "memset");
     ck(cudaMemsetAsync(B.scan_mark, 0, sizeof(int32_t) * std::max<int64_t>(3 * nodes * MGPU_MAX_GROUPS, 1), ctx->stream),
        "memset");
     ck(cudaMemsetAsync(B.scan_count, 0, sizeof(int32_t) * 3, ctx->stream), "memset");
@@ -1643,7 +1647,7 @@ int64_t mgpu_batch_estimate_bytes(const mgpu_graph* graphs, int32_t num_graphs, 
                      8 * nodes * MGPU_MAX_GROUPS * 12;
     b += 8 * tr;                                             // fixed travelers
     b += 24 * nodes + 4 * 2 * 3 * nodes * MGPU_MAX_GROUPS + 4 * nodes + 3 * nodes + 16 * (nodes + 1);
-    b += edges * (4 + 4 + 8 + 1 + 1 + 4 + 8 + 8 + MGPU_MAX_GROUPS);
+    b += edges * (4 + 4 + 8 + 1 + 1 + 4 + 8 + 8 + 4 + MGPU_MAX_GROUPS);
     b += num_graphs * (int64_t)(sizeof(DevGraph) + sizeof(GraphRt) + 8) + 64 * 1024;
     return b + b / 10;
 }

@@ -45,6 +45,13 @@ __global__ void k_phase_begin(BatchDev B, double dt_exchange)
             B.order_cnt[k] = 0;
         }
     }
+    if (gi == 0 && B.fix_meta) {
+        B.fix_meta[0] = 0;
+        B.fix_meta[1] = 0;
+    }
+    if (gi == 0 && B.scan_count) {
+        B.scan_count[0] = B.scan_count[1] = B.scan_count[2] = 0; // the exact path's work lists
+    }
     GraphRt& rt = B.rt[gi];
     rt.fallback = 0;
     if (rt.t < rt.tmax) {

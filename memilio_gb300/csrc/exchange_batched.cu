@@ -52,6 +52,18 @@ __device__ __forceinline__ bool edge_departed(const BatchDev& B, const DevGraph&
     return g.Ke == 0 ? B.edge_static_any[e] != 0 : B.edge_pending[e] != 0;
 }
 
+// record that edge e got a fix count in this return (for the cleanup pass)
+__device__ __forceinline__ void fix_edge_push(const BatchDev& B, int64_t e)
+{
+    const int32_t pos = atomicAdd(B.fix_meta, 1);
+    if (pos < B.fix_cap) {
+        B.fix_edges[pos] = (int32_t)e;
+    }
+    else {
+        B.fix_meta[1] = 1;
+    }
+}
+
 // append a (node, age group) item, node * MAX_GROUPS + group, to exact-scan
 // work list `list` once
 __device__ __forceinline__ void list_push(const BatchDev& B, int list, int64_t item)
@@ -1205,9 +1217,23 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_RETURN_MIN_BLO
 // those travelers). A few passes settle the chains of fixes; a graph with items
 // still marked after the last pass takes the sequential pass.
 
-__global__ void k_list_reset(BatchDev B, int list)
+// The three work lists rotate over the scan passes: pass p reads list p % 3 and
+// fills list (p + 1) % 3; the interval start empties all three, and pass p >= 1
+// empties list (p + 2) % 3, which pass p + 1 fills (its last reader, pass p - 1,
+// has finished). The return pass fills list 0.
+__device__ __forceinline__ int scan_list_in(int pass)
 {
-    B.scan_count[list] = 0;
+    return pass % 3;
+}
+__device__ __forceinline__ int scan_list_out(int pass)
+{
+    return (pass + 1) % 3;
+}
+__device__ __forceinline__ void scan_list_prepare(const BatchDev& B, int pass)
+{
+    if (pass >= 1 && blockIdx.x == 0 && threadIdx.x == 0) {
+        B.scan_count[(pass + 2) % 3] = 0;
+    }
 }
 
 // Exact fix of one (edge, age group) against the running state y: with
@@ -1254,8 +1280,9 @@ __device__ __forceinline__ int fix_group(const double (&y)[kC], double (&t)[kC])
 template <class R>
 __global__ void k_xg_scan(BatchDev B, int pass)
 {
-    const int lin    = pass == 0 ? 0 : 1 + ((pass - 1) & 1);
-    const int lout   = 1 + (pass & 1);
+    const int lin    = scan_list_in(pass);
+    const int lout   = scan_list_out(pass);
+    scan_list_prepare(B, pass);
     const int cnt    = B.scan_count[lin];
     const int64_t NG = B.num_nodes * MGPU_MAX_GROUPS;
     if (blockIdx.x == 0 && threadIdx.x == 0 && cnt > 0) {
@@ -1289,6 +1316,9 @@ __global__ void k_xg_scan(BatchDev B, int pass)
             double* mf     = B.mfix + B.trav_off[e] + gr * kC;
             if (nfix) {
                 changed = prev == 0;
+                if (prev == 0) {
+                    fix_edge_push(B, e);
+                }
 #pragma unroll
                 for (int c = 0; c < kC; ++c) {
                     changed = changed || __ldcg(mf + c) != t[c];
@@ -1464,8 +1494,9 @@ __device__ __forceinline__ int fix_group_ff(const FF (&y)[kC], FF (&t)[kC])
 __global__ void k_xf_scan(BatchDev B, int pass)
 {
     constexpr unsigned kFull = 0xffffffffu;
-    const int lin    = pass == 0 ? 0 : 1 + ((pass - 1) & 1);
-    const int lout   = 1 + (pass & 1);
+    const int lin    = scan_list_in(pass);
+    const int lout   = scan_list_out(pass);
+    scan_list_prepare(B, pass);
     const int cnt    = B.scan_count[lin];
     const int64_t NG = B.num_nodes * MGPU_MAX_GROUPS;
     const int lane   = threadIdx.x & 31;
@@ -1582,6 +1613,9 @@ __global__ void k_xf_scan(BatchDev B, int pass)
                     bool changed = false;
                     if (nfix) {
                         changed = prev == 0;
+                        if (prev == 0) {
+                            fix_edge_push(B, e);
+                        }
 #pragma unroll
                         for (int c = 0; c < kC; ++c) {
                             const float2 old = __ldcg(mf + c);
@@ -1634,26 +1668,31 @@ __global__ void k_xg_scan_done(BatchDev B, int last_list)
     }
 }
 
-// Fix counts of the parallel path; clears the per-(edge, group) fix records.
+// Counts the fixes of this return and clears the per-edge fix counts: over the
+// edges pushed by the scans (an edge can be listed more than once; the exchange
+// of its count word makes only the first visit count), or over all edges when
+// the list overflowed.
 __global__ void k_xg_cleanup(BatchDev B, int64_t ne)
 {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ne) {
-        return;
+    static_assert(MGPU_MAX_GROUPS == 8, "one 8-byte count word per edge");
+    const int64_t pushed = B.fix_meta[0];
+    const bool all       = B.fix_meta[1] != 0 || pushed > B.fix_cap;
+    const int64_t n      = all ? ne : pushed;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = all ? i : B.fix_edges[i];
+        unsigned long long* word = reinterpret_cast<unsigned long long*>(B.fix_cnt) + e;
+        if (*word == 0ull) {
+            continue;
+        }
+        const unsigned long long w = atomicExch(word, 0ull);
+        unsigned f                 = 0;
+        for (int q = 0; q < 8; ++q) {
+            f += (unsigned)(w >> (8 * q)) & 0xffu;
+        }
+        if (f && !B.rt[B.edge_graph[e]].fallback) {
+            atomicAdd(&B.counters[CNT_UNDERFLOW], (unsigned long long)f);
+        }
     }
-    const uint2 w = reinterpret_cast<const uint2*>(B.fix_cnt)[e]; // MAX_GROUPS == 8 bytes
-    if ((w.x | w.y) == 0) {
-        return;
-    }
-    unsigned f = 0;
-    for (int q = 0; q < 4; ++q) {
-        f += (w.x >> (8 * q)) & 0xffu;
-        f += (w.y >> (8 * q)) & 0xffu;
-    }
-    if (!B.rt[B.edge_graph[e]].fallback) {
-        atomicAdd(&B.counters[CNT_UNDERFLOW], (unsigned long long)f);
-    }
-    reinterpret_cast<uint2*>(B.fix_cnt)[e] = make_uint2(0u, 0u);
 }
 
 // Exact serial return loop of one graph (one warp per graph) for the graphs
@@ -1822,7 +1861,6 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
     // exact underflow path over the work lists (list 0 was filled by the return pass)
     const unsigned scan_blocks = 152 * 8;
     for (int pass = 0; pass < kXbScanPasses; ++pass) {
-        k_list_reset<<<1, 1, 0, s>>>(B, 1 + (pass & 1));
         if (std::is_same<R, float>::value) {
             k_xf_scan<<<scan_blocks, 128, 0, s>>>(B, pass);
         }
@@ -1830,15 +1868,13 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
             k_xg_scan<R><<<scan_blocks, 128, 0, s>>>(B, pass);
         }
     }
-    const int last = 1 + ((kXbScanPasses - 1) & 1);
-    k_xg_scan_done<<<scan_blocks, 128, 0, s>>>(B, last);
-    k_list_reset<<<1, 1, 0, s>>>(B, 0);
+    k_xg_scan_done<<<scan_blocks, 128, 0, s>>>(B, kXbScanPasses % 3); // the list the last pass filled
     if (!mixed || any_edge_dampings) {
         // (mixed batches without edge dampings return in place)
         k_xb_commit<<<blocks_of(nn * n_max, 256), 256, 0, s>>>(B, 0, nn, (int)n_max);
     }
     k_xb_sequential<R><<<B.num_graphs, 32, 0, s>>>(B, 0, B.num_graphs);
-    k_xg_cleanup<<<blocks_of(ne, 256), 256, 0, s>>>(B, ne);
+    k_xg_cleanup<<<152 * 4, 256, 0, s>>>(B, ne);
     mark(2);
     if (any_edge_dampings) {
         k_xb_edge_flags<<<blocks_of(ne, 256), 256, 0, s>>>(B, 0, ne);
@@ -1861,7 +1897,7 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
         k_xb_depart<R><<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
         *launches += 1;
     }
-    *launches += 4 + 2 * kXbScanPasses + ((!mixed || any_edge_dampings) ? 1 : 0);
+    *launches += 3 + kXbScanPasses + ((!mixed || any_edge_dampings) ? 1 : 0);
 }
 
 } // namespace
@@ -1876,8 +1912,8 @@ int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampi
     const int extra  = !any_edge_dampings ? 0 : (mixed ? 3 : 1);
     const int commit = (!mixed || any_edge_dampings) ? 1 : 0;
     // return and departure passes (one per age-group count when mixed); the exact
-    // path: scan passes with their list resets, done, reset, sequential, cleanup
-    return prep + 4 + (mixed ? 2 * group_lists : 2) + 2 * kXbScanPasses + commit + extra;
+    // path: scan passes, done, sequential, cleanup
+    return prep + 3 + (mixed ? 2 * group_lists : 2) + kXbScanPasses + commit + extra;
 }
 
 void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,

@@ -113,6 +113,9 @@ struct BatchDev {
     int32_t* scan_list;          // [3][num_nodes * MAX_GROUPS] items node * MAX_GROUPS + group
     int32_t* scan_count;         // [3]
     uint8_t* fix_cnt;            // [num_edges][MAX_GROUPS] fixed compartments per edge and age group
+    int32_t* fix_edges;          // [fix_cap] edges whose fix counts became nonzero in this interval
+    int32_t* fix_meta;           // [2]: entries pushed, overflow flag (zeroed at each interval start)
+    int64_t fix_cap;
     const int64_t* trav_off;     // [num_edges] offset of each edge's travelers
     const int64_t* out_ptr;      // [num_nodes+1] CSR (edges sorted by (src, dst))
     const int64_t* in_ptr;       // [num_nodes+1] CSC
