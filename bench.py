@@ -276,10 +276,13 @@ def h2d_bytes(graphs) -> int:
 #   mixed node kernel)
 BYTES_PER_ITEM = {"return": 256, "depart": 288, "exact": 256}
 # DRAM bytes (read + write) per (node, group) item of one launch, from one ncu
-# capture of a 256-sample x 400-node ensemble (profiles/ncu_k_xf_return_256x400.md,
-# profiles/ncu_k_xf_depart_256x400.md): 212.9 MB and 179.7 MB for 614,400 items.
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of a 256-sample x
+# 400-node ensemble: 236.4 MB (return) and 156.6 MB (departure) for 614,400 items.
 # The traffic grows in proportion to the items, so it scales to the full launch.
-NCU_BYTES_PER_ITEM = {"return": (177.251072e6 + 35.664384e6) / 614400, "depart": (125.641728e6 + 54.061312e6) / 614400}
+NCU_BYTES_PER_ITEM = {"return": (162.609408e6 + 73.811456e6) / 614400, "depart": (110.047488e6 + 46.544896e6) / 614400}
+# the same for the mixed node kernel, per node instance of one interval
+# (223.8 MB for 102,400 instances)
+NCU_ODE_BYTES_PER_INSTANCE = (178.190080e6 + 45.599744e6) / 102400
 
 
 def main():
@@ -373,14 +376,17 @@ def main():
     fp32_peak = 152 * 128 * 2 * f_sm * 1e6 / 1e12  # TFLOP/s at the sampled clock
     achieved = flops_launch / (ode_ms_launch / 1e3) / 1e12
     roofline = {"bound": "fp32" if prec == N.PRECISION_MIXED else "fp64",
-                "kernel": "k_ode_batched<6,float>" if prec == N.PRECISION_MIXED else (
+                "kernel": "k_ode_mixed<6>" if prec == N.PRECISION_MIXED else (
                     "k_ode_batched<6,double>" if prec == N.PRECISION_FP64 else "k_ode_plain"),
                 "achieved": achieved, "unit": "TFLOP/s",
                 "peak": fp32_peak if prec == N.PRECISION_MIXED else 1.25,
                 "peak_source": ("nominal FP32 FMA rate (152 SMs x 128 lanes x 2) at the sampled median SM clock; "
                                 "MEASURED_PEAKS.json holds no FP32 figure") if prec == N.PRECISION_MIXED else
                                "nominal GB300 FP64 rate",
-                "frac": None, "traffic": None,
+                "frac": None,
+                "traffic": (NCU_ODE_BYTES_PER_INSTANCE * sum(g.num_nodes for g in graphs)
+                            if prec == N.PRECISION_MIXED else None),
+                "traffic_source": "ncu DRAM bytes per node instance of a 256-sample capture, times the instances",
                 "ode_share_of_step": tm["ode_ms"] / max(tm["advance_ms"], 1e-9),
                 "exchange_ms_per_step": tm["exchange_ms"], "ode_ms_per_step": tm["ode_ms"],
                 "algorithmic_flops_per_launch": flops_launch, "avg_launch_ms": ode_ms_launch}

@@ -11,7 +11,7 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-from .layout import GraphArrays, MgpuGraph, MgpuIntegratorOpts, integrator_opts
+from .layout import GraphArrays, MgpuGraph, MgpuIntegratorOpts, graphs_as_ctypes, integrator_opts
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("MIOGPU_LIB") or os.path.join(HERE, "lib", "libmiogpu.so")
@@ -273,7 +273,7 @@ class Batch:
     def __init__(self, ctx: Context, graphs: Sequence[GraphArrays], t0: float = 0.0, opts: MgpuSolverOpts = None):
         self.ctx = ctx
         self.graphs = list(graphs)
-        self._arr = (MgpuGraph * len(self.graphs))(*[g.as_ctypes() for g in self.graphs])
+        self._arr = graphs_as_ctypes(self.graphs)
         self._h = ctypes.c_void_p()
         opts = opts or solver_opts()
         ctx.check(lib().mgpu_batch_create(ctx.handle, self._arr, len(self.graphs), t0, ctypes.byref(opts),

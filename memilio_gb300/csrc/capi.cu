@@ -5,6 +5,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -26,6 +29,9 @@ struct mgpu_context {
     std::string error    = "";
     int64_t budget       = 0; // 0 = free HBM
     int64_t allocated    = 0;
+    // page-locked host staging of batch uploads, kept for the next batch (grown on demand)
+    void* pinned         = nullptr;
+    size_t pinned_bytes  = 0;
 };
 
 int mgpu::context_device_stream(const mgpu_context* ctx, int* device, cudaStream_t* stream)
@@ -101,32 +107,62 @@ struct DevPool {
     }
 };
 
-// Host staging buffers whose elements are all written before use: no zero fill.
+
+// A typed view of part of the staging arena (the container interface that
+// DevPool::upload and the packing code use).
 template <class T>
-struct NoInit : std::allocator<T> {
+struct HostSpan {
     using value_type = T;
-    template <class U>
-    struct rebind {
-        using other = NoInit<U>;
-    };
-    NoInit() = default;
-    template <class U>
-    NoInit(const NoInit<U>&)
+    T* p     = nullptr;
+    size_t n = 0;
+    T* data() const
     {
+        return p;
     }
-    template <class U>
-    void construct(U* p) noexcept
+    size_t size() const
     {
-        ::new ((void*)p) U;
+        return n;
     }
-    template <class U, class... A>
-    void construct(U* p, A&&... a)
+    bool empty() const
     {
-        ::new ((void*)p) U(std::forward<A>(a)...);
+        return n == 0;
+    }
+    T& operator[](size_t i) const
+    {
+        return p[i];
     }
 };
-template <class T>
-using HostBuf = std::vector<T, NoInit<T>>;
+
+// Host staging of one batch upload in the context's page-locked buffer: the
+// arrays are laid out first (take), then placed in one block (place), so that
+// the uploads run at the page-locked copy rate and need no zero fill.
+struct StagingArena {
+    mgpu_context* ctx;
+    size_t bytes = 0;
+    std::vector<std::pair<void**, size_t>> items;
+    template <class T>
+    void take(HostSpan<T>& s, int64_t count)
+    {
+        s.n = (size_t)std::max<int64_t>(count, 0);
+        items.emplace_back(reinterpret_cast<void**>(&s.p), bytes);
+        bytes += (s.n * sizeof(T) + 255) & ~(size_t)255;
+    }
+    void place()
+    {
+        if (bytes > ctx->pinned_bytes) {
+            if (ctx->pinned) {
+                ck(cudaFreeHost(ctx->pinned), "cudaFreeHost");
+                ctx->pinned       = nullptr;
+                ctx->pinned_bytes = 0;
+            }
+            ck(cudaHostAlloc(&ctx->pinned, bytes, cudaHostAllocDefault), "cudaHostAlloc");
+            ctx->pinned_bytes = bytes;
+        }
+        for (auto& it : items) {
+            *it.first = static_cast<char*>(ctx->pinned) + it.second;
+        }
+    }
+};
 
 // f(i) for i in [0, n) on the host's cores (chunks handed out in order); the
 // first exception of any worker is rethrown here.
@@ -262,6 +298,7 @@ struct mgpu_batch {
     std::vector<double> t_host;  // mirror of rt.t
     std::vector<double> tmax_host;
     double* d_tmax = nullptr;
+    double* d_out  = nullptr; // FP64 read-back buffer of float-float states (allocated on first read)
     // batched solver work lists per age-group count
     std::map<int, std::pair<int32_t*, int64_t>> inst_by_G;
     int instances_per_block = 0;
@@ -346,6 +383,14 @@ __global__ void k_split_pairs(const double* v, int64_t n, float* hi, float* lo, 
     const float l = __double2float_rn(v[i] - (double)h);
     hi[i] = hi2[i] = h;
     lo[i] = lo2[i] = l;
+}
+
+__global__ void k_pairs_to_double(const float* hi, const float* lo, int64_t n, double* out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        out[i] = (double)hi[i] + (double)lo[i];
+    }
 }
 
 __global__ void k_to_float(const double* v, int64_t n, float* out)
@@ -441,6 +486,22 @@ __global__ void k_reset(BatchDev B, const double* init_state, const float* init_
         B.rt[tid]   = r;
     }
 }
+
+// Phase times of a batch creation on stderr when MIOGPU_TRACE is set.
+struct PhaseTrace {
+    bool on = std::getenv("MIOGPU_TRACE") != nullptr;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now(), last = t0;
+    void mark(const char* what)
+    {
+        if (!on) {
+            return;
+        }
+        const auto now = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "miogpu: %-28s %8.2f ms\n", what,
+                     std::chrono::duration<double, std::milli>(now - last).count());
+        last = now;
+    }
+};
 
 // Upload graphs into one set of pools. `with_edges` false: edges ignored.
 void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, double t0, double dt0,
@@ -566,16 +627,42 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         fail(MGPU_INVALID_VALUE, "batch too large: more than 2^31 - 1 edges in one batch");
     }
     // edge index arrays and damping times, each distinct array once, on the host's cores
+    PhaseTrace trace;
+    trace.mark("layout");
     parallel_for(num_graphs, [&](int64_t i) {
         validate_graph_arrays(graphs[i], with_edges && check_edges[i], check_times[i], true);
     });
-    // host staging (every element is written below, so no zero fill)
-    HostBuf<double> h_par(par), h_con(con), h_dtt(dtt), h_dtv(dtv), h_state(st), h_ec(ec), h_edt(edt), h_edv(edv);
+    trace.mark("checks");
+    // host staging in the context's page-locked buffer (every element is written below)
+    HostSpan<double> h_par, h_con, h_dtt, h_dtv, h_state, h_ec, h_edt, h_edv;
+    HostSpan<int32_t> h_node_graph, h_edge_graph, h_src, h_dst;
+    HostSpan<uint8_t> h_any;
+    HostSpan<int64_t> h_trav_off, h_in_ptr, h_in_edges, h_in_mid;
+    HostSpan<int2> h_in_se;
+    StagingArena arena{ctx};
+    arena.take(h_par, par);
+    arena.take(h_con, con);
+    arena.take(h_dtt, dtt);
+    arena.take(h_dtv, dtv);
+    arena.take(h_state, st);
+    arena.take(h_ec, ec);
+    arena.take(h_edt, edt);
+    arena.take(h_edv, edv);
+    arena.take(h_node_graph, nodes);
+    arena.take(h_edge_graph, edges);
+    arena.take(h_src, edges);
+    arena.take(h_dst, edges);
+    arena.take(h_any, edges);
+    arena.take(h_trav_off, edges);
+    arena.take(h_in_ptr, nodes + 1);
+    arena.take(h_in_edges, edges);
+    arena.take(h_in_mid, nodes);
+    arena.take(h_in_se, edges);
+    ck(cudaStreamSynchronize(ctx->stream), "staging sync"); // an earlier upload may still read the buffer
+    arena.place();
+    trace.mark("page-locked staging");
     // FP32 coefficient records (rec_vec layout) of the mixed exchange; the factor slots stay zero
     std::vector<float> h_ecr(b->opts.precision == MGPU_PRECISION_MIXED ? ecf / kC * kRec : 0, 0.0f);
-    HostBuf<int32_t> h_node_graph(nodes), h_edge_graph(edges), h_src(edges), h_dst(edges);
-    HostBuf<uint8_t> h_any(edges);
-    HostBuf<int64_t> h_trav_off(edges), h_in_ptr(nodes + 1), h_in_edges(edges);
     std::vector<int64_t> h_out_ptr(nodes + 1, 0);
     std::vector<int32_t> mob_mask(num_graphs, 0);
     // Graphs pack into disjoint ranges of the staging buffers, on the host's
@@ -693,6 +780,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         dg[i].mob_mask = mob_mask[i];
         B.mob_union |= mob_mask[i];
     }
+    trace.mark("packing");
     B.graphs         = b->pool.upload(dg);
     std::vector<GraphRt> h_rt(num_graphs);
     for (auto& r : h_rt) {
@@ -805,8 +893,6 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.in_ptr   = b->pool.upload(h_in_ptr);
     B.in_edges = b->pool.upload(h_in_edges);
     {
-        HostBuf<int2> h_in_se(edges);
-        HostBuf<int64_t> h_in_mid(nodes);
         parallel_for(num_graphs, [&](int64_t i) {
             const DevGraph& d = dg[i];
             for (int64_t k = d.edge0; k < d.edge0 + d.E; ++k) {
@@ -823,6 +909,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         });
         B.in_se  = b->pool.upload(h_in_se);
         B.in_mid = b->pool.upload(h_in_mid);
+        trace.mark("uploads, in-edge indices");
     }
     B.scratch_stride = std::max<int64_t>(scratch_slots, 1);
     B.scratch_nmax   = (int32_t)b->n_max;
@@ -862,6 +949,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.order_cnt = b->pool.alloc<int32_t>(2 * (MGPU_MAX_GROUPS + 1));
     ck(cudaMemsetAsync(B.order_cnt, 0, sizeof(int32_t) * 2 * (MGPU_MAX_GROUPS + 1), ctx->stream), "memset");
     ck(cudaStreamSynchronize(ctx->stream), "upload sync");
+    trace.mark("tables, lists, sync");
     staging.release();
 }
 
@@ -1019,6 +1107,9 @@ void mgpu_destroy(mgpu_context* ctx)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
+    if (ctx->pinned) {
+        cudaFreeHost(ctx->pinned);
+    }
     delete ctx;
 }
 
@@ -1573,6 +1664,32 @@ int mgpu_batch_query(mgpu_batch* b, int32_t* done)
     });
 }
 
+// Float-float node states [off, off + cnt) as FP64 into host memory: combined on
+// the device (hi + lo in FP64 is exact), copied into the context's page-locked
+// staging, then into `out` on the host's cores.
+void read_pairs(mgpu_batch* b, int64_t off, int64_t cnt, double* out)
+{
+    cudaStream_t s = b->ctx->stream;
+    if (!b->d_out) {
+        b->d_out = b->pool.alloc<double>(b->state_total);
+    }
+    k_pairs_to_double<<<(unsigned)std::max<int64_t>((cnt + 255) / 256, 1), 256, 0, s>>>(
+        b->dev.st_hi + off, b->dev.st_lo + off, cnt, b->d_out + off);
+    ck(cudaGetLastError(), "k_pairs_to_double");
+    ck(cudaStreamSynchronize(s), "sync");
+    HostSpan<double> stage;
+    StagingArena arena{b->ctx};
+    arena.take(stage, cnt);
+    arena.place();
+    ck(cudaMemcpyAsync(stage.data(), b->d_out + off, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s), "d2h state");
+    ck(cudaStreamSynchronize(s), "sync");
+    const int64_t chunk = 1 << 20;
+    parallel_for((cnt + chunk - 1) / chunk, [&](int64_t k) {
+        const int64_t a = k * chunk;
+        std::memcpy(out + a, stage.data() + a, sizeof(double) * (size_t)std::min(chunk, cnt - a));
+    });
+}
+
 int mgpu_batch_get_graph_state(mgpu_batch* b, int32_t graph, double* out)
 {
     if (!b) {
@@ -1590,13 +1707,7 @@ int mgpu_batch_get_graph_state(mgpu_batch* b, int32_t graph, double* out)
         }
         cudaStream_t s = b->ctx->stream;
         if (b->pairs) {
-            std::vector<float> hi(cnt), lo(cnt);
-            ck(cudaMemcpyAsync(hi.data(), b->dev.st_hi + off, sizeof(float) * cnt, cudaMemcpyDeviceToHost, s), "d2h");
-            ck(cudaMemcpyAsync(lo.data(), b->dev.st_lo + off, sizeof(float) * cnt, cudaMemcpyDeviceToHost, s), "d2h");
-            ck(cudaStreamSynchronize(s), "sync");
-            for (int64_t k = 0; k < cnt; ++k) {
-                out[k] = (double)hi[k] + (double)lo[k];
-            }
+            read_pairs(b, off, cnt, out);
         }
         else {
             ck(cudaMemcpyAsync(out, b->dev.state + off, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s), "d2h");
@@ -1640,7 +1751,7 @@ int64_t mgpu_batch_estimate_bytes(const mgpu_graph* graphs, int32_t num_graphs, 
         nmax = std::max<int64_t>(nmax, N);
     }
     int64_t b = 8 * (par + con + dtt + dtv + ec + edt + edv) + (mixed ? 4 * (tr / kC) * kRec : 0); // inputs, FP32 coefficients
-    b += mixed ? 4 * st * 8 + 4 * nodes * MGPU_MAX_GROUPS * kTabF + 4 * (con + dtv) : 8 * st * 4;
+    b += mixed ? 4 * st * 8 + 8 * st + 4 * nodes * MGPU_MAX_GROUPS * kTabF + 4 * (con + dtv) : 8 * st * 4;
     // snapshots (mixed: two slots of records), factors, auxiliary values
     b += plain ? 8 * st + 8 * tr + 8 * 8 * nmax * 60
                : (mixed ? 4 * 2 * (st / kC) * kRec : 8 * st * 2 + 8 * nodes * MGPU_MAX_GROUPS * 4) +
@@ -1939,17 +2050,8 @@ int mgpu_batch_get_state(mgpu_batch* b, double* out)
         }
         ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
         if (b->pairs) {
-            // float-float pairs, combined in FP64 on the host
-            std::vector<float> hi(b->state_total), lo(b->state_total);
-            ck(cudaMemcpyAsync(hi.data(), b->dev.st_hi, sizeof(float) * b->state_total, cudaMemcpyDeviceToHost,
-                               b->ctx->stream),
-               "d2h state");
-            ck(cudaMemcpyAsync(lo.data(), b->dev.st_lo, sizeof(float) * b->state_total, cudaMemcpyDeviceToHost,
-                               b->ctx->stream),
-               "d2h state");
-            ck(cudaStreamSynchronize(b->ctx->stream), "sync");
-            for (int64_t i = 0; i < b->state_total; ++i) {
-                out[i] = (double)hi[i] + (double)lo[i];
+            if (b->state_total > 0) {
+                read_pairs(b, 0, b->state_total, out);
             }
             return MGPU_OK;
         }

@@ -60,18 +60,18 @@ class MgpuGraph(ctypes.Structure):
         ("num_contact_matrices", ctypes.c_int32),
         ("num_damping_points", ctypes.c_int32),
         ("num_edge_damping_points", ctypes.c_int32),
-        ("params", ctypes.POINTER(ctypes.c_double)),
-        ("contact_baseline", ctypes.POINTER(ctypes.c_double)),
-        ("contact_minimum", ctypes.POINTER(ctypes.c_double)),
-        ("damping_times", ctypes.POINTER(ctypes.c_double)),
-        ("damping_values", ctypes.POINTER(ctypes.c_double)),
-        ("init_state", ctypes.POINTER(ctypes.c_double)),
-        ("edge_src", ctypes.POINTER(ctypes.c_int32)),
-        ("edge_dst", ctypes.POINTER(ctypes.c_int32)),
-        ("edge_coeff_baseline", ctypes.POINTER(ctypes.c_double)),
-        ("edge_coeff_minimum", ctypes.POINTER(ctypes.c_double)),
-        ("edge_damping_times", ctypes.POINTER(ctypes.c_double)),
-        ("edge_damping_values", ctypes.POINTER(ctypes.c_double)),
+        ("params", ctypes.c_void_p),  # const double*
+        ("contact_baseline", ctypes.c_void_p),  # const double*
+        ("contact_minimum", ctypes.c_void_p),  # const double*
+        ("damping_times", ctypes.c_void_p),  # const double*
+        ("damping_values", ctypes.c_void_p),  # const double*
+        ("init_state", ctypes.c_void_p),  # const double*
+        ("edge_src", ctypes.c_void_p),  # const int32_t*
+        ("edge_dst", ctypes.c_void_p),  # const int32_t*
+        ("edge_coeff_baseline", ctypes.c_void_p),  # const double*
+        ("edge_coeff_minimum", ctypes.c_void_p),  # const double*
+        ("edge_damping_times", ctypes.c_void_p),  # const double*
+        ("edge_damping_values", ctypes.c_void_p),  # const double*
     ]
 
 
@@ -91,18 +91,19 @@ def integrator_opts(method=METHOD_CASH_KARP54, abs_tol=1e-10, rel_tol=1e-5, dt_m
     return MgpuIntegratorOpts(method, 0, abs_tol, rel_tol, dt_min, dt_max)
 
 
-def _dptr(a: Optional[np.ndarray]):
+def _addr(a: Optional[np.ndarray], dtype) -> Optional[int]:
+    """Address of a C-contiguous array of `dtype` (None for an empty one)."""
     if a is None or a.size == 0:
-        return ctypes.POINTER(ctypes.c_double)()
-    assert a.dtype == np.float64 and a.flags.c_contiguous
-    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        return None
+    assert a.dtype == dtype and a.flags.c_contiguous
+    if a.flags.writeable:
+        return ctypes.addressof(ctypes.c_char.from_buffer(a))  # (a faster route to the data pointer)
+    return a.__array_interface__["data"][0]
 
 
-def _iptr(a: Optional[np.ndarray]):
-    if a is None or a.size == 0:
-        return ctypes.POINTER(ctypes.c_int32)()
-    assert a.dtype == np.int32 and a.flags.c_contiguous
-    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+def graphs_as_ctypes(graphs) -> ctypes.Array:
+    """An mgpu_graph array of `graphs` (the arrays must outlive its use)."""
+    return (MgpuGraph * len(graphs))(*[g.as_ctypes() for g in graphs])
 
 
 @dataclass
@@ -183,25 +184,16 @@ class GraphArrays:
         return NUM_COMPARTMENTS * self.num_groups
 
     def as_ctypes(self) -> MgpuGraph:
-        g = MgpuGraph()
-        g.num_nodes = self.num_nodes
-        g.num_groups = self.num_groups
-        g.num_edges = self.num_edges
-        g.num_contact_matrices = self.num_contact_matrices
-        g.num_damping_points = self.num_damping_points
-        g.num_edge_damping_points = self.edge_damping_times.shape[1]
-        g.params = _dptr(self.params)
-        g.contact_baseline = _dptr(self.contact_baseline)
-        g.contact_minimum = _dptr(self.contact_minimum)
-        g.damping_times = _dptr(self.damping_times)
-        g.damping_values = _dptr(self.damping_values)
-        g.init_state = _dptr(self.init_state)
-        g.edge_src = _iptr(self.edge_src)
-        g.edge_dst = _iptr(self.edge_dst)
-        g.edge_coeff_baseline = _dptr(self.edge_coeff_baseline)
-        g.edge_coeff_minimum = _dptr(self.edge_coeff_minimum)
-        g.edge_damping_times = _dptr(self.edge_damping_times)
-        g.edge_damping_values = _dptr(self.edge_damping_values)
+        """The mgpu_graph view of the arrays (they must outlive its use)."""
+        f8, i4 = np.float64, np.int32
+        a = _addr
+        g = MgpuGraph(self.num_nodes, self.num_groups, self.num_edges, self.num_contact_matrices,
+                      self.num_damping_points, self.edge_damping_times.shape[1],
+                      a(self.params, f8), a(self.contact_baseline, f8), a(self.contact_minimum, f8),
+                      a(self.damping_times, f8), a(self.damping_values, f8), a(self.init_state, f8),
+                      a(self.edge_src, i4), a(self.edge_dst, i4), a(self.edge_coeff_baseline, f8),
+                      a(self.edge_coeff_minimum, f8), a(self.edge_damping_times, f8),
+                      a(self.edge_damping_values, f8))
         self._c = g
         return g
 
