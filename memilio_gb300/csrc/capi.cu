@@ -65,7 +65,11 @@ void ck(cudaError_t e, const char* what)
     }
 }
 
-// Device allocations owned by a batch or a call.
+// Device allocations owned by a batch or a call, stream-ordered on the
+// context's stream (cudaMallocAsync / cudaFreeAsync): a release does not wait
+// for the work of other streams, so batches created and destroyed while others
+// run (the serving loop) do not stall them; freed blocks stay in the device's
+// memory pool for the next batch.
 struct DevPool {
     mgpu_context* ctx = nullptr;
     std::vector<std::pair<void*, int64_t>> blocks;
@@ -80,7 +84,11 @@ struct DevPool {
                                std::to_string(ctx->budget) + " bytes)");
         }
         void* p = nullptr;
-        ck(cudaMalloc(&p, nb), "cudaMalloc");
+        const cudaError_t e = cudaMallocAsync(&p, nb, ctx->stream);
+        if (e != cudaSuccess) {
+            cudaGetLastError(); // an allocation failure leaves no error behind for later launch checks
+            ck(e, "cudaMallocAsync");
+        }
         blocks.emplace_back(p, nb);
         bytes += nb;
         ctx->allocated += nb;
@@ -99,7 +107,7 @@ struct DevPool {
     void release()
     {
         for (auto& b : blocks) {
-            cudaFree(b.first);
+            cudaFreeAsync(b.first, ctx->stream);
             ctx->allocated -= b.second;
         }
         blocks.clear();
@@ -1095,6 +1103,15 @@ int mgpu_create(int device, mgpu_context** out)
         delete ctx;
         return MGPU_CUDA_ERROR;
     }
+    // batch allocations come from the device's default memory pool; keep freed
+    // blocks there (for the process's next batch) instead of returning them at
+    // every synchronisation
+    cudaMemPool_t pool = nullptr;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
     *out = ctx;
     return MGPU_OK;
 }
@@ -1109,6 +1126,11 @@ void mgpu_destroy(mgpu_context* ctx)
     cudaStreamDestroy(ctx->stream);
     if (ctx->pinned) {
         cudaFreeHost(ctx->pinned);
+    }
+    // return the pool's unused blocks to the device
+    cudaMemPool_t pool = nullptr;
+    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) {
+        cudaMemPoolTrimTo(pool, 0);
     }
     delete ctx;
 }
