@@ -300,7 +300,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--uneven", type=int, default=4096, help="graphs of the uneven-batch leg (0 = skip)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window per rate (0 = skip)")
-    ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 800.0])
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 800.0, 3200.0])
     args = ap.parse_args()
 
     from memilio_gb300 import replicas as R
