@@ -231,6 +231,20 @@ int mgpu_batch_get_state(mgpu_batch* batch, double* out);
 int mgpu_batch_get_time(mgpu_batch* batch, double* out);
 /* Replace the node states (e.g. after a host-side intervention) [sum_b N_b][10 G_b]. */
 int mgpu_batch_set_state(mgpu_batch* batch, const double* state);
+/*
+ * Replace the damping cache of contact matrix `matrix` of one node between two
+ * advances: the accumulated damping matrices of Dampings::update_cache
+ * (memilio/epidemiology/damping.h:570-600) after dampings were added at run
+ * time, e.g. by dynamic NPIs (osecir::Simulation::advance, models/ode_secir/
+ * model.h:289-367, implement_dynamic_npis in epidemiology/dynamic_npis.h).
+ * times [num_points] (first -DBL_MAX, last DBL_MAX), values [num_points][G][G];
+ * num_points may not exceed the graph's num_damping_points (the cache is padded
+ * with its last point). The graph's damping arrays must not have been shared
+ * with another graph of the batch (same host pointers at creation):
+ * MGPU_UNSUPPORTED otherwise.
+ */
+int mgpu_batch_set_damping_cache(mgpu_batch* batch, int32_t graph, int32_t node, int32_t matrix, int32_t num_points,
+                                 const double* times, const double* values);
 int mgpu_batch_get_stats(mgpu_batch* batch, mgpu_stats* out);
 /*
  * Asynchronous advance, for request loops that keep several batches in flight

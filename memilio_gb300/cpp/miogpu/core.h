@@ -137,6 +137,14 @@ struct DampingLevel {
     {
         return value;
     }
+    friend constexpr bool operator==(DampingLevel a, DampingLevel b)
+    {
+        return a.value == b.value;
+    }
+    friend constexpr bool operator!=(DampingLevel a, DampingLevel b)
+    {
+        return a.value != b.value;
+    }
     int value;
 };
 
@@ -148,6 +156,14 @@ struct DampingType {
     constexpr int get() const
     {
         return value;
+    }
+    friend constexpr bool operator==(DampingType a, DampingType b)
+    {
+        return a.value == b.value;
+    }
+    friend constexpr bool operator!=(DampingType a, DampingType b)
+    {
+        return a.value != b.value;
     }
     int value;
 };
@@ -289,6 +305,27 @@ public:
     {
         return m_list;
     }
+    size_t size() const
+    {
+        return m_list.size();
+    }
+    const Damping& operator[](size_t i) const
+    {
+        return m_list.at(i);
+    }
+    /* Dampings::remove (damping.h:336-340) */
+    void remove(size_t i)
+    {
+        m_list.erase(m_list.begin() + (std::ptrdiff_t)i);
+    }
+    size_t rows() const
+    {
+        return m_rows;
+    }
+    size_t cols() const
+    {
+        return m_cols;
+    }
     void clear()
     {
         m_list.clear();
@@ -404,6 +441,11 @@ public:
     const Dampings& get_dampings() const
     {
         return m_dampings;
+    }
+    /* DampingMatrixExpression::remove_damping (contact_matrix.h:106-109) */
+    void remove_damping(size_t i)
+    {
+        m_dampings.remove(i);
     }
     void clear_dampings()
     {

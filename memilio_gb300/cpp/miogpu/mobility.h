@@ -261,7 +261,8 @@ struct GraphArrays {
 /* Packs models (one per node, with its current state) and edge coefficients. */
 template <class ModelT, class EdgeT>
 GraphArrays pack_graph(const std::vector<const ModelT*>& models, const std::vector<const std::vector<double>*>& states,
-                       const std::vector<Edge<EdgeT>>& edges, std::function<const MobilityParameters<double>&(const EdgeT&)> params_of)
+                       const std::vector<Edge<EdgeT>>& edges, std::function<const MobilityParameters<double>&(const EdgeT&)> params_of,
+                       int extra_damping_points = 0)
 {
     GraphArrays a;
     a.N = (int)models.size();
@@ -279,6 +280,9 @@ GraphArrays pack_graph(const std::vector<const ModelT*>& models, const std::vect
         K = std::max(K, recs.back().K);
     }
     a.M = recs[0].M;
+    if (extra_damping_points > 0) {
+        K = std::max(K, 2) + extra_damping_points; // room for dampings added at run time
+    }
     a.K = K;
     const size_t GG = (size_t)a.G * a.G;
     for (auto& r : recs) {
@@ -379,6 +383,9 @@ public:
             if (tmax - t_next < 1e-12 * std::max(1.0, std::abs(tmax))) {
                 t_next = tmax;
             }
+            if (m_any_npis) {
+                apply_dynamic_npis(t_next);
+            }
             check(mgpu_batch_advance(m_batch, t_next, nullptr), ctx, "mgpu_batch_advance");
             m_t = t_next;
             record();
@@ -407,6 +414,69 @@ public:
     }
 
 private:
+    /* Room for damping-cache points added by dynamic NPIs during a run. */
+    static constexpr int kNpiDampingPoints = 64;
+
+    /* The dynamic-NPI check of every node at the start of its next chunk
+     * (osecir::Simulation::advance, model.h:299-350, reached through
+     * SimulationNode::advance): enacted NPIs change the node's contact
+     * dampings, whose new cache goes to the batch. A chunk ends at the active
+     * NPI's end (model.h:352-357); that end must lie on the exchange grid. */
+    void apply_dynamic_npis(double t_next)
+    {
+        mgpu_context* ctx = Device::context();
+        std::vector<double> all;
+        if (!m_record) {
+            all.resize(m_arrays.state.size());
+            check(mgpu_batch_get_state(m_batch, all.data()), ctx, "mgpu_batch_get_state");
+        }
+        const size_t n = (size_t)m_arrays.G * osecir::num_compartments;
+        auto& nodes    = m_graph.nodes();
+        for (size_t v = 0; v < nodes.size(); ++v) {
+            auto& sim   = nodes[v].property.get_simulation();
+            auto& model = sim.get_model();
+            using FPT   = double;
+            const auto& npis = model.parameters.template get<osecir::DynamicNPIsInfectedSymptoms<FPT>>();
+            if (npis.get_thresholds().empty()) {
+                continue;
+            }
+            std::vector<double> y = m_record ? nodes[v].property.get_result().get_last_value()
+                                             : std::vector<double>(all.begin() + (long)(v * n),
+                                                                   all.begin() + (long)((v + 1) * n));
+            auto& contacts = model.parameters.template get<osecir::ContactPatterns<FPT>>();
+            if (check_dynamic_npis(npis, sim.get_dynamic_npi_state(), contacts, m_t,
+                                   osecir::get_infections_relative(sim, m_t, y))) {
+                upload_dampings((int)v, contacts);
+            }
+            const double te = sim.get_dynamic_npi_state().t_end;
+            if (m_t < te && te < t_next - 1e-12 * std::max(1.0, std::abs(t_next))) {
+                throw Error(MGPU_UNSUPPORTED, "a dynamic NPI ends inside an exchange interval: choose its duration, "
+                                              "delay and directive end on the exchange grid");
+            }
+        }
+    }
+
+    void upload_dampings(int v, const ContactMatrixGroup& contacts)
+    {
+        const int K     = m_arrays.K;
+        const size_t GG = (size_t)m_arrays.G * m_arrays.G;
+        for (size_t m = 0; m < contacts.get_num_matrices(); ++m) {
+            std::vector<double> times;
+            std::vector<Matrix> vals;
+            contacts[m].get_dampings().cache(times, vals);
+            if ((int)times.size() > K) {
+                throw Error(MGPU_UNSUPPORTED, "dynamic NPIs exceeded the damping-cache capacity of the batch");
+            }
+            std::vector<double> flat;
+            for (auto& mat : vals) {
+                flat.insert(flat.end(), mat.data(), mat.data() + GG);
+            }
+            check(mgpu_batch_set_damping_cache(m_batch, 0, v, (int32_t)m, (int32_t)times.size(), times.data(),
+                                               flat.data()),
+                  Device::context(), "mgpu_batch_set_damping_cache");
+        }
+    }
+
     void ensure_batch()
     {
         if (m_batch) {
@@ -424,10 +494,18 @@ private:
             sp.push_back(&s);
         }
         using EdgeT    = typename GraphT::EdgeProperty;
+        m_any_npis = false;
+        for (auto* mdl : models) {
+            m_any_npis = m_any_npis || !mdl->parameters.template get<osecir::DynamicNPIsInfectedSymptoms<double>>()
+                                            .get_thresholds()
+                                            .empty();
+        }
         m_arrays       = detail::pack_graph<typename std::decay_t<decltype(*models[0])>, EdgeT>(
-            models, sp, m_graph.edges(), [](const EdgeT& e) -> const MobilityParameters<double>& {
+            models, sp, m_graph.edges(),
+            [](const EdgeT& e) -> const MobilityParameters<double>& {
                 return e.get_parameters();
-            });
+            },
+            m_any_npis ? kNpiDampingPoints : 0);
         mgpu_graph g     = m_arrays.view();
         mgpu_solver_opts o;
         mgpu_default_solver_opts(&o);
@@ -458,6 +536,7 @@ private:
     GraphT m_graph;
     int m_precision   = MGPU_PRECISION_FP64;
     bool m_record     = true;
+    bool m_any_npis   = false;
     mgpu_batch* m_batch = nullptr;
     detail::GraphArrays m_arrays;
 };

@@ -13,6 +13,7 @@
 #define MIOGPU_FACADE_OSECIR_H
 
 #include "core.h"
+#include "dynamic_npis.h"
 
 namespace miogpu
 {
@@ -122,6 +123,15 @@ struct ContactPatterns {
     }
 };
 
+/* Dynamic NPIs on the symptomatic infections (parameters.h DynamicNPIsInfectedSymptoms). */
+template <typename FP = double>
+struct DynamicNPIsInfectedSymptoms {
+    static const char* name()
+    {
+        return "DynamicNPIsInfectedSymptoms";
+    }
+};
+
 /* mio::osecir::Parameters: the node record of include/miogpu_layout.h with the
  * reference's defaults (get_default of every tag), plus the contact patterns. */
 template <typename FP = double>
@@ -153,6 +163,9 @@ public:
     {
         if constexpr (std::is_same<Tag, ContactPatterns<FP>>::value) {
             return static_cast<ContactMatrixGroup&>(m_contacts);
+        }
+        else if constexpr (std::is_same<Tag, DynamicNPIsInfectedSymptoms<FP>>::value) {
+            return static_cast<DynamicNPIs<FP>&>(m_npis);
         }
         else if constexpr (Tag::scalar >= 0) {
             return static_cast<double&>(m_rec[Tag::scalar]);
@@ -245,6 +258,7 @@ private:
     size_t m_G;
     std::vector<double> m_rec;
     ContactMatrixGroup m_contacts;
+    DynamicNPIs<FP> m_npis;
 };
 
 /* Compartment populations per age group (Populations<FP, AgeGroup, InfectionState>),
@@ -442,9 +456,43 @@ public:
         m_result.add_time_point(t0, model.get_initial_values());
     }
 
+    /* osecir::Simulation::advance (model.h:289-367): without dynamic NPIs one
+     * integration to tmax; with them, chunks of at most one day (ending at the
+     * active NPI's end when that comes first), each after the NPI check at its
+     * start, which may add dampings to the contact patterns. */
+    std::vector<FP> advance(FP tmax)
+    {
+        auto& npis = m_model.parameters.template get<DynamicNPIsInfectedSymptoms<FP>>();
+        if (npis.get_thresholds().empty()) {
+            return advance_base(tmax);
+        }
+        FP t = m_result.get_last_time();
+        while (t < tmax) {
+            check_dynamic_npis(npis, m_npi, m_model.parameters.template get<ContactPatterns<FP>>(), t,
+                               get_infections_relative(*this, t, m_result.get_last_value()));
+            FP dt_eff = std::min<FP>(1.0, tmax - t);
+            if (t < m_npi.t_end) {
+                dt_eff = std::min<FP>(dt_eff, m_npi.t_end - t);
+            }
+            advance_base(t + dt_eff);
+            t = t + dt_eff;
+        }
+        return m_result.get_last_value();
+    }
+
+    /* The NPI state: the active threshold and its end (m_dynamic_npi). */
+    const DynamicNPIState& get_dynamic_npi_state() const
+    {
+        return m_npi;
+    }
+    DynamicNPIState& get_dynamic_npi_state()
+    {
+        return m_npi;
+    }
+
     /* Integrates to tmax (SystemIntegrator::advance, integrator.h:184-249) and
      * returns the last value; every accepted step is appended to the result. */
-    std::vector<FP> advance(FP tmax)
+    std::vector<FP> advance_base(FP tmax)
     {
         const FP t0 = m_result.get_last_time();
         if (!(tmax > t0)) {
@@ -518,7 +566,21 @@ private:
     TimeSeries<FP> m_result;
     FP m_dt;
     IntegratorCore m_core;
+    DynamicNPIState m_npi;
 };
+
+/* get_infections_relative (model.h:413-423): the symptomatic infections of the
+ * value vector y relative to the model's total population. */
+template <typename FP>
+FP get_infections_relative(const Simulation<FP>& sim, FP /*t*/, const std::vector<FP>& y)
+{
+    const auto& model = sim.get_model();
+    FP sum_inf        = 0;
+    for (size_t g = 0; g < model.num_groups(); ++g) {
+        sum_inf += y[g * num_compartments + (size_t)InfectionState::InfectedSymptoms];
+    }
+    return sum_inf / model.populations.get_total();
+}
 
 /* mio::FlowSimulation (compartments/flow_simulation.h:36-102): the integrator's
  * state is the accumulated flows; get_result() holds the populations and

@@ -6,6 +6,9 @@
 //   facade_check flows      GPU: simulate_flows (FlowSimulation)
 //   facade_check graph      GPU: make_mobility_sim(...).advance, every boundary
 //   facade_check study      GPU: ParameterStudy over 4 sampled graphs
+//   facade_check npi_logic  host only: implement_dynamic_npis and the NPI check
+//                           of Simulation::advance with the state held fixed
+//   facade_check npi_graph  GPU: a graph simulation with dynamic NPIs (FP64 and mixed)
 //
 // The Python side rebuilds the same inputs from the printed arrays and checks
 // the outputs against the FP64 oracle.
@@ -325,6 +328,173 @@ int mode_study()
     return 0;
 }
 
+void print_dampings(const char* key, const ContactMatrixGroup& c, bool comma = true)
+{
+    std::printf("\"%s\": [", key);
+    for (size_t m = 0; m < c.get_num_matrices(); ++m) {
+        std::printf("%s[", m ? ", " : "");
+        const Dampings& d = c[m].get_dampings();
+        for (size_t i = 0; i < d.size(); ++i) {
+            std::printf("%s[%.17g, %d, %d, %.17g]", i ? ", " : "", d[i].time.get(), d[i].level.get(), d[i].type.get(),
+                        d[i].values[0]);
+        }
+        std::printf("]");
+    }
+    std::printf("]%s\n", comma ? "," : "");
+}
+
+// The chunk loop of osecir::Simulation::advance (model.h:299-365) with the
+// integration left out, as the reference's tests do with a mock simulation.
+void advance_fixed_state(ContactMatrixGroup& c, const DynamicNPIs<double>& npis, DynamicNPIState& st, double t0,
+                         double tmax, double inf_rel)
+{
+    double t = t0;
+    while (t < tmax) {
+        check_dynamic_npis(npis, st, c, t, inf_rel);
+        double dt = std::min(1.0, tmax - t);
+        if (t < st.t_end) {
+            dt = std::min(dt, st.t_end - t);
+        }
+        t += dt;
+    }
+}
+
+int mode_npi_logic()
+{
+    auto constant = [](const std::vector<double>& g) {
+        return Matrix::Constant(g.size(), g.size(), g[0]);
+    };
+    std::printf("{");
+    {
+        // two matrices without dampings, one NPI on both (test_dynamic_npis.cpp implement_empty)
+        ContactMatrixGroup c(2, 2);
+        std::vector<DampingSampling<double>> npis{
+            DampingSampling<double>(0.8, DampingLevel(0), DampingType(0), SimulationTime<double>(0), {0, 1}, {1.0, 1.0})};
+        implement_dynamic_npis(c, npis, SimulationTime<double>(0.45), SimulationTime<double>(0.6), constant);
+        print_dampings("implement_empty", c);
+    }
+    {
+        // test_dynamic_npis.cpp implement: existing dampings of several types and levels
+        ContactMatrixGroup c(2, 3);
+        c[0].add_damping(0.15, DampingLevel(0), DampingType(0), SimulationTime<double>(0.3));
+        c[0].add_damping(0.2, DampingLevel(0), DampingType(0), SimulationTime<double>(0.4));
+        c[0].add_damping(0.25, DampingLevel(0), DampingType(1), SimulationTime<double>(0.5));
+        c[0].add_damping(0.35, DampingLevel(0), DampingType(0), SimulationTime<double>(0.7));
+        c[1].add_damping(0.25, DampingLevel(1), DampingType(1), SimulationTime<double>(0.5));
+        c[1].add_damping(0.45, DampingLevel(0), DampingType(0), SimulationTime<double>(0.9));
+        implement_dynamic_npis(c,
+                               std::vector<DampingSampling<double>>{DampingSampling<double>(
+                                   0.4, DampingLevel(0), DampingType(0), SimulationTime<double>(0), {0, 1}, {1, 1, 1})},
+                               SimulationTime<double>(0.45), SimulationTime<double>(0.6), constant);
+        print_dampings("implement_first", c);
+        implement_dynamic_npis(c,
+                               std::vector<DampingSampling<double>>{DampingSampling<double>(
+                                   0.3, DampingLevel(0), DampingType(0), SimulationTime<double>(0), {0}, {1, 1, 1})},
+                               SimulationTime<double>(0.3), SimulationTime<double>(0.9), constant);
+        print_dampings("implement_second", c);
+    }
+    // one group: 10 symptomatic of 110 against a threshold of 0.05 * base (test_dynamic_npis.cpp secir_*)
+    auto npis_of = [](double value, double base, double delay, double duration) {
+        DynamicNPIs<double> n;
+        n.set_threshold(0.05 * base, {DampingSampling<double>(value, DampingLevel(0), DampingType(0),
+                                                              SimulationTime<double>(0), {0}, {1.0})});
+        n.set_duration(SimulationTime<double>(duration));
+        n.set_base_value(base);
+        n.set_implementation_delay(SimulationTime<double>(delay));
+        return n;
+    };
+    {
+        ContactMatrixGroup c(1, 1);
+        DynamicNPIState st;
+        advance_fixed_state(c, npis_of(1.0, 23000, 0.0, 5.0), st, 0.0, 3.0, 1.0 / 101.0);
+        print_dampings("threshold_safe", c);
+    }
+    {
+        ContactMatrixGroup c(1, 1);
+        DynamicNPIState st;
+        advance_fixed_state(c, npis_of(1.0, 50000, 0.0, 5.0), st, 0.0, 3.0, 10.0 / 110.0);
+        print_dampings("threshold_exceeded", c);
+    }
+    {
+        ContactMatrixGroup c(1, 1);
+        DynamicNPIState st;
+        advance_fixed_state(c, npis_of(0.5, 50000, 3.0, 5.0), st, 0.0, 3.0, 10.0 / 110.0);
+        print_dampings("delayed_t0", c);
+    }
+    {
+        ContactMatrixGroup c(1, 1);
+        DynamicNPIState st;
+        advance_fixed_state(c, npis_of(0.5, 50000, 2.0, 5.0), st, 1.0, 5.0, 10.0 / 110.0);
+        print_dampings("delayed_t1", c);
+    }
+    {
+        ContactMatrixGroup c(1, 1);
+        DynamicNPIState st;
+        advance_fixed_state(c, npis_of(0.5, 50000, 10.0, 5.0), st, 1.0, 4.0, 10.0 / 110.0);
+        print_dampings("delayed_long", c);
+    }
+    {
+        // keep-alive: the threshold stays exceeded past the NPI's end
+        ContactMatrixGroup c(1, 1);
+        DynamicNPIState st;
+        advance_fixed_state(c, npis_of(0.5, 50000, 0.0, 2.0), st, 0.0, 7.0, 10.0 / 110.0);
+        print_dampings("keep_alive", c, false);
+    }
+    std::printf("}\n");
+    return 0;
+}
+
+// Every node of the three-node graph with dynamic NPIs on the symptomatic
+// infections: a threshold most nodes cross within the run, an implementation
+// delay of one day and three-day NPIs (on the exchange grid).
+MobilitySimGraph<Simulation<double>> three_nodes_npi(int G)
+{
+    auto graph = three_nodes(G);
+    DynamicNPIs<double> npis;
+    npis.set_threshold(2.0, {DampingSampling<double>(0.5, DampingLevel(0), DampingType(0), SimulationTime<double>(0),
+                                                     {0}, std::vector<double>((size_t)G, 1.0))});
+    npis.set_threshold(6.0, {DampingSampling<double>(0.8, DampingLevel(2), DampingType(0), SimulationTime<double>(0),
+                                                     {0}, std::vector<double>((size_t)G, 1.0))});
+    npis.set_duration(SimulationTime<double>(3.0));
+    npis.set_implementation_delay(SimulationTime<double>(1.0));
+    npis.set_base_value(1e5);
+    for (auto& n : graph.nodes()) {
+        n.property.get_simulation().get_model().parameters.get<DynamicNPIsInfectedSymptoms<double>>() = npis;
+    }
+    return graph;
+}
+
+int mode_npi_graph()
+{
+    std::printf("{");
+    for (int precision : {MGPU_PRECISION_FP64, MGPU_PRECISION_MIXED}) {
+        auto graph = three_nodes_npi(2);
+        auto a     = arrays_of(graph);
+        auto sim   = make_mobility_sim(0.0, 0.5, std::move(graph));
+        sim.set_precision(precision);
+        sim.advance(12.0);
+        std::vector<double> fin, enacted;
+        for (auto& n : sim.get_graph().nodes()) {
+            auto v = n.property.get_result().get_last_value();
+            fin.insert(fin.end(), v.begin(), v.end());
+            enacted.push_back(n.property.get_simulation().get_dynamic_npi_state().enacted);
+        }
+        if (precision == MGPU_PRECISION_FP64) {
+            print_graph_arrays(a);
+            print_dampings("initial_dampings", three_nodes(2).nodes()[0].property.get_simulation().get_model()
+                                                   .parameters.get<ContactPatterns<double>>());
+        }
+        const char* tag = precision == MGPU_PRECISION_FP64 ? "fp64" : "mixed";
+        char key[64];
+        std::snprintf(key, sizeof key, "final_%s", tag);
+        print_vec(key, fin);
+        std::snprintf(key, sizeof key, "enacted_%s", tag);
+        print_vec(key, enacted, precision == MGPU_PRECISION_FP64);
+    }
+    std::printf("}\n");
+    return 0;
+}
+
 } // namespace
 
 int main(int argc, char** argv)
@@ -348,6 +518,12 @@ int main(int argc, char** argv)
         }
         if (!std::strcmp(mode, "study")) {
             return mode_study();
+        }
+        if (!std::strcmp(mode, "npi_logic")) {
+            return mode_npi_logic();
+        }
+        if (!std::strcmp(mode, "npi_graph")) {
+            return mode_npi_graph();
         }
     }
     catch (const Error& e) {

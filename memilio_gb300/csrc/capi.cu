@@ -14,6 +14,7 @@
 #include <cstring>
 #include <exception>
 #include <functional>
+#include <limits>
 #include <map>
 #include <tuple>
 #include <new>
@@ -297,6 +298,8 @@ struct mgpu_batch {
     int64_t n_max      = 0;
     std::vector<int32_t> N, G, n;
     std::vector<int64_t> node0, edge0, state_off;
+    std::vector<DevGraph> host_graphs; // the graph records as uploaded
+    std::vector<char> damping_shared;  // damping arrays shared with another graph (same host pointers)
     int64_t state_total = 0;
     double* init_state  = nullptr; // initial states (for reset)
     float* init_hi      = nullptr; // the same as float-float pairs (mixed solver)
@@ -789,6 +792,19 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         B.mob_union |= mob_mask[i];
     }
     trace.mark("packing");
+    b->host_graphs = dg;
+    b->damping_shared.assign(num_graphs, 0);
+    {
+        std::map<int64_t, int> users;
+        for (int i = 0; i < num_graphs; ++i) {
+            if (dg[i].K) {
+                ++users[dg[i].dtime_off];
+            }
+        }
+        for (int i = 0; i < num_graphs; ++i) {
+            b->damping_shared[i] = dg[i].K && users[dg[i].dtime_off] > 1;
+        }
+    }
     B.graphs         = b->pool.upload(dg);
     std::vector<GraphRt> h_rt(num_graphs);
     for (auto& r : h_rt) {
@@ -2081,6 +2097,59 @@ int mgpu_batch_get_state(mgpu_batch* b, double* out)
                            b->ctx->stream),
            "d2h state");
         ck(cudaStreamSynchronize(b->ctx->stream), "sync");
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_set_damping_cache(mgpu_batch* b, int32_t graph, int32_t node, int32_t matrix, int32_t num_points,
+                                 const double* times, const double* values)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!times || !values || graph < 0 || graph >= b->num_graphs) {
+            fail(MGPU_INVALID_VALUE, "null array or graph index out of range");
+        }
+        const DevGraph& d = b->host_graphs[graph];
+        if (node < 0 || node >= d.N || matrix < 0 || matrix >= d.M) {
+            fail(MGPU_OUT_OF_RANGE, "node or contact matrix index out of range");
+        }
+        if (d.K == 0 || num_points < 2 || num_points > d.K) {
+            fail(MGPU_INVALID_VALUE, "num_points must lie in [2, num_damping_points of the graph]");
+        }
+        if (b->damping_shared[graph]) {
+            fail(MGPU_UNSUPPORTED, "the graph's damping arrays are shared with another graph of the batch");
+        }
+        for (int k = 1; k < num_points; ++k) {
+            if (!(times[k] >= times[k - 1])) {
+                fail(MGPU_INVALID_VALUE, "damping cache times must be non-decreasing");
+            }
+        }
+        const long GG = (long)d.G * d.G;
+        std::vector<double> t((size_t)d.K), v((size_t)d.K * GG);
+        for (int k = 0; k < d.K; ++k) {
+            const int src = std::min(k, num_points - 1);
+            t[(size_t)k]  = k < num_points ? times[k] : std::numeric_limits<double>::max();
+            std::memcpy(v.data() + (size_t)k * GG, values + (size_t)src * GG, sizeof(double) * GG);
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        cudaStream_t s    = b->ctx->stream;
+        const int64_t row = (int64_t)node * d.M + matrix;
+        double* dt        = const_cast<double*>(b->dev.dtimes) + d.dtime_off + row * d.K;
+        double* dv        = const_cast<double*>(b->dev.dvals) + d.dval_off + row * d.K * GG;
+        ck(cudaMemcpyAsync(dt, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice, s), "h2d damping times");
+        ck(cudaMemcpyAsync(dv, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice, s), "h2d damping values");
+        if (b->dev.dvals_f) {
+            // the mixed solver's FP32 copy (rounded to nearest, as at creation)
+            std::vector<float> vf(v.size());
+            for (size_t i = 0; i < v.size(); ++i) {
+                vf[i] = (float)v[i];
+            }
+            float* dvf = const_cast<float*>(b->dev.dvals_f) + d.dval_off + row * d.K * GG;
+            ck(cudaMemcpyAsync(dvf, vf.data(), sizeof(float) * vf.size(), cudaMemcpyHostToDevice, s), "h2d damping values");
+        }
+        ck(cudaStreamSynchronize(s), "sync");
         return MGPU_OK;
     });
 }

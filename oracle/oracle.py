@@ -178,3 +178,73 @@ def damping_cache(rows, cols, times, levels, types, matrices, cap=64):
                                 _p(out_t), _p(out_m))
     assert k > 0
     return out_t[:k].copy(), out_m[:k].copy()
+
+
+class OrcNpiSampling(ctypes.Structure):
+    _fields_ = [("value", ctypes.c_double), ("level", ctypes.c_int32), ("type", ctypes.c_int32),
+                ("num_matrices", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("matrices", ctypes.POINTER(ctypes.c_int32)), ("group_weights", ctypes.POINTER(ctypes.c_double))]
+
+
+class OrcDynamicNpis(ctypes.Structure):
+    _fields_ = [("num_thresholds", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("thresholds", ctypes.POINTER(ctypes.c_double)), ("first", ctypes.POINTER(ctypes.c_int32)),
+                ("samplings", ctypes.POINTER(OrcNpiSampling)), ("duration", ctypes.c_double),
+                ("delay", ctypes.c_double), ("base_value", ctypes.c_double), ("directive_begin", ctypes.c_double),
+                ("directive_end", ctypes.c_double)]
+
+
+class OrcDamping(ctypes.Structure):
+    _fields_ = [("time", ctypes.c_double), ("level", ctypes.c_int32), ("type", ctypes.c_int32),
+                ("matrix", ctypes.c_int32), ("pad", ctypes.c_int32), ("coeffs", ctypes.POINTER(ctypes.c_double))]
+
+
+def graph_run_npi(g: GraphArrays, t0: float, tmax: float, npis: dict, dampings, dt_exchange: float = 0.5,
+                  dt0: float = 0.1, opts=None):
+    """make_mobility_sim(...).advance(tmax) with the same dynamic NPIs on every node.
+
+    npis: {"thresholds": [(threshold, [(value, level, type, [matrices], [group weights]), ...]), ...],
+           "duration", "delay", "base_value", "directive_begin", "directive_end"};
+    dampings: the nodes' initial contact dampings [(time, level, type, matrix, G x G coefficients), ...].
+    Returns (final [N, 10G], enactments per node [N], stats)."""
+    L = lib()
+    if not hasattr(L.orc_graph_run_npi, "_typed"):
+        P = ctypes.POINTER
+        d = ctypes.c_double
+        L.orc_graph_run_npi.argtypes = [P(MgpuGraph), d, d, d, d, P(MgpuIntegratorOpts), P(OrcDynamicNpis),
+                                        ctypes.c_int, P(OrcDamping), P(d), P(ctypes.c_int32), P(OrcStats)]
+        L.orc_graph_run_npi._typed = True
+    opts = opts or integrator_opts()
+    keep = []
+    samp, first, thr = [], [0], []
+    for threshold, items in npis["thresholds"]:
+        thr.append(threshold)
+        for value, level, typ, mats, weights in items:
+            m = np.ascontiguousarray(mats, np.int32)
+            w = np.ascontiguousarray(weights, np.float64)
+            keep += [m, w]
+            samp.append(OrcNpiSampling(value, level, typ, len(m), 0, m.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                       _p(w)))
+        first.append(len(samp))
+    thr_a = np.ascontiguousarray(thr, np.float64)
+    first_a = np.ascontiguousarray(first, np.int32)
+    samp_a = (OrcNpiSampling * max(len(samp), 1))(*samp)
+    p = OrcDynamicNpis(len(thr), 0, _p(thr_a), first_a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), samp_a,
+                       npis.get("duration", 14.0), npis.get("delay", 0.0), npis.get("base_value", 1.0),
+                       npis.get("directive_begin", np.finfo(np.float64).min),
+                       npis.get("directive_end", np.finfo(np.float64).max))
+    damp = []
+    for time, level, typ, mat, coeffs in dampings:
+        c = np.ascontiguousarray(coeffs, np.float64)
+        keep.append(c)
+        damp.append(OrcDamping(time, level, typ, mat, 0, _p(c)))
+    damp_a = (OrcDamping * max(len(damp), 1))(*damp)
+    fin = np.zeros((g.num_nodes, g.n))
+    cnt = np.zeros(g.num_nodes, np.int32)
+    st = OrcStats()
+    cg = g.as_ctypes()
+    rc = L.orc_graph_run_npi(ctypes.byref(cg), t0, tmax, dt_exchange, dt0, ctypes.byref(opts), ctypes.byref(p),
+                             len(damp), damp_a, _p(fin), cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                             ctypes.byref(st))
+    assert rc == 0
+    return fin, cnt, st.as_dict()

@@ -27,6 +27,7 @@
 #include <cstring>
 #include <limits>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 namespace
@@ -646,6 +647,260 @@ struct GraphRun {
         es.return_mobile = !es.return_mobile;
     }
 
+    // ---- dynamic NPIs (models/ode_secir/model.h:289-367, epidemiology/dynamic_npis.h) ----
+    struct ODamping {
+        double time;
+        int level, type;
+        std::vector<double> m; // G x G
+    };
+    struct NpiNode {
+        std::vector<std::vector<ODamping>> lists; // per contact matrix, sorted by (time, type, level)
+        std::vector<double> ctimes, cvals;        // the node's damping caches [M][K], [M][K][G][G]
+        double thr   = std::numeric_limits<double>::lowest(); // m_dynamic_npi
+        double t_end = 0.0;
+        double total = 0.0; // the model's total population (populations.get_total())
+        int count    = 0;
+    };
+    const orc_dynamic_npis* npis = nullptr;
+    std::vector<int> thr_order; // thresholds in descending order
+    std::vector<NpiNode> npi;
+
+    // floating_point_greater_equal (math/floating_point.h:136-139), rel_tol = DBL_MIN
+    static bool fp_ge(double v1, double v2, double abs_tol)
+    {
+        return !(v1 - v2 < -(abs_tol + std::numeric_limits<double>::min() * std::max(std::fabs(v1), std::fabs(v2))));
+    }
+
+    // Dampings::add_ (damping.h:603-614): sorted by (time, type, level), an equal key replaced
+    static void add_damping(std::vector<ODamping>& l, const ODamping& d)
+    {
+        auto key = [](const ODamping& x) {
+            return std::make_tuple(x.time, x.type, x.level);
+        };
+        auto it = std::lower_bound(l.begin(), l.end(), d, [&](const ODamping& a, const ODamping& b) {
+            return key(a) < key(b);
+        });
+        if (it != l.end() && key(*it) == key(d)) {
+            *it = d;
+        }
+        else {
+            l.insert(it, d);
+        }
+    }
+
+    void init_npis(const orc_dynamic_npis* p, int num_dampings, const orc_damping* dampings)
+    {
+        npis           = p;
+        const int G    = g->num_groups;
+        const int M    = g->num_contact_matrices;
+        thr_order.resize(p->num_thresholds);
+        for (int k = 0; k < p->num_thresholds; ++k) {
+            thr_order[k] = k;
+        }
+        std::stable_sort(thr_order.begin(), thr_order.end(), [&](int a, int b) {
+            return p->thresholds[a] > p->thresholds[b];
+        });
+        npi.resize(g->num_nodes);
+        for (int v = 0; v < g->num_nodes; ++v) {
+            auto& nn = npi[v];
+            nn.lists.assign(M, {});
+            for (int d = 0; d < num_dampings; ++d) {
+                const orc_damping& x = dampings[d];
+                add_damping(nn.lists[x.matrix],
+                            {x.time, x.level, x.type, std::vector<double>(x.coeffs, x.coeffs + (long)G * G)});
+            }
+            for (int j = 0; j < n; ++j) {
+                nn.total += g->init_state[(long)v * n + j];
+            }
+            rebuild_cache(v);
+        }
+    }
+
+    // Dampings::update_cache for every contact matrix of node v, padded to one K
+    void rebuild_cache(int v)
+    {
+        auto& nn      = npi[v];
+        const int G   = g->num_groups;
+        const int M   = g->num_contact_matrices;
+        const long GG = (long)G * G;
+        std::vector<std::vector<double>> ts(M), vs(M);
+        int K = 0;
+        for (int m = 0; m < M; ++m) {
+            const auto& l = nn.lists[m];
+            const int nd  = (int)l.size();
+            std::vector<double> times(nd), mats((size_t)nd * GG);
+            std::vector<int32_t> levels(nd), types(nd);
+            for (int d = 0; d < nd; ++d) {
+                times[d]  = l[d].time;
+                levels[d] = l[d].level;
+                types[d]  = l[d].type;
+                std::copy(l[d].m.begin(), l[d].m.end(), mats.begin() + (long)d * GG);
+            }
+            ts[m].resize(nd + 2);
+            vs[m].resize((size_t)(nd + 2) * GG);
+            const int k = orc_damping_cache(G, G, nd, times.data(), levels.data(), types.data(), mats.data(), nd + 2,
+                                            ts[m].data(), vs[m].data());
+            ts[m].resize(k);
+            vs[m].resize((size_t)k * GG);
+            K = std::max(K, k);
+        }
+        nn.ctimes.clear();
+        nn.cvals.clear();
+        for (int m = 0; m < M; ++m) {
+            while ((int)ts[m].size() < K) {
+                ts[m].push_back(std::numeric_limits<double>::max());
+                vs[m].insert(vs[m].end(), vs[m].end() - GG, vs[m].end());
+            }
+            nn.ctimes.insert(nn.ctimes.end(), ts[m].begin(), ts[m].end());
+            nn.cvals.insert(nn.cvals.end(), vs[m].begin(), vs[m].end());
+        }
+        views[v].K      = K;
+        views[v].dtimes = nn.ctimes.data();
+        views[v].dvals  = nn.cvals.data();
+    }
+
+    // make_contact_damping_matrix (damping_sampling.h:282-288)
+    std::vector<double> contact_damping(const orc_npi_sampling& s) const
+    {
+        const int G = g->num_groups;
+        std::vector<double> m((size_t)G * G);
+        for (int i = 0; i < G; ++i) {
+            for (int j = 0; j < G; ++j) {
+                const double gi = s.value * s.group_weights[i], gj = s.value * s.group_weights[j];
+                m[(size_t)i * G + j] = 1.0 - std::sqrt((1.0 - gi) * (1.0 - gj));
+            }
+        }
+        return m;
+    }
+
+    // get_active_damping (dynamic_npis.h:246-258)
+    std::vector<double> active_damping(const std::vector<ODamping>& l, int level, int type, double t) const
+    {
+        for (size_t k = l.size(); k-- > 0;) {
+            if (l[k].level == level && l[k].type == type && l[k].time <= t) {
+                return l[k].m;
+            }
+        }
+        return std::vector<double>((size_t)g->num_groups * g->num_groups, 0.0);
+    }
+
+    // implement_dynamic_npis (dynamic_npis.h:335-391)
+    void implement(int v, int thr, double begin, double end)
+    {
+        auto& nn = npi[v];
+        for (int s = npis->first[thr]; s < npis->first[thr + 1]; ++s) {
+            const orc_npi_sampling& smp = npis->samplings[s];
+            for (int q = 0; q < smp.num_matrices; ++q) {
+                auto& l                       = nn.lists[smp.matrices[q]];
+                const std::vector<double> act = active_damping(l, smp.level, smp.type, begin);
+                const std::vector<double> act_end = active_damping(l, smp.level, smp.type, end);
+                const std::vector<double> value   = contact_damping(smp);
+                bool implemented                  = false;
+                bool less                         = false;
+                std::vector<double> mx(value.size());
+                for (size_t i = 0; i < value.size(); ++i) {
+                    less  = less || act[i] < value[i];
+                    mx[i] = std::max(value[i], act[i]);
+                }
+                if (less) {
+                    add_damping(l, {begin, smp.level, smp.type, mx});
+                    implemented = true;
+                }
+                std::vector<size_t> idx; // get_damping_indices (dynamic_npis.h:232-244)
+                for (size_t i = 0; i < l.size(); ++i) {
+                    if (l[i].level == smp.level && l[i].type == smp.type && l[i].time > begin && l[i].time < end) {
+                        idx.push_back(i);
+                    }
+                }
+                for (size_t i : idx) {
+                    ODamping d = l[i];
+                    for (size_t k = 0; k < d.m.size(); ++k) {
+                        d.m[k] = std::max(d.m[k], value[k]);
+                    }
+                    add_damping(l, d);
+                    implemented = true;
+                }
+                if (implemented) {
+                    add_damping(l, {end, smp.level, smp.type, act_end});
+                }
+            }
+        }
+        // remove dampings that repeat the previous value of their (level, type)
+        for (auto& l : nn.lists) {
+            for (int i = 0; i < (int)l.size() - 1; ++i) {
+                const size_t cur = l.size() - 1 - (size_t)i;
+                for (size_t k = cur; k-- > 0;) {
+                    if (l[k].level == l[cur].level && l[k].type == l[cur].type) {
+                        if (l[k].m == l[cur].m) {
+                            l.erase(l.begin() + (long)cur);
+                        }
+                        break;
+                    }
+                }
+            }
+        }
+    }
+
+    // The check at the start of a chunk (model.h:299-350).
+    void check_npis(int v, double t)
+    {
+        const orc_dynamic_npis& p = *npis;
+        if (p.num_thresholds == 0) {
+            return;
+        }
+        auto& nn           = npi[v];
+        const double delay = t > 0 ? p.delay : 0.0;
+        if (!(fp_ge(t, p.directive_begin, 1e-10) && t < p.directive_end)) {
+            return;
+        }
+        const auto& y = nodes[v].y;
+        double sum    = 0.0;
+        for (int gi = 0; gi < g->num_groups; ++gi) {
+            sum += y[(long)gi * kC + MGPU_ISY];
+        }
+        const double inf_rel = sum / nn.total * p.base_value;
+        int thr              = -1;
+        for (int k : thr_order) { // get_max_exceeded_threshold: the highest threshold below the value
+            if (inf_rel > p.thresholds[k]) {
+                thr = k;
+                break;
+            }
+        }
+        const bool expired = fp_ge(t, nn.t_end, 1e-10);
+        if (thr < 0 || !(p.thresholds[thr] > nn.thr || expired)) {
+            return;
+        }
+        const bool renewal = expired && !(p.thresholds[thr] > nn.thr);
+        const double eff   = renewal ? 0.0 : delay;
+        if (!(t + eff < p.directive_end)) {
+            return;
+        }
+        const double t_start = t + eff;
+        const double t_end   = std::min(p.directive_end, t_start + p.duration);
+        nn.thr               = p.thresholds[thr];
+        nn.t_end             = t_end;
+        const double tsd     = (!renewal && t_start > 0) ? t_start + 1.0 : t_start;
+        implement(v, thr, tsd, t_end + 1.0);
+        nn.count += 1;
+        rebuild_cache(v);
+    }
+
+    // osecir::Simulation::advance with dynamic NPIs: chunks of at most a day,
+    // ending at the active NPI's end, each after the check at its start.
+    void advance_node_npi(int v, double tmax)
+    {
+        double t = nodes[v].t;
+        while (t < tmax) {
+            check_npis(v, t);
+            double dt_eff = std::min(1.0, tmax - t);
+            if (t < npi[v].t_end) {
+                dt_eff = std::min(dt_eff, npi[v].t_end - t);
+            }
+            advance_node(v, t + dt_eff);
+            t = t + dt_eff;
+        }
+    }
+
     // GraphSimulation::advance (mobility/graph_simulation.h:101-120).
     void run(double t0, double tmax, double dt_exchange, double* out_states)
     {
@@ -657,7 +912,12 @@ struct GraphRun {
                 dt = tmax - t;
             }
             for (int v = 0; v < g->num_nodes; ++v) {
-                advance_node(v, t + dt);
+                if (npis) {
+                    advance_node_npi(v, t + dt);
+                }
+                else {
+                    advance_node(v, t + dt);
+                }
             }
             t += dt;
             for (int e = 0; e < g->num_edges; ++e) {
@@ -852,6 +1112,33 @@ int orc_graph_run(const mgpu_graph* g, double t0, double tmax, double dt_exchang
     run.run(t0, tmax, dt_exchange, out_states);
     if (final_state) {
         run.write_final(final_state);
+    }
+    run.add_stats(stats);
+    return 0;
+}
+
+int orc_graph_run_npi(const mgpu_graph* g, double t0, double tmax, double dt_exchange, double dt0,
+                      const mgpu_integrator_opts* opts, const orc_dynamic_npis* npis, int num_dampings,
+                      const orc_damping* dampings, double* final_state, int32_t* npi_count, orc_stats* stats)
+{
+    if (!graph_ok(g) || !opts || !npis || !(dt_exchange > 0) || (num_dampings > 0 && !dampings)) {
+        return -1;
+    }
+    for (int d = 0; d < num_dampings; ++d) {
+        if (dampings[d].matrix < 0 || dampings[d].matrix >= g->num_contact_matrices || !dampings[d].coeffs) {
+            return -1;
+        }
+    }
+    GraphRun run(g, t0, dt0, *opts);
+    run.init_npis(npis, num_dampings, dampings);
+    run.run(t0, tmax, dt_exchange, nullptr);
+    if (final_state) {
+        run.write_final(final_state);
+    }
+    if (npi_count) {
+        for (int v = 0; v < g->num_nodes; ++v) {
+            npi_count[v] = run.npi[v].count;
+        }
     }
     run.add_stats(stats);
     return 0;

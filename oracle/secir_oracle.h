@@ -82,6 +82,39 @@ int orc_damping_cache(int rows, int cols, int num_dampings, const double* times,
                       const int32_t* types, const double* matrices, int cap, double* out_times,
                       double* out_matrices);
 
+/* Dynamic NPIs (epidemiology/dynamic_npis.h, damping_sampling.h): one NPI of a
+ * threshold, a damping of value * group weights on the listed contact
+ * matrices; thresholds in any order with their NPIs samplings[first[k] ..
+ * first[k+1]). */
+typedef struct orc_npi_sampling {
+    double value;
+    int32_t level, type, num_matrices, pad;
+    const int32_t* matrices;
+    const double* group_weights; /* [G] */
+} orc_npi_sampling;
+typedef struct orc_dynamic_npis {
+    int32_t num_thresholds, pad;
+    const double* thresholds;
+    const int32_t* first; /* [num_thresholds + 1] */
+    const orc_npi_sampling* samplings;
+    double duration, delay, base_value, directive_begin, directive_end;
+} orc_dynamic_npis;
+/* One contact damping of a node's initial list (the list every node starts with). */
+typedef struct orc_damping {
+    double time;
+    int32_t level, type, matrix, pad;
+    const double* coeffs; /* [G][G] */
+} orc_damping;
+
+/* orc_graph_run with the same dynamic NPIs on every node (osecir::Simulation::
+ * advance, models/ode_secir/model.h:289-367, reached through
+ * SimulationNode::advance): the nodes' contact dampings start from `dampings`
+ * (the graph's damping caches are not used) and change as NPIs are enacted.
+ * npi_count [N] receives the number of enactments per node. */
+int orc_graph_run_npi(const mgpu_graph* g, double t0, double tmax, double dt_exchange, double dt0,
+                      const mgpu_integrator_opts* opts, const orc_dynamic_npis* npis, int num_dampings,
+                      const orc_damping* dampings, double* final_state, int32_t* npi_count, orc_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

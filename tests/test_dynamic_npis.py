@@ -1,0 +1,122 @@
+"""Dynamic NPIs (osecir::Simulation::advance, cpp/models/ode_secir/model.h:289-367;
+implement_dynamic_npis and DynamicNPIs, cpp/memilio/epidemiology/dynamic_npis.h).
+
+Host-only: the facade's damping lists after implement_dynamic_npis and after the
+NPI check of Simulation::advance with the state held fixed equal the
+expectations of the reference's tests (cpp/tests/test_dynamic_npis.cpp:
+implement_empty :145-170, implement :172-317, secir_threshold_safe :421-450,
+secir_threshold_exceeded :452-482, secir_delayed_implementation :484-539). The
+oracle's restatement runs a graph without thresholds exactly as without NPIs.
+GPU: a graph simulation with NPIs through the facade (device solver, caches
+replaced with mgpu_batch_set_damping_cache) against the oracle.
+"""
+import json
+import subprocess
+
+import numpy as np
+import pytest
+
+from memilio_gb300 import build as B
+from memilio_gb300 import layout as L
+from memilio_gb300 import workloads as W
+from oracle import oracle as O
+
+from tests.test_facade import graph_of, scaled
+
+
+@pytest.fixture(scope="module")
+def programs():
+    return B.build_facade()
+
+
+def run(programs, mode):
+    r = subprocess.run([programs["facade_check"], mode], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    return json.loads(r.stdout)
+
+
+def lists(d):
+    """[(time, level, type, value)] per matrix, times rounded for comparison."""
+    return [[(round(t, 12), lv, ty, round(v, 12)) for t, lv, ty, v in m] for m in d]
+
+
+def test_implement_dynamic_npis_matches_reference_tests(programs):
+    d = run(programs, "npi_logic")
+    assert lists(d["implement_empty"]) == [[(0.45, 0, 0, 0.8), (0.6, 0, 0, 0.0)]] * 2
+    assert lists(d["implement_first"]) == [
+        [(0.3, 0, 0, 0.15), (0.4, 0, 0, 0.2), (0.45, 0, 0, 0.4), (0.5, 0, 1, 0.25), (0.6, 0, 0, 0.2),
+         (0.7, 0, 0, 0.35)],
+        [(0.45, 0, 0, 0.4), (0.5, 1, 1, 0.25), (0.6, 0, 0, 0.0), (0.9, 0, 0, 0.45)]]
+    assert lists(d["implement_second"]) == [
+        [(0.3, 0, 0, 0.3), (0.45, 0, 0, 0.4), (0.5, 0, 1, 0.25), (0.6, 0, 0, 0.3), (0.7, 0, 0, 0.35)],
+        [(0.45, 0, 0, 0.4), (0.5, 1, 1, 0.25), (0.6, 0, 0, 0.0), (0.9, 0, 0, 0.45)]]
+
+
+def contact_at(dampings, t, baseline=1.0):
+    """ContactMatrixGroup::get_matrix_at of a 1 x 1 matrix with these dampings."""
+    if not dampings:
+        return baseline
+    times = [x[0] for x in dampings]
+    ct, cm = O.damping_cache(1, 1, times, [x[1] for x in dampings], [x[2] for x in dampings],
+                             np.array([x[3] for x in dampings]).reshape(-1, 1, 1))
+    ub = int(np.searchsorted(ct, t, side="right"))
+    lo, hi = cm[ub - 1, 0, 0], cm[ub, 0, 0]
+    x0, x1 = ct[ub] - 1.0, ct[ub]
+    d = lo if t <= x0 else (hi if t >= x1 else 0.5 * (lo - hi) * np.cos(np.pi / (x1 - x0) * (t - x0)) + 0.5 * (lo + hi))
+    return baseline - d * baseline
+
+
+def test_npi_check_matches_reference_tests(programs):
+    d = run(programs, "npi_logic")
+    assert d["threshold_safe"] == [[]]
+    assert len(d["threshold_exceeded"][0]) == 2
+    t0 = d["delayed_t0"][0]  # t0 = 0: no delay at the start, full effect at once
+    for t in (0.0, 1.0, 3.0):
+        assert contact_at(t0, t) == 0.5
+    t1 = d["delayed_t1"][0]  # t0 = 1, delay 2: ramp over [3, 4]
+    assert contact_at(t1, 3.0) == 1.0 and contact_at(t1, 4.0) == 0.5
+    tl = d["delayed_long"][0]  # delay 10: ramp over [11, 12]
+    assert contact_at(tl, 11.0) == 1.0 and contact_at(tl, 12.0) == 0.5
+    # keep-alive: renewed at expiry without a dip
+    ka = d["keep_alive"][0]
+    assert all(contact_at(ka, t) == 0.5 for t in np.arange(0.0, 8.01, 0.25))
+
+
+def test_oracle_without_thresholds_equals_plain_run():
+    g = W.mobility_graph(seed=5, N=8, G=2, out_degree=3)
+    _, fin0, _ = O.graph_run(g, 0.0, 10.0, record=False)
+    fin, cnt, _ = O.graph_run_npi(g, 0.0, 10.0, {"thresholds": []}, [])
+    np.testing.assert_array_equal(fin, fin0)
+    assert not cnt.any()
+
+
+def test_oracle_npis_enact_and_conserve():
+    g = W.mobility_graph(seed=5, N=8, G=2, out_degree=3)
+    npis = {"thresholds": [(1e-6, [(0.5, 0, 0, [0], [1.0, 1.0])])], "duration": 3.0, "delay": 1.0}
+    fin, cnt, _ = O.graph_run_npi(g, 0.0, 10.0, npis, [])
+    _, fin0, _ = O.graph_run(g, 0.0, 10.0, record=False)
+    assert cnt.min() >= 1
+    np.testing.assert_allclose(fin.sum(), g.init_state.sum(), rtol=1e-12)
+    # fewer contacts, fewer infections
+    assert fin.reshape(8, 2, 10)[..., L.S].sum() > fin0.reshape(8, 2, 10)[..., L.S].sum()
+
+
+def npis_of_facade_graph(G):
+    """The NPIs of facade_check's npi_graph mode (three_nodes_npi)."""
+    ones = [1.0] * G
+    return {"thresholds": [(2.0, [(0.5, 0, 0, [0], ones)]), (6.0, [(0.8, 2, 0, [0], ones)])],
+            "duration": 3.0, "delay": 1.0, "base_value": 1e5}
+
+
+@pytest.mark.gpu
+def test_graph_simulation_with_npis_matches_oracle(programs):
+    d = run(programs, "npi_graph")
+    g = graph_of(d)
+    G = g.num_groups
+    init = [(t, lv, ty, m, np.full((G, G), v)) for m, lst in enumerate(d["initial_dampings"]) for t, lv, ty, v in lst]
+    fin, cnt, _ = O.graph_run_npi(g, 0.0, 12.0, npis_of_facade_graph(G), init)
+    assert cnt.sum() > 0  # NPIs were enacted in this run
+    np.testing.assert_array_equal(np.array(d["enacted_fp64"]), cnt)
+    assert scaled(d["final_fp64"], fin, G) < 1e-10
+    np.testing.assert_array_equal(np.array(d["enacted_mixed"]), cnt)
+    assert scaled(d["final_mixed"], fin, G) < 1e-5
