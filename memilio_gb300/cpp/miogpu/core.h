@@ -617,6 +617,58 @@ private:
     std::vector<FP> m_v;
 };
 
+/* interpolate_simulation_result (data/analyze_result.h:186-268): the values at
+ * the given sorted times, linear between the neighbouring time points
+ * (linear_interpolation, math/interpolation.h:44-48); a first (last) time at or
+ * before (after) the series takes its first (last) value. */
+template <typename FP>
+TimeSeries<FP> interpolate_simulation_result(const TimeSeries<FP>& r, const std::vector<FP>& times)
+{
+    TimeSeries<FP> out(r.get_num_elements());
+    if (times.empty() || r.get_num_time_points() == 0) {
+        return out;
+    }
+    const size_t n = r.get_num_elements();
+    size_t k       = 0;
+    if (r.get_time(0) >= times[0]) {
+        out.add_time_point(times[0], r.value_ptr(0));
+        ++k;
+    }
+    std::vector<FP> v(n);
+    for (size_t i = 0; i + 1 < r.get_num_time_points() && k < times.size();) {
+        if (r.get_time(i) < times[k] && r.get_time(i + 1) >= times[k]) {
+            const FP w    = (times[k] - r.get_time(i)) / (r.get_time(i + 1) - r.get_time(i));
+            const FP* y1  = r.value_ptr(i);
+            const FP* y2  = r.value_ptr(i + 1);
+            for (size_t j = 0; j < n; ++j) {
+                v[j] = y1[j] + w * (y2[j] - y1[j]);
+            }
+            out.add_time_point(times[k], v);
+            ++k;
+        }
+        else {
+            ++i;
+        }
+    }
+    if (k < times.size() && r.get_last_time() < times[k]) {
+        out.add_time_point(times[k], r.get_last_value());
+    }
+    return out;
+}
+
+/* The same at every whole day from ceil(t0 - abs_tol) to floor(tmax + abs_tol). */
+template <typename FP>
+TimeSeries<FP> interpolate_simulation_result(const TimeSeries<FP>& r, FP abs_tol = FP(100) * FP(1e-12))
+{
+    const int day0    = (int)std::ceil(r.get_time(0) - abs_tol);
+    const int day_max = (int)std::floor(r.get_last_time() + abs_tol);
+    std::vector<FP> tps;
+    for (int d = day0; d <= day_max; ++d) {
+        tps.push_back(FP(d));
+    }
+    return interpolate_simulation_result(r, tps);
+}
+
 /* The integrator core of a simulation (ControlledStepperWrapper with Cash-Karp
  * 5(4), stepper_wrapper.h:56-202, or RKIntegratorCore, adapt_rk.h). */
 struct IntegratorCore {

@@ -9,6 +9,7 @@
 //   facade_check npi_logic  host only: implement_dynamic_npis and the NPI check
 //                           of Simulation::advance with the state held fixed
 //   facade_check npi_graph  GPU: a graph simulation with dynamic NPIs (FP64 and mixed)
+//   facade_check interpolate  host only: interpolate_simulation_result of small series
 //
 // The Python side rebuilds the same inputs from the printed arrays and checks
 // the outputs against the FP64 oracle.
@@ -495,6 +496,52 @@ int mode_npi_graph()
     return 0;
 }
 
+void print_series(const char* key, const TimeSeries<double>& ts, bool comma = true)
+{
+    std::printf("\"%s\": {", key);
+    std::vector<double> t, v;
+    for (size_t i = 0; i < ts.get_num_time_points(); ++i) {
+        t.push_back(ts.get_time(i));
+        const double* p = ts.value_ptr(i);
+        v.insert(v.end(), p, p + ts.get_num_elements());
+    }
+    print_vec("t", t);
+    print_vec("v", v, false);
+    std::printf("}%s\n", comma ? "," : "");
+}
+
+TimeSeries<double> series(size_t n, const std::vector<std::pair<double, std::vector<double>>>& pts)
+{
+    TimeSeries<double> ts(n);
+    for (auto& p : pts) {
+        ts.add_time_point(p.first, p.second);
+    }
+    return ts;
+}
+
+int mode_interpolate()
+{
+    // the series of the reference's tests (cpp/tests/test_analyze_result.cpp:68-175)
+    std::printf("{");
+    print_series("simple", interpolate_simulation_result(series(
+                               1, {{0.0, {0.1}}, {0.5, {0.2}}, {1.5, {0.3}}, {2.5, {0.4}}, {3.5, {0.5}}, {4.5, {0.6}},
+                                   {5.5, {0.7}}})));
+    print_series("complex", interpolate_simulation_result(series(2, {{0.0, {1.0, 2.0}}, {1.5, {3.0, 10.0}},
+                                                                     {2.1, {5.0, 3.0}}})));
+    print_series("exact_day", interpolate_simulation_result(series(
+                                  1, {{0.0, {0.0}}, {0.5, {1.0}}, {1.0, {2.0}}, {2.1, {3.0}}, {3.0, {4.0}}})));
+    print_series("default_tol",
+                 interpolate_simulation_result(series(1, {{0.0 + 1e-15, {0.0}}, {1.0, {0.0}}, {2.0 - 1e-15, {0.0}}})));
+    print_series("given_tol", interpolate_simulation_result(
+                                  series(1, {{0.0 + 1e-2, {0.0}}, {1.0, {0.0}}, {2.0 - 1e-3, {0.0}}}), 5e-3));
+    print_series("chosen", interpolate_simulation_result(series(1, {{0.1, {0.0}}, {0.9, {1.0}}, {1.4, {2.0}},
+                                                                    {2.5, {3.0}}, {3.0, {4.0}}}),
+                                                         std::vector<double>{0.2, 0.6, 1.0, 1.3, 2.4}),
+                 false);
+    std::printf("}\n");
+    return 0;
+}
+
 } // namespace
 
 int main(int argc, char** argv)
@@ -524,6 +571,9 @@ int main(int argc, char** argv)
         }
         if (!std::strcmp(mode, "npi_graph")) {
             return mode_npi_graph();
+        }
+        if (!std::strcmp(mode, "interpolate")) {
+            return mode_interpolate();
         }
     }
     catch (const Error& e) {

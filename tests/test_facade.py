@@ -149,3 +149,19 @@ def test_example_program_runs():
     assert len(lines) == 2 and all("t=30.0" in l for l in lines)
     totals = [float(l.split("(total ")[1].split(",")[0]) for l in lines]
     assert abs(sum(totals) - 30000.0) < 1e-6  # 20000 + 10000 residents, conserved by the exchange
+
+
+def test_interpolate_simulation_result_matches_reference_tests(programs):
+    # expectations of cpp/tests/test_analyze_result.cpp:68-175
+    d = run(programs, "interpolate")
+    near = lambda a, b: np.testing.assert_allclose(a, b, rtol=0, atol=1e-12)
+    near(d["simple"]["t"], [0, 1, 2, 3, 4, 5])
+    near(d["simple"]["v"], [0.1, 0.25, 0.35, 0.45, 0.55, 0.65])
+    near(d["complex"]["t"], [0, 1, 2])
+    near(d["complex"]["v"], [1, 2, 1 + 2 * 2 / 3, 2 + 8 * 2 / 3, 3 + 2 * 5 / 6, 10 - 7 * 5 / 6])
+    near(d["exact_day"]["t"], [0, 1, 2, 3])
+    near(d["exact_day"]["v"][1:3], [2.0, 2.0 + 10 / 11])
+    near(d["default_tol"]["t"], [0, 1, 2])
+    near(d["given_tol"]["t"], [1, 2])
+    near(d["chosen"]["t"], [0.2, 0.6, 1.0, 1.3, 2.4])
+    near(d["chosen"]["v"], [1 / 8, 5 / 8, 1.2, 1.8, 2 + 10 / 11])
