@@ -120,3 +120,47 @@ def test_graph_simulation_with_npis_matches_oracle(programs):
     assert scaled(d["final_fp64"], fin, G) < 1e-10
     np.testing.assert_array_equal(np.array(d["enacted_mixed"]), cnt)
     assert scaled(d["final_mixed"], fin, G) < 1e-5
+
+
+@pytest.mark.gpu
+def test_set_damping_cache_between_advances():
+    from memilio_gb300 import _native as N
+    ctx = N.Context(0)
+    g1 = W.mobility_graph(seed=7, N=6, G=2, out_degree=3)
+    # g2: a second damping at day 4 on node 2 (same cache as g1 before day 3)
+    t1, v1 = g1.damping_times[2, 0], g1.damping_values[2, 0]
+    G = g1.num_groups
+    t_new = np.array([t1[0], 4.0, t1[1], t1[2]])
+    v_new = np.stack([v1[0], np.full((G, G), 0.25), v1[1] + 0.25 - v1[1] * 0.25, v1[2] + 0.25 - v1[2] * 0.25])
+    assert t1.size == 3 and t1[1] > 5.0
+    K = 4  # room for the extra point: pad every cache by repeating its last point
+    pad = lambda g: L.GraphArrays(G, g.params, g.contact_baseline, g.contact_minimum,
+                                  np.concatenate([g.damping_times, np.full(g.damping_times.shape[:2] + (1,), L.DBL_MAX)], 2),
+                                  np.concatenate([g.damping_values, g.damping_values[:, :, -1:]], 2),
+                                  g.init_state, g.edge_src, g.edge_dst, g.edge_coeff_baseline)
+    a = pad(g1)
+    b = pad(g1)
+    b.damping_times[2, 0] = t_new
+    b.damping_values[2, 0] = v_new
+    for prec in (N.PRECISION_FP64, N.PRECISION_MIXED):
+        ba = N.Batch(ctx, [a], 0.0, N.solver_opts(precision=prec))
+        bb = N.Batch(ctx, [b], 0.0, N.solver_opts(precision=prec))
+        ba.advance(2.0)
+        ba.set_damping_cache(0, 2, 0, t_new, v_new)
+        ba.advance(8.0)
+        bb.advance(8.0)
+        if prec == N.PRECISION_FP64:
+            np.testing.assert_array_equal(ba.states()[0], bb.states()[0])
+        else:
+            # (the FP32 contact rows of the two caches round differently before day 3)
+            assert scaled(ba.states()[0], bb.states()[0], G) < 1e-6
+        with pytest.raises(N.MgpuError):
+            ba.set_damping_cache(0, 2, 0, np.zeros(K + 1), np.zeros((K + 1, G, G)))  # more points than room
+        ba.close()
+        bb.close()
+    # a damping cache shared by two graphs of a batch cannot be replaced for one of them
+    bs = N.Batch(ctx, [a, a], 0.0, N.solver_opts())
+    with pytest.raises(N.MgpuError):
+        bs.set_damping_cache(0, 2, 0, t_new, v_new)
+    bs.close()
+    ctx.close()
