@@ -245,6 +245,26 @@ int mgpu_batch_set_state(mgpu_batch* batch, const double* state);
  */
 int mgpu_batch_set_damping_cache(mgpu_batch* batch, int32_t graph, int32_t node, int32_t matrix, int32_t num_points,
                                  const double* times, const double* values);
+/*
+ * The same for the mobility coefficients of one edge (MobilityEdge's
+ * coefficient dampings, e.g. after the edge's dynamic NPIs were enacted,
+ * mobility/metapopulation_mobility_instant.h:549-566): times [num_points],
+ * values [num_points][10 G], num_points <= the graph's num_edge_damping_points;
+ * MGPU_UNSUPPORTED if the graph shares its edge coefficient arrays with another.
+ */
+int mgpu_batch_set_edge_damping_cache(mgpu_batch* batch, int32_t graph, int32_t edge, int32_t num_points,
+                                      const double* times, const double* values);
+/*
+ * One exchange interval in two halves (GraphSimulation::advance,
+ * mobility/graph_simulation.h:101-120: all nodes advance, then all edges
+ * apply): step_nodes begins the next interval towards tmax (or tmax_per_graph)
+ * and solves the nodes to its end; between the halves the node states are the
+ * states before the exchange (SimulationNode::get_last_state) and edge caches
+ * may be replaced; step_exchange applies the exchange that ends the interval.
+ * Batched precisions only. mgpu_batch_advance refuses while a half is pending.
+ */
+int mgpu_batch_step_nodes(mgpu_batch* batch, double tmax, const double* tmax_per_graph);
+int mgpu_batch_step_exchange(mgpu_batch* batch);
 int mgpu_batch_get_stats(mgpu_batch* batch, mgpu_stats* out);
 /*
  * Asynchronous advance, for request loops that keep several batches in flight

@@ -28,7 +28,8 @@ PRECISION_MIXED = 2
 # every entry point declared in include/miogpu.h
 EXPORTED = ["mgpu_default_solver_opts", "mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_set_memory_budget",
             "mgpu_eval_rhs", "mgpu_simulate", "mgpu_batch_create", "mgpu_batch_advance", "mgpu_batch_get_state",
-            "mgpu_batch_get_time", "mgpu_batch_set_state", "mgpu_batch_set_damping_cache", "mgpu_batch_get_stats", "mgpu_batch_get_timing",
+            "mgpu_batch_get_time", "mgpu_batch_set_state", "mgpu_batch_set_damping_cache", "mgpu_batch_set_edge_damping_cache",
+            "mgpu_batch_step_nodes", "mgpu_batch_step_exchange", "mgpu_batch_get_stats", "mgpu_batch_get_timing",
             "mgpu_batch_device_bytes", "mgpu_batch_reset", "mgpu_batch_destroy", "mgpu_simulate_final_noalloc",
             "mgpu_batch_launch", "mgpu_batch_query", "mgpu_batch_autotune", "mgpu_simulate_dt", "mgpu_simulate_flows", "mgpu_batch_ensemble_stats", "mgpu_batch_get_graph_state", "mgpu_batch_estimate_bytes",
             "mgpu_default_server_opts", "mgpu_server_create", "mgpu_server_destroy", "mgpu_server_submit",
@@ -134,6 +135,9 @@ def lib():
     L.mgpu_batch_get_time.argtypes = [vp, P(d)]
     L.mgpu_batch_set_state.argtypes = [vp, P(d)]
     L.mgpu_batch_set_damping_cache.argtypes = [vp] + [ctypes.c_int32] * 4 + [P(d), P(d)]
+    L.mgpu_batch_set_edge_damping_cache.argtypes = [vp] + [ctypes.c_int32] * 3 + [P(d), P(d)]
+    L.mgpu_batch_step_nodes.argtypes = [vp, d, P(d)]
+    L.mgpu_batch_step_exchange.argtypes = [vp]
     L.mgpu_batch_get_stats.argtypes = [vp, P(MgpuStats)]
     L.mgpu_batch_get_timing.argtypes = [vp, P(MgpuTiming)]
     L.mgpu_batch_reset.argtypes = [vp, d]
@@ -308,6 +312,18 @@ class Batch:
         flat = np.ascontiguousarray(flat, np.float64)
         assert flat.size == self.total
         self.ctx.check(lib().mgpu_batch_set_state(self._h, _dp(flat)))
+
+    def set_edge_damping_cache(self, graph: int, edge: int, times, values):
+        """mgpu_batch_set_edge_damping_cache: times [K'], values [K'][10G]."""
+        t = np.ascontiguousarray(times, np.float64)
+        v = np.ascontiguousarray(values, np.float64)
+        self.ctx.check(lib().mgpu_batch_set_edge_damping_cache(self._h, graph, edge, t.shape[0], _dp(t), _dp(v)))
+
+    def step_nodes(self, tmax: float):
+        self.ctx.check(lib().mgpu_batch_step_nodes(self._h, float(tmax), ctypes.POINTER(ctypes.c_double)()))
+
+    def step_exchange(self):
+        self.ctx.check(lib().mgpu_batch_step_exchange(self._h))
 
     def set_damping_cache(self, graph: int, node: int, matrix: int, times, values):
         """mgpu_batch_set_damping_cache: times [K'], values [K'][G][G]."""

@@ -231,8 +231,8 @@ inline bool equal(const Matrix& a, const Matrix& b)
  * NPI raises the active damping of its (level, type) to at least its value over
  * [begin, end) and restores the previous one at end; afterwards dampings that
  * repeat the previous value of their (level, type) are removed. */
-template <typename FP, class MakeMatrix>
-void implement_dynamic_npis(ContactMatrixGroup& group, const std::vector<DampingSampling<FP>>& npis,
+template <typename FP, class Group, class MakeMatrix>
+void implement_dynamic_npis(Group& group, const std::vector<DampingSampling<FP>>& npis,
                             SimulationTime<double> begin, SimulationTime<double> end, MakeMatrix&& make_matrix)
 {
     for (const auto& npi : npis) {
@@ -289,6 +289,18 @@ void implement_dynamic_npis(ContactMatrixGroup& group, const std::vector<Damping
     });
 }
 
+/* make_mobility_damping_vector (damping_sampling.h:290-306): the per-group values
+ * spread over each group's entries of a mobility coefficient vector of size n. */
+inline Matrix make_mobility_damping_vector(size_t n, const std::vector<double>& g)
+{
+    Matrix m(n, 1);
+    const size_t per = n / g.size();
+    for (size_t i = 0; i < n; ++i) {
+        m[i] = g[i / per];
+    }
+    return m;
+}
+
 /* floating_point_greater_equal (math/floating_point.h:136-139) with rel_tol = DBL_MIN. */
 inline bool fp_greater_equal(double v1, double v2, double abs_tol)
 {
@@ -339,6 +351,36 @@ bool check_dynamic_npis(const DynamicNPIs<FP>& npis, DynamicNPIState& st, Contac
     const double t_start_damping = (!renewal && t_start > 0) ? t_start + 1.0 : t_start;
     implement_dynamic_npis(contacts, exceeded->second, SimulationTime<double>(t_start_damping),
                            SimulationTime<double>(t_end + 1.0));
+    return true;
+}
+
+/* The dynamic-NPI check of a mobility edge at the start of its exchange
+ * (MobilityEdge::apply_mobility, metapopulation_mobility_instant.h:549-566):
+ * with `inf_rel` the relative symptomatic infections of the edge's source
+ * before the exchange, enact the NPIs of the highest exceeded threshold on the
+ * edge's coefficients over [t, t + duration) if they are stronger than the
+ * active ones or those expired. Returns true if the coefficients changed. */
+template <typename FP, class CoefficientGroup>
+bool check_edge_dynamic_npis(const DynamicNPIs<FP>& npis, DynamicNPIState& st, CoefficientGroup& coeffs, double t,
+                             double inf_rel)
+{
+    if (npis.get_thresholds().empty()) {
+        return false;
+    }
+    auto exceeded      = npis.get_max_exceeded_threshold(inf_rel * npis.get_base_value());
+    const bool expired = fp_greater_equal(t, st.t_end, 1e-10);
+    if (exceeded == npis.get_thresholds().end() || !(exceeded->first > st.threshold || expired)) {
+        return false;
+    }
+    const double t_end = t + npis.get_duration().get();
+    st.threshold       = exceeded->first;
+    st.t_end           = t_end;
+    st.enacted += 1;
+    const size_t n = coeffs[0].rows();
+    implement_dynamic_npis(coeffs, exceeded->second, SimulationTime<double>(t), SimulationTime<double>(t_end),
+                           [n](const std::vector<double>& g) {
+                               return make_mobility_damping_vector(n, g);
+                           });
     return true;
 }
 

@@ -155,9 +155,19 @@ public:
     {
         return m_coeffs;
     }
+    /* The edge's dynamic NPIs on the source's symptomatic infections (:237-244). */
+    DynamicNPIs<FP>& get_dynamic_npis_infected()
+    {
+        return m_dynamic_npis;
+    }
+    const DynamicNPIs<FP>& get_dynamic_npis_infected() const
+    {
+        return m_dynamic_npis;
+    }
 
 private:
     MobilityCoefficientGroup m_coeffs;
+    DynamicNPIs<FP> m_dynamic_npis;
 };
 
 /* mio::MobilityEdge (:300-623): the edge property of a simulation graph. */
@@ -177,9 +187,23 @@ public:
     {
         return m_params;
     }
+    MobilityParameters<FP>& get_parameters()
+    {
+        return m_params;
+    }
+    /* The edge's NPI state (m_dynamic_npi). */
+    DynamicNPIState& get_dynamic_npi_state()
+    {
+        return m_npi;
+    }
+    const DynamicNPIState& get_dynamic_npi_state() const
+    {
+        return m_npi;
+    }
 
 private:
     MobilityParameters<FP> m_params;
+    DynamicNPIState m_npi;
 };
 
 /* mio::SimulationNode (:39-101): a node's simulation and its results. */
@@ -262,7 +286,7 @@ struct GraphArrays {
 template <class ModelT, class EdgeT>
 GraphArrays pack_graph(const std::vector<const ModelT*>& models, const std::vector<const std::vector<double>*>& states,
                        const std::vector<Edge<EdgeT>>& edges, std::function<const MobilityParameters<double>&(const EdgeT&)> params_of,
-                       int extra_damping_points = 0)
+                       int extra_damping_points = 0, int extra_edge_damping_points = 0)
 {
     GraphArrays a;
     a.N = (int)models.size();
@@ -334,6 +358,32 @@ GraphArrays pack_graph(const std::vector<const ModelT*>& models, const std::vect
         ecs.push_back(&c);
     }
     a.Ke = edges.empty() ? 0 : flatten_damping_caches(ecs, a.edge_damping_times, a.edge_damping_values);
+    if (extra_edge_damping_points > 0 && !edges.empty()) {
+        // room for coefficient dampings added at run time: pad every edge's cache
+        const int Ke = std::max(a.Ke, 2) + extra_edge_damping_points;
+        std::vector<double> t, v;
+        for (size_t e = 0; e < edges.size(); ++e) {
+            for (int k = 0; k < Ke; ++k) {
+                if (a.Ke && k < a.Ke) {
+                    t.push_back(a.edge_damping_times[e * (size_t)a.Ke + (size_t)k]);
+                    v.insert(v.end(), a.edge_damping_values.begin() + (long)((e * (size_t)a.Ke + (size_t)k) * n),
+                             a.edge_damping_values.begin() + (long)((e * (size_t)a.Ke + (size_t)k + 1) * n));
+                }
+                else if (a.Ke) {
+                    t.push_back(std::numeric_limits<double>::max());
+                    v.insert(v.end(), a.edge_damping_values.begin() + (long)((e * (size_t)a.Ke + (size_t)a.Ke - 1) * n),
+                             a.edge_damping_values.begin() + (long)((e * (size_t)a.Ke + (size_t)a.Ke) * n));
+                }
+                else {
+                    t.push_back(k == 0 ? std::numeric_limits<double>::lowest() : std::numeric_limits<double>::max());
+                    v.insert(v.end(), n, 0.0);
+                }
+            }
+        }
+        a.Ke                  = Ke;
+        a.edge_damping_times  = std::move(t);
+        a.edge_damping_values = std::move(v);
+    }
     return a;
 }
 
@@ -386,7 +436,15 @@ public:
             if (m_any_npis) {
                 apply_dynamic_npis(t_next);
             }
-            check(mgpu_batch_advance(m_batch, t_next, nullptr), ctx, "mgpu_batch_advance");
+            if (m_any_edge_npis) {
+                // the edges' NPI checks see the nodes' states between their solves and the exchange
+                check(mgpu_batch_step_nodes(m_batch, t_next, nullptr), ctx, "mgpu_batch_step_nodes");
+                apply_edge_npis(t_next);
+                check(mgpu_batch_step_exchange(m_batch), ctx, "mgpu_batch_step_exchange");
+            }
+            else {
+                check(mgpu_batch_advance(m_batch, t_next, nullptr), ctx, "mgpu_batch_advance");
+            }
             m_t = t_next;
             record();
         }
@@ -456,6 +514,45 @@ private:
         }
     }
 
+    /* MobilityEdge::apply_mobility's NPI check (metapopulation_mobility_instant.h:
+     * 549-566) for every edge with thresholds, on its source's state before the
+     * exchange at t; enacted NPIs change the edge's coefficient cache. */
+    void apply_edge_npis(double t)
+    {
+        mgpu_context* ctx = Device::context();
+        std::vector<double> all(m_arrays.state.size());
+        check(mgpu_batch_get_state(m_batch, all.data()), ctx, "mgpu_batch_get_state");
+        const size_t n = (size_t)m_arrays.G * osecir::num_compartments;
+        auto& edges    = m_graph.edges();
+        for (size_t e = 0; e < edges.size(); ++e) {
+            auto& params     = edges[e].property.get_parameters();
+            const auto& npis = params.get_dynamic_npis_infected();
+            if (npis.get_thresholds().empty()) {
+                continue;
+            }
+            const size_t u = edges[e].start_node_idx;
+            std::vector<double> y(all.begin() + (long)(u * n), all.begin() + (long)((u + 1) * n));
+            const auto& src_sim = m_graph.nodes()[u].property.get_simulation();
+            if (!check_edge_dynamic_npis(npis, edges[e].property.get_dynamic_npi_state(), params.get_coefficients(), t,
+                                         osecir::get_infections_relative(src_sim, t, y))) {
+                continue;
+            }
+            std::vector<double> times;
+            std::vector<Matrix> vals;
+            params.get_coefficients()[0].get_dampings().cache(times, vals);
+            if ((int)times.size() > m_arrays.Ke) {
+                throw Error(MGPU_UNSUPPORTED, "edge NPIs exceeded the coefficient-cache capacity of the batch");
+            }
+            std::vector<double> flat;
+            for (auto& m : vals) {
+                flat.insert(flat.end(), m.data(), m.data() + n);
+            }
+            check(mgpu_batch_set_edge_damping_cache(m_batch, 0, (int32_t)e, (int32_t)times.size(), times.data(),
+                                                    flat.data()),
+                  ctx, "mgpu_batch_set_edge_damping_cache");
+        }
+    }
+
     void upload_dampings(int v, const ContactMatrixGroup& contacts)
     {
         const int K     = m_arrays.K;
@@ -494,6 +591,12 @@ private:
             sp.push_back(&s);
         }
         using EdgeT    = typename GraphT::EdgeProperty;
+        m_any_edge_npis = false;
+        for (auto& e : m_graph.edges()) {
+            m_any_edge_npis = m_any_edge_npis || !e.property.get_parameters().get_dynamic_npis_infected()
+                                                      .get_thresholds()
+                                                      .empty();
+        }
         m_any_npis = false;
         for (auto* mdl : models) {
             m_any_npis = m_any_npis || !mdl->parameters.template get<osecir::DynamicNPIsInfectedSymptoms<double>>()
@@ -505,7 +608,7 @@ private:
             [](const EdgeT& e) -> const MobilityParameters<double>& {
                 return e.get_parameters();
             },
-            m_any_npis ? kNpiDampingPoints : 0);
+            m_any_npis ? kNpiDampingPoints : 0, m_any_edge_npis ? kNpiDampingPoints : 0);
         mgpu_graph g     = m_arrays.view();
         mgpu_solver_opts o;
         mgpu_default_solver_opts(&o);
@@ -537,6 +640,7 @@ private:
     int m_precision   = MGPU_PRECISION_FP64;
     bool m_record     = true;
     bool m_any_npis   = false;
+    bool m_any_edge_npis = false;
     mgpu_batch* m_batch = nullptr;
     detail::GraphArrays m_arrays;
 };

@@ -9,6 +9,7 @@
 //   facade_check npi_logic  host only: implement_dynamic_npis and the NPI check
 //                           of Simulation::advance with the state held fixed
 //   facade_check npi_graph  GPU: a graph simulation with dynamic NPIs (FP64 and mixed)
+//   facade_check npi_edges  GPU: the same with dynamic NPIs on the mobility edges too
 //   facade_check interpolate  host only: interpolate_simulation_result of small series
 //
 // The Python side rebuilds the same inputs from the printed arrays and checks
@@ -496,6 +497,60 @@ int mode_npi_graph()
     return 0;
 }
 
+// Dynamic NPIs on every mobility edge of three_nodes_npi: a lower threshold
+// than the nodes' (the edges see their sources' states before every exchange)
+// and two-day NPIs that halve, then cut by 80 %, the commuters.
+DynamicNPIs<double> edge_npis(int G)
+{
+    DynamicNPIs<double> npis;
+    npis.set_threshold(1.0, {DampingSampling<double>(0.5, DampingLevel(0), DampingType(0), SimulationTime<double>(0),
+                                                     {0}, std::vector<double>((size_t)G, 1.0))});
+    npis.set_threshold(4.0, {DampingSampling<double>(0.8, DampingLevel(1), DampingType(0), SimulationTime<double>(0),
+                                                     {0}, std::vector<double>((size_t)G, 1.0))});
+    npis.set_duration(SimulationTime<double>(2.0));
+    npis.set_base_value(1e5);
+    return npis;
+}
+
+int mode_npi_edges()
+{
+    std::printf("{");
+    for (int precision : {MGPU_PRECISION_FP64, MGPU_PRECISION_MIXED}) {
+        auto graph = three_nodes_npi(2);
+        for (auto& e : graph.edges()) {
+            e.property.get_parameters().get_dynamic_npis_infected() = edge_npis(2);
+        }
+        auto a   = arrays_of(graph);
+        auto sim = make_mobility_sim(0.0, 0.5, std::move(graph));
+        sim.set_precision(precision);
+        sim.advance(12.0);
+        std::vector<double> fin, enacted, edge_enacted;
+        for (auto& n : sim.get_graph().nodes()) {
+            auto v = n.property.get_result().get_last_value();
+            fin.insert(fin.end(), v.begin(), v.end());
+            enacted.push_back(n.property.get_simulation().get_dynamic_npi_state().enacted);
+        }
+        for (auto& e : sim.get_graph().edges()) {
+            edge_enacted.push_back(e.property.get_dynamic_npi_state().enacted);
+        }
+        if (precision == MGPU_PRECISION_FP64) {
+            print_graph_arrays(a);
+            print_dampings("initial_dampings", three_nodes(2).nodes()[0].property.get_simulation().get_model()
+                                                   .parameters.get<ContactPatterns<double>>());
+        }
+        const char* tag = precision == MGPU_PRECISION_FP64 ? "fp64" : "mixed";
+        char key[64];
+        std::snprintf(key, sizeof key, "final_%s", tag);
+        print_vec(key, fin);
+        std::snprintf(key, sizeof key, "enacted_%s", tag);
+        print_vec(key, enacted);
+        std::snprintf(key, sizeof key, "edge_enacted_%s", tag);
+        print_vec(key, edge_enacted, precision == MGPU_PRECISION_FP64);
+    }
+    std::printf("}\n");
+    return 0;
+}
+
 void print_series(const char* key, const TimeSeries<double>& ts, bool comma = true)
 {
     std::printf("\"%s\": {", key);
@@ -571,6 +626,9 @@ int main(int argc, char** argv)
         }
         if (!std::strcmp(mode, "npi_graph")) {
             return mode_npi_graph();
+        }
+        if (!std::strcmp(mode, "npi_edges")) {
+            return mode_npi_edges();
         }
         if (!std::strcmp(mode, "interpolate")) {
             return mode_interpolate();

@@ -300,6 +300,9 @@ struct mgpu_batch {
     std::vector<int64_t> node0, edge0, state_off;
     std::vector<DevGraph> host_graphs; // the graph records as uploaded
     std::vector<char> damping_shared;  // damping arrays shared with another graph (same host pointers)
+    std::vector<char> coeff_shared;    // edge coefficient arrays shared with another graph
+    bool half_step     = false;        // an interval begun by mgpu_batch_step_nodes awaits its exchange
+    std::vector<double> half_t_next;   // its end per graph
     int64_t state_total = 0;
     double* init_state  = nullptr; // initial states (for reset)
     float* init_hi      = nullptr; // the same as float-float pairs (mixed solver)
@@ -803,6 +806,16 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         }
         for (int i = 0; i < num_graphs; ++i) {
             b->damping_shared[i] = dg[i].K && users[dg[i].dtime_off] > 1;
+        }
+        std::map<int64_t, int> cusers;
+        for (int i = 0; i < num_graphs; ++i) {
+            if (dg[i].E) {
+                ++cusers[dg[i].ecoef_off];
+            }
+        }
+        b->coeff_shared.assign(num_graphs, 0);
+        for (int i = 0; i < num_graphs; ++i) {
+            b->coeff_shared[i] = dg[i].E && cusers[dg[i].ecoef_off] > 1;
         }
     }
     B.graphs         = b->pool.upload(dg);
@@ -1449,6 +1462,9 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
         return MGPU_INVALID_VALUE;
     }
     return guarded(b->ctx, [&]() -> int {
+        if (b->half_step) {
+            fail(MGPU_INVALID_VALUE, "the interval begun by mgpu_batch_step_nodes awaits mgpu_batch_step_exchange");
+        }
         ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
         cudaStream_t s = b->ctx->stream;
         for (int i = 0; i < b->num_graphs; ++i) {
@@ -2071,6 +2087,7 @@ int mgpu_batch_reset(mgpu_batch* b, double t0)
         ++b->launches;
         ck(cudaGetLastError(), "k_reset");
         ck(cudaStreamSynchronize(b->ctx->stream), "sync");
+        b->half_step = false;
         b->t_host.assign(b->num_graphs, t0);
         b->tmax_host.assign(b->num_graphs, t0);
         return MGPU_OK;
@@ -2151,6 +2168,117 @@ int mgpu_batch_set_damping_cache(mgpu_batch* b, int32_t graph, int32_t node, int
         }
         ck(cudaStreamSynchronize(s), "sync");
         return MGPU_OK;
+    });
+}
+
+int mgpu_batch_set_edge_damping_cache(mgpu_batch* b, int32_t graph, int32_t edge, int32_t num_points,
+                                      const double* times, const double* values)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!times || !values || graph < 0 || graph >= b->num_graphs) {
+            fail(MGPU_INVALID_VALUE, "null array or graph index out of range");
+        }
+        const DevGraph& d = b->host_graphs[graph];
+        if (edge < 0 || edge >= d.E) {
+            fail(MGPU_OUT_OF_RANGE, "edge index out of range");
+        }
+        if (d.Ke == 0 || num_points < 2 || num_points > d.Ke) {
+            fail(MGPU_INVALID_VALUE, "num_points must lie in [2, num_edge_damping_points of the graph]");
+        }
+        if (b->coeff_shared[graph]) {
+            fail(MGPU_UNSUPPORTED, "the graph's edge coefficient arrays are shared with another graph of the batch");
+        }
+        for (int k = 1; k < num_points; ++k) {
+            if (!(times[k] >= times[k - 1])) {
+                fail(MGPU_INVALID_VALUE, "damping cache times must be non-decreasing");
+            }
+        }
+        const int n = d.n;
+        std::vector<double> t((size_t)d.Ke), v((size_t)d.Ke * n);
+        for (int k = 0; k < d.Ke; ++k) {
+            const int src = std::min(k, num_points - 1);
+            t[(size_t)k]  = k < num_points ? times[k] : std::numeric_limits<double>::max();
+            std::memcpy(v.data() + (size_t)k * n, values + (size_t)src * n, sizeof(double) * n);
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        cudaStream_t s = b->ctx->stream;
+        double* dt     = const_cast<double*>(b->dev.edt) + d.edt_off + (int64_t)edge * d.Ke;
+        double* dv     = const_cast<double*>(b->dev.edv) + d.edv_off + (int64_t)edge * d.Ke * n;
+        ck(cudaMemcpyAsync(dt, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice, s), "h2d damping times");
+        ck(cudaMemcpyAsync(dv, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice, s), "h2d damping values");
+        ck(cudaStreamSynchronize(s), "sync");
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_step_nodes(mgpu_batch* b, double tmax, const double* tmax_per_graph)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (b->opts.precision == MGPU_PRECISION_FP64_PLAIN) {
+            fail(MGPU_UNSUPPORTED, "interval steps need a batched precision");
+        }
+        if (b->half_step) {
+            fail(MGPU_INVALID_VALUE, "the begun interval awaits mgpu_batch_step_exchange");
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        cudaStream_t s = b->ctx->stream;
+        for (int i = 0; i < b->num_graphs; ++i) {
+            b->tmax_host[i] = tmax_per_graph ? tmax_per_graph[i] : tmax;
+        }
+        ck(cudaMemcpyAsync(b->d_tmax, b->tmax_host.data(), sizeof(double) * b->num_graphs, cudaMemcpyHostToDevice,
+                           s),
+           "h2d tmax");
+        // the interval's end per graph (k_phase_begin)
+        b->half_t_next = b->t_host;
+        for (int i = 0; i < b->num_graphs; ++i) {
+            const double t = b->t_host[i];
+            if (t < b->tmax_host[i]) {
+                b->half_t_next[i] = t + std::min(b->opts.dt_exchange, b->tmax_host[i] - t);
+            }
+        }
+        const BatchDev& B = b->dev;
+        k_set_tmax<<<(b->num_graphs + 127) / 128, 128, 0, s>>>(B.rt, b->d_tmax, b->num_graphs);
+        launch_phase_begin(B, b->opts.dt_exchange, s);
+        for (auto& kv : b->inst_by_G) {
+            auto it       = b->tuned.find(kv.first);
+            const int ipb = it != b->tuned.end() ? it->second.first : b->instances_per_block;
+            const int grd = it != b->tuned.end() ? it->second.second : 0;
+            launch_ode_batched(B, kv.first, b->opts.precision, kv.second.first, kv.second.second, ipb, grd, s);
+        }
+        ck(cudaGetLastError(), "step launch");
+        b->launches += 2 + node_kernel_launches(b);
+        b->half_step = true;
+        return check_device_error(b);
+    });
+}
+
+int mgpu_batch_step_exchange(mgpu_batch* b)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!b->half_step) {
+            fail(MGPU_INVALID_VALUE, "no interval begun by mgpu_batch_step_nodes");
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        cudaStream_t s    = b->ctx->stream;
+        const BatchDev& B = b->dev;
+        int64_t l         = 0;
+        launch_exchange_batched(B, b->opts.precision, b->n_max, b->any_edge_dampings, s, &l, nullptr);
+        launch_phase_end(B, s);
+        ck(cudaGetLastError(), "step launch");
+        b->launches += l + 1;
+        b->phases += 1;
+        b->half_step = false;
+        b->t_host    = b->half_t_next;
+        return check_device_error(b);
     });
 }
 

@@ -199,23 +199,8 @@ class OrcDamping(ctypes.Structure):
                 ("matrix", ctypes.c_int32), ("pad", ctypes.c_int32), ("coeffs", ctypes.POINTER(ctypes.c_double))]
 
 
-def graph_run_npi(g: GraphArrays, t0: float, tmax: float, npis: dict, dampings, dt_exchange: float = 0.5,
-                  dt0: float = 0.1, opts=None):
-    """make_mobility_sim(...).advance(tmax) with the same dynamic NPIs on every node.
-
-    npis: {"thresholds": [(threshold, [(value, level, type, [matrices], [group weights]), ...]), ...],
-           "duration", "delay", "base_value", "directive_begin", "directive_end"};
-    dampings: the nodes' initial contact dampings [(time, level, type, matrix, G x G coefficients), ...].
-    Returns (final [N, 10G], enactments per node [N], stats)."""
-    L = lib()
-    if not hasattr(L.orc_graph_run_npi, "_typed"):
-        P = ctypes.POINTER
-        d = ctypes.c_double
-        L.orc_graph_run_npi.argtypes = [P(MgpuGraph), d, d, d, d, P(MgpuIntegratorOpts), P(OrcDynamicNpis),
-                                        ctypes.c_int, P(OrcDamping), P(d), P(ctypes.c_int32), P(OrcStats)]
-        L.orc_graph_run_npi._typed = True
-    opts = opts or integrator_opts()
-    keep = []
+def _dynamic_npis(npis: dict, keep: list):
+    """OrcDynamicNpis of an NPI dict; the arrays it points to are appended to keep."""
     samp, first, thr = [], [0], []
     for threshold, items in npis["thresholds"]:
         thr.append(threshold)
@@ -229,10 +214,35 @@ def graph_run_npi(g: GraphArrays, t0: float, tmax: float, npis: dict, dampings, 
     thr_a = np.ascontiguousarray(thr, np.float64)
     first_a = np.ascontiguousarray(first, np.int32)
     samp_a = (OrcNpiSampling * max(len(samp), 1))(*samp)
-    p = OrcDynamicNpis(len(thr), 0, _p(thr_a), first_a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), samp_a,
-                       npis.get("duration", 14.0), npis.get("delay", 0.0), npis.get("base_value", 1.0),
-                       npis.get("directive_begin", np.finfo(np.float64).min),
-                       npis.get("directive_end", np.finfo(np.float64).max))
+    keep += [thr_a, first_a, samp_a]
+    return OrcDynamicNpis(len(thr), 0, _p(thr_a), first_a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), samp_a,
+                          npis.get("duration", 14.0), npis.get("delay", 0.0), npis.get("base_value", 1.0),
+                          npis.get("directive_begin", np.finfo(np.float64).min),
+                          npis.get("directive_end", np.finfo(np.float64).max))
+
+
+def graph_run_npi(g: GraphArrays, t0: float, tmax: float, npis: dict, dampings, dt_exchange: float = 0.5,
+                  dt0: float = 0.1, opts=None, edge_npis: dict = None):
+    """make_mobility_sim(...).advance(tmax) with the same dynamic NPIs on every node.
+
+    npis: {"thresholds": [(threshold, [(value, level, type, [matrices], [group weights]), ...]), ...],
+           "duration", "delay", "base_value", "directive_begin", "directive_end"};
+    dampings: the nodes' initial contact dampings [(time, level, type, matrix, G x G coefficients), ...];
+    edge_npis: the same NPIs on every edge (MobilityParameters::get_dynamic_npis_infected; the
+    matrices of a sampling are ignored), or None. Returns (final [N, 10G], enactments per node [N],
+    stats), and with edge_npis also the enactments per edge [E] after the node counts."""
+    L = lib()
+    if not hasattr(L.orc_graph_run_npi, "_typed"):
+        P = ctypes.POINTER
+        d = ctypes.c_double
+        L.orc_graph_run_npi.argtypes = [P(MgpuGraph), d, d, d, d, P(MgpuIntegratorOpts), P(OrcDynamicNpis),
+                                        ctypes.c_int, P(OrcDamping), P(OrcDynamicNpis), P(d), P(ctypes.c_int32),
+                                        P(ctypes.c_int32), P(OrcStats)]
+        L.orc_graph_run_npi._typed = True
+    opts = opts or integrator_opts()
+    keep = []
+    p = _dynamic_npis(npis, keep)
+    ep = _dynamic_npis(edge_npis, keep) if edge_npis is not None else None
     damp = []
     for time, level, typ, mat, coeffs in dampings:
         c = np.ascontiguousarray(coeffs, np.float64)
@@ -241,10 +251,14 @@ def graph_run_npi(g: GraphArrays, t0: float, tmax: float, npis: dict, dampings, 
     damp_a = (OrcDamping * max(len(damp), 1))(*damp)
     fin = np.zeros((g.num_nodes, g.n))
     cnt = np.zeros(g.num_nodes, np.int32)
+    ecnt = np.zeros(max(g.num_edges, 1), np.int32)
     st = OrcStats()
     cg = g.as_ctypes()
     rc = L.orc_graph_run_npi(ctypes.byref(cg), t0, tmax, dt_exchange, dt0, ctypes.byref(opts), ctypes.byref(p),
-                             len(damp), damp_a, _p(fin), cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
-                             ctypes.byref(st))
+                             len(damp), damp_a, ctypes.byref(ep) if ep is not None else None, _p(fin),
+                             cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                             ecnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), ctypes.byref(st))
     assert rc == 0
+    if edge_npis is not None:
+        return fin, cnt, ecnt[:g.num_edges], st.as_dict()
     return fin, cnt, st.as_dict()

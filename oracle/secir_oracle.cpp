@@ -545,6 +545,9 @@ struct GraphRun {
         auto& from  = nodes[u];
         auto& to    = nodes[v];
         const int G = g->num_groups;
+        if (enpis) {
+            check_edge_npis(e, t);
+        }
         // returns (:568-603)
         for (long i = (long)es.ret_t.size() - 1; i >= 0; --i) {
             if (es.ret_t[i] <= t) {
@@ -593,7 +596,12 @@ struct GraphRun {
         // departure (:605-621)
         if (!es.return_mobile) {
             std::vector<double> c(n);
-            edge_coeffs_at(g, e, t, c.data());
+            if (enpis) {
+                edge_coeffs_npi(e, t, c.data());
+            }
+            else {
+                edge_coeffs_at(g, e, t, c.data());
+            }
             bool any = false;
             for (int j = 0; j < n; ++j) {
                 any = any || (c[j] > 0.0);
@@ -774,70 +782,81 @@ struct GraphRun {
     }
 
     // get_active_damping (dynamic_npis.h:246-258)
-    std::vector<double> active_damping(const std::vector<ODamping>& l, int level, int type, double t) const
+    static std::vector<double> active_damping(const std::vector<ODamping>& l, int level, int type, double t,
+                                              size_t size)
     {
         for (size_t k = l.size(); k-- > 0;) {
             if (l[k].level == level && l[k].type == type && l[k].time <= t) {
                 return l[k].m;
             }
         }
-        return std::vector<double>((size_t)g->num_groups * g->num_groups, 0.0);
+        return std::vector<double>(size, 0.0);
     }
 
-    // implement_dynamic_npis (dynamic_npis.h:335-391)
+    // one NPI on one damping list (implement_dynamic_npis, dynamic_npis.h:338-369)
+    void implement_list(std::vector<ODamping>& l, int level, int type, double begin, double end,
+                        const std::vector<double>& value) const
+    {
+        const std::vector<double> act     = active_damping(l, level, type, begin, value.size());
+        const std::vector<double> act_end = active_damping(l, level, type, end, value.size());
+        bool implemented                  = false;
+        bool less                         = false;
+        std::vector<double> mx(value.size());
+        for (size_t i = 0; i < value.size(); ++i) {
+            less  = less || act[i] < value[i];
+            mx[i] = std::max(value[i], act[i]);
+        }
+        if (less) {
+            add_damping(l, {begin, level, type, mx});
+            implemented = true;
+        }
+        std::vector<size_t> idx; // get_damping_indices (dynamic_npis.h:232-244)
+        for (size_t i = 0; i < l.size(); ++i) {
+            if (l[i].level == level && l[i].type == type && l[i].time > begin && l[i].time < end) {
+                idx.push_back(i);
+            }
+        }
+        for (size_t i : idx) {
+            ODamping d = l[i];
+            for (size_t k = 0; k < d.m.size(); ++k) {
+                d.m[k] = std::max(d.m[k], value[k]);
+            }
+            add_damping(l, d);
+            implemented = true;
+        }
+        if (implemented) {
+            add_damping(l, {end, level, type, act_end});
+        }
+    }
+
+    // remove dampings that repeat the previous value of their (level, type) (dynamic_npis.h:372-390)
+    static void dedupe(std::vector<ODamping>& l)
+    {
+        for (int i = 0; i < (int)l.size() - 1; ++i) {
+            const size_t cur = l.size() - 1 - (size_t)i;
+            for (size_t k = cur; k-- > 0;) {
+                if (l[k].level == l[cur].level && l[k].type == l[cur].type) {
+                    if (l[k].m == l[cur].m) {
+                        l.erase(l.begin() + (long)cur);
+                    }
+                    break;
+                }
+            }
+        }
+    }
+
+    // implement_dynamic_npis (dynamic_npis.h:335-391) on the contact matrices of node v
     void implement(int v, int thr, double begin, double end)
     {
         auto& nn = npi[v];
         for (int s = npis->first[thr]; s < npis->first[thr + 1]; ++s) {
             const orc_npi_sampling& smp = npis->samplings[s];
             for (int q = 0; q < smp.num_matrices; ++q) {
-                auto& l                       = nn.lists[smp.matrices[q]];
-                const std::vector<double> act = active_damping(l, smp.level, smp.type, begin);
-                const std::vector<double> act_end = active_damping(l, smp.level, smp.type, end);
-                const std::vector<double> value   = contact_damping(smp);
-                bool implemented                  = false;
-                bool less                         = false;
-                std::vector<double> mx(value.size());
-                for (size_t i = 0; i < value.size(); ++i) {
-                    less  = less || act[i] < value[i];
-                    mx[i] = std::max(value[i], act[i]);
-                }
-                if (less) {
-                    add_damping(l, {begin, smp.level, smp.type, mx});
-                    implemented = true;
-                }
-                std::vector<size_t> idx; // get_damping_indices (dynamic_npis.h:232-244)
-                for (size_t i = 0; i < l.size(); ++i) {
-                    if (l[i].level == smp.level && l[i].type == smp.type && l[i].time > begin && l[i].time < end) {
-                        idx.push_back(i);
-                    }
-                }
-                for (size_t i : idx) {
-                    ODamping d = l[i];
-                    for (size_t k = 0; k < d.m.size(); ++k) {
-                        d.m[k] = std::max(d.m[k], value[k]);
-                    }
-                    add_damping(l, d);
-                    implemented = true;
-                }
-                if (implemented) {
-                    add_damping(l, {end, smp.level, smp.type, act_end});
-                }
+                implement_list(nn.lists[smp.matrices[q]], smp.level, smp.type, begin, end, contact_damping(smp));
             }
         }
-        // remove dampings that repeat the previous value of their (level, type)
         for (auto& l : nn.lists) {
-            for (int i = 0; i < (int)l.size() - 1; ++i) {
-                const size_t cur = l.size() - 1 - (size_t)i;
-                for (size_t k = cur; k-- > 0;) {
-                    if (l[k].level == l[cur].level && l[k].type == l[cur].type) {
-                        if (l[k].m == l[cur].m) {
-                            l.erase(l.begin() + (long)cur);
-                        }
-                        break;
-                    }
-                }
-            }
+            dedupe(l);
         }
     }
 
@@ -899,6 +918,117 @@ struct GraphRun {
             advance_node(v, t + dt_eff);
             t = t + dt_eff;
         }
+    }
+
+    // ---- edge NPIs (MobilityEdge::apply_mobility, metapopulation_mobility_instant.h:549-566) ----
+    struct EdgeNpi {
+        std::vector<ODamping> list; // coefficient dampings, vectors of 10 G
+        std::vector<double> ctimes, cvals;
+        double thr   = std::numeric_limits<double>::lowest();
+        double t_end = 0.0;
+        int count    = 0;
+    };
+    const orc_dynamic_npis* enpis = nullptr;
+    std::vector<int> ethr_order;
+    std::vector<EdgeNpi> enpi;
+    std::vector<double> node_total; // the models' total populations
+
+    void init_edge_npis(const orc_dynamic_npis* p)
+    {
+        enpis = p;
+        ethr_order.resize(p->num_thresholds);
+        for (int k = 0; k < p->num_thresholds; ++k) {
+            ethr_order[k] = k;
+        }
+        std::stable_sort(ethr_order.begin(), ethr_order.end(), [&](int a, int b) {
+            return p->thresholds[a] > p->thresholds[b];
+        });
+        enpi.assign(g->num_edges, {});
+        for (int e = 0; e < g->num_edges; ++e) {
+            rebuild_edge_cache(e);
+        }
+        node_total.assign(g->num_nodes, 0.0);
+        for (int v = 0; v < g->num_nodes; ++v) {
+            for (int j = 0; j < n; ++j) {
+                node_total[v] += g->init_state[(long)v * n + j];
+            }
+        }
+    }
+
+    void rebuild_edge_cache(int e)
+    {
+        auto& en     = enpi[e];
+        const int nd = (int)en.list.size();
+        std::vector<double> times(nd), mats((size_t)nd * n);
+        std::vector<int32_t> levels(nd), types(nd);
+        for (int d = 0; d < nd; ++d) {
+            times[d]  = en.list[d].time;
+            levels[d] = en.list[d].level;
+            types[d]  = en.list[d].type;
+            std::copy(en.list[d].m.begin(), en.list[d].m.end(), mats.begin() + (long)d * n);
+        }
+        en.ctimes.assign(nd + 2, 0.0);
+        en.cvals.assign((size_t)(nd + 2) * n, 0.0);
+        const int k = orc_damping_cache(n, 1, nd, times.data(), levels.data(), types.data(), mats.data(), nd + 2,
+                                        en.ctimes.data(), en.cvals.data());
+        en.ctimes.resize(k);
+        en.cvals.resize((size_t)k * n);
+    }
+
+    // DampingMatrixExpression::get_matrix_at of the edge's coefficients with its own cache
+    void edge_coeffs_npi(int e, double t, double* c) const
+    {
+        const auto& en  = enpi[e];
+        const int K     = (int)en.ctimes.size();
+        const double* B = g->edge_coeff_baseline + (long)e * n;
+        const double* L = g->edge_coeff_minimum ? g->edge_coeff_minimum + (long)e * n : nullptr;
+        for (int i = 0; i < n; ++i) {
+            const double D  = damping_coeff_at(en.ctimes.data(), en.cvals.data(), K, n, i, t);
+            const double Li = L ? L[i] : 0.0;
+            c[i]            = 0.0 + (B[i] - D * (B[i] - Li));
+        }
+    }
+
+    void check_edge_npis(int e, double t)
+    {
+        const orc_dynamic_npis& p = *enpis;
+        if (p.num_thresholds == 0) {
+            return;
+        }
+        auto& en      = enpi[e];
+        const int u   = g->edge_src[e];
+        const auto& y = nodes[u].last_state; // SimulationNode::get_last_state
+        double sum    = 0.0;
+        for (int gi = 0; gi < g->num_groups; ++gi) {
+            sum += y[(long)gi * kC + MGPU_ISY];
+        }
+        const double inf_rel = sum / node_total[u] * p.base_value;
+        int thr              = -1;
+        for (int k : ethr_order) {
+            if (inf_rel > p.thresholds[k]) {
+                thr = k;
+                break;
+            }
+        }
+        const bool expired = fp_ge(t, en.t_end, 1e-10);
+        if (thr < 0 || !(p.thresholds[thr] > en.thr || expired)) {
+            return;
+        }
+        const double t_end = t + p.duration;
+        en.thr             = p.thresholds[thr];
+        en.t_end           = t_end;
+        const int G        = g->num_groups;
+        for (int s = p.first[thr]; s < p.first[thr + 1]; ++s) {
+            const orc_npi_sampling& smp = p.samplings[s];
+            std::vector<double> value(n); // make_mobility_damping_vector (damping_sampling.h:290-306)
+            for (int i = 0; i < n; ++i) {
+                value[i] = smp.value * smp.group_weights[i / (n / G)];
+            }
+            implement_list(en.list, smp.level, smp.type, t, t_end, value);
+        }
+        dedupe(en.list);
+        en.count += 1;
+        rebuild_edge_cache(e);
     }
 
     // GraphSimulation::advance (mobility/graph_simulation.h:101-120).
@@ -1119,9 +1249,11 @@ int orc_graph_run(const mgpu_graph* g, double t0, double tmax, double dt_exchang
 
 int orc_graph_run_npi(const mgpu_graph* g, double t0, double tmax, double dt_exchange, double dt0,
                       const mgpu_integrator_opts* opts, const orc_dynamic_npis* npis, int num_dampings,
-                      const orc_damping* dampings, double* final_state, int32_t* npi_count, orc_stats* stats)
+                      const orc_damping* dampings, const orc_dynamic_npis* edge_npis, double* final_state,
+                      int32_t* npi_count, int32_t* edge_npi_count, orc_stats* stats)
 {
-    if (!graph_ok(g) || !opts || !npis || !(dt_exchange > 0) || (num_dampings > 0 && !dampings)) {
+    if (!graph_ok(g) || !opts || !npis || !(dt_exchange > 0) || (num_dampings > 0 && !dampings) ||
+        (edge_npis && g->num_edge_damping_points != 0)) {
         return -1;
     }
     for (int d = 0; d < num_dampings; ++d) {
@@ -1131,7 +1263,15 @@ int orc_graph_run_npi(const mgpu_graph* g, double t0, double tmax, double dt_exc
     }
     GraphRun run(g, t0, dt0, *opts);
     run.init_npis(npis, num_dampings, dampings);
+    if (edge_npis) {
+        run.init_edge_npis(edge_npis);
+    }
     run.run(t0, tmax, dt_exchange, nullptr);
+    if (edge_npi_count && edge_npis) {
+        for (int e = 0; e < g->num_edges; ++e) {
+            edge_npi_count[e] = run.enpi[e].count;
+        }
+    }
     if (final_state) {
         run.write_final(final_state);
     }

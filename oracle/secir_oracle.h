@@ -106,14 +106,20 @@ typedef struct orc_damping {
     const double* coeffs; /* [G][G] */
 } orc_damping;
 
-/* orc_graph_run with the same dynamic NPIs on every node (osecir::Simulation::
+/* orc_graph_run with the same dynamic NPIs on every node, and optionally the
+ * same edge NPIs on every edge (edge_npis, MobilityEdge::apply_mobility,
+ * mobility/metapopulation_mobility_instant.h:549-566: checked on the source's
+ * state before each exchange, the coefficient dampings starting empty; the
+ * graph must have no edge damping cache); edge_npi_count [E] receives the
+ * enactments per edge. (The rest as for the nodes:) (osecir::Simulation::
  * advance, models/ode_secir/model.h:289-367, reached through
  * SimulationNode::advance): the nodes' contact dampings start from `dampings`
  * (the graph's damping caches are not used) and change as NPIs are enacted.
  * npi_count [N] receives the number of enactments per node. */
 int orc_graph_run_npi(const mgpu_graph* g, double t0, double tmax, double dt_exchange, double dt0,
                       const mgpu_integrator_opts* opts, const orc_dynamic_npis* npis, int num_dampings,
-                      const orc_damping* dampings, double* final_state, int32_t* npi_count, orc_stats* stats);
+                      const orc_damping* dampings, const orc_dynamic_npis* edge_npis, double* final_state,
+                      int32_t* npi_count, int32_t* edge_npi_count, orc_stats* stats);
 
 #ifdef __cplusplus
 }

@@ -8,7 +8,9 @@ implement_empty :145-170, implement :172-317, secir_threshold_safe :421-450,
 secir_threshold_exceeded :452-482, secir_delayed_implementation :484-539). The
 oracle's restatement runs a graph without thresholds exactly as without NPIs.
 GPU: a graph simulation with NPIs through the facade (device solver, caches
-replaced with mgpu_batch_set_damping_cache) against the oracle.
+replaced with mgpu_batch_set_damping_cache) against the oracle, with and
+without NPIs on the mobility edges (MobilityEdge::apply_mobility,
+cpp/memilio/mobility/metapopulation_mobility_instant.h:549-566).
 """
 import json
 import subprocess
@@ -101,6 +103,39 @@ def test_oracle_npis_enact_and_conserve():
     assert fin.reshape(8, 2, 10)[..., L.S].sum() > fin0.reshape(8, 2, 10)[..., L.S].sum()
 
 
+def edge_npis_of(G):
+    """The edge NPIs of facade_check's npi_edges mode (edge_npis)."""
+    ones = [1.0] * G
+    return {"thresholds": [(1.0, [(0.5, 0, 0, [0], ones)]), (4.0, [(0.8, 1, 0, [0], ones)])],
+            "duration": 2.0, "base_value": 1e5}
+
+
+def test_oracle_edge_npis():
+    g = W.mobility_graph(seed=5, N=8, G=2, out_degree=3)
+    fin0, cnt0, _ = O.graph_run_npi(g, 0.0, 10.0, {"thresholds": []}, [])
+    # edge NPIs without thresholds: the run without NPIs
+    fin, cnt, ecnt, _ = O.graph_run_npi(g, 0.0, 10.0, {"thresholds": []}, [], edge_npis={"thresholds": []})
+    np.testing.assert_array_equal(fin, fin0)
+    assert not ecnt.any()
+    # a threshold every source crosses at once: every edge enacts at the first exchange and, with
+    # one-day NPIs, again at every expiry
+    ones = [1.0, 1.0]
+    enp = {"thresholds": [(1e-9, [(0.6, 0, 0, [0], ones)])], "duration": 1.0}
+    fin, cnt, ecnt, _ = O.graph_run_npi(g, 0.0, 10.0, {"thresholds": []}, [], edge_npis=enp)
+    assert ecnt.shape == (g.num_edges,) and (ecnt == 10).all()
+    np.testing.assert_allclose(fin.sum(), g.init_state.sum(), rtol=1e-12)
+    assert np.abs(fin - fin0).max() > 1e-6  # fewer commuters change the epidemic
+    # full damping of the commuters: the nodes run as if unconnected
+    enp_all = {"thresholds": [(1e-9, [(1.0, 0, 0, [0], ones)])], "duration": 100.0}
+    fin, _, ecnt, _ = O.graph_run_npi(g, 0.0, 10.0, {"thresholds": []}, [], edge_npis=enp_all)
+    assert (ecnt == 1).all()
+    solo = L.GraphArrays(g.num_groups, g.params, g.contact_baseline, g.contact_minimum, g.damping_times,
+                         g.damping_values, g.init_state, np.zeros(0, np.int32), np.zeros(0, np.int32),
+                         np.zeros((0, g.n)))
+    _, fin_solo, _ = O.graph_run(solo, 0.0, 10.0, record=False)
+    np.testing.assert_allclose(fin, fin_solo, rtol=1e-9, atol=1e-9)
+
+
 def npis_of_facade_graph(G):
     """The NPIs of facade_check's npi_graph mode (three_nodes_npi)."""
     ones = [1.0] * G
@@ -164,3 +199,17 @@ def test_set_damping_cache_between_advances():
         bs.set_damping_cache(0, 2, 0, t_new, v_new)
     bs.close()
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_graph_simulation_with_edge_npis_matches_oracle(programs):
+    d = run(programs, "npi_edges")
+    g = graph_of(d)
+    G = g.num_groups
+    init = [(t, lv, ty, m, np.full((G, G), v)) for m, lst in enumerate(d["initial_dampings"]) for t, lv, ty, v in lst]
+    fin, cnt, ecnt, _ = O.graph_run_npi(g, 0.0, 12.0, npis_of_facade_graph(G), init, edge_npis=edge_npis_of(G))
+    assert ecnt.sum() > 0  # edge NPIs were enacted in this run
+    for tag, tol in (("fp64", 1e-10), ("mixed", 1e-5)):
+        np.testing.assert_array_equal(np.array(d["enacted_" + tag]), cnt)
+        np.testing.assert_array_equal(np.array(d["edge_enacted_" + tag]), ecnt)
+        assert scaled(d["final_" + tag], fin, G) < tol
