@@ -398,3 +398,94 @@ class MobilitySimulation:
 
     def get_t(self) -> float:
         return self.t
+
+
+class GraphParameterStudy:
+    """osecir.GraphParameterStudy(graph, t0, tmax, dt, num_runs)
+    (bindings/compartments/parameter_studies.h:88-122 over ParameterStudy::run_serial,
+    cpp/memilio/compartments/parameter_studies.h): num_runs copies of the graph,
+    each sampled and simulated from t0 to tmax with exchanges every dt
+    (make_sampled_graph_simulation(graph, t0, dt, dt)).
+
+    All runs go to the GPU as ONE batch. `sample` takes draw_sample's place: a
+    callable that changes a copy of the graph (its nodes' models and populations,
+    its edges' coefficients) in place, given the copy and the run index; without
+    it every run simulates the graph as given. (The reference's Random123 draws
+    are not reproduced.)"""
+
+    def __init__(self, graph: MobilityGraph, t0: float, tmax: float, dt: float, num_runs: int,
+                 sample=None, precision: int = N.PRECISION_FP64):
+        if num_runs < 1:
+            raise ValueError("num_runs must be at least 1")
+        self._graph = graph
+        self._t0, self._tmax, self._dt = float(t0), float(tmax), float(dt)
+        self._num_runs = int(num_runs)
+        self._sample = sample
+        self._precision = precision
+
+    @property
+    def num_runs(self) -> int:
+        return self._num_runs
+
+    @property
+    def t0(self) -> float:
+        return self._t0
+
+    @property
+    def tmax(self) -> float:
+        return self._tmax
+
+    @property
+    def dt(self) -> float:
+        return self._dt
+
+    @property
+    def parameters(self) -> MobilityGraph:
+        return self._graph
+
+    def _sampled_graphs(self):
+        """The sampled copies of the graph, one per run."""
+        import copy
+        runs = []
+        for r in range(self._num_runs):
+            g = copy.deepcopy(self._graph)
+            if self._sample is not None:
+                self._sample(g, r)
+            for node in g._nodes:  # each run starts from its sampled populations
+                node.property.result = TimeSeries(node.property.model.populations.numel())
+                node.property.result.add_time_point(self._t0, node.property.model.populations.array())
+            runs.append(g)
+        return runs
+
+    def _arrays(self, runs):
+        return [_graph_arrays([n.property.model for n in g._nodes],
+                              [n.property.result.get_last_value() for n in g._nodes],
+                              [(e.start_node_idx, e.end_node_idx, e.property.coeffs) for e in g._edges])
+                for g in runs]
+
+    def run(self, handle_result=None):
+        """Simulate every run; with handle_result(graph, run_index) each result
+        graph is handed over in run order, else the result graphs are returned.
+        A result graph's node results hold the state after every exchange."""
+        runs = self._sampled_graphs()
+        arrays = self._arrays(runs)
+        batch = N.Batch(_context(), arrays, self._t0,
+                        N.solver_opts(precision=self._precision, dt_exchange=self._dt, dt0=self._dt))
+        try:
+            t = self._t0
+            while t < self._tmax:
+                t_next = min(t + self._dt, self._tmax)
+                if self._tmax - t_next < 1e-12 * max(1.0, abs(self._tmax)):
+                    t_next = self._tmax
+                batch.advance(t_next)
+                t = t_next
+                for g, a, st in zip(runs, arrays, batch.states()):
+                    for v, node in enumerate(g._nodes):
+                        node.property.result.add_time_point(t, st[v].reshape(a.n))
+        finally:
+            batch.close()
+        if handle_result is None:
+            return runs
+        for r, g in enumerate(runs):
+            handle_result(g, r)
+        return None

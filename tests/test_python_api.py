@@ -4,7 +4,8 @@ example scripts' calls (pycode/examples/simulation/ode_secir_simple.py,
 ode_secir_mobility.py) run unchanged apart from the imports. Host-only: the
 parameter and population API, the damping cache against the oracle's
 restatement of Dampings::update_cache, interpolation against the reference's
-tests. GPU: simulate and MobilitySimulation against the FP64 oracle."""
+tests, GraphParameterStudy's sampled runs. GPU: simulate, MobilitySimulation
+and GraphParameterStudy against the FP64 oracle."""
 import numpy as np
 import pytest
 
@@ -94,6 +95,66 @@ def test_graph_keeps_edges_sorted():
     g.add_edge(0, 1, 0.1 * np.ones(10))
     g.add_edge(1, 0, 0.1 * np.ones(10))
     assert [(g.get_edge(i).start_node_idx, g.get_edge(i).end_node_idx) for i in range(3)] == [(0, 1), (1, 0), (2, 0)]
+
+
+def two_node_graph():
+    graph = osecir.MobilityGraph()
+    graph.add_node(id=0, model=simple_model(10000.0), t0=0)
+    graph.add_node(id=1, model=simple_model(2000.0, exposed=0.0), t0=0)
+    coeffs = 0.1 * np.ones(10)
+    coeffs[State.Dead] = 0
+    graph.add_edge(0, 1, mio.MobilityParameters(coeffs))
+    graph.add_edge(1, 0, mio.MobilityParameters(coeffs))
+    return graph
+
+
+def sample_run(graph, run):
+    """A seeded stand-in for draw_sample: per run, other initial exposed and exposure times."""
+    rng = np.random.default_rng(run)
+    for node in (graph.get_node(i) for i in range(graph.num_nodes)):
+        m = node.property.model
+        m.populations[mio.AgeGroup(0), State.Exposed] = float(rng.uniform(50.0, 150.0))
+        m.parameters.TimeExposed[mio.AgeGroup(0)] = float(rng.uniform(2.5, 4.0))
+
+
+def test_parameter_study_samples_copies():
+    graph = two_node_graph()
+    study = osecir.GraphParameterStudy(graph, 0.0, 10.0, 0.5, 3, sample=sample_run)
+    assert (study.num_runs, study.t0, study.tmax, study.dt) == (3, 0.0, 10.0, 0.5)
+    runs = study._sampled_graphs()
+    assert len(runs) == 3
+    e0 = [r.get_node(0).property.model.populations[mio.AgeGroup(0), State.Exposed] for r in runs]
+    assert len(set(e0)) == 3  # every run drew its own values
+    # the graph itself is not changed, and each run starts from its sampled populations
+    assert graph.get_node(0).property.model.populations[mio.AgeGroup(0), State.Exposed] == 100.0
+    for r in runs:
+        res = r.get_node(0).property.result
+        assert res.get_num_time_points() == 1
+        np.testing.assert_array_equal(res.get_last_value(), r.get_node(0).property.model.populations.array())
+    again = study._sampled_graphs()  # runs are reproducible
+    assert [r.get_node(0).property.model.parameters.TimeExposed[mio.AgeGroup(0)] for r in again] == \
+        [r.get_node(0).property.model.parameters.TimeExposed[mio.AgeGroup(0)] for r in runs]
+    with pytest.raises(ValueError):
+        osecir.GraphParameterStudy(graph, 0.0, 10.0, 0.5, 0)
+
+
+@pytest.mark.gpu
+def test_parameter_study_matches_oracle():
+    study = osecir.GraphParameterStudy(two_node_graph(), 0.0, 10.0, 0.5, 3, sample=sample_run)
+    seen = []
+    study.run(lambda g, r: seen.append((r, g)))
+    assert [r for r, _ in seen] == [0, 1, 2]
+    expect = study._arrays(study._sampled_graphs())
+    for (r, g), a in zip(seen, expect):
+        rec, fin, _ = O.graph_run(a, 0.0, 10.0, dt_exchange=0.5, dt0=0.5)
+        for v in range(2):
+            got = g.get_node(v).property.result
+            assert got.get_num_time_points() == 21
+            np.testing.assert_allclose(got.get_last_value(), fin[v], rtol=1e-10, atol=1e-10 * fin[v].sum())
+            np.testing.assert_allclose(got.get_value(10), rec[9, v], rtol=1e-10, atol=1e-10 * fin[v].sum())
+    results = osecir.GraphParameterStudy(two_node_graph(), 0.0, 10.0, 0.5, 2, sample=sample_run).run()
+    np.testing.assert_allclose(results[1].get_node(1).property.result.get_last_value(),
+                               seen[1][1].get_node(1).property.result.get_last_value(), rtol=1e-12, atol=1e-9)
 
 
 @pytest.mark.gpu
