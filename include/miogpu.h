@@ -227,6 +227,12 @@ int mgpu_batch_reset(mgpu_batch* batch, double t0);
 
 /* Node states (result last values) of all graphs, concatenated [sum_b N_b][10 G_b]. */
 int mgpu_batch_get_state(mgpu_batch* batch, double* out);
+/* Per node, the sum over its age groups of one compartment of its current
+ * state, all graphs concatenated [sum_b N_b]: the numerator of the dynamic-NPI
+ * check's get_infections_relative (cpp/models/ode_secir/model.h:413-423, with
+ * compartment = MGPU_ISY), reduced on the device so that the check reads one
+ * value per node instead of the whole state. */
+int mgpu_batch_get_compartment_sums(mgpu_batch* batch, int32_t compartment, double* out);
 /* Graph times GraphSimulation::get_t() [num_graphs]. */
 int mgpu_batch_get_time(mgpu_batch* batch, double* out);
 /* Replace the node states (e.g. after a host-side intervention) [sum_b N_b][10 G_b]. */

@@ -29,7 +29,7 @@ PRECISION_MIXED = 2
 EXPORTED = ["mgpu_default_solver_opts", "mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_set_memory_budget",
             "mgpu_eval_rhs", "mgpu_simulate", "mgpu_batch_create", "mgpu_batch_advance", "mgpu_batch_get_state",
             "mgpu_batch_get_time", "mgpu_batch_set_state", "mgpu_batch_set_damping_cache", "mgpu_batch_set_edge_damping_cache",
-            "mgpu_batch_step_nodes", "mgpu_batch_step_exchange", "mgpu_batch_get_stats", "mgpu_batch_get_timing",
+            "mgpu_batch_step_nodes", "mgpu_batch_step_exchange", "mgpu_batch_get_compartment_sums", "mgpu_batch_get_stats", "mgpu_batch_get_timing",
             "mgpu_batch_device_bytes", "mgpu_batch_reset", "mgpu_batch_destroy", "mgpu_simulate_final_noalloc",
             "mgpu_batch_launch", "mgpu_batch_query", "mgpu_batch_autotune", "mgpu_simulate_dt", "mgpu_simulate_flows", "mgpu_batch_ensemble_stats", "mgpu_batch_get_graph_state", "mgpu_batch_estimate_bytes",
             "mgpu_default_server_opts", "mgpu_server_create", "mgpu_server_destroy", "mgpu_server_submit",
@@ -138,6 +138,7 @@ def lib():
     L.mgpu_batch_set_edge_damping_cache.argtypes = [vp] + [ctypes.c_int32] * 3 + [P(d), P(d)]
     L.mgpu_batch_step_nodes.argtypes = [vp, d, P(d)]
     L.mgpu_batch_step_exchange.argtypes = [vp]
+    L.mgpu_batch_get_compartment_sums.argtypes = [vp, ctypes.c_int32, P(d)]
     L.mgpu_batch_get_stats.argtypes = [vp, P(MgpuStats)]
     L.mgpu_batch_get_timing.argtypes = [vp, P(MgpuTiming)]
     L.mgpu_batch_reset.argtypes = [vp, d]
@@ -324,6 +325,12 @@ class Batch:
 
     def step_exchange(self):
         self.ctx.check(lib().mgpu_batch_step_exchange(self._h))
+
+    def compartment_sums(self, compartment: int) -> np.ndarray:
+        """mgpu_batch_get_compartment_sums: per node (all graphs), the sum over age groups of one compartment."""
+        out = np.zeros(sum(g.num_nodes for g in self.graphs))
+        self.ctx.check(lib().mgpu_batch_get_compartment_sums(self._h, compartment, _dp(out)))
+        return out
 
     def set_damping_cache(self, graph: int, node: int, matrix: int, times, values):
         """mgpu_batch_set_damping_cache: times [K'], values [K'][G][G]."""

@@ -428,8 +428,11 @@ public:
     {
         ensure_batch();
         mgpu_context* ctx = Device::context();
+        // NPI checks need every exchange boundary; without them and without
+        // recording, one batch advance covers the whole span
+        const bool per_interval = m_record || m_any_npis || m_any_edge_npis;
         while (m_t < tmax) {
-            double t_next = m_record ? std::min(m_t + m_dt, tmax) : tmax;
+            double t_next = per_interval ? std::min(m_t + m_dt, tmax) : tmax;
             if (tmax - t_next < 1e-12 * std::max(1.0, std::abs(tmax))) {
                 t_next = tmax;
             }
@@ -446,7 +449,9 @@ public:
                 check(mgpu_batch_advance(m_batch, t_next, nullptr), ctx, "mgpu_batch_advance");
             }
             m_t = t_next;
-            record();
+            if (m_record || m_t >= tmax) {
+                record();
+            }
         }
     }
     double get_t() const
@@ -483,13 +488,13 @@ private:
     void apply_dynamic_npis(double t_next)
     {
         mgpu_context* ctx = Device::context();
-        std::vector<double> all;
+        std::vector<double> sums; // without recorded results: the symptomatic infections per node, summed on the device
         if (!m_record) {
-            all.resize(m_arrays.state.size());
-            check(mgpu_batch_get_state(m_batch, all.data()), ctx, "mgpu_batch_get_state");
+            sums.resize(m_graph.nodes().size());
+            check(mgpu_batch_get_compartment_sums(m_batch, MGPU_ISY, sums.data()), ctx,
+                  "mgpu_batch_get_compartment_sums");
         }
-        const size_t n = (size_t)m_arrays.G * osecir::num_compartments;
-        auto& nodes    = m_graph.nodes();
+        auto& nodes = m_graph.nodes();
         for (size_t v = 0; v < nodes.size(); ++v) {
             auto& sim   = nodes[v].property.get_simulation();
             auto& model = sim.get_model();
@@ -498,12 +503,11 @@ private:
             if (npis.get_thresholds().empty()) {
                 continue;
             }
-            std::vector<double> y = m_record ? nodes[v].property.get_result().get_last_value()
-                                             : std::vector<double>(all.begin() + (long)(v * n),
-                                                                   all.begin() + (long)((v + 1) * n));
+            const double inf_rel =
+                m_record ? osecir::get_infections_relative(sim, m_t, nodes[v].property.get_result().get_last_value())
+                         : osecir::get_infections_relative_of_sum(sim, sums[v]);
             auto& contacts = model.parameters.template get<osecir::ContactPatterns<FPT>>();
-            if (check_dynamic_npis(npis, sim.get_dynamic_npi_state(), contacts, m_t,
-                                   osecir::get_infections_relative(sim, m_t, y))) {
+            if (check_dynamic_npis(npis, sim.get_dynamic_npi_state(), contacts, m_t, inf_rel)) {
                 upload_dampings((int)v, contacts);
             }
             const double te = sim.get_dynamic_npi_state().t_end;
@@ -520,8 +524,8 @@ private:
     void apply_edge_npis(double t)
     {
         mgpu_context* ctx = Device::context();
-        std::vector<double> all(m_arrays.state.size());
-        check(mgpu_batch_get_state(m_batch, all.data()), ctx, "mgpu_batch_get_state");
+        std::vector<double> sums(m_graph.nodes().size()); // the sources' symptomatic infections after their solves
+        check(mgpu_batch_get_compartment_sums(m_batch, MGPU_ISY, sums.data()), ctx, "mgpu_batch_get_compartment_sums");
         const size_t n = (size_t)m_arrays.G * osecir::num_compartments;
         auto& edges    = m_graph.edges();
         for (size_t e = 0; e < edges.size(); ++e) {
@@ -530,11 +534,10 @@ private:
             if (npis.get_thresholds().empty()) {
                 continue;
             }
-            const size_t u = edges[e].start_node_idx;
-            std::vector<double> y(all.begin() + (long)(u * n), all.begin() + (long)((u + 1) * n));
+            const size_t u      = edges[e].start_node_idx;
             const auto& src_sim = m_graph.nodes()[u].property.get_simulation();
             if (!check_edge_dynamic_npis(npis, edges[e].property.get_dynamic_npi_state(), params.get_coefficients(), t,
-                                         osecir::get_infections_relative(src_sim, t, y))) {
+                                         osecir::get_infections_relative_of_sum(src_sim, sums[u]))) {
                 continue;
             }
             std::vector<double> times;

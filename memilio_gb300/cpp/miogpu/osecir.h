@@ -581,6 +581,12 @@ FP get_infections_relative(const Simulation<FP>& sim, FP /*t*/, const std::vecto
     }
     return sum_inf / model.populations.get_total();
 }
+/* The same from the symptomatic infections summed over the age groups. */
+template <typename FP>
+FP get_infections_relative_of_sum(const Simulation<FP>& sim, FP sum_inf)
+{
+    return sum_inf / sim.get_model().populations.get_total();
+}
 
 /* mio::FlowSimulation (compartments/flow_simulation.h:36-102): the integrator's
  * state is the accumulated flows; get_result() holds the populations and

@@ -545,7 +545,30 @@ int mode_npi_edges()
         std::snprintf(key, sizeof key, "enacted_%s", tag);
         print_vec(key, enacted);
         std::snprintf(key, sizeof key, "edge_enacted_%s", tag);
-        print_vec(key, edge_enacted, precision == MGPU_PRECISION_FP64);
+        print_vec(key, edge_enacted);
+    }
+    {
+        // the same FP64 run recording only at tmax: the checks read the device's per-node sums
+        auto graph = three_nodes_npi(2);
+        for (auto& e : graph.edges()) {
+            e.property.get_parameters().get_dynamic_npis_infected() = edge_npis(2);
+        }
+        auto sim = make_mobility_sim(0.0, 0.5, std::move(graph));
+        sim.set_record_boundaries(false);
+        sim.advance(12.0);
+        std::vector<double> fin, enacted;
+        for (auto& n : sim.get_graph().nodes()) {
+            auto v = n.property.get_result().get_last_value();
+            fin.insert(fin.end(), v.begin(), v.end());
+            enacted.push_back(n.property.get_simulation().get_dynamic_npi_state().enacted);
+        }
+        for (auto& e : sim.get_graph().edges()) {
+            enacted.push_back(e.property.get_dynamic_npi_state().enacted);
+        }
+        std::printf("\"num_points_norecord\": %zu,\n",
+                    sim.get_graph().nodes()[0].property.get_result().get_num_time_points());
+        print_vec("final_norecord", fin);
+        print_vec("enacted_norecord", enacted, false);
     }
     std::printf("}\n");
     return 0;

@@ -313,6 +313,7 @@ struct mgpu_batch {
     std::vector<double> tmax_host;
     double* d_tmax = nullptr;
     double* d_out  = nullptr; // FP64 read-back buffer of float-float states (allocated on first read)
+    double* d_sums = nullptr; // per-node compartment sums (allocated on first use)
     // batched solver work lists per age-group count
     std::map<int, std::pair<int32_t*, int64_t>> inst_by_G;
     int instances_per_block = 0;
@@ -2308,6 +2309,48 @@ int mgpu_batch_set_state(mgpu_batch* b, const double* state)
                            b->ctx->stream),
            "h2d state");
         ck(cudaStreamSynchronize(b->ctx->stream), "sync");
+        return MGPU_OK;
+    });
+}
+
+__global__ void k_compartment_sums(BatchDev B, int c, double* out)
+{
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= B.num_nodes) {
+        return;
+    }
+    const DevGraph& g  = B.graphs[B.node_graph[v]];
+    const int64_t base = g.state_off + (v - g.node0) * (int64_t)g.G * kC + c;
+    double s           = 0.0;
+    for (int gr = 0; gr < g.G; ++gr) {
+        s += state_get(B, base + (int64_t)gr * kC);
+    }
+    out[v] = s;
+}
+
+int mgpu_batch_get_compartment_sums(mgpu_batch* b, int32_t compartment, double* out)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!out || compartment < 0 || compartment >= kC) {
+            fail(MGPU_INVALID_VALUE, "null output or compartment out of range");
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        cudaStream_t s   = b->ctx->stream;
+        const int64_t nn = b->dev.num_nodes;
+        if (nn == 0) {
+            return MGPU_OK;
+        }
+        if (!b->d_sums) {
+            b->d_sums = b->pool.alloc<double>(nn);
+        }
+        k_compartment_sums<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(b->dev, compartment, b->d_sums);
+        ck(cudaGetLastError(), "k_compartment_sums");
+        ck(cudaMemcpyAsync(out, b->d_sums, sizeof(double) * nn, cudaMemcpyDeviceToHost, s), "d2h sums");
+        ck(cudaStreamSynchronize(s), "sync");
+        ++b->launches;
         return MGPU_OK;
     });
 }

@@ -213,3 +213,31 @@ def test_graph_simulation_with_edge_npis_matches_oracle(programs):
         np.testing.assert_array_equal(np.array(d["enacted_" + tag]), cnt)
         np.testing.assert_array_equal(np.array(d["edge_enacted_" + tag]), ecnt)
         assert scaled(d["final_" + tag], fin, G) < tol
+    # recording only at tmax: the checks read the per-node sums of the device, the same run
+    assert d["num_points_norecord"] == 2
+    np.testing.assert_array_equal(d["final_norecord"], d["final_fp64"])
+    np.testing.assert_array_equal(d["enacted_norecord"], list(d["enacted_fp64"]) + list(d["edge_enacted_fp64"]))
+
+
+@pytest.mark.gpu
+def test_compartment_sums_equal_state_sums():
+    from memilio_gb300 import _native as N
+    ctx = N.Context(0)
+    graphs = [W.mobility_graph(seed=3, N=5, G=2, out_degree=2), W.mobility_graph(seed=4, N=7, G=3, out_degree=3)]
+    for prec in (N.PRECISION_FP64, N.PRECISION_MIXED):
+        b = N.Batch(ctx, graphs, 0.0, N.solver_opts(precision=prec))
+        b.advance(2.0)
+        states = b.states()
+        for c in (L.S, L.ISY, L.D):
+            want = []
+            for g, st in zip(graphs, states):
+                for v in range(g.num_nodes):
+                    s = 0.0
+                    for gr in range(g.num_groups):
+                        s += st[v, gr * 10 + c]
+                    want.append(s)
+            np.testing.assert_array_equal(b.compartment_sums(c), np.array(want))
+        with pytest.raises(N.MgpuError):
+            b.compartment_sums(10)
+        b.close()
+    ctx.close()
