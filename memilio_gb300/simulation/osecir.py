@@ -489,3 +489,96 @@ class GraphParameterStudy:
         for r, g in enumerate(runs):
             handle_result(g, r)
         return None
+
+
+class _StudySimulation:
+    """osecir.Simulation as ParameterStudy.run hands it over: the run's sampled
+    model and its result (every accepted step)."""
+
+    def __init__(self, model: Model, result: TimeSeries):
+        self._model = model
+        self._result = result
+
+    @property
+    def model(self) -> Model:
+        return self._model
+
+    @property
+    def result(self) -> TimeSeries:
+        return self._result
+
+    def get_result(self) -> TimeSeries:
+        return self._result
+
+
+class ParameterStudy:
+    """osecir.ParameterStudy(model, t0, tmax, dt, num_runs) (bind_OdeParameterStudy,
+    bindings/compartments/parameter_studies.h:56-86): num_runs sampled copies of
+    one model, each simulated from t0 to tmax with initial step dt; all runs are
+    integrated together on the GPU (one lane group per run). `sample(model_copy,
+    run_index)` takes draw_sample's place, as for GraphParameterStudy."""
+
+    def __init__(self, model: Model, t0: float, tmax: float, dt: float, num_runs: int, sample=None):
+        if num_runs < 1:
+            raise ValueError("num_runs must be at least 1")
+        self._model = model
+        self._t0, self._tmax, self._dt = float(t0), float(tmax), float(dt)
+        self._num_runs = int(num_runs)
+        self._sample = sample
+
+    @property
+    def num_runs(self) -> int:
+        return self._num_runs
+
+    @property
+    def t0(self) -> float:
+        return self._t0
+
+    @property
+    def tmax(self) -> float:
+        return self._tmax
+
+    @property
+    def dt(self) -> float:
+        return self._dt
+
+    @property
+    def parameters(self) -> Model:
+        return self._model
+
+    def _sampled_models(self) -> List[Model]:
+        import copy
+        runs = []
+        for r in range(self._num_runs):
+            m = copy.deepcopy(self._model)
+            if self._sample is not None:
+                self._sample(m, r)
+            runs.append(m)
+        return runs
+
+    def run(self, handle_result=None):
+        """Simulate every run; with handle_result(simulation, run_index) each is
+        handed over in run order, else the simulations are returned."""
+        models = self._sampled_models()
+        g = _graph_arrays(models, [m.populations.array() for m in models])
+        cap = 4096
+        while True:
+            try:
+                res = _context().simulate(g, list(range(len(models))), self._t0, self._tmax, self._dt,
+                                          max_points=cap)
+                break
+            except N.MgpuError as e:
+                if e.code != _OUT_OF_RANGE or cap >= 1 << 22:
+                    raise
+                cap *= 4
+        sims = []
+        for m, (t, y) in zip(models, res):
+            ts = TimeSeries(g.n)
+            for k in range(t.size):
+                ts.add_time_point(t[k], y[k])
+            sims.append(_StudySimulation(m, ts))
+        if handle_result is None:
+            return sims
+        for r, s in enumerate(sims):
+            handle_result(s, r)
+        return None

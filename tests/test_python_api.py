@@ -157,6 +157,39 @@ def test_parameter_study_matches_oracle():
                                seen[1][1].get_node(1).property.result.get_last_value(), rtol=1e-12, atol=1e-9)
 
 
+def sample_model(model, run):
+    rng = np.random.default_rng(100 + run)
+    model.populations[mio.AgeGroup(0), State.Exposed] = float(rng.uniform(50.0, 150.0))
+    model.parameters.TimeInfectedSymptoms[mio.AgeGroup(0)] = float(rng.uniform(5.0, 7.0))
+
+
+def test_model_parameter_study_samples_copies():
+    m = simple_model()
+    study = osecir.ParameterStudy(m, 0.0, 20.0, 0.1, 4, sample=sample_model)
+    runs = study._sampled_models()
+    assert len({r.parameters.TimeInfectedSymptoms[mio.AgeGroup(0)] for r in runs}) == 4
+    assert m.populations[mio.AgeGroup(0), State.Exposed] == 100.0
+    assert study.parameters is m and study.num_runs == 4
+
+
+@pytest.mark.gpu
+def test_model_parameter_study_matches_oracle():
+    study = osecir.ParameterStudy(simple_model(), 0.0, 30.0, 0.1, 4, sample=sample_model)
+    sims = study.run()
+    for r, (sim, m) in enumerate(zip(sims, study._sampled_models())):
+        g = osecir._graph_arrays([m], [m.populations.array()])
+        t, y, _ = O.simulate(g, 0, 0.0, 30.0, 0.1)
+        got = sim.result
+        assert got.get_num_time_points() == t.size
+        np.testing.assert_allclose(got.as_ndarray()[0], t, rtol=0, atol=1e-9)
+        np.testing.assert_allclose(got.get_last_value(), y[-1], rtol=1e-9, atol=1e-9 * 83000)
+        assert sim.model.parameters.TimeInfectedSymptoms[mio.AgeGroup(0)] == \
+            m.parameters.TimeInfectedSymptoms[mio.AgeGroup(0)]
+    seen = []
+    study.run(lambda s, r: seen.append(r))
+    assert seen == [0, 1, 2, 3]
+
+
 @pytest.mark.gpu
 def test_simulate_matches_oracle():
     m = simple_model()
