@@ -14,8 +14,8 @@ from .. import _native as N
 from .. import layout as L
 from . import AgeGroup, Damping, MobilityParameters, TimeSeries, damping_cache, interpolate_simulation_result
 
-__all__ = ["InfectionState", "Model", "simulate", "MobilityGraph", "MobilitySimulation",
-           "interpolate_simulation_result"]
+__all__ = ["InfectionState", "Parameters", "Populations", "Model", "simulate", "simulate_flows", "MobilityGraph",
+           "MobilitySimulation", "ParameterStudy", "GraphParameterStudy", "interpolate_simulation_result"]
 
 
 class InfectionState(enum.IntEnum):
@@ -303,6 +303,27 @@ def simulate(t0: float, tmax: float, dt: float, model: Model) -> TimeSeries:
     for k in range(t.size):
         ts.add_time_point(t[k], y[k])
     return ts
+
+
+def simulate_flows(t0: float, tmax: float, dt: float, model: Model) -> List[TimeSeries]:
+    """osecir::simulate_flows (models/ode_secir/model.h:404-410,
+    compartments/flow_simulation.h): [populations, flows] of every accepted step,
+    the flows (15 per age group) accumulated from zero; on the GPU."""
+    g = _graph_arrays([model], [model.populations.array()])
+    cap = 4096
+    while True:
+        try:
+            (t, f, y), = _context().simulate_flows(g, [0], float(t0), float(tmax), float(dt), max_points=cap)
+            break
+        except N.MgpuError as e:
+            if e.code != _OUT_OF_RANGE or cap >= 1 << 22:
+                raise
+            cap *= 4
+    pops, flows = TimeSeries(g.n), TimeSeries(f.shape[1])
+    for k in range(t.size):
+        pops.add_time_point(t[k], y[k])
+        flows.add_time_point(t[k], f[k])
+    return [pops, flows]
 
 
 class _Node:

@@ -191,6 +191,18 @@ def test_model_parameter_study_matches_oracle():
 
 
 @pytest.mark.gpu
+def test_simulate_flows_matches_oracle():
+    m = simple_model()
+    pops, flows = osecir.simulate_flows(0, 30, 0.1, m)
+    g = osecir._graph_arrays([m], [m.populations.array()])
+    t, f, y, _ = O.simulate_flows(g, 0, 0.0, 30.0, 0.1)
+    assert pops.get_num_time_points() == flows.get_num_time_points() == t.size
+    np.testing.assert_allclose(flows.as_ndarray()[0], t, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(flows.get_last_value(), f[-1], rtol=1e-9, atol=1e-9 * 83000)
+    np.testing.assert_allclose(pops.get_last_value(), y[-1], rtol=1e-9, atol=1e-9 * 83000)
+
+
+@pytest.mark.gpu
 def test_simulate_matches_oracle():
     m = simple_model()
     r = osecir.simulate(0, 50, 0.1, m)
