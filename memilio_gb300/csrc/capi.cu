@@ -1463,6 +1463,9 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
         return MGPU_INVALID_VALUE;
     }
     return guarded(b->ctx, [&]() -> int {
+        if (b->async_active) {
+            fail(MGPU_INVALID_VALUE, "an asynchronous advance is in progress");
+        }
         if (b->half_step) {
             fail(MGPU_INVALID_VALUE, "the interval begun by mgpu_batch_step_nodes awaits mgpu_batch_step_exchange");
         }
@@ -1636,6 +1639,9 @@ int mgpu_batch_launch(mgpu_batch* b, double tmax, const double* tmax_per_graph, 
         }
         if (b->opts.precision == MGPU_PRECISION_FP64_PLAIN) {
             fail(MGPU_UNSUPPORTED, "asynchronous advance needs a batched precision");
+        }
+        if (b->half_step) {
+            fail(MGPU_INVALID_VALUE, "the interval begun by mgpu_batch_step_nodes awaits mgpu_batch_step_exchange");
         }
         ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
         cudaStream_t s = b->ctx->stream;
@@ -1826,6 +1832,9 @@ int mgpu_batch_autotune(mgpu_batch* b, int32_t* instances_per_block, int32_t* gr
     return guarded(b->ctx, [&]() -> int {
         if (b->opts.precision == MGPU_PRECISION_FP64_PLAIN) {
             fail(MGPU_UNSUPPORTED, "the autotuner schedules the batched solvers");
+        }
+        if (b->half_step) {
+            fail(MGPU_INVALID_VALUE, "the interval begun by mgpu_batch_step_nodes awaits mgpu_batch_step_exchange");
         }
         if (b->async_active) {
             fail(MGPU_INVALID_VALUE, "an asynchronous advance is in progress");
@@ -2078,6 +2087,9 @@ int mgpu_batch_reset(mgpu_batch* b, double t0)
         return MGPU_INVALID_VALUE;
     }
     return guarded(b->ctx, [&]() -> int {
+        if (b->async_active) {
+            fail(MGPU_INVALID_VALUE, "an asynchronous advance is in progress");
+        }
         ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
         const int64_t n = std::max<int64_t>(
             std::max<int64_t>(b->state_total, b->dev.num_nodes),
@@ -2227,6 +2239,9 @@ int mgpu_batch_step_nodes(mgpu_batch* b, double tmax, const double* tmax_per_gra
         if (b->half_step) {
             fail(MGPU_INVALID_VALUE, "the begun interval awaits mgpu_batch_step_exchange");
         }
+        if (b->async_active) {
+            fail(MGPU_INVALID_VALUE, "an asynchronous advance is in progress");
+        }
         ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
         cudaStream_t s = b->ctx->stream;
         for (int i = 0; i < b->num_graphs; ++i) {
@@ -2291,6 +2306,10 @@ int mgpu_batch_set_state(mgpu_batch* b, const double* state)
     return guarded(b->ctx, [&]() -> int {
         if (!state) {
             fail(MGPU_INVALID_VALUE, "null input");
+        }
+        if (b->half_step || b->async_active) {
+            // the departure snapshots of a begun interval come from the states its solves left
+            fail(MGPU_INVALID_VALUE, "states can be replaced only between whole intervals");
         }
         ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
         if (b->pairs) {

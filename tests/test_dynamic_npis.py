@@ -241,3 +241,30 @@ def test_compartment_sums_equal_state_sums():
             b.compartment_sums(10)
         b.close()
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_step_api_order_is_enforced():
+    from memilio_gb300 import _native as N
+    ctx = N.Context(0)
+    g = W.mobility_graph(seed=9, N=4, G=2, out_degree=2)
+    b = N.Batch(ctx, [g], 0.0, N.solver_opts(precision=N.PRECISION_FP64))
+    ref = N.Batch(ctx, [g], 0.0, N.solver_opts(precision=N.PRECISION_FP64))
+    with pytest.raises(N.MgpuError):
+        b.step_exchange()  # no interval begun
+    b.step_nodes(0.5)
+    for call in (lambda: b.advance(1.0), lambda: b.step_nodes(0.5), lambda: b.set_state(ref.state_flat())):
+        with pytest.raises(N.MgpuError):
+            call()
+    b.step_exchange()
+    b.step_nodes(1.0)
+    b.step_exchange()
+    ref.advance(1.0)  # two split intervals equal two whole ones
+    np.testing.assert_array_equal(b.state_flat(), ref.state_flat())
+    b.close()
+    ref.close()
+    plain = N.Batch(ctx, [g], 0.0, N.solver_opts(precision=N.PRECISION_FP64_PLAIN))
+    with pytest.raises(N.MgpuError):
+        plain.step_nodes(0.5)
+    plain.close()
+    ctx.close()
