@@ -3,7 +3,7 @@ SECIR simulations (1024 samples x 400 nodes, ~30 out-edges per node, 6 age
 groups, 90 days, mobility exchange every 0.5 days).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--precision mixed|fp64|plain] [--samples S] [--nodes N] [--days D]
+                  [--precision mixed|mixed_fp64_control|fp64|plain] [--samples S] [--nodes N] [--days D]
 
 One step = one full solve of the ensemble (all samples, all 90 days).
 `value`: inputs resident in HBM (mgpu_batch_reset, then mgpu_batch_advance),
@@ -12,6 +12,9 @@ from host buffers per step: mgpu_batch_create (H2D of every input),
 mgpu_batch_advance, mgpu_batch_get_state (D2H of every node state).
 --impl reference: the FP64 CPU restatement of the reference path (the
 checker), all host threads, one graph per thread, on a bounded sample.
+After the timed region: the oracle's final states of the CPU-baseline sample
+give every precision's per-compartment error (`oracle_error`), and the other
+batched precisions run the same ensemble once each (`precision_legs`).
 Under torchrun every rank solves its own S samples (weak scaling, no collective).
 """
 from __future__ import annotations
@@ -285,13 +288,57 @@ NCU_BYTES_PER_ITEM = {"return": (162.609408e6 + 73.811456e6) / 614400, "depart":
 NCU_ODE_BYTES_PER_INSTANCE = (178.190080e6 + 45.599744e6) / 102400
 
 
+# --precision names, the ABI's precision constants and the arithmetic each computes in
+PRECISION_NAMES = {"mixed": "PRECISION_MIXED", "mixed_fp64_control": "PRECISION_MIXED_FP64_CONTROL",
+                   "fp64": "PRECISION_FP64", "plain": "PRECISION_FP64_PLAIN"}
+DTYPES = {"mixed": "f32 (float-float state)", "mixed_fp64_control": "f32 (f64 state, error norm, controller)",
+          "fp64": "f64", "plain": "f64"}
+ERROR_FLOOR = 1e-6  # absolute floor of the per-compartment error, a fraction of the age group's population
+
+
+def precision_error(O, got, ref, graphs) -> dict:
+    """Per-compartment relative error of final states against the oracle's:
+    max and percentiles over every compartment of every sampled graph, with the
+    floor stated; and the largest error relative to the age group's population."""
+    errs = [O.compartment_error(a, r, g.num_groups, ERROR_FLOOR) for a, r, g in zip(got, ref, graphs)]
+    grp = max(float(O.compartment_error(a, r, g.num_groups, 1.0).max()) for a, r, g in zip(got, ref, graphs))
+    return dict(O.error_summary(errs), floor=ERROR_FLOOR, max_group_scaled=grp,
+                measure="|gpu - oracle| / max(|oracle|, floor * N_group), final states",
+                sample=f"{len(graphs)} samples x {graphs[0].num_nodes} nodes, every compartment of every node")
+
+
+def precision_legs(N, ctx, graphs, days, prec_main, O, ref_final, sample) -> dict:
+    """The batched precisions other than the headline's on the first samples of
+    the same ensemble, one advance each: node-days/s (device time) and the error
+    of the oracle-checked samples."""
+    out = {}
+    for name in ("fp64", "mixed_fp64_control", "mixed"):
+        p = getattr(N, PRECISION_NAMES[name])
+        if p == prec_main:
+            continue
+        b = N.Batch(ctx, graphs, 0.0, N.solver_opts(precision=p))
+        b.advance(0.5)  # warm-up (the interval's CUDA graph is captured here)
+        b.reset(0.0)
+        b.advance(days)
+        ms = b.timing()["advance_ms"]
+        st = b.stats()
+        got = b.states()[:len(sample)]
+        b.close()
+        out[name] = {"value": sum(g.num_nodes for g in graphs) * days / (ms / 1e3), "unit": UNIT,
+                     "ms": ms, "samples": len(graphs), "dtype": DTYPES[name],
+                     "attempts_per_node_day": (st["accepted_steps"] + st["rejected_steps"]) /
+                                              (sum(g.num_nodes for g in graphs) * days),
+                     "oracle_error": precision_error(O, got, ref_final, sample)}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "plain"])
+    ap.add_argument("--precision", default="mixed", choices=list(PRECISION_NAMES))
     ap.add_argument("--samples", type=int, default=1024)
     ap.add_argument("--nodes", type=int, default=400)
     ap.add_argument("--days", type=float, default=90.0)
@@ -299,8 +346,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--uneven", type=int, default=4096, help="graphs of the uneven-batch leg (0 = skip)")
-    ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window per rate (0 = skip)")
-    ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 800.0, 3200.0])
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="arrival window per rate (0 = skip)")
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 800.0])
+    ap.add_argument("--legs-samples", type=int, default=256,
+                    help="samples of the ensemble the other batched precisions run once each (0 = skip)")
     args = ap.parse_args()
 
     from memilio_gb300 import replicas as R
@@ -326,7 +375,7 @@ def main():
     from memilio_gb300 import _native as N
     from memilio_gb300 import build as B
     B.build()
-    prec = {"mixed": N.PRECISION_MIXED, "fp64": N.PRECISION_FP64, "plain": N.PRECISION_FP64_PLAIN}[args.precision]
+    prec = getattr(N, PRECISION_NAMES[args.precision])
     graphs = graphs_builder(args.samples)
     nd_step = sum(g.num_nodes for g in graphs) * args.days
     ctx = N.Context(local)
@@ -373,15 +422,17 @@ def main():
     flops_launch = tm["attempts"] * flops_per_attempt(6) / max(tm["ode_launches"], 1)
     clocks = clk.summary()
     f_sm = clocks["sm_mhz"] or 1965.0
-    fp32_peak = 152 * 128 * 2 * f_sm * 1e6 / 1e12  # TFLOP/s at the sampled clock
+    num_sms = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = num_sms * 128 * 2 * f_sm * 1e6 / 1e12  # TFLOP/s at the sampled clock
     achieved = flops_launch / (ode_ms_launch / 1e3) / 1e12
-    roofline = {"bound": "fp32" if prec == N.PRECISION_MIXED else "fp64",
-                "kernel": "k_ode_mixed<6>" if prec == N.PRECISION_MIXED else (
-                    "k_ode_batched<6,double>" if prec == N.PRECISION_FP64 else "k_ode_plain"),
+    mixed = prec in (N.PRECISION_MIXED, N.PRECISION_MIXED_FP64_CONTROL)
+    roofline = {"bound": "fp32" if mixed else "fp64",
+                "kernel": {N.PRECISION_MIXED: "k_ode_mixed<6,false>", N.PRECISION_MIXED_FP64_CONTROL:
+                           "k_ode_mixed<6,true>", N.PRECISION_FP64: "k_ode_batched<6>"}.get(prec, "k_ode_plain"),
                 "achieved": achieved, "unit": "TFLOP/s",
-                "peak": fp32_peak if prec == N.PRECISION_MIXED else 1.25,
-                "peak_source": ("nominal FP32 FMA rate (152 SMs x 128 lanes x 2) at the sampled median SM clock; "
-                                "MEASURED_PEAKS.json holds no FP32 figure") if prec == N.PRECISION_MIXED else
+                "peak": fp32_peak if mixed else 1.25,
+                "peak_source": (f"nominal FP32 FMA rate ({num_sms} SMs x 128 lanes x 2) at the sampled median SM "
+                                "clock; MEASURED_PEAKS.json holds no FP32 figure") if mixed else
                                "nominal GB300 FP64 rate",
                 "frac": None,
                 "traffic": (NCU_ODE_BYTES_PER_INSTANCE * sum(g.num_nodes for g in graphs)
@@ -395,7 +446,7 @@ def main():
              "depart": tm["depart_ms"]}
     roofline["parts_ms_per_step"] = parts
     dominant = max(parts, key=parts.get)
-    if prec == N.PRECISION_MIXED and dominant in ("return", "depart", "exact"):
+    if mixed and dominant in ("return", "depart", "exact"):
         # the exchange pass that dominates the step, against the measured HBM copy rate
         peaks = measured_peaks()
         items = sum(g.num_nodes * g.num_groups for g in graphs)
@@ -456,24 +507,32 @@ def main():
     uneven = uneven_leg(N, ctx, args) if rank == 0 and args.uneven > 0 else None
     serving = serving_leg(N, ctx, args) if rank == 0 and args.serve_seconds > 0 else None
 
-    cpu = None
+    cpu, oracle_error, legs = None, None, None
     if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
         cores = os.cpu_count() or 1
         sample = graphs[:cores]
-        v, _ = cpu_baseline_run(sample, args.days, cores)
+        ref_final, el, _ = O.ensemble_run(sample, 0.0, args.days, num_threads=cores)
+        v = sum(g.num_nodes for g in sample) * args.days / el
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{len(sample)} samples x {args.nodes} nodes x {args.days:g} days, one graph per thread"}
+        # the same runs are the checker: every precision's final states against them
+        got = np.split(final[:sum(g.num_nodes * g.n for g in sample)], np.cumsum([g.num_nodes * g.n for g in sample])[:-1])
+        oracle_error = dict(precision_error(O, got, ref_final, sample), precision=args.precision)
+        if args.legs_samples > 0 and prec != N.PRECISION_FP64_PLAIN:
+            legs = precision_legs(N, ctx, graphs[:max(args.legs_samples, len(sample))], args.days, prec, O,
+                                  ref_final, sample)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": {"mixed": "f32+f64", "fp64": "f64", "plain": "f64"}[args.precision],
+            "vs_baseline": None, "dtype": DTYPES[args.precision],
             "data": "synthetic (seeded)", "config": workload_config(args), "clocks": clocks,
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
             "attempts_per_node_day": attempts_step / nd_step, "wall_s_timed": t_wall,
             "exchange_per_step": exchange_stats, "plain_fp64": plain, "device_bytes": dev_bytes,
-            "uneven_batch": uneven, "serving": serving,
+            "uneven_batch": uneven, "serving": serving, "oracle_error": oracle_error, "precision_legs": legs,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -41,7 +41,12 @@ enum mgpu_status {
 enum mgpu_precision {
     MGPU_PRECISION_FP64_PLAIN = 0, /* one thread per node, FP64, stage vectors in HBM (the plain drop-in) */
     MGPU_PRECISION_FP64       = 1, /* batched lane-per-age-group solver, FP64 throughout */
-    MGPU_PRECISION_MIXED      = 2  /* batched: FP32 flows and stages, FP64 state, error norm, controller */
+    MGPU_PRECISION_MIXED      = 2, /* batched: FP32 flows, stage combinations, error norm and step-size
+                                      controller on an FP32 interval clock; node states as float-float
+                                      pairs (~48-bit significand) updated with exact TwoSum */
+    MGPU_PRECISION_MIXED_FP64_CONTROL = 3 /* batched: FP32 flows and stage combinations; FP64 state
+                                      accumulation, embedded-error norm, step-size controller and
+                                      interval clock (the exchange as in MGPU_PRECISION_MIXED) */
 };
 
 typedef struct mgpu_context mgpu_context;
@@ -184,6 +189,8 @@ int mgpu_simulate_dt(mgpu_context* ctx, const mgpu_graph* graph, int32_t count, 
  * Set-up: the first call on each device looks up the work space's device
  * address (cudaGetSymbolAddress), which may load the library's device code;
  * make that first call before any stream capture begins on that device.
+ * The address is kept for the life of the process: after cudaDeviceReset (a
+ * new primary context) the library must not be used again in that process.
  *
  * Overlapping calls race: all calls on one device share the one work space, so
  * a call must not start while another call's kernel may still run (on another
@@ -216,13 +223,57 @@ int mgpu_batch_create(mgpu_context* ctx, const mgpu_graph* graphs, int32_t num_g
  * for every graph: node solves, then MobilityEdge::apply_mobility
  * (metapopulation_mobility_instant.h:544-623) every dt_exchange. tmax_per_graph
  * [num_graphs] gives each graph its own horizon; NULL uses `tmax` for all.
+ *
+ * Graphs fail one by one: a node instance that hits the step cap
+ * (max_steps_per_interval) or ends an interval with a NaN/Inf state marks its
+ * own graph failed and the batch carries on; every other graph completes as if
+ * it ran alone. The call then returns MGPU_STEP_FAILED (the message names the
+ * failed graphs) and mgpu_batch_get_failed lists them. In the reference every
+ * ParameterStudy run is an independent simulation and a failed adaptive step
+ * logs and continues (cpp/memilio/compartments/parameter_studies.h:288-345,
+ * cpp/memilio/math/integrator.h:236-246).
  */
 int mgpu_batch_advance(mgpu_batch* batch, double tmax, const double* tmax_per_graph);
+
+/*
+ * Commuter statistics of the edges of one graph: MobilityEdge's mobility
+ * results (MobilityEdge::add_mobility_result_time_point,
+ * cpp/memilio/mobility/metapopulation_mobility_instant.h:423-447, with the save
+ * indices of MobilityParameters, :145-170, 241-244). At every departure and at
+ * every return (after the underflow fix) of an edge that carries travelers,
+ * one time point: the exchange time, the travelers' sum over each of num_sets
+ * sets of flat compartment indices (g * 10 + c, summed in the set's order), and
+ * their sum over all compartments. The sets apply to every edge of the graph:
+ * set_offsets [num_sets + 1] (set_offsets[0] = 0), set_indices
+ * [set_offsets[num_sets]]. capacity: time points kept per edge (one advance of
+ * D days with 0.5-day exchanges makes 2 D). Recording starts with the next
+ * advance and restarts at mgpu_batch_reset; num_sets = 0 switches it off for
+ * the graph. Batched precisions only (MGPU_UNSUPPORTED for
+ * MGPU_PRECISION_FP64_PLAIN).
+ */
+int mgpu_batch_set_commuter_stats(mgpu_batch* batch, int32_t graph, int32_t num_sets, const int32_t* set_offsets,
+                                  const int32_t* set_indices, int32_t capacity);
+/* The recorded time points of every edge of the graph (edges in the graph's
+ * (start, end) order): counts [E], times [E][capacity], values
+ * [E][capacity][num_sets + 1] (times and values may be NULL). MGPU_OUT_OF_RANGE
+ * if an edge recorded more points than the capacity (the first ones are kept;
+ * counts holds the true numbers). */
+int mgpu_batch_get_commuter_stats(mgpu_batch* batch, int32_t graph, int32_t* counts, double* times, double* values);
+
+/* Failure flags of the node solves since creation or the last reset, per graph
+ * [num_graphs]: 0, or MGPU_FAILED_STEP_CAP | MGPU_FAILED_NONFINITE; and the
+ * number of failed graphs (either output may be NULL, not both). During an
+ * asynchronous advance it waits for the intervals launched so far and reports
+ * their flags. */
+#define MGPU_FAILED_STEP_CAP 1
+#define MGPU_FAILED_NONFINITE 2
+int mgpu_batch_get_failed(mgpu_batch* batch, int32_t* flags, int32_t* num_failed);
 
 /* Restart every graph at time t0 from the initial states given at creation,
  * with the inputs still resident on the device: the equivalent of building
  * a fresh make_mobility_sim(t0, dt, graph) from the same graph
- * (cpp/memilio/mobility/metapopulation_mobility_instant.h:656-678). */
+ * (cpp/memilio/mobility/metapopulation_mobility_instant.h:656-678). Clears the
+ * failure flags. */
 int mgpu_batch_reset(mgpu_batch* batch, double t0);
 
 /* Node states (result last values) of all graphs, concatenated [sum_b N_b][10 G_b]. */

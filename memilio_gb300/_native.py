@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 from typing import Optional, Sequence
 
 import numpy as np
@@ -24,6 +25,9 @@ STATUS_NAMES = {0: "OK", 1: "UnknownError", 2: "OutOfRange", 3: "InvalidValue", 
 PRECISION_FP64_PLAIN = 0
 PRECISION_FP64 = 1
 PRECISION_MIXED = 2
+PRECISION_MIXED_FP64_CONTROL = 3
+FAILED_STEP_CAP = 1
+FAILED_NONFINITE = 2
 
 # every entry point declared in include/miogpu.h
 EXPORTED = ["mgpu_default_solver_opts", "mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_set_memory_budget",
@@ -31,7 +35,8 @@ EXPORTED = ["mgpu_default_solver_opts", "mgpu_create", "mgpu_destroy", "mgpu_las
             "mgpu_batch_get_time", "mgpu_batch_set_state", "mgpu_batch_set_damping_cache", "mgpu_batch_set_edge_damping_cache",
             "mgpu_batch_step_nodes", "mgpu_batch_step_exchange", "mgpu_batch_get_compartment_sums", "mgpu_batch_get_stats", "mgpu_batch_get_timing",
             "mgpu_batch_device_bytes", "mgpu_batch_reset", "mgpu_batch_destroy", "mgpu_simulate_final_noalloc",
-            "mgpu_batch_launch", "mgpu_batch_query", "mgpu_batch_autotune", "mgpu_simulate_dt", "mgpu_simulate_flows", "mgpu_batch_ensemble_stats", "mgpu_batch_get_graph_state", "mgpu_batch_estimate_bytes",
+            "mgpu_batch_launch", "mgpu_batch_query", "mgpu_batch_get_failed", "mgpu_batch_set_commuter_stats",
+            "mgpu_batch_get_commuter_stats", "mgpu_batch_autotune", "mgpu_simulate_dt", "mgpu_simulate_flows", "mgpu_batch_ensemble_stats", "mgpu_batch_get_graph_state", "mgpu_batch_estimate_bytes",
             "mgpu_default_server_opts", "mgpu_server_create", "mgpu_server_destroy", "mgpu_server_submit",
             "mgpu_server_step", "mgpu_server_take", "mgpu_server_memory_in_use", "mgpu_server_num_batches"]
 
@@ -148,6 +153,9 @@ def lib():
                                               P(MgpuIntegratorOpts), vp, vp]
     L.mgpu_batch_launch.argtypes = [vp, d, P(d), i32, P(i32)]
     L.mgpu_batch_query.argtypes = [vp, P(i32)]
+    L.mgpu_batch_get_failed.argtypes = [vp, P(i32), P(i32)]
+    L.mgpu_batch_set_commuter_stats.argtypes = [vp, i32, i32, P(i32), P(i32), i32]
+    L.mgpu_batch_get_commuter_stats.argtypes = [vp, i32, P(i32), P(d), P(d)]
     L.mgpu_batch_autotune.argtypes = [vp, P(i32), P(i32)]
     L.mgpu_batch_ensemble_stats.argtypes = [vp, P(d), i32, P(d), P(d)]
     L.mgpu_batch_get_graph_state.argtypes = [vp, i32, P(d)]
@@ -203,6 +211,7 @@ class Context:
 
     def __init__(self, device: int = 0):
         self._h = ctypes.c_void_p()
+        self._batches = weakref.WeakSet()  # batches to close before the context
         rc = lib().mgpu_create(device, ctypes.byref(self._h))
         if rc != OK:
             raise MgpuError(rc, "mgpu_create failed")
@@ -217,6 +226,8 @@ class Context:
 
     def close(self):
         if self._h:
+            for b in list(self._batches):
+                b.close()
             lib().mgpu_destroy(self._h)
             self._h = ctypes.c_void_p()
 
@@ -284,6 +295,7 @@ class Batch:
         opts = opts or solver_opts()
         ctx.check(lib().mgpu_batch_create(ctx.handle, self._arr, len(self.graphs), t0, ctypes.byref(opts),
                                           ctypes.byref(self._h)))
+        ctx._batches.add(self)
         self.sizes = [g.num_nodes * g.n for g in self.graphs]
         self.total = int(sum(self.sizes))
 
@@ -294,6 +306,56 @@ class Batch:
             self.ctx.check(lib().mgpu_batch_advance(self._h, float(tmax), _dp(tpg)))
         else:
             self.ctx.check(lib().mgpu_batch_advance(self._h, float(tmax), ctypes.POINTER(ctypes.c_double)()))
+
+    def launch(self, tmax: float, max_phases: int) -> int:
+        """mgpu_batch_launch: enqueue up to max_phases intervals of an advance to tmax
+        without waiting; returns the intervals still to launch."""
+        rem = ctypes.c_int32()
+        self.ctx.check(lib().mgpu_batch_launch(self._h, float(tmax), ctypes.POINTER(ctypes.c_double)(),
+                                               int(max_phases), ctypes.byref(rem)))
+        return rem.value
+
+    def query(self) -> bool:
+        """mgpu_batch_query: True when the launched intervals have finished."""
+        done = ctypes.c_int32()
+        self.ctx.check(lib().mgpu_batch_query(self._h, ctypes.byref(done)))
+        return bool(done.value)
+
+    def set_commuter_stats(self, graph: int, save_sets, capacity: int):
+        """mgpu_batch_set_commuter_stats: record the edges' mobility results of one
+        graph with these sets of flat compartment indices (empty: stop)."""
+        off = np.zeros(len(save_sets) + 1, np.int32)
+        for i, st in enumerate(save_sets):
+            off[i + 1] = off[i] + len(st)
+        idx = np.ascontiguousarray(np.concatenate([np.asarray(st, np.int32) for st in save_sets])
+                                   if save_sets else np.zeros(1, np.int32), np.int32)
+        ip = ctypes.POINTER(ctypes.c_int32)
+        self.ctx.check(lib().mgpu_batch_set_commuter_stats(self._h, int(graph), len(save_sets), off.ctypes.data_as(ip),
+                                                           idx.ctypes.data_as(ip), int(capacity)))
+        self._stats = getattr(self, "_stats", {})
+        self._stats[graph] = (len(save_sets), int(capacity))
+
+    def commuter_stats(self, graph: int):
+        """mgpu_batch_get_commuter_stats: (counts [E], times [E, capacity],
+        values [E, capacity, sets + 1]) of one graph."""
+        S, cap = self._stats[graph]
+        E = max(self.graphs[graph].num_edges, 1)
+        counts = np.zeros(E, np.int32)
+        times = np.zeros((E, cap))
+        values = np.zeros((E, cap, S + 1))
+        self.ctx.check(lib().mgpu_batch_get_commuter_stats(self._h, int(graph),
+                                                           counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                                           _dp(times), _dp(values)))
+        E = self.graphs[graph].num_edges
+        return counts[:E], times[:E], values[:E]
+
+    def failed(self) -> np.ndarray:
+        """mgpu_batch_get_failed: per graph 0, or FAILED_STEP_CAP | FAILED_NONFINITE."""
+        f = np.zeros(max(len(self.graphs), 1), np.int32)
+        n = ctypes.c_int32()
+        self.ctx.check(lib().mgpu_batch_get_failed(self._h, f.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                                   ctypes.byref(n)))
+        return f[:len(self.graphs)]
 
     def state_flat(self, out: Optional[np.ndarray] = None) -> np.ndarray:
         if out is None:

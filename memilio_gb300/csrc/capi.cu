@@ -16,6 +16,8 @@
 #include <functional>
 #include <limits>
 #include <map>
+#include <mutex>
+#include <set>
 #include <tuple>
 #include <new>
 #include <string>
@@ -34,6 +36,15 @@ struct mgpu_context {
     void* pinned         = nullptr;
     size_t pinned_bytes  = 0;
 };
+
+namespace
+{
+// Live batches of every context. mgpu_destroy releases a context's remaining
+// batches first; destroying a batch that is no longer registered (destroyed
+// already, or released with its context) does nothing.
+std::mutex g_batches_mutex;
+std::set<mgpu_batch*> g_batches;
+} // namespace
 
 int mgpu::context_device_stream(const mgpu_context* ctx, int* device, cudaStream_t* stream)
 {
@@ -323,6 +334,10 @@ struct mgpu_batch {
     int64_t launches        = 0;
     int64_t phases          = 0;
     int64_t seq_exchanges   = 0;
+    // commuter statistics per graph (mgpu_batch_set_commuter_stats): descriptors as
+    // uploaded to dev.estats, and the device buffers of all graphs that record
+    std::vector<EdgeStatsDev> stats_host;
+    DevPool stats_pool;
     // CUDA graph of one batched interval
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_failed          = false;
@@ -353,7 +368,17 @@ struct mgpu_batch {
         if (ev_async) {
             cudaEventDestroy(ev_async);
         }
+        stats_pool.release();
         pool.release();
+    }
+
+    // the captured interval holds the kernels' parameters: capture again after they change
+    void drop_graph()
+    {
+        if (graph_exec) {
+            cudaGraphExecDestroy(graph_exec);
+            graph_exec = nullptr;
+        }
     }
 
     cudaEvent_t phase_event(size_t i)
@@ -496,9 +521,13 @@ __global__ void k_reset(BatchDev B, const double* init_state, const float* init_
     if (tid < B.num_graphs) {
         GraphRt r;
         memset(&r, 0, sizeof(r));
-        r.t         = t0;
-        r.tmax      = t0;
-        B.rt[tid]   = r;
+        r.t              = t0;
+        r.tmax           = t0;
+        B.rt[tid]        = r;
+        B.graph_err[tid] = 0; // a restarted graph has not failed
+    }
+    if (tid == 0) {
+        *B.err = 0;
     }
 }
 
@@ -677,7 +706,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     arena.place();
     trace.mark("page-locked staging");
     // FP32 coefficient records (rec_vec layout) of the mixed exchange; the factor slots stay zero
-    std::vector<float> h_ecr(b->opts.precision == MGPU_PRECISION_MIXED ? ecf / kC * kRec : 0, 0.0f);
+    std::vector<float> h_ecr(is_mixed(b->opts.precision) ? ecf / kC * kRec : 0, 0.0f);
     std::vector<int64_t> h_out_ptr(nodes + 1, 0);
     std::vector<int32_t> mob_mask(num_graphs, 0);
     // Graphs pack into disjoint ranges of the staging buffers, on the host's
@@ -834,7 +863,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.dtimes     = b->pool.upload(h_dtt);
     B.dvals      = b->pool.upload(h_dtv);
     b->dt0     = dt0;
-    b->pairs   = b->opts.precision == MGPU_PRECISION_MIXED;
+    b->pairs   = is_mixed(b->opts.precision);
     B.st_hi    = B.st_lo = B.v0_hi = B.v0_lo = B.yn_hi = B.yn_lo = nullptr;
     B.state    = nullptr;
     B.v0       = nullptr;
@@ -887,7 +916,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.tab_f      = nullptr;
     B.contact_f  = nullptr;
     B.dvals_f    = nullptr;
-    if (b->opts.precision == MGPU_PRECISION_MIXED) {
+    if (is_mixed(b->opts.precision)) {
         // FP32 node constants, contact and damping pools of the mixed solver
         // derived on the device from the uploaded FP64 pools (no second host copy, no second upload)
         float* tab = b->pool.alloc<float>(nodes * MGPU_MAX_GROUPS * kTabF);
@@ -959,8 +988,10 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.opts.max_steps = b->opts.max_steps_per_interval > 0 ? b->opts.max_steps_per_interval : 100000;
     B.opts.method    = b->opts.integrator.method;
     B.err            = b->pool.alloc<int32_t>(1);
+    B.graph_err      = b->pool.alloc<int32_t>(num_graphs);
     B.counters       = b->pool.alloc<unsigned long long>(CNT_NUM);
     ck(cudaMemsetAsync(B.err, 0, sizeof(int32_t), ctx->stream), "memset");
+    ck(cudaMemsetAsync(B.graph_err, 0, sizeof(int32_t) * std::max(num_graphs, 1), ctx->stream), "memset");
     ck(cudaMemsetAsync(B.counters, 0, sizeof(unsigned long long) * CNT_NUM, ctx->stream), "memset");
     b->d_tmax = b->pool.alloc<double>(num_graphs);
     b->t_host.assign(num_graphs, t0);
@@ -980,7 +1011,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         auto it     = b->inst_by_G.find(G);
         B.glist[G]  = it != b->inst_by_G.end() ? it->second.first : nullptr;
         B.gcount[G] = it != b->inst_by_G.end() ? it->second.second : 0;
-        B.gorder[G] = (b->opts.precision == MGPU_PRECISION_MIXED && B.gcount[G] > 0)
+        B.gorder[G] = (is_mixed(b->opts.precision) && B.gcount[G] > 0)
                           ? b->pool.alloc<int32_t>(B.gcount[G])
                           : nullptr;
     }
@@ -991,17 +1022,45 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     staging.release();
 }
 
+// The per-graph failure words of the batch ([num_graphs], ERR_STEP_CAP / ERR_NONFINITE).
+std::vector<int32_t> read_graph_errors(mgpu_batch* b)
+{
+    std::vector<int32_t> f((size_t)b->num_graphs, 0);
+    if (b->num_graphs > 0) {
+        ck(cudaMemcpyAsync(f.data(), b->dev.graph_err, sizeof(int32_t) * f.size(), cudaMemcpyDeviceToHost,
+                           b->ctx->stream),
+           "read graph error words");
+        ck(cudaStreamSynchronize(b->ctx->stream), "sync");
+    }
+    return f;
+}
+
+// MGPU_STEP_FAILED when instances of some graphs hit the step cap or produced
+// non-finite states; those graphs are named (mgpu_batch_get_failed lists all),
+// and every other graph of the batch has completed normally.
 int check_device_error(mgpu_batch* b)
 {
     int32_t err = 0;
     ck(cudaMemcpyAsync(&err, b->dev.err, sizeof(err), cudaMemcpyDeviceToHost, b->ctx->stream), "read error word");
     ck(cudaStreamSynchronize(b->ctx->stream), "sync");
-    if (err & (ERR_STEP_CAP | ERR_NONFINITE)) {
-        fail(MGPU_STEP_FAILED, std::string("node solve failed:") + ((err & ERR_STEP_CAP) ? " step cap reached" : "") +
-                                   ((err & ERR_NONFINITE) ? " non-finite state" : ""));
+    if (err & ~(ERR_STEP_CAP | ERR_NONFINITE)) {
+        fail(MGPU_UNKNOWN_ERROR, "device error word " + std::to_string(err));
     }
     if (err) {
-        fail(MGPU_UNKNOWN_ERROR, "device error word " + std::to_string(err));
+        const std::vector<int32_t> f = read_graph_errors(b);
+        std::string which;
+        int failed = 0;
+        for (int i = 0; i < b->num_graphs; ++i) {
+            if (f[(size_t)i]) {
+                if (++failed <= 8) {
+                    which += " " + std::to_string(i) + ((f[(size_t)i] & ERR_STEP_CAP) ? " (step cap)" : "") +
+                             ((f[(size_t)i] & ERR_NONFINITE) ? " (non-finite state)" : "");
+                }
+            }
+        }
+        fail(MGPU_STEP_FAILED, "node solves failed in " + std::to_string(failed) + " of " +
+                                   std::to_string(b->num_graphs) + " graphs:" + which + (failed > 8 ? " ..." : "") +
+                                   "; the other graphs completed (mgpu_batch_get_failed)");
     }
     return MGPU_OK;
 }
@@ -1009,7 +1068,7 @@ int check_device_error(mgpu_batch* b)
 // node-solve launches per interval: one per age-group count (mixed: with its ordering pass)
 int64_t node_kernel_launches(const mgpu_batch* b)
 {
-    return (int64_t)b->inst_by_G.size() * (b->opts.precision == MGPU_PRECISION_MIXED ? 2 : 1);
+    return (int64_t)b->inst_by_G.size() * (is_mixed(b->opts.precision) ? 2 : 1);
 }
 
 // One batched interval: interval bookkeeping, node solves per G, exchange.
@@ -1152,6 +1211,24 @@ void mgpu_destroy(mgpu_context* ctx)
         return;
     }
     cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    // the context's remaining batches free their device memory on its stream, before it goes
+    std::vector<mgpu_batch*> mine;
+    {
+        std::lock_guard<std::mutex> lock(g_batches_mutex);
+        for (auto it = g_batches.begin(); it != g_batches.end();) {
+            if ((*it)->ctx == ctx) {
+                mine.push_back(*it);
+                it = g_batches.erase(it);
+            }
+            else {
+                ++it;
+            }
+        }
+    }
+    for (mgpu_batch* b : mine) {
+        delete b;
+    }
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
     if (ctx->pinned) {
@@ -1429,7 +1506,7 @@ int mgpu_batch_create(mgpu_context* ctx, const mgpu_graph* graphs, int32_t num_g
         if (!(o.dt_exchange > 0) || !(o.dt0 > 0)) {
             fail(MGPU_INVALID_VALUE, "dt0 and dt_exchange must be > 0");
         }
-        if (o.precision < MGPU_PRECISION_FP64_PLAIN || o.precision > MGPU_PRECISION_MIXED) {
+        if (o.precision < MGPU_PRECISION_FP64_PLAIN || o.precision > MGPU_PRECISION_MIXED_FP64_CONTROL) {
             fail(MGPU_INVALID_VALUE, "unknown precision");
         }
         if (o.precision != MGPU_PRECISION_FP64_PLAIN && o.integrator.method != MGPU_METHOD_CASH_KARP54) {
@@ -1451,6 +1528,10 @@ int mgpu_batch_create(mgpu_context* ctx, const mgpu_graph* graphs, int32_t num_g
         catch (...) {
             delete b;
             throw;
+        }
+        {
+            std::lock_guard<std::mutex> lock(g_batches_mutex);
+            g_batches.insert(b);
         }
         *out = b;
         return MGPU_OK;
@@ -1556,7 +1637,7 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
                 ode_launches += (int64_t)b->inst_by_G.size(); // node-solve kernels (their ordering passes excluded)
             }
             b->launches +=
-                P * (2 + node_kernel_launches(b) + exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size()));
+                P * (2 + node_kernel_launches(b) + exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size(), b->dev.estats != nullptr));
             b->phases += P;
         }
         else {
@@ -1577,7 +1658,7 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
                 }
             }
             const int64_t per_phase = 2 + node_kernel_launches(b) +
-                                      exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size());
+                                      exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size(), b->dev.estats != nullptr);
             for (int64_t p = 0; p < P; ++p) {
                 if (b->graph_exec) {
                     ck(cudaGraphLaunch(b->graph_exec, s), "cudaGraphLaunch");
@@ -1688,7 +1769,7 @@ int mgpu_batch_launch(mgpu_batch* b, double tmax, const double* tmax_per_graph, 
         }
         ck(cudaGetLastError(), "launch");
         b->launches += n * (2 + node_kernel_launches(b) +
-                            exchange_batched_launches(b->opts.precision, b->dev.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size()));
+                            exchange_batched_launches(b->opts.precision, b->dev.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size(), b->dev.estats != nullptr));
         b->phases += n;
         b->async_left -= n;
         ck(cudaEventRecord(b->ev_async, s), "cudaEventRecord");
@@ -1791,7 +1872,7 @@ int64_t mgpu_batch_estimate_bytes(const mgpu_graph* graphs, int32_t num_graphs, 
         mgpu_default_solver_opts(&o);
     }
     const bool plain = o.precision == MGPU_PRECISION_FP64_PLAIN;
-    const bool mixed = o.precision == MGPU_PRECISION_MIXED;
+    const bool mixed = is_mixed(o.precision);
     int64_t nodes = 0, edges = 0, st = 0, tr = 0, par = 0, con = 0, dtv = 0, dtt = 0, ec = 0, edv = 0, edt = 0,
             nmax = 0;
     for (int i = 0; i < num_graphs; ++i) {
@@ -1874,6 +1955,12 @@ int mgpu_batch_autotune(mgpu_batch* b, int32_t* instances_per_block, int32_t* gr
             keep(B.rt, sizeof(GraphRt) * (size_t)b->num_graphs);
             keep(B.counters, sizeof(unsigned long long) * CNT_NUM);
             keep(B.err, sizeof(int32_t));
+            keep(B.graph_err, sizeof(int32_t) * (size_t)b->num_graphs);
+            for (int i = 0; i < b->num_graphs && !b->stats_host.empty(); ++i) {
+                if (b->stats_host[(size_t)i].num_sets) {
+                    keep(b->stats_host[(size_t)i].count, sizeof(int32_t) * (size_t)b->host_graphs[(size_t)i].E);
+                }
+            }
             keep(b->d_tmax, sizeof(double) * (size_t)b->num_graphs);
             restore_all = [&]() {
                 for (auto& x : saved) {
@@ -2099,6 +2186,14 @@ int mgpu_batch_reset(mgpu_batch* b, double t0)
                                                                           b->dt0);
         ++b->launches;
         ck(cudaGetLastError(), "k_reset");
+        for (int i = 0; i < b->num_graphs && !b->stats_host.empty(); ++i) {
+            const EdgeStatsDev& S = b->stats_host[(size_t)i];
+            if (S.num_sets) {
+                ck(cudaMemsetAsync(S.count, 0, sizeof(int32_t) * std::max(b->host_graphs[(size_t)i].E, 1),
+                                   b->ctx->stream),
+                   "memset");
+            }
+        }
         ck(cudaStreamSynchronize(b->ctx->stream), "sync");
         b->half_step = false;
         b->t_host.assign(b->num_graphs, t0);
@@ -2138,6 +2233,11 @@ int mgpu_batch_set_damping_cache(mgpu_batch* b, int32_t graph, int32_t node, int
         return MGPU_INVALID_VALUE;
     }
     return guarded(b->ctx, [&]() -> int {
+        if (b->async_active) {
+            // a cache written now would take effect at an interval boundary that
+            // depends on how the advance was split into launches
+            fail(MGPU_INVALID_VALUE, "an asynchronous advance is in progress");
+        }
         if (!times || !values || graph < 0 || graph >= b->num_graphs) {
             fail(MGPU_INVALID_VALUE, "null array or graph index out of range");
         }
@@ -2191,6 +2291,9 @@ int mgpu_batch_set_edge_damping_cache(mgpu_batch* b, int32_t graph, int32_t edge
         return MGPU_INVALID_VALUE;
     }
     return guarded(b->ctx, [&]() -> int {
+        if (b->async_active) {
+            fail(MGPU_INVALID_VALUE, "an asynchronous advance is in progress");
+        }
         if (!times || !values || graph < 0 || graph >= b->num_graphs) {
             fail(MGPU_INVALID_VALUE, "null array or graph index out of range");
         }
@@ -2412,6 +2515,184 @@ int mgpu_batch_get_stats(mgpu_batch* b, mgpu_stats* out)
     });
 }
 
+int mgpu_batch_set_commuter_stats(mgpu_batch* b, int32_t graph, int32_t num_sets, const int32_t* set_offsets,
+                                  const int32_t* set_indices, int32_t capacity)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (b->async_active || b->half_step) {
+            fail(MGPU_INVALID_VALUE, "an advance is in progress");
+        }
+        if (b->opts.precision == MGPU_PRECISION_FP64_PLAIN) {
+            fail(MGPU_UNSUPPORTED, "commuter statistics need a batched precision");
+        }
+        if (graph < 0 || graph >= b->num_graphs) {
+            fail(MGPU_OUT_OF_RANGE, "graph index out of range");
+        }
+        if (num_sets < 0 || (num_sets > 0 && (!set_offsets || !set_indices || capacity < 1))) {
+            fail(MGPU_INVALID_VALUE, "index sets (offsets, indices) and capacity >= 1 needed");
+        }
+        const DevGraph& d = b->host_graphs[(size_t)graph];
+        if (num_sets > 0) {
+            if (set_offsets[0] != 0) {
+                fail(MGPU_INVALID_VALUE, "set_offsets[0] must be 0");
+            }
+            for (int i = 0; i < num_sets; ++i) {
+                if (set_offsets[i + 1] < set_offsets[i]) {
+                    fail(MGPU_INVALID_VALUE, "set_offsets must be non-decreasing");
+                }
+            }
+            for (int q = 0; q < set_offsets[num_sets]; ++q) {
+                if (set_indices[q] < 0 || set_indices[q] >= d.n) {
+                    fail(MGPU_OUT_OF_RANGE, "compartment index outside [0, 10 G)");
+                }
+            }
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        cudaStream_t s = b->ctx->stream;
+        if (b->stats_host.empty()) {
+            b->stats_host.assign((size_t)b->num_graphs, EdgeStatsDev{});
+        }
+        // the buffers of every graph that keeps recording are laid out again (the
+        // pool frees all at once); recorded points of the other graphs are kept
+        std::vector<EdgeStatsDev> old = b->stats_host;
+        DevPool fresh;
+        fresh.ctx = b->ctx;
+        std::vector<EdgeStatsDev> next((size_t)b->num_graphs, EdgeStatsDev{});
+        for (int i = 0; i < b->num_graphs; ++i) {
+            const bool is_new = i == graph;
+            const int32_t S   = is_new ? num_sets : old[(size_t)i].num_sets;
+            if (S == 0) {
+                continue;
+            }
+            const int64_t E   = std::max(b->host_graphs[(size_t)i].E, 1);
+            const int32_t cap = is_new ? capacity : old[(size_t)i].capacity;
+            EdgeStatsDev& x   = next[(size_t)i];
+            x.num_sets        = S;
+            x.capacity        = cap;
+            int32_t* sp       = fresh.alloc<int32_t>(S + 1);
+            const int64_t ni  = is_new ? set_offsets[S] : 0;
+            int32_t* si       = fresh.alloc<int32_t>(is_new ? ni : 1);
+            x.count           = fresh.alloc<int32_t>(E);
+            x.times           = fresh.alloc<double>(E * cap);
+            x.values          = fresh.alloc<double>(E * cap * (S + 1));
+            if (is_new) {
+                ck(cudaMemcpyAsync(sp, set_offsets, sizeof(int32_t) * (S + 1), cudaMemcpyHostToDevice, s), "h2d");
+                if (ni > 0) {
+                    ck(cudaMemcpyAsync(si, set_indices, sizeof(int32_t) * ni, cudaMemcpyHostToDevice, s), "h2d");
+                }
+                ck(cudaMemsetAsync(x.count, 0, sizeof(int32_t) * E, s), "memset");
+                x.set_ptr = sp;
+                x.set_idx = si;
+            }
+            else {
+                // carry the other graphs' sets and recorded points over
+                const EdgeStatsDev& o = old[(size_t)i];
+                int32_t np = 0;
+                ck(cudaMemcpyAsync(&np, o.set_ptr + S, sizeof(int32_t), cudaMemcpyDeviceToHost, s), "d2h");
+                ck(cudaStreamSynchronize(s), "sync");
+                int32_t* si2 = fresh.alloc<int32_t>(std::max(np, 1));
+                ck(cudaMemcpyAsync(sp, o.set_ptr, sizeof(int32_t) * (S + 1), cudaMemcpyDeviceToDevice, s), "d2d");
+                ck(cudaMemcpyAsync(si2, o.set_idx, sizeof(int32_t) * np, cudaMemcpyDeviceToDevice, s), "d2d");
+                ck(cudaMemcpyAsync(x.count, o.count, sizeof(int32_t) * E, cudaMemcpyDeviceToDevice, s), "d2d");
+                ck(cudaMemcpyAsync(x.times, o.times, sizeof(double) * E * cap, cudaMemcpyDeviceToDevice, s), "d2d");
+                ck(cudaMemcpyAsync(x.values, o.values, sizeof(double) * E * cap * (S + 1), cudaMemcpyDeviceToDevice,
+                                   s),
+                   "d2d");
+                x.set_ptr = sp;
+                x.set_idx = si2;
+            }
+        }
+        bool any = false;
+        for (const auto& x : next) {
+            any = any || x.num_sets > 0;
+        }
+        EdgeStatsDev* table = any ? fresh.upload(next) : nullptr;
+        ck(cudaStreamSynchronize(s), "sync");
+        b->stats_pool.release();
+        b->stats_pool = fresh;
+        b->stats_host = next;
+        b->dev.estats = table;
+        b->drop_graph();
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_get_commuter_stats(mgpu_batch* b, int32_t graph, int32_t* counts, double* times, double* values)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (b->async_active) {
+            fail(MGPU_INVALID_VALUE, "an asynchronous advance is in progress");
+        }
+        if (graph < 0 || graph >= b->num_graphs) {
+            fail(MGPU_OUT_OF_RANGE, "graph index out of range");
+        }
+        if (b->stats_host.empty() || b->stats_host[(size_t)graph].num_sets == 0) {
+            fail(MGPU_INVALID_VALUE, "the graph records no commuter statistics");
+        }
+        if (!counts) {
+            fail(MGPU_INVALID_VALUE, "null counts");
+        }
+        const EdgeStatsDev& x = b->stats_host[(size_t)graph];
+        const int64_t E       = b->host_graphs[(size_t)graph].E;
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        cudaStream_t s = b->ctx->stream;
+        if (E > 0) {
+            ck(cudaMemcpyAsync(counts, x.count, sizeof(int32_t) * E, cudaMemcpyDeviceToHost, s), "d2h");
+            if (times) {
+                ck(cudaMemcpyAsync(times, x.times, sizeof(double) * E * x.capacity, cudaMemcpyDeviceToHost, s), "d2h");
+            }
+            if (values) {
+                ck(cudaMemcpyAsync(values, x.values, sizeof(double) * E * x.capacity * (x.num_sets + 1),
+                                   cudaMemcpyDeviceToHost, s),
+                   "d2h");
+            }
+        }
+        ck(cudaStreamSynchronize(s), "sync");
+        for (int64_t e = 0; e < E; ++e) {
+            if (counts[e] > x.capacity) {
+                fail(MGPU_OUT_OF_RANGE, "an edge recorded more time points than the capacity (" +
+                                            std::to_string(counts[e]) + " > " + std::to_string(x.capacity) +
+                                            "); the first capacity points were kept");
+            }
+        }
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_get_failed(mgpu_batch* b, int32_t* flags, int32_t* num_failed)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!flags && !num_failed) {
+            fail(MGPU_INVALID_VALUE, "null outputs");
+        }
+        // (read-only: during an asynchronous advance, after the launched intervals)
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        const std::vector<int32_t> f = read_graph_errors(b);
+        int32_t n = 0;
+        for (int i = 0; i < b->num_graphs; ++i) {
+            const int32_t bits = (f[(size_t)i] & ERR_STEP_CAP ? MGPU_FAILED_STEP_CAP : 0) |
+                                 (f[(size_t)i] & ERR_NONFINITE ? MGPU_FAILED_NONFINITE : 0);
+            if (flags) {
+                flags[i] = bits;
+            }
+            n += bits ? 1 : 0;
+        }
+        if (num_failed) {
+            *num_failed = n;
+        }
+        return MGPU_OK;
+    });
+}
+
 int64_t mgpu_batch_device_bytes(const mgpu_batch* b)
 {
     return b ? b->pool.bytes : 0;
@@ -2419,8 +2700,11 @@ int64_t mgpu_batch_device_bytes(const mgpu_batch* b)
 
 void mgpu_batch_destroy(mgpu_batch* b)
 {
-    if (!b) {
-        return;
+    {
+        std::lock_guard<std::mutex> lock(g_batches_mutex);
+        if (!b || g_batches.erase(b) == 0) {
+            return; // not a live batch: destroyed already or released with its context
+        }
     }
     cudaSetDevice(b->ctx->device);
     cudaStreamSynchronize(b->ctx->stream);

@@ -343,6 +343,33 @@ __device__ __forceinline__ void return_travelers_ref(const BatchDev& B, const De
     }
 }
 
+// MobilityEdge::add_mobility_result_time_point (metapopulation_mobility_instant.h:423-447):
+// the sums of the travelers m [10 G] over each index set, in the set's order, then
+// over all compartments, as a time point t of local edge le.
+__device__ void record_edge_stats(const EdgeStatsDev& S, int64_t le, int n, double t, const double* m)
+{
+    const int32_t k = S.count[le];
+    S.count[le]     = k + 1;
+    if (k >= S.capacity) {
+        return;
+    }
+    const int64_t row           = le * S.capacity + k;
+    S.times[row]                = t;
+    double* v                   = S.values + row * (S.num_sets + 1);
+    for (int i = 0; i < S.num_sets; ++i) {
+        double sum = 0.0;
+        for (int q = S.set_ptr[i]; q < S.set_ptr[i + 1]; ++q) {
+            sum += m[S.set_idx[q]];
+        }
+        v[i] = sum;
+    }
+    double total = 0.0;
+    for (int j = 0; j < n; ++j) {
+        total += m[j];
+    }
+    v[S.num_sets] = total;
+}
+
 // Row i of the contact matrix at time t (contact_matrix_at, one row), padded
 // to MAX_GROUPS entries.
 __device__ __forceinline__ void contact_row(const NodeModel& nm, int i, double t, double (&Crow)[MGPU_MAX_GROUPS])
@@ -1763,6 +1790,9 @@ __global__ void k_xb_sequential(BatchDev B, int g0, int ng)
             }
         }
         __syncwarp();
+        if (B.estats && B.estats[gi].num_sets && lane == 0) {
+            record_edge_stats(B.estats[gi], e - g.edge0, n, rt.t_next, m);
+        }
         for (int j = lane; j < n; j += 32) {
             state_set(B, ou + j, state_get(B, ou + j) + m[j]);
         }
@@ -1802,6 +1832,67 @@ __global__ void k_xb_commit(BatchDev B, int64_t n0, int64_t nn, int n_max)
     else {
         B.state[o] = B.ynew[o];
     }
+}
+
+// Commuter statistics of one exchange, one thread per edge of the graphs that
+// record them. returns = true: after the return passes and the exact path (before
+// the cleanup clears the fix counts), the returning travelers after the underflow
+// fix (graphs that took the sequential pass record there); false: after the
+// departure passes (before the interval ends), the departing travelers.
+template <class R>
+__global__ void k_edge_stats(BatchDev B, bool returns)
+{
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= B.num_edges) {
+        return;
+    }
+    const int gi          = B.edge_graph[e];
+    const EdgeStatsDev& S = B.estats[gi];
+    if (S.num_sets == 0) {
+        return;
+    }
+    const DevGraph& g = B.graphs[gi];
+    const GraphRt& rt = B.rt[gi];
+    if (returns ? (!xb_returning(rt) || rt.fallback) : !xb_departing(rt)) {
+        return;
+    }
+    if (!edge_departed(B, g, e)) {
+        return; // no travelers on this edge
+    }
+    double m[MGPU_MAX_GROUPS * kC];
+    for (int gr = 0; gr < g.G; ++gr) {
+        double t[kC];
+        if (returns) {
+            if (B.fix_cnt[e * MGPU_MAX_GROUPS + gr] != 0) {
+                // the travelers after the fix, as the exact path published them
+                if constexpr (std::is_same<R, float>::value) {
+                    const float2* mf = reinterpret_cast<const float2*>(B.mfix + B.trav_off[e] + gr * kC);
+                    for (int c = 0; c < kC; ++c) {
+                        t[c] = (double)mf[c].x + (double)mf[c].y;
+                    }
+                }
+                else {
+                    for (int c = 0; c < kC; ++c) {
+                        t[c] = B.mfix[B.trav_off[e] + gr * kC + c];
+                    }
+                }
+            }
+            else {
+                return_travelers<R>(B, g, rt, e, gr, t);
+            }
+        }
+        else {
+            R md[kC];
+            depart_travelers<R>(B, g, e, gr, rt.snap_slot ^ 1, rt.t_next, md);
+            for (int c = 0; c < kC; ++c) {
+                t[c] = (double)md[c];
+            }
+        }
+        for (int c = 0; c < kC; ++c) {
+            m[gr * kC + c] = t[c];
+        }
+    }
+    record_edge_stats(S, e - g.edge0, g.n, rt.t_next, m);
 }
 
 inline unsigned blocks_of(int64_t n, int t)
@@ -1874,6 +1965,10 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
         k_xb_commit<<<blocks_of(nn * n_max, 256), 256, 0, s>>>(B, 0, nn, (int)n_max);
     }
     k_xb_sequential<R><<<B.num_graphs, 32, 0, s>>>(B, 0, B.num_graphs);
+    if (B.estats) {
+        k_edge_stats<R><<<blocks_of(ne, 128), 128, 0, s>>>(B, true);
+        *launches += 1;
+    }
     k_xg_cleanup<<<152 * 4, 256, 0, s>>>(B, ne);
     mark(2);
     if (any_edge_dampings) {
@@ -1897,14 +1992,18 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
         k_xb_depart<R><<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
         *launches += 1;
     }
+    if (B.estats) {
+        k_edge_stats<R><<<blocks_of(ne, 128), 128, 0, s>>>(B, false);
+        *launches += 1;
+    }
     *launches += 3 + kXbScanPasses + ((!mixed || any_edge_dampings) ? 1 : 0);
 }
 
 } // namespace
 
-int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings, int group_lists)
+int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings, int group_lists, bool stats)
 {
-    const bool mixed = precision == MGPU_PRECISION_MIXED;
+    const bool mixed = is_mixed(precision);
     const int prep   = mixed ? 0 : 1; // the node pass (inside the node kernel when mixed)
     if (!has_edges) {
         return prep;
@@ -1913,13 +2012,13 @@ int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampi
     const int commit = (!mixed || any_edge_dampings) ? 1 : 0;
     // return and departure passes (one per age-group count when mixed); the exact
     // path: scan passes, done, sequential, cleanup
-    return prep + 3 + (mixed ? 2 * group_lists : 2) + kXbScanPasses + commit + extra;
+    return prep + 3 + (mixed ? 2 * group_lists : 2) + kXbScanPasses + commit + extra + (stats ? 2 : 0);
 }
 
 void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,
                              cudaStream_t s, int64_t* launches, cudaEvent_t* ev)
 {
-    if (precision == MGPU_PRECISION_MIXED) {
+    if (is_mixed(precision)) {
         launch_xb<float>(B, n_max, any_edge_dampings, s, launches, ev);
     }
     else {

@@ -67,6 +67,20 @@ struct DevOpts {
     int32_t method;
 };
 
+// Commuter statistics of the edges of one graph (MobilityEdge's mobility
+// results, add_mobility_result_time_point): per edge, one time point per
+// departure and per return, the travelers' sums over num_sets sets of flat
+// compartment indices and their total.
+struct EdgeStatsDev {
+    int32_t num_sets;        // 0: not recorded
+    int32_t capacity;        // time points kept per edge
+    const int32_t* set_ptr;  // [num_sets + 1]
+    const int32_t* set_idx;  // [set_ptr[num_sets]]
+    int32_t* count;          // [E] time points recorded (later ones beyond capacity are counted only)
+    double* times;           // [E][capacity]
+    double* values;          // [E][capacity][num_sets + 1]
+};
+
 // All device pointers of a batch.
 struct BatchDev {
     int32_t num_graphs;
@@ -135,7 +149,9 @@ struct BatchDev {
     int64_t scratch_stride;      // node slots (distance between consecutive components)
     int32_t scratch_nmax;        // components per scratch vector
     DevOpts opts;
-    int32_t* err;                // device error word
+    const EdgeStatsDev* estats;  // [num_graphs] commuter statistics, or null (none recorded)
+    int32_t* err;                // device error word (ERR_* bits of the whole batch)
+    int32_t* graph_err;          // [num_graphs] ERR_STEP_CAP / ERR_NONFINITE of each graph's own instances
     unsigned long long* counters; // [8]: accepted, rejected, failed, underflow, sequential
 };
 
@@ -180,6 +196,25 @@ __host__ __device__ inline int64_t rec_elem(int64_t r0, int G, int gr, int p)
 // before each return: lambda, r1, r2, r3, r6, r7, r10, r11, r12, r13, r14 and a
 // flag (1: one Euler step of the interval's length may drive a compartment negative).
 constexpr int kAux = 12;
+
+// A node instance of graph gi hit the step cap or ended its interval with a
+// non-finite state: recorded for that graph (the other graphs of the batch run
+// on unaffected) and in the batch's error word.
+__device__ __forceinline__ void report_instance_failure(const BatchDev& B, int gi, bool cap_hit, bool nonfinite)
+{
+    const int32_t bits = (cap_hit ? ERR_STEP_CAP : 0) | (nonfinite ? ERR_NONFINITE : 0);
+    if (bits) {
+        atomicOr(B.graph_err + gi, bits);
+        atomicOr(B.err, bits);
+    }
+}
+
+// The mixed solvers keep node states as float-float pairs and share the FP32
+// exchange; they differ only in the node kernel's step arithmetic.
+__host__ __device__ inline bool is_mixed(int precision)
+{
+    return precision == MGPU_PRECISION_MIXED || precision == MGPU_PRECISION_MIXED_FP64_CONTROL;
+}
 
 __host__ __device__ inline int param_stride(int G)
 {
@@ -544,7 +579,8 @@ int exchange_launches(bool has_edges);
 void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,
                              cudaStream_t s, int64_t* launches,
                              cudaEvent_t* ev = nullptr);
-int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings, int group_lists);
+int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings, int group_lists,
+                              bool stats);
 
 // Device and stream of a context (for entry points defined outside capi.cu).
 int context_device_stream(const mgpu_context* ctx, int* device, cudaStream_t* stream);

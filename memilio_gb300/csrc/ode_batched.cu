@@ -10,14 +10,18 @@
 // segment. Each instance has its own adaptive dt: segments of one warp step
 // independently.
 //
-// Arithmetic (template Real):
-//   Real = double : FP64 throughout, the reference's evaluation order.
-//   Real = float  : flows, stage states and stage combinations in FP32;
-//                   the state, its update, the error norm's max and the
-//                   step-size controller in FP64. The update is applied in
-//                   flow space (each flow increment leaves its source and
-//                   enters its target with the same FP64 value), so every
-//                   node conserves its population to FP64 rounding.
+// Kernels:
+//   k_ode_batched<G>         FP64 throughout, the reference's evaluation order
+//                            (MGPU_PRECISION_FP64).
+//   k_ode_mixed<G, false>    FP32 flows, stage combinations, error norm and
+//                            step-size controller on an FP32 interval clock; the
+//                            node state as float-float pairs updated in flow
+//                            space with exact TwoSum (MGPU_PRECISION_MIXED).
+//   k_ode_mixed<G, true>     FP32 flows and stage combinations; the state
+//                            update, the error norm, the controller and the
+//                            clock in FP64 (MGPU_PRECISION_MIXED_FP64_CONTROL).
+// In both mixed kernels every flow increment leaves its source and enters its
+// target with the same value, so every node conserves its population.
 //
 // Integrator: ControlledStepperWrapper<cash_karp54> inside
 // SystemIntegrator::advance (memilio/math/stepper_wrapper.h:112-163,
@@ -77,63 +81,23 @@ __device__ inline void contact_row_at(const NodeModel& nm, int i, double t, doub
     }
 }
 
-// Per-lane constants of one node instance for one interval.
-template <int G, class Real>
+// Per-lane constants of one node instance for one interval (FP64 solver).
+template <int G>
 struct Seg {
     int base;
     unsigned mask;
     int gi;
     NodeModel nm;
     // own group
-    Real a_tnt, beta, xi, rho, rho_max;
-    Real r1, r2, r3, r6, r7, r11, r13, r14, r10l, r12l, cps, dps, tisev;
+    double a_tnt, beta, xi, rho, rho_max;
+    double r1, r2, r3, r6, r7, r11, r13, r14, r10l, r12l, cps, dps, tisev;
     // scalars
-    Real tnt_cap, tnt_cap2, icu_lo, icu_cap;
+    double tnt_cap, tnt_cap2, icu_lo, icu_cap;
     double season_k, start_day;
-    // contact row as P + Q c(t) on [t_lo, t_hi) (single contact matrix only)
-    bool fast;
-    Real P[G], Q[G];
-    double t_lo, t_hi, ramp_xl;
-    Real ramp_scale;
 };
 
-template <int G, class Real>
-__device__ void seg_load_contact(Seg<G, Real>& X, double t)
-{
-    const NodeModel& nm = X.nm;
-    const long GG       = (long)G * G;
-    const double* Bm    = nm.cm + (long)X.gi * G;
-    const double* Lm    = Bm + GG;
-    if (nm.K == 0) {
-#pragma unroll
-        for (int j = 0; j < G; ++j) {
-            X.P[j] = (Real)(Bm[j] - 0.0 * (Bm[j] - Lm[j]));
-            X.Q[j] = (Real)0;
-        }
-        X.t_lo       = -INFINITY;
-        X.t_hi       = INFINITY;
-        X.ramp_xl    = INFINITY;
-        X.ramp_scale = (Real)0;
-        return;
-    }
-    const double* T  = nm.dtimes;
-    const int ub     = damping_upper_bound(T, nm.K, t);
-    const double* Dl = nm.dvals + (long)(ub - 1) * GG + (long)X.gi * G;
-    const double* Dr = Dl + GG;
-#pragma unroll
-    for (int j = 0; j < G; ++j) {
-        const double BL = Bm[j] - Lm[j];
-        X.P[j]          = (Real)(Bm[j] - (0.5 * (Dl[j] + Dr[j])) * BL);
-        X.Q[j]          = (Real)(-(0.5 * (Dl[j] - Dr[j])) * BL);
-    }
-    X.t_lo       = T[ub - 1];
-    X.t_hi       = T[ub];
-    X.ramp_xl    = T[ub] - 1.0;
-    X.ramp_scale = (Real)(1.0 / (T[ub] - X.ramp_xl));
-}
-
-template <int G, class Real>
-__device__ void seg_load(Seg<G, Real>& X, const BatchDev& B, const DevGraph& g, int64_t local, double t)
+template <int G>
+__device__ void seg_load(Seg<G>& X, const BatchDev& B, const DevGraph& g, int64_t local)
 {
     X.nm                 = node_model(B, g, local);
     const NodeModel& nm  = X.nm;
@@ -147,42 +111,38 @@ __device__ void seg_load(Seg<G, Real>& X, const BatchDev& B, const DevGraph& g, 
     const double dps     = nm.gp(MGPU_G_DEATHS_PER_SEVERE, i);
     const double dpc     = nm.gp(MGPU_G_DEATHS_PER_CRITICAL, i);
     const double ticri   = nm.gp(MGPU_G_TIME_ICRI, i);
-    X.a_tnt              = (Real)((1 - mu) / tins);
-    X.beta               = (Real)nm.gp(MGPU_G_TRANSMISSION_PROB, i);
-    X.xi                 = (Real)nm.gp(MGPU_G_REL_TRANSMISSION_NS, i);
-    X.rho                = (Real)nm.gp(MGPU_G_RISK_FROM_SYMPTOMATIC, i);
-    X.rho_max            = (Real)nm.gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, i);
-    X.r1                 = (Real)(1.0 / nm.gp(MGPU_G_TIME_EXPOSED, i));
-    X.r2                 = (Real)((1 - mu) * (1 / tins));
-    X.r3                 = (Real)(mu * (1.0 / tins));
-    X.r6                 = (Real)(sev / tisy);
-    X.r7                 = (Real)((1 - sev) / tisy);
-    X.r11                = (Real)((1.0 - cps - dps) / tisev);
-    X.r13                = (Real)(dpc / ticri);
-    X.r14                = (Real)((1.0 - dpc) / ticri);
-    X.r10l               = (Real)(cps / tisev);
-    X.r12l               = (Real)((dps + (cps - cps)) / tisev);
-    X.cps                = (Real)cps;
-    X.dps                = (Real)dps;
-    X.tisev              = (Real)tisev;
+    X.a_tnt              = (1 - mu) / tins;
+    X.beta               = nm.gp(MGPU_G_TRANSMISSION_PROB, i);
+    X.xi                 = nm.gp(MGPU_G_REL_TRANSMISSION_NS, i);
+    X.rho                = nm.gp(MGPU_G_RISK_FROM_SYMPTOMATIC, i);
+    X.rho_max            = nm.gp(MGPU_G_MAX_RISK_FROM_SYMPTOMATIC, i);
+    X.r1                 = 1.0 / nm.gp(MGPU_G_TIME_EXPOSED, i);
+    X.r2                 = (1 - mu) * (1 / tins);
+    X.r3                 = mu * (1.0 / tins);
+    X.r6                 = sev / tisy;
+    X.r7                 = (1 - sev) / tisy;
+    X.r11                = (1.0 - cps - dps) / tisev;
+    X.r13                = dpc / ticri;
+    X.r14                = (1.0 - dpc) / ticri;
+    X.r10l               = cps / tisev;
+    X.r12l               = (dps + (cps - cps)) / tisev;
+    X.cps                = cps;
+    X.dps                = dps;
+    X.tisev              = tisev;
     const double cap     = nm.scalar(MGPU_P_TNT_CAPACITY);
-    X.tnt_cap            = (Real)cap;
-    X.tnt_cap2           = (Real)(cap * nm.scalar(MGPU_P_TNT_MAX_RISK));
+    X.tnt_cap            = cap;
+    X.tnt_cap2           = cap * nm.scalar(MGPU_P_TNT_MAX_RISK);
     const double icu_cap = nm.scalar(MGPU_P_ICU_CAPACITY);
-    X.icu_lo             = (Real)(0.90 * icu_cap);
-    X.icu_cap            = (Real)icu_cap;
+    X.icu_lo             = 0.90 * icu_cap;
+    X.icu_cap            = icu_cap;
     X.season_k           = nm.scalar(MGPU_P_SEASONALITY);
     X.start_day          = nm.scalar(MGPU_P_START_DAY);
-    X.fast               = std::is_same<Real, float>::value && nm.M == 1;
-    if (X.fast) {
-        seg_load_contact(X, t);
-    }
 }
 
-template <int G, class Real>
-__device__ __forceinline__ Real seg_sum(const Seg<G, Real>& X, Real v)
+template <int G>
+__device__ __forceinline__ double seg_sum(const Seg<G>& X, double v)
 {
-    Real s = (Real)0;
+    double s = 0.0;
 #pragma unroll
     for (int k = 0; k < G; ++k) {
         s += __shfl_sync(X.mask, v, X.base + k);
@@ -192,64 +152,35 @@ __device__ __forceinline__ Real seg_sum(const Seg<G, Real>& X, Real v)
 
 // Flows of the lane's age group (osecir::Model::get_flows, models/ode_secir/model.h:82-214)
 // and the derivative of its 10 compartments (FlowModel::get_derivatives, flow_model.h:112-125).
-template <int G, class Real>
-__device__ __forceinline__ void seg_rhs(Seg<G, Real>& X, const Real (&u)[kC], double tau, Real (&fl)[kF],
-                                        Real (&kc)[kC])
+template <int G>
+__device__ __forceinline__ void seg_rhs(Seg<G>& X, const double (&u)[kC], double tau, double (&fl)[kF],
+                                        double (&kc)[kC])
 {
-    constexpr bool fp64 = std::is_same<Real, double>::value;
-    const Real tnt      = seg_sum(X, X.a_tnt * u[INS_]);
-    const Real icu      = seg_sum(X, u[ICRI_]);
+    const double tnt = seg_sum(X, X.a_tnt * u[INS_]);
+    const double icu = seg_sum(X, u[ICRI_]);
     // own group as source j of the contact sum
-    const Real risk  = smoother_cosine(tnt, X.tnt_cap, X.tnt_cap2, X.rho, X.rho_max);
-    const Real Nj    = u[S_] + u[E_] + u[INS_] + u[ISY_] + u[ISEV_] + u[ICRI_] + u[R_];
-    const Real divN  = (Nj < (Real)kZeroTol) ? (Real)0 : (Real)1 / Nj;
-    const Real press = X.xi * u[INS_] + risk * u[ISY_];
-    Real f0          = (Real)0;
-    if constexpr (fp64) {
-        const double season =
-            X.season_k == 0.0 ? 1.0 : (1 + X.season_k * sin(kPi * ((X.start_day + tau) / 182.5 + 0.5)));
-        double C[G];
-        contact_row_at(X.nm, X.gi, tau, C);
+    const double risk  = smoother_cosine(tnt, X.tnt_cap, X.tnt_cap2, X.rho, X.rho_max);
+    const double Nj    = u[S_] + u[E_] + u[INS_] + u[ISY_] + u[ISEV_] + u[ICRI_] + u[R_];
+    const double divN  = (Nj < kZeroTol) ? 0.0 : 1.0 / Nj;
+    const double press = X.xi * u[INS_] + risk * u[ISY_];
+    const double season =
+        X.season_k == 0.0 ? 1.0 : (1 + X.season_k * sin(kPi * ((X.start_day + tau) / 182.5 + 0.5)));
+    double C[G];
+    contact_row_at(X.nm, X.gi, tau, C);
+    double f0 = 0.0;
 #pragma unroll
-        for (int j = 0; j < G; ++j) {
-            const double dN = __shfl_sync(X.mask, divN, X.base + j);
-            const double pr = __shfl_sync(X.mask, press, X.base + j);
-            const double cont = season * C[j];
-            f0 += u[S_] * cont * dN * X.beta * pr;
-        }
-    }
-    else {
-        const float season =
-            X.season_k == 0.0 ? 1.0f
-                              : 1.0f + (float)X.season_k * sinpif((float)((X.start_day + tau) * (1.0 / 182.5) + 0.5));
-        const float w = divN * press;
-        float acc     = 0.0f;
-        if (X.fast) {
-            if (!(tau >= X.t_lo && tau < X.t_hi)) {
-                seg_load_contact(X, tau);
-            }
-            const float c = (tau <= X.ramp_xl) ? 1.0f : cospif((float)(tau - X.ramp_xl) * X.ramp_scale);
-#pragma unroll
-            for (int j = 0; j < G; ++j) {
-                acc += (X.P[j] + X.Q[j] * c) * __shfl_sync(X.mask, w, X.base + j);
-            }
-        }
-        else {
-            double C[G];
-            contact_row_at(X.nm, X.gi, tau, C);
-#pragma unroll
-            for (int j = 0; j < G; ++j) {
-                acc += (float)C[j] * __shfl_sync(X.mask, w, X.base + j);
-            }
-        }
-        f0 = u[S_] * X.beta * season * acc;
+    for (int j = 0; j < G; ++j) {
+        const double dN   = __shfl_sync(X.mask, divN, X.base + j);
+        const double pr   = __shfl_sync(X.mask, press, X.base + j);
+        const double cont = season * C[j];
+        f0 += u[S_] * cont * dN * X.beta * pr;
     }
     // ICU smoother for CriticalPerSevere
-    Real r10 = X.r10l, r12 = X.r12l;
+    double r10 = X.r10l, r12 = X.r12l;
     if (!(icu <= X.icu_lo)) {
-        const Real crit_adj = smoother_cosine(icu, X.icu_lo, X.icu_cap, X.cps, (Real)0);
-        r10                 = crit_adj / X.tisev;
-        r12                 = (X.dps + (X.cps - crit_adj)) / X.tisev;
+        const double crit_adj = smoother_cosine(icu, X.icu_lo, X.icu_cap, X.cps, 0.0);
+        r10                   = crit_adj / X.tisev;
+        r12                   = (X.dps + (X.cps - crit_adj)) / X.tisev;
     }
     fl[0]  = f0;
     fl[1]  = X.r1 * u[E_];
@@ -279,8 +210,8 @@ __device__ __forceinline__ void seg_rhs(Seg<G, Real>& X, const Real (&u)[kC], do
     kc[D_]    = fl[12] + fl[13];
 }
 
-template <int G, class Real>
-__device__ __forceinline__ double seg_max(const Seg<G, Real>& X, double v)
+template <int G>
+__device__ __forceinline__ double seg_max(const Seg<G>& X, double v)
 {
     double m = v;
 #pragma unroll
@@ -290,17 +221,16 @@ __device__ __forceinline__ double seg_max(const Seg<G, Real>& X, double v)
     return m;
 }
 
-template <int G, class Real>
+template <int G>
 __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* inst, int64_t count)
 {
-    constexpr bool fp64 = std::is_same<Real, double>::value;
-    constexpr int IPW   = 32 / G;
-    const int lane      = threadIdx.x & 31;
-    const int seg       = lane / G;
+    constexpr int IPW = 32 / G;
+    const int lane    = threadIdx.x & 31;
+    const int seg     = lane / G;
     if (seg >= IPW) {
         return;
     }
-    Seg<G, Real> X;
+    Seg<G> X;
     X.gi   = lane - seg * G;
     X.base = seg * G;
     X.mask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << X.base);
@@ -308,7 +238,6 @@ __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* 
     const int64_t nw  = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const DevOpts o   = B.opts;
     unsigned long long n_acc = 0, n_rej = 0, n_fail = 0;
-    bool cap_hit = false, nonfinite = false;
 
     for (int64_t slot = wid * IPW + seg; slot < count; slot += nw * IPW) {
         const int64_t node = inst[slot];
@@ -328,7 +257,8 @@ __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* 
         double t          = B.node_t[node];
         double dt         = B.node_dt[node];
         const double tmax = rt.t_next;
-        seg_load(X, B, g, local, t);
+        seg_load(X, B, g, local);
+        bool cap_hit = false;
 
         // SystemIntegrator::advance
         const double t0   = t;
@@ -348,9 +278,7 @@ __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* 
             // ControlledStepperWrapper::step
             bool success     = false;
             bool is_dt_valid = true;
-            double dt_used   = dt;
-            Real phi[kF];   // mixed: flow increments of the attempt
-            double yn[kC];  // fp64: 5th-order result
+            double yn[kC]; // 5th-order result
             while (!success && is_dt_valid) {
                 if (dt < dt_min) {
                     is_dt_valid = false;
@@ -361,65 +289,35 @@ __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* 
                     ++n_rej;
                     continue;
                 }
-                dt_used = dt;
                 // ---- one Cash-Karp attempt ----
-                Real k[5][kC];
-                Real kc[kC], fl[kF], xe[kC];
-                Real y0[kC];
-#pragma unroll
-                for (int c = 0; c < kC; ++c) {
-                    y0[c] = (Real)y[c];
-                }
-                seg_rhs(X, y0, t, fl, kc);
+                double k[5][kC];
+                double kc[kC], fl[kF], xe[kC];
+                seg_rhs(X, y, t, fl, kc);
 #pragma unroll
                 for (int c = 0; c < kC; ++c) {
                     k[0][c] = kc[c];
-                    xe[c]   = (Real)(bk_db[0] * dt) * kc[c];
-                }
-                if constexpr (!fp64) {
-#pragma unroll
-                    for (int f = 0; f < kF; ++f) {
-                        phi[f] = (Real)(bk_b5[0] * dt) * fl[f];
-                    }
-                }
-                if constexpr (fp64) {
-#pragma unroll
-                    for (int c = 0; c < kC; ++c) {
-                        yn[c] = y[c] + (bk_b5[0] * dt) * kc[c];
-                    }
+                    xe[c]   = (bk_db[0] * dt) * kc[c];
+                    yn[c]   = y[c] + (bk_b5[0] * dt) * kc[c];
                 }
 #pragma unroll
                 for (int s = 1; s < 6; ++s) {
-                    Real u[kC];
+                    double u[kC];
 #pragma unroll
                     for (int c = 0; c < kC; ++c) {
-                        Real v = y0[c];
+                        double v = y[c];
 #pragma unroll
                         for (int j = 0; j < s; ++j) {
-                            v = v + (Real)(bk_a[s][j] * dt) * k[j][c];
+                            v = v + (bk_a[s][j] * dt) * k[j][c];
                         }
                         u[c] = v;
                     }
                     seg_rhs(X, u, t + bk_c[s] * dt, fl, kc);
 #pragma unroll
                     for (int c = 0; c < kC; ++c) {
-                        xe[c] = xe[c] + (Real)(bk_db[s] * dt) * kc[c];
+                        xe[c] = xe[c] + (bk_db[s] * dt) * kc[c];
+                        yn[c] = yn[c] + (bk_b5[s] * dt) * kc[c];
                         if (s < 5) {
                             k[s][c] = kc[c];
-                        }
-                    }
-                    if constexpr (fp64) {
-#pragma unroll
-                        for (int c = 0; c < kC; ++c) {
-                            yn[c] = yn[c] + (bk_b5[s] * dt) * kc[c];
-                        }
-                    }
-                    else {
-                        if (s == 2 || s == 3 || s == 5) {
-#pragma unroll
-                            for (int f = 0; f < kF; ++f) {
-                                phi[f] = phi[f] + (Real)(bk_b5[s] * dt) * fl[f];
-                            }
                         }
                     }
                 }
@@ -427,9 +325,7 @@ __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* 
                 double el = 0.0;
 #pragma unroll
                 for (int c = 0; c < kC; ++c) {
-                    const Real r = fabs(xe[c]) / ((Real)o.abs_tol +
-                                                  (Real)o.rel_tol * (fabs(y0[c]) + (Real)dt * fabs(k[0][c])));
-                    el           = fmax(el, (double)r);
+                    el = fmax(el, fabs(xe[c]) / (o.abs_tol + o.rel_tol * (fabs(y[c]) + dt * fabs(k[0][c]))));
                 }
                 const double err = seg_max(X, el);
                 // ---- controller ----
@@ -460,24 +356,14 @@ __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* 
             else {
                 ++n_acc;
             }
-            (void)dt_used;
             // apply the (last) attempt
-            if constexpr (fp64) {
 #pragma unroll
-                for (int c = 0; c < kC; ++c) {
-                    y[c] = yn[c];
-                }
-            }
-            else {
-#pragma unroll
-                for (int f = 0; f < kF; ++f) {
-                    const double p = (double)phi[f];
-                    y[kFlowSrcI(f)] -= p;
-                    y[kFlowDstI(f)] += p;
-                }
+            for (int c = 0; c < kC; ++c) {
+                y[c] = yn[c];
             }
         }
         dt = fmax(dt, dt_restore);
+        bool nonfinite = false;
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
             yp[c]     = y[c];
@@ -487,12 +373,7 @@ __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* 
             B.node_t[node]  = t;
             B.node_dt[node] = dt;
         }
-    }
-    if (cap_hit) {
-        atomicOr(B.err, ERR_STEP_CAP);
-    }
-    if (nonfinite) {
-        atomicOr(B.err, ERR_NONFINITE);
+        report_instance_failure(B, gidx, cap_hit, nonfinite);
     }
     if (X.gi == 0) {
         if (n_acc) {
@@ -547,31 +428,18 @@ __device__ __forceinline__ void df_renorm(float& hi, float& lo)
     hi            = s;
 }
 
-#ifndef MGPU_ODE_TAB_LOADS
-#define MGPU_ODE_TAB_LOADS 0
-#endif
-
 template <int G>
 struct SegF {
     int base;
     unsigned mask;
     int gi;
     NodeModel nm;
-    // per-(node, group) constants (TF_* of the FP32 table): in registers, or
-    // read through L1 at every use with MGPU_ODE_TAB_LOADS (fewer registers)
-#if MGPU_ODE_TAB_LOADS
-    const float* tab;
-    __device__ __forceinline__ float tc(int i) const
-    {
-        return __ldg(tab + i);
-    }
-#else
+    // per-(node, group) constants (TF_* of the FP32 table), in registers
     float tabv[kTabF];
     __device__ __forceinline__ float tc(int i) const
     {
         return tabv[i];
     }
-#endif
     float season_s0;
     bool fast;
     float P[G], Q[G];
@@ -638,14 +506,10 @@ __device__ void segf_load(SegF<G>& X, const BatchDev& B, const DevGraph& g, int6
     const float* T = B.tab_f + ((g.node0 + local) * MGPU_MAX_GROUPS + X.gi) * kTabF;
     X.t_base       = t_base;
     X.t_base_f     = (float)t_base;
-#if MGPU_ODE_TAB_LOADS
-    X.tab = T;
-#else
 #pragma unroll
     for (int q = 0; q < kTabF; ++q) {
         X.tabv[q] = T[q];
     }
-#endif
     X.season_s0    = (float)((nm.scalar(MGPU_P_START_DAY) + t_base) * (1.0 / 182.5) + 0.5);
     X.fast         = nm.M == 1;
     if (X.fast) {
@@ -745,16 +609,36 @@ __device__ __forceinline__ void segf_rhs(SegF<G>& X, const float (&u)[kC], float
 
 // shared memory per lane of the mixed solver: 5 stage derivative vectors and the flow increments
 constexpr int kOdeSmemPerLane = 5 * kC + kF;
-template <int G>
-#ifndef MGPU_MIXED_THREADS
-#define MGPU_MIXED_THREADS 128 // largest block of the mixed node kernel
-#endif
-#ifndef MGPU_MIXED_MIN_BLOCKS
-#define MGPU_MIXED_MIN_BLOCKS 3 // resident blocks per SM the register budget must allow
-#endif
-__global__ void __launch_bounds__(MGPU_MIXED_THREADS, MGPU_MIXED_MIN_BLOCKS) k_ode_mixed(BatchDev B, const int32_t* inst,
-                                                                         int64_t count)
+constexpr int kMixedThreads   = 128; // largest block of the mixed node kernels
+// resident blocks per SM the register budget must allow (measured best for the
+// FP32 step; the FP64 step holds its state and clock in FP64 registers)
+constexpr int kMixedMinBlocks    = 3;
+constexpr int kMixedMinBlocks64  = 2;
+
+// Odeint's error measure of one compartment: |x_err| / (abs + rel (|x| + dt |dxdt|))
+__device__ __forceinline__ float err_ratio(float xe, float x, float dxdt, float dt, float abs_tol, float rel_tol)
 {
+    // (an approximate quotient: the controller needs no correctly rounded ratios)
+    return __fdividef(fabsf(xe), abs_tol + rel_tol * (fabsf(x) + dt * fabsf(dxdt)));
+}
+__device__ __forceinline__ double err_ratio(float xe, double x, float dxdt, double dt, double abs_tol,
+                                            double rel_tol)
+{
+    return fabs((double)xe) / (abs_tol + rel_tol * (fabs(x) + dt * fabs((double)dxdt)));
+}
+
+// One exchange interval of every active instance of the list, mixed precision.
+// CTL64 = false: the state as float-float pairs (hi + lo) updated with exact
+// TwoSum; the error norm, the controller and the interval clock in FP32.
+// CTL64 = true : the state accumulated in FP64; the error norm (from the FP32
+// error estimate), the controller and the interval clock in FP64.
+// In both, the right-hand side and the stage combinations run in FP32 from the
+// FP32 rounding of the state.
+template <int G, bool CTL64>
+__global__ void __launch_bounds__(kMixedThreads, CTL64 ? kMixedMinBlocks64 : kMixedMinBlocks)
+    k_ode_mixed(BatchDev B, const int32_t* inst, int64_t count)
+{
+    using Clk         = typename std::conditional<CTL64, double, float>::type;
     constexpr int IPW = 32 / G;
     const int lane    = threadIdx.x & 31;
     const int seg     = lane / G;
@@ -767,10 +651,10 @@ __global__ void __launch_bounds__(MGPU_MIXED_THREADS, MGPU_MIXED_MIN_BLOCKS) k_o
     X.mask            = (((1u << G) - 1u) << X.base);
     const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw  = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const DevOpts o      = B.opts;
-    const float abs_f    = (float)o.abs_tol, rel_f = (float)o.rel_tol;
-    const float o_dt_min = (float)o.dt_min; // DBL_MIN becomes 0: no lower bound, as in FP64
-    const float o_dt_max = (float)o.dt_max; // DBL_MAX becomes +inf
+    const DevOpts o    = B.opts;
+    const Clk abs_tol  = (Clk)o.abs_tol, rel_tol = (Clk)o.rel_tol;
+    const Clk o_dt_min = (Clk)o.dt_min; // FP32: DBL_MIN becomes 0, no lower bound, as in FP64
+    const Clk o_dt_max = (Clk)o.dt_max; // FP32: DBL_MAX becomes +inf
     // stage derivatives k_0..k_4: [warp][stage*10 + c][lane] (conflict-free columns)
     extern __shared__ float ode_smem[];
     float* skw = ode_smem + (threadIdx.x >> 5) * (kOdeSmemPerLane * 32);
@@ -778,7 +662,6 @@ __global__ void __launch_bounds__(MGPU_MIXED_THREADS, MGPU_MIXED_MIN_BLOCKS) k_o
     // the 5th-order flow increments of the attempt, after the stage derivatives
 #define SP(f) skw[(5 * kC + (f)) * 32 + lane]
     unsigned long long n_acc = 0, n_rej = 0, n_fail = 0;
-    bool cap_hit = false, nonfinite = false;
 
     for (int64_t slot = wid * IPW + seg; slot < count; slot += nw * IPW) {
         const int64_t node = inst[slot];
@@ -792,11 +675,16 @@ __global__ void __launch_bounds__(MGPU_MIXED_THREADS, MGPU_MIXED_MIN_BLOCKS) k_o
         const int64_t so    = g.state_off + local * g.n + X.gi * kC;
         float* yhi          = B.st_hi + so;
         float* ylo          = B.st_lo + so;
+        // hi: the FP32 state the stages start from; lo (FP32 step) or y64 (FP64 step) the accumulator
         float hi[kC], lo[kC];
+        double y64[CTL64 ? kC : 1];
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
             hi[c] = yhi[c];
             lo[c] = ylo[c];
+            if constexpr (CTL64) {
+                y64[c] = (double)hi[c] + (double)lo[c];
+            }
         }
         const double t_start = B.node_t[node];
         const double tmax    = rt.t_next;
@@ -846,16 +734,17 @@ __global__ void __launch_bounds__(MGPU_MIXED_THREADS, MGPU_MIXED_MIN_BLOCKS) k_o
             a[2]      = make_float4(v[8], v[9], v[10], v[11]);
         }
 
-        // SystemIntegrator::advance on an interval-relative FP32 clock: tr runs
-        // from 0 to span (0.5 days is exact in FP32); a step clipped to the
-        // remaining span lands exactly on it.
-        const float span  = (float)(tmax - t_start);
-        const float eps_t = (float)kZeroTol * span;
-        float tr          = 0.0f;
-        float dt          = (float)B.node_dt[node];
-        float dt_restore  = 0.0f;
-        float dt_min      = o_dt_min;
-        int steps         = 0;
+        // SystemIntegrator::advance on an interval-relative clock: tr runs from
+        // 0 to span (0.5 days is exact in FP32); a step clipped to the remaining
+        // span lands exactly on it.
+        const Clk span   = (Clk)(tmax - t_start);
+        const Clk eps_t  = (Clk)kZeroTol * span;
+        Clk tr           = 0;
+        Clk dt           = (Clk)B.node_dt[node];
+        Clk dt_restore   = 0;
+        Clk dt_min       = o_dt_min;
+        int steps        = 0;
+        bool cap_hit     = false;
         while (span - tr > eps_t) {
             if (steps++ >= o.max_steps) {
                 cap_hit = true;
@@ -867,25 +756,25 @@ __global__ void __launch_bounds__(MGPU_MIXED_THREADS, MGPU_MIXED_MIN_BLOCKS) k_o
                     dt_restore = dt;
                 }
                 dt     = span - tr;
-                dt_min = fminf(span - tr, dt_min);
+                dt_min = fmin(span - tr, dt_min);
                 last   = true;
             }
             // ControlledStepperWrapper::step
-            bool success     = false;
-            bool is_dt_valid = true;
-            const float dt_try0 = dt;
+            bool success      = false;
+            bool is_dt_valid  = true;
+            const Clk dt_try0 = dt;
             while (!success && is_dt_valid) {
                 if (dt < dt_min) {
                     is_dt_valid = false;
                     dt          = dt_min;
                 }
-                if (o_dt_max != 0.0f && fabsf(dt) > o_dt_max) {
+                if (o_dt_max != 0 && fabs(dt) > o_dt_max) {
                     dt = o_dt_max;
                     ++n_rej;
                     continue;
                 }
-                const float dtf  = dt;
-                const float trel = tr;
+                const float dtf  = (float)dt;
+                const float trel = (float)tr;
                 float kc[kC], fl[kF];
                 // the six stages: one copy of the right-hand side in the code,
                 // stage derivatives in this lane's shared-memory column
@@ -948,39 +837,51 @@ __global__ void __launch_bounds__(MGPU_MIXED_THREADS, MGPU_MIXED_MIN_BLOCKS) k_o
                     }
                 }
                 // Odeint error measure, max over the instance
-                float el = 0.0f;
+                Clk el = 0;
 #pragma unroll
                 for (int c = 0; c < kC; ++c) {
-                    const float den = abs_f + rel_f * (fabsf(hi[c]) + dtf * fabsf(SK(0, c)));
-                    // (an approximate quotient: the controller needs no correctly rounded ratios)
-                    el = fmaxf(el, __fdividef(fabsf(xe[c]), den));
+                    if constexpr (CTL64) {
+                        el = fmax(el, err_ratio(xe[c], y64[c], SK(0, c), dt, abs_tol, rel_tol));
+                    }
+                    else {
+                        el = fmaxf(el, err_ratio(xe[c], hi[c], SK(0, c), dtf, abs_tol, rel_tol));
+                    }
                 }
 #pragma unroll
                 for (int q = 0; q < G; ++q) {
-                    el = fmaxf(el, __shfl_sync(X.mask, el, X.base + q));
+                    el = fmax(el, __shfl_sync(X.mask, el, X.base + q));
                 }
-                // controller (Odeint rules) on the FP32 clock
-                if (el > 1.0f) {
-                    dt *= fmaxf(0.9f * exp2f(__log2f(el) * (-1.0f / 3.0f)), 0.2f);
-                    if (o_dt_max != 0.0f) {
-                        dt = fminf(dt, o_dt_max);
+                // controller (Odeint rules)
+                if (el > 1) {
+                    if constexpr (CTL64) {
+                        dt *= fmax(0.9 * pow(el, -1.0 / 3.0), 0.2);
+                    }
+                    else {
+                        dt *= fmaxf(0.9f * exp2f(__log2f(el) * (-1.0f / 3.0f)), 0.2f);
+                    }
+                    if (o_dt_max != 0) {
+                        dt = fmin(dt, o_dt_max);
                     }
                     ++n_rej;
                 }
                 else {
                     // the step taken with the clipped size reaches the boundary exactly
                     tr = (last && dt == dt_try0) ? span : tr + dt;
-                    if (el < 0.5f) {
-                        const float e = fmaxf(0.00032f /* 5^-5 */, el);
-                        dt *= 0.9f * exp2f(__log2f(e) * -0.2f);
-                        if (o_dt_max != 0.0f) {
-                            dt = fminf(dt, o_dt_max);
+                    if (el < (Clk)0.5) {
+                        if constexpr (CTL64) {
+                            dt *= 0.9 * pow(fmax(0.00032 /* 5^-5 */, el), -1.0 / 5.0);
+                        }
+                        else {
+                            dt *= 0.9f * exp2f(__log2f(fmaxf(0.00032f /* 5^-5 */, el)) * -0.2f);
+                        }
+                        if (o_dt_max != 0) {
+                            dt = fmin(dt, o_dt_max);
                         }
                     }
                     success = true;
                 }
             }
-            dt = fmaxf(dt, dt_min);
+            dt = fmax(dt, dt_min);
             if (!success) {
                 tr += dt_min;
                 ++n_fail;
@@ -988,21 +889,40 @@ __global__ void __launch_bounds__(MGPU_MIXED_THREADS, MGPU_MIXED_MIN_BLOCKS) k_o
             else {
                 ++n_acc;
             }
-            // flow-space update of the (last) attempt: exact TwoSum on both ends of each flow
+            // flow-space update of the (last) attempt: each increment leaves its
+            // source and enters its target with the same value
+            if constexpr (CTL64) {
 #pragma unroll
-            for (int f = 0; f < kF; ++f) {
-                const float ph = SP(f);
-                df_add(hi[kFlowSrcI(f)], lo[kFlowSrcI(f)], -ph);
-                df_add(hi[kFlowDstI(f)], lo[kFlowDstI(f)], ph);
+                for (int f = 0; f < kF; ++f) {
+                    const double ph = (double)SP(f);
+                    y64[kFlowSrcI(f)] -= ph;
+                    y64[kFlowDstI(f)] += ph;
+                }
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    hi[c] = (float)y64[c];
+                }
             }
+            else {
 #pragma unroll
-            for (int c = 0; c < kC; ++c) {
-                df_renorm(hi[c], lo[c]);
+                for (int f = 0; f < kF; ++f) {
+                    const float ph = SP(f);
+                    df_add(hi[kFlowSrcI(f)], lo[kFlowSrcI(f)], -ph);
+                    df_add(hi[kFlowDstI(f)], lo[kFlowDstI(f)], ph);
+                }
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    df_renorm(hi[c], lo[c]);
+                }
             }
         }
-        dt = fmaxf(dt, dt_restore);
+        dt             = fmax(dt, dt_restore);
+        bool nonfinite = false;
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
+            if constexpr (CTL64) {
+                lo[c] = (float)(y64[c] - (double)hi[c]);
+            }
             yhi[c]    = hi[c];
             ylo[c]    = lo[c];
             nonfinite = nonfinite || !isfinite(hi[c]);
@@ -1011,8 +931,9 @@ __global__ void __launch_bounds__(MGPU_MIXED_THREADS, MGPU_MIXED_MIN_BLOCKS) k_o
             B.node_t[node]  = (tr >= span) ? tmax : t_start + (double)tr;
             B.node_dt[node] = (double)dt;
         }
+        report_instance_failure(B, gidx, cap_hit, nonfinite);
         // Departure at the interval's end (the exchange's node pass, done here):
-        // the snapshot record, i.e. the FP32 rounding of hi + lo, the ISy mobility
+        // the snapshot record, i.e. the FP32 rounding of the state, the ISy mobility
         // factor and the commuter nondetection (get_mobility_factors,
         // models/ode_secir/model.h:687-715), into the free snapshot slot.
         if (rt.do_depart && g.E > 0) {
@@ -1038,12 +959,8 @@ __global__ void __launch_bounds__(MGPU_MIXED_THREADS, MGPU_MIXED_MIN_BLOCKS) k_o
             }
         }
     }
-    if (cap_hit) {
-        atomicOr(B.err, ERR_STEP_CAP);
-    }
-    if (nonfinite) {
-        atomicOr(B.err, ERR_NONFINITE);
-    }
+#undef SK
+#undef SP
     if (X.gi == 0) {
         if (n_acc) {
             atomicAdd(&B.counters[CNT_ACCEPTED], n_acc);
@@ -1108,16 +1025,21 @@ int launch_g(const BatchDev& B, int precision, const int32_t* inst, int64_t coun
     if (blocks < 1) {
         blocks = 1;
     }
-    if (precision == MGPU_PRECISION_MIXED) {
+    if (is_mixed(precision)) {
         const size_t smem = (size_t)(threads / 32) * kOdeSmemPerLane * 32 * sizeof(float);
         if (B.gorder[G] && inst == B.glist[G] && count == B.gcount[G]) {
             k_ode_order<<<(unsigned)((count + 127) / 128), 128, 0, s>>>(B, G);
             inst = B.gorder[G];
         }
-        k_ode_mixed<G><<<(unsigned)blocks, threads, smem, s>>>(B, inst, count);
+        if (precision == MGPU_PRECISION_MIXED_FP64_CONTROL) {
+            k_ode_mixed<G, true><<<(unsigned)blocks, threads, smem, s>>>(B, inst, count);
+        }
+        else {
+            k_ode_mixed<G, false><<<(unsigned)blocks, threads, smem, s>>>(B, inst, count);
+        }
     }
     else {
-        k_ode_batched<G, double><<<(unsigned)blocks, threads, 0, s>>>(B, inst, count);
+        k_ode_batched<G><<<(unsigned)blocks, threads, 0, s>>>(B, inst, count);
     }
     return 0;
 }

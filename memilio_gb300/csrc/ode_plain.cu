@@ -323,15 +323,14 @@ __global__ void k_ode_plain(BatchDev B, int64_t node_begin, int64_t node_end, in
         system_advance(f, w, g.n, rt.t_next, t, dt, o, c, [](double, const SVec&) {});
     B.node_t[node]  = t;
     B.node_dt[node] = dt;
-    if (!ok) {
-        atomicOr(B.err, ERR_STEP_CAP);
-    }
+    bool nonfinite  = false;
     for (int i = 0; i < g.n; ++i) {
         if (!isfinite(y[i])) {
-            atomicOr(B.err, ERR_NONFINITE);
+            nonfinite = true;
             break;
         }
     }
+    report_instance_failure(B, gi, !ok, nonfinite);
     add_counts(B, c);
 }
 
@@ -651,6 +650,10 @@ extern "C" int mgpu_simulate_final_noalloc(mgpu_context* ctx, int32_t num_groups
     B.opts.method    = opts->method;
     const int threads = 64;
     const int blocks  = (count + threads - 1) / threads;
-    k_simulate_final<<<blocks, threads, 0, stream>>>(B, g, count, t0, tmax, dt0, y_out, status);
-    return cudaGetLastError() == cudaSuccess ? MGPU_OK : MGPU_CUDA_ERROR;
+    // cudaLaunchKernel reports this launch's own status; an error that an
+    // earlier, unrelated launch of the caller left pending stays the caller's
+    void* args[] = {&B, &g, &count, &t0, &tmax, &dt0, &y_out, &status};
+    const cudaError_t e =
+        cudaLaunchKernel(reinterpret_cast<const void*>(&k_simulate_final), dim3(blocks), dim3(threads), args, 0, stream);
+    return e == cudaSuccess ? MGPU_OK : MGPU_CUDA_ERROR;
 }

@@ -104,18 +104,29 @@ mgpu_context* take_ctx(mgpu_server* s)
 }
 
 // Completes the requests of r whose horizon lies within the finished intervals.
+// Each request gets its own status: a request whose node solves failed (step cap,
+// non-finite state) is reported as MGPU_STEP_FAILED, and the other requests of
+// its batch complete normally; any other batch status fails every request.
 int deliver(mgpu_server* s, Running& r, bool all_done, int32_t batch_status)
 {
     int n = 0;
+    std::vector<int32_t> failed;
     for (size_t i = 0; i < r.reqs.size(); ++i) {
         if (r.delivered[i] || (!all_done && r.reqs[i].phases > r.finished)) {
             continue;
         }
         Done d;
         d.id        = r.reqs[i].id;
-        d.status    = batch_status;
+        d.status    = batch_status == MGPU_STEP_FAILED ? MGPU_OK : batch_status;
         const int64_t cnt = (int64_t)r.reqs[i].graph.num_nodes * 10 * r.reqs[i].graph.num_groups;
         d.state.resize((size_t)cnt);
+        if (d.status == MGPU_OK && failed.empty()) {
+            failed.assign(r.reqs.size(), 0);
+            d.status = mgpu_batch_get_failed(r.batch, failed.data(), nullptr);
+        }
+        if (d.status == MGPU_OK && failed[i]) {
+            d.status = MGPU_STEP_FAILED;
+        }
         if (d.status == MGPU_OK) {
             d.status = mgpu_batch_get_graph_state(r.batch, (int32_t)i, d.state.data());
         }

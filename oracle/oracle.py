@@ -58,6 +58,10 @@ def lib():
                                        P(d), P(d), P(OrcStats)]
         L.orc_damping_cache.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P(d), P(ctypes.c_int32),
                                         P(ctypes.c_int32), P(d), ctypes.c_int, P(d), P(d)]
+        i32p = P(ctypes.c_int32)
+        L.orc_graph_run_commuters.argtypes = [P(MgpuGraph), d, d, d, d, P(MgpuIntegratorOpts), ctypes.c_int, i32p,
+                                              i32p, ctypes.c_int, P(d), i32p, P(d), P(d), P(OrcStats)]
+        L.orc_departure_commuters.argtypes = [P(MgpuGraph), ctypes.c_int, d, ctypes.c_int, i32p, i32p, P(d)]
         _lib = L
     return _lib
 
@@ -163,6 +167,76 @@ def ensemble_run(graphs, t0: float, tmax: float, dt_exchange: float = 0.5, dt0: 
         res.append(out[off:off + s].reshape(g.num_nodes, g.n))
         off += s
     return res, el.value, st.as_dict()
+
+
+def _sets(save_sets):
+    """CSR form (offsets, indices) of a list of index sets."""
+    offsets = np.zeros(len(save_sets) + 1, np.int32)
+    for i, st in enumerate(save_sets):
+        offsets[i + 1] = offsets[i] + len(st)
+    indices = np.ascontiguousarray(np.concatenate([np.asarray(st, np.int32) for st in save_sets])
+                                   if save_sets else np.zeros(0, np.int32), np.int32)
+    return offsets, indices
+
+
+def graph_run_commuters(g: GraphArrays, t0: float, tmax: float, save_sets, capacity: int = 1024,
+                        dt_exchange: float = 0.5, dt0: float = 0.1, opts=None):
+    """graph_run recording every edge's mobility results with the given save
+    indices (MobilityEdge::add_mobility_result_time_point). Returns (final
+    [N, 10G], counts [E], times [E, capacity], values [E, capacity, sets + 1], stats)."""
+    L = lib()
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    opts = opts or integrator_opts()
+    offsets, indices = _sets(save_sets)
+    S, E = len(save_sets), g.num_edges
+    fin = np.zeros((g.num_nodes, g.n))
+    counts = np.zeros(max(E, 1), np.int32)
+    times = np.zeros((max(E, 1), capacity))
+    values = np.zeros((max(E, 1), capacity, S + 1))
+    st = OrcStats()
+    cg = g.as_ctypes()
+    rc = L.orc_graph_run_commuters(ctypes.byref(cg), t0, tmax, dt_exchange, dt0, ctypes.byref(opts), S,
+                                   offsets.ctypes.data_as(i32p), indices.ctypes.data_as(i32p), capacity, _p(fin),
+                                   counts.ctypes.data_as(i32p), _p(times), _p(values), ctypes.byref(st))
+    assert rc == 0
+    return fin, counts[:E], times[:E], values[:E], st.as_dict()
+
+
+def departure_commuters(g: GraphArrays, edge: int, t: float, save_sets) -> np.ndarray:
+    """One apply_mobility(t, 0, from, to) of `edge` on the initial states: the
+    mobility result it records [sets + 1]."""
+    offsets, indices = _sets(save_sets)
+    out = np.zeros(len(save_sets) + 1)
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    cg = g.as_ctypes()
+    rc = lib().orc_departure_commuters(ctypes.byref(cg), edge, t, len(save_sets), offsets.ctypes.data_as(i32p),
+                                       indices.ctypes.data_as(i32p), _p(out))
+    assert rc == 0
+    return out
+
+
+def compartment_error(got, ref, num_groups: int, floor: float = 1e-6) -> np.ndarray:
+    """Per-compartment relative error of `got` against the oracle's `ref`:
+
+        |got - ref| / max(|ref|, floor * N_g)
+
+    N_g is the population of the (node, age group) the compartment belongs to
+    (the sum of its ten compartments in `ref`), so `floor` is the absolute
+    floor as a fraction of the age group. Arrays of any leading shape with
+    10 * num_groups values last; the result has shape [..., num_groups, 10]."""
+    got = np.asarray(got, np.float64).reshape(-1, num_groups, NUM_COMPARTMENTS)
+    ref = np.asarray(ref, np.float64).reshape(-1, num_groups, NUM_COMPARTMENTS)
+    n_g = ref.sum(axis=2, keepdims=True)
+    den = np.maximum(np.abs(ref), floor * n_g)
+    den = np.where(den > 0.0, den, 1.0)  # an empty age group: absolute error
+    return np.abs(got - ref) / den
+
+
+def error_summary(errs) -> dict:
+    """max, p99 and p99.9 of compartment_error arrays (one or a list)."""
+    e = np.concatenate([np.ravel(x) for x in (errs if isinstance(errs, (list, tuple)) else [errs])])
+    return {"max": float(e.max()), "p99": float(np.percentile(e, 99)), "p999": float(np.percentile(e, 99.9)),
+            "values": int(e.size)}
 
 
 def damping_cache(rows, cols, times, levels, types, matrices, cap=64):

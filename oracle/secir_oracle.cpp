@@ -491,6 +491,32 @@ struct GraphRun {
     std::vector<EdgeState> edges;
     Counters cnt;
     int64_t rhs_evals = 0, underflow_fixes = 0;
+    // MobilityEdge::m_saved_compartment_indices (metapopulation_mobility_instant.h:427) and
+    // m_mobility_results, the same sets on every edge; empty: nothing is recorded
+    std::vector<std::vector<int>> save_sets;
+    std::vector<std::vector<double>> result_t, result_v; // per edge: times, [points][sets + 1]
+
+    // MobilityEdge::add_mobility_result_time_point (metapopulation_mobility_instant.h:423-447):
+    // the travelers' sums over each set of indices, then over all compartments.
+    void add_mobility_result_time_point(int e, double t, const std::vector<double>& m)
+    {
+        if (save_sets.empty()) {
+            return;
+        }
+        result_t[e].push_back(t);
+        for (const auto& set : save_sets) {
+            double sum = 0.0;
+            for (int index : set) {
+                sum += m[index];
+            }
+            result_v[e].push_back(sum);
+        }
+        double total = 0.0;
+        for (int j = 0; j < n; ++j) {
+            total += m[j];
+        }
+        result_v[e].push_back(total);
+    }
 
     GraphRun(const mgpu_graph* g_, double t0, double dt0, const mgpu_integrator_opts& o)
         : g(g_)
@@ -588,6 +614,7 @@ struct GraphRun {
                 for (int j = 0; j < n; ++j) {
                     to.y[j] -= m[j];
                 }
+                add_mobility_result_time_point(e, t, m);
                 es.trav.erase(es.trav.begin() + i);
                 es.trav_t.erase(es.trav_t.begin() + i);
                 es.ret_t.erase(es.ret_t.begin() + i);
@@ -647,6 +674,7 @@ struct GraphRun {
                 for (int j = 0; j < n; ++j) {
                     from.y[j] -= m[j];
                 }
+                add_mobility_result_time_point(e, t, m);
                 es.trav.push_back(std::move(m));
                 es.trav_t.push_back(t);
                 es.ret_t.push_back(t + dt);
@@ -1244,6 +1272,73 @@ int orc_graph_run(const mgpu_graph* g, double t0, double tmax, double dt_exchang
         run.write_final(final_state);
     }
     run.add_stats(stats);
+    return 0;
+}
+
+int orc_graph_run_commuters(const mgpu_graph* g, double t0, double tmax, double dt_exchange, double dt0,
+                            const mgpu_integrator_opts* opts, int num_sets, const int32_t* set_offsets,
+                            const int32_t* set_indices, int capacity, double* final_state, int32_t* counts,
+                            double* times, double* values, orc_stats* stats)
+{
+    if (!graph_ok(g) || !opts || !(dt_exchange > 0) || num_sets < 1 || !set_offsets || !set_indices ||
+        capacity < 0 || !counts) {
+        return -1;
+    }
+    GraphRun run(g, t0, dt0, *opts);
+    const int n = g->num_groups * kC;
+    for (int i = 0; i < num_sets; ++i) {
+        std::vector<int> set;
+        for (int q = set_offsets[i]; q < set_offsets[i + 1]; ++q) {
+            if (set_indices[q] < 0 || set_indices[q] >= n) {
+                return -1;
+            }
+            set.push_back(set_indices[q]);
+        }
+        run.save_sets.push_back(set);
+    }
+    run.result_t.resize(g->num_edges);
+    run.result_v.resize(g->num_edges);
+    run.run(t0, tmax, dt_exchange, nullptr);
+    for (int e = 0; e < g->num_edges; ++e) {
+        const int np = (int)run.result_t[e].size();
+        counts[e]    = np;
+        for (int k = 0; k < np && k < capacity; ++k) {
+            times[(long)e * capacity + k] = run.result_t[e][k];
+            for (int i = 0; i <= num_sets; ++i) {
+                values[((long)e * capacity + k) * (num_sets + 1) + i] = run.result_v[e][(long)k * (num_sets + 1) + i];
+            }
+        }
+    }
+    if (final_state) {
+        run.write_final(final_state);
+    }
+    run.add_stats(stats);
+    return 0;
+}
+
+int orc_departure_commuters(const mgpu_graph* g, int edge, double t, int num_sets, const int32_t* set_offsets,
+                            const int32_t* set_indices, double* values)
+{
+    if (!graph_ok(g) || edge < 0 || edge >= g->num_edges || num_sets < 1 || !set_offsets || !set_indices ||
+        !values) {
+        return -1;
+    }
+    mgpu_integrator_opts o{};
+    o.abs_tol = 1e-10;
+    o.rel_tol = 1e-5;
+    o.dt_min  = 0.0;
+    o.dt_max  = 0.0;
+    GraphRun run(g, t, 0.1, o);
+    for (int i = 0; i < num_sets; ++i) {
+        run.save_sets.emplace_back(set_indices + set_offsets[i], set_indices + set_offsets[i + 1]);
+    }
+    run.result_t.resize(g->num_edges);
+    run.result_v.resize(g->num_edges);
+    run.apply_mobility(edge, t, 0.0);
+    if (run.result_v[edge].size() != (size_t)(num_sets + 1)) {
+        return -1;
+    }
+    std::copy(run.result_v[edge].begin(), run.result_v[edge].end(), values);
     return 0;
 }
 

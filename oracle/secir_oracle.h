@@ -67,6 +67,25 @@ int orc_graph_run(const mgpu_graph* g, double t0, double tmax, double dt_exchang
                   const mgpu_integrator_opts* opts, double* out_states, double* final_state,
                   orc_stats* stats);
 
+/* orc_graph_run recording MobilityEdge's mobility results
+ * (add_mobility_result_time_point, mobility/metapopulation_mobility_instant.h:
+ * 423-447) on every edge with the same save indices: num_sets sets of flat
+ * compartment indices, set_offsets [num_sets + 1], set_indices. Per edge:
+ * counts [E] time points (one per departure, one per return), times
+ * [E][capacity], values [E][capacity][num_sets + 1] (the sets' sums of the
+ * travelers, then their total). */
+int orc_graph_run_commuters(const mgpu_graph* g, double t0, double tmax, double dt_exchange, double dt0,
+                            const mgpu_integrator_opts* opts, int num_sets, const int32_t* set_offsets,
+                            const int32_t* set_indices, int capacity, double* final_state, int32_t* counts,
+                            double* times, double* values, orc_stats* stats);
+
+/* One MobilityEdge::apply_mobility(t, 0, node_from, node_to) of edge `edge` on
+ * the graph's initial states (a departure, as the reference's
+ * test_mobility.cpp add_mobility_result_time_point does): the mobility result
+ * it records, values [num_sets + 1]. */
+int orc_departure_commuters(const mgpu_graph* g, int edge, double t, int num_sets, const int32_t* set_offsets,
+                            const int32_t* set_indices, double* values);
+
 /* ParameterStudy-style ensemble: graphs[0..num_graphs) each run independently,
  * one graph per thread, num_threads std::threads (0 = all hardware threads).
  * final_states is the concatenation of each graph's [N_b][10G] block.

@@ -7,7 +7,8 @@ Sources (read-only reference tree):
   cpp/tests/data/secihurd-compare-cashkarp.csv (test_odesecir_ageres.cpp:110-189, bounded Cash-Karp)
   cpp/tests/data/secihurd-compare.csv          (test_odesecir.cpp:39-112, test_odesecir_ageres.cpp:27-108, RKF45)
 
-Usage: python tests/golden/make_golden.py [reference_root]
+Usage: python tests/golden/make_golden.py <reference_root>
+(the root of the MEmilio source tree, the directory holding cpp/ and pycode/)
 """
 import os
 import shutil
@@ -22,7 +23,9 @@ FILES = [
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    root = sys.argv[1]
     here = os.path.dirname(os.path.abspath(__file__))
     for rel in FILES:
         shutil.copyfile(os.path.join(root, rel), os.path.join(here, os.path.basename(rel)))

@@ -268,3 +268,34 @@ def test_step_api_order_is_enforced():
         plain.step_nodes(0.5)
     plain.close()
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_async_advance_refuses_interleaved_calls():
+    # while an advance launched with mgpu_batch_launch is in progress, every call
+    # that would change the state, the clock or the caches in between is refused;
+    # the advance then completes as one whole mgpu_batch_advance would
+    from memilio_gb300 import _native as N
+    ctx = N.Context(0)
+    g = W.mobility_graph(seed=9, N=6, G=2, out_degree=2)
+    for prec in (N.PRECISION_FP64, N.PRECISION_MIXED):
+        b = N.Batch(ctx, [g], 0.0, N.solver_opts(precision=prec))
+        ref = N.Batch(ctx, [g], 0.0, N.solver_opts(precision=prec))
+        ref.advance(2.0)
+        state0 = ref.state_flat()
+        assert b.launch(2.0, 1) == 3  # four intervals, one launched
+        times, vals = g.damping_times[0, 0], g.damping_values[0, 0]
+        refused = (lambda: b.advance(2.0), lambda: b.reset(0.0), lambda: b.step_nodes(0.5),
+                   lambda: b.set_state(state0), lambda: b.set_damping_cache(0, 0, 0, times, vals))
+        for call in refused:
+            with pytest.raises(N.MgpuError):
+                call()
+        rem = 3
+        while rem:
+            rem = b.launch(2.0, 1)
+        while not b.query():
+            pass
+        np.testing.assert_array_equal(b.state_flat(), state0)
+        b.close()
+        ref.close()
+    ctx.close()

@@ -76,3 +76,47 @@ def test_damping_cache_combines_levels():
     assert list(t[1:-1]) == [1.0, 2.0]
     assert m[1, 0, 0] == 0.2
     np.testing.assert_allclose(m[2, 0, 0], 1 - (1 - 0.5) * (1 - 0.5))
+
+
+def _commuter_test_graph(insc=0.0, isyc=0.0):
+    """Two nodes of the one-group model of the reference's mobility-result test
+    (cpp/tests/test_mobility.cpp:217-283) joined by an edge with coefficients 0.1."""
+    G = 1
+    p = np.zeros(L.param_stride(G))
+    p[L.P_ICU_CAPACITY] = L.DBL_MAX
+    p[L.P_TNT_CAPACITY] = L.DBL_MAX
+    p[L.P_TNT_MAX_RISK] = 5.0
+    for k, v in ((L.G_TIME_EXPOSED, 1.0), (L.G_TIME_INS, 1.0), (L.G_TIME_ISY, 1.0), (L.G_TIME_ISEV, 1.0),
+                 (L.G_TIME_ICRI, 1.0), (L.G_TRANSMISSION_PROB, 1.0), (L.G_RISK_FROM_SYMPTOMATIC, 1.0),
+                 (L.G_MAX_RISK_FROM_SYMPTOMATIC, 1.0), (L.G_REL_TRANSMISSION_NS, 1.0), (L.G_SEVERE_PER_ISY, 0.5)):
+        p[L.group_param_index(k, 0, G)] = v
+    y = np.zeros(10)
+    y[L.INS], y[L.INSC], y[L.ISY], y[L.ISYC] = 10.0, insc, 20.0, isyc
+    y[L.S] = 1000.0 - 30.0  # set_difference_from_total(S, 1000) before the confirmed compartments were set
+    base = np.full((2, 1, 1, 1), 5.0)
+    return L.GraphArrays(G, np.stack([p, p]), base, np.zeros_like(base), np.zeros((2, 1, 0)),
+                         np.zeros((2, 1, 0, 1, 1)), np.stack([y, y]), np.array([0], np.int32),
+                         np.array([1], np.int32), np.full((1, 10), 0.1))
+
+
+def test_mobility_results_match_the_reference_test():
+    # MobilityEdge::add_mobility_result_time_point (metapopulation_mobility_instant.h:423-447):
+    # the save-index sets (INS + INSC, ISy + ISyC) and the total of the departing travelers
+    sets = [[L.INS, L.INSC], [L.ISY, L.ISYC]]
+    np.testing.assert_allclose(O.departure_commuters(_commuter_test_graph(), 0, 0.0, sets), [1.0, 2.0, 100.0],
+                               rtol=0, atol=1e-12)
+    np.testing.assert_allclose(O.departure_commuters(_commuter_test_graph(100.0, 30.0), 0, 0.0, sets),
+                               [11.0, 5.0, 113.0], rtol=0, atol=1e-12)
+
+
+def test_mobility_results_of_a_graph_run():
+    # one time point per departure and per return; the run itself is unchanged by recording
+    g = W.mobility_graph(seed=3, N=10, G=2, out_degree=3, stress=True)
+    sets = [[L.INS, L.INSC, 10 + L.INS, 10 + L.INSC], [L.ISY, L.ISYC, 10 + L.ISY, 10 + L.ISYC]]
+    fin, counts, times, values, st = O.graph_run_commuters(g, 0.0, 5.0, sets, capacity=16)
+    _, fin0, _ = O.graph_run(g, 0.0, 5.0, record=False)
+    np.testing.assert_array_equal(fin, fin0)
+    assert (counts == 10).all()
+    np.testing.assert_allclose(times[0, :10], np.arange(1, 11) * 0.5)
+    # a departure's total equals the coefficient-weighted source state it took
+    assert (values[:, :10, 2] > 0).all() and (values[:, :10, 2] >= values[:, :10, 0] + values[:, :10, 1]).all()

@@ -88,3 +88,53 @@ def test_oversize_call_is_rejected(ctx):
     assert rc == OUT_OF_RANGE
     fits = SCRATCH_BYTES // (640 * g.num_groups)
     assert fits >= 1000  # about 1092 nodes at six age groups
+
+
+def test_without_dampings_null_arrays(ctx):
+    # K = 0: the damping arrays are NULL and the contact matrix is constant
+    torch = pytest.importorskip("torch")
+    g6 = W.single_node(seed=31, G=6, count=24)
+    n_nodes = g6.num_nodes
+    g = L.GraphArrays(g6.num_groups, g6.params, g6.contact_baseline, g6.contact_minimum,
+                      np.zeros((n_nodes, 1, 0)), np.zeros((n_nodes, 1, 0, 6, 6)), g6.init_state,
+                      np.zeros(0, np.int32), np.zeros(0, np.int32), np.zeros((0, g6.n)))
+    t0, tmax, dt0 = 0.0, 30.0, 0.1
+    opts = L.integrator_opts()
+    ref = ctx.simulate(g, np.arange(n_nodes), t0, tmax, dt0, opts)
+    want = np.stack([y[-1] for _, y in ref])
+    d = _device_inputs(torch, g)
+    assert d["dtimes"] is None and d["dvals"] is None
+    y_out = torch.empty_like(d["y0"])
+    status = torch.full((n_nodes,), -1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    assert _call(ctx, g, d, n_nodes, t0, tmax, dt0, opts, y_out, status) == 0
+    torch.cuda.synchronize()
+    assert (status.cpu().numpy() == 0).all()
+    got = y_out.cpu().numpy()
+    assert (np.abs(got - want) / np.maximum(np.abs(want), 1.0)).max() <= TOL
+
+
+def test_non_finite_state_sets_status_bit(ctx):
+    # a NaN in one node's initial state: that node reports bit 1 (non-finite),
+    # the others are unaffected. (A NaN error norm is accepted by the controller,
+    # so the step size and the clock stay finite and the node still reaches tmax.)
+    torch = pytest.importorskip("torch")
+    g = W.single_node(seed=37, G=6, count=8)
+    count = g.num_nodes
+    t0, tmax, dt0 = 0.0, 10.0, 0.1
+    opts = L.integrator_opts()
+    ref = ctx.simulate(g, np.arange(count), t0, tmax, dt0, opts)
+    want = np.stack([y[-1] for _, y in ref])
+    d = _device_inputs(torch, g)
+    d["y0"][3, 1] = float("nan")
+    y_out = torch.empty_like(d["y0"])
+    status = torch.full((count,), -1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    assert _call(ctx, g, d, count, t0, tmax, dt0, opts, y_out, status) == 0
+    torch.cuda.synchronize()
+    st = status.cpu().numpy()
+    assert st[3] & 2
+    assert (np.delete(st, 3) == 0).all()
+    got = np.delete(y_out.cpu().numpy(), 3, axis=0)
+    ok = np.delete(want, 3, axis=0)
+    assert (np.abs(got - ok) / np.maximum(np.abs(ok), 1.0)).max() <= TOL
