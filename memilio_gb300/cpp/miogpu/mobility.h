@@ -133,19 +133,30 @@ private:
     DampingMatrixExpression m_coeffs;
 };
 
+/* Sets of flat compartment indices whose travelers are summed in the edge's
+ * mobility results (MobilityParameters' save indices, :145-170). */
+using SaveIndices = std::vector<std::vector<size_t>>;
+
 /* mio::MobilityParameters (:106-290). */
 template <typename FP = double>
 class MobilityParameters
 {
 public:
-    explicit MobilityParameters(const std::vector<FP>& coeffs)
+    explicit MobilityParameters(const std::vector<FP>& coeffs, const SaveIndices& save_indices = {})
         : m_coeffs(1, coeffs.size())
+        , m_save_indices(save_indices)
     {
         std::copy(coeffs.begin(), coeffs.end(), m_coeffs[0].get_baseline().data());
     }
-    explicit MobilityParameters(const MobilityCoefficientGroup& coeffs)
+    explicit MobilityParameters(const MobilityCoefficientGroup& coeffs, const SaveIndices& save_indices = {})
         : m_coeffs(coeffs)
+        , m_save_indices(save_indices)
     {
+    }
+    /* The groups of compartments the edge's mobility results sum up (:241-244). */
+    const SaveIndices& get_save_indices() const
+    {
+        return m_save_indices;
     }
     MobilityCoefficientGroup& get_coefficients()
     {
@@ -168,6 +179,7 @@ public:
 private:
     MobilityCoefficientGroup m_coeffs;
     DynamicNPIs<FP> m_dynamic_npis;
+    SaveIndices m_save_indices;
 };
 
 /* mio::MobilityEdge (:300-623): the edge property of a simulation graph. */
@@ -177,11 +189,41 @@ class MobilityEdge
 public:
     explicit MobilityEdge(const MobilityParameters<FP>& params)
         : m_params(params)
+        , m_save_indices(params.get_save_indices())
+        , m_results(m_save_indices.size() + 1)
+    {
+    }
+    MobilityEdge(const MobilityParameters<FP>& params, const SaveIndices& save_indices)
+        : m_params(params)
+        , m_save_indices(save_indices)
+        , m_results(m_save_indices.size() + 1)
     {
     }
     explicit MobilityEdge(const std::vector<FP>& coeffs)
         : m_params(coeffs)
+        , m_results(1)
     {
+    }
+    MobilityEdge(const std::vector<FP>& coeffs, const SaveIndices& save_indices)
+        : m_params(coeffs)
+        , m_save_indices(save_indices)
+        , m_results(m_save_indices.size() + 1)
+    {
+    }
+    /* The travelers' sums over the save-index sets and their total, one time
+     * point per departure and per return (get_mobility_results, :371-383,
+     * add_mobility_result_time_point, :423-447); empty without save indices. */
+    TimeSeries<FP>& get_mobility_results()
+    {
+        return m_results;
+    }
+    const TimeSeries<FP>& get_mobility_results() const
+    {
+        return m_results;
+    }
+    const SaveIndices& get_save_indices() const
+    {
+        return m_save_indices;
     }
     const MobilityParameters<FP>& get_parameters() const
     {
@@ -204,6 +246,8 @@ public:
 private:
     MobilityParameters<FP> m_params;
     DynamicNPIState m_npi;
+    SaveIndices m_save_indices;
+    TimeSeries<FP> m_results;
 };
 
 /* mio::SimulationNode (:39-101): a node's simulation and its results. */
@@ -428,6 +472,9 @@ public:
     {
         ensure_batch();
         mgpu_context* ctx = Device::context();
+        if (!m_save_sets.empty()) {
+            arm_mobility_results(tmax);
+        }
         // NPI checks need every exchange boundary; without them and without
         // recording, one batch advance covers the whole span
         const bool per_interval = m_record || m_any_npis || m_any_edge_npis;
@@ -452,6 +499,9 @@ public:
             if (m_record || m_t >= tmax) {
                 record();
             }
+        }
+        if (!m_save_sets.empty()) {
+            collect_mobility_results();
         }
     }
     double get_t() const
@@ -577,10 +627,63 @@ private:
         }
     }
 
+    /* Commuter statistics of this advance: recording restarts with room for
+     * one time point per exchange up to tmax. */
+    void arm_mobility_results(double tmax)
+    {
+        std::vector<int32_t> offsets(1, 0), indices;
+        for (auto& set : m_save_sets) {
+            for (size_t j : set) {
+                indices.push_back((int32_t)j);
+            }
+            offsets.push_back((int32_t)indices.size());
+        }
+        indices.push_back(0); // never empty
+        const int32_t capacity = (int32_t)std::ceil((tmax - m_t) / m_dt + 1e-9) + 1;
+        check(mgpu_batch_set_commuter_stats(m_batch, 0, (int32_t)m_save_sets.size(), offsets.data(), indices.data(),
+                                            std::max(capacity, 1)),
+              Device::context(), "mgpu_batch_set_commuter_stats");
+        m_stats_capacity = std::max(capacity, 1);
+    }
+    /* Appends the recorded time points to every edge with save indices. */
+    void collect_mobility_results()
+    {
+        auto& edges     = m_graph.edges();
+        const size_t E  = edges.size();
+        const size_t S1 = m_save_sets.size() + 1;
+        std::vector<int32_t> counts(std::max<size_t>(E, 1));
+        std::vector<double> times(std::max<size_t>(E, 1) * (size_t)m_stats_capacity);
+        std::vector<double> values(times.size() * S1);
+        check(mgpu_batch_get_commuter_stats(m_batch, 0, counts.data(), times.data(), values.data()),
+              Device::context(), "mgpu_batch_get_commuter_stats");
+        for (size_t e = 0; e < E; ++e) {
+            auto& prop = edges[e].property;
+            if (prop.get_save_indices().empty()) {
+                continue;
+            }
+            for (int32_t k = 0; k < counts[e]; ++k) {
+                const size_t row = e * (size_t)m_stats_capacity + (size_t)k;
+                prop.get_mobility_results().add_time_point(times[row], values.data() + row * S1);
+            }
+        }
+    }
+
     void ensure_batch()
     {
         if (m_batch) {
             return;
+        }
+        // the edges' save indices: the device records one set list per graph
+        m_save_sets.clear();
+        for (auto& e : m_graph.edges()) {
+            const auto& si = e.property.get_save_indices();
+            if (si.empty()) {
+                continue;
+            }
+            if (!m_save_sets.empty() && si != m_save_sets) {
+                throw Error(MGPU_UNSUPPORTED, "edges of one graph with different save indices");
+            }
+            m_save_sets = si;
         }
         std::vector<const typename std::decay_t<decltype(m_graph.nodes()[0].property.get_simulation().get_model())>*>
             models;
@@ -646,6 +749,8 @@ private:
     bool m_any_edge_npis = false;
     mgpu_batch* m_batch = nullptr;
     detail::GraphArrays m_arrays;
+    SaveIndices m_save_sets; // the edges' save indices (all equal)
+    int32_t m_stats_capacity = 0;
 };
 
 template <class Sim>

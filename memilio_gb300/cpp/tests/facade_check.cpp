@@ -6,6 +6,7 @@
 //   facade_check flows      GPU: simulate_flows (FlowSimulation)
 //   facade_check graph      GPU: make_mobility_sim(...).advance, every boundary
 //   facade_check study      GPU: ParameterStudy over 4 sampled graphs
+//   facade_check commuters  GPU: the edges' mobility results (commuter statistics)
 //   facade_check npi_logic  host only: implement_dynamic_npis and the NPI check
 //                           of Simulation::advance with the state held fixed
 //   facade_check npi_graph  GPU: a graph simulation with dynamic NPIs (FP64 and mixed)
@@ -274,6 +275,51 @@ int mode_graph()
     print_vec("t", t);
     print_vec("states", states);
     std::printf("\"t_end\": %.17g}\n", sim.get_t());
+    return 0;
+}
+
+// Mobility results of every edge (MobilityEdge(coeffs, save_indices),
+// get_mobility_results) with the save indices of cpp/examples/ode_secir_graph.cpp
+// (INS + INSC and ISy + ISyC of every age group), over two advances.
+int mode_commuters()
+{
+    const int G = 2;
+    SaveIndices sets(2);
+    for (size_t g = 0; g < (size_t)G; ++g) {
+        sets[0].push_back(g * 10 + (size_t)InfectionState::InfectedNoSymptoms);
+        sets[0].push_back(g * 10 + (size_t)InfectionState::InfectedNoSymptomsConfirmed);
+        sets[1].push_back(g * 10 + (size_t)InfectionState::InfectedSymptoms);
+        sets[1].push_back(g * 10 + (size_t)InfectionState::InfectedSymptomsConfirmed);
+    }
+    MobilitySimGraph<Simulation<double>> graph;
+    for (int v = 0; v < 3; ++v) {
+        graph.add_node(100 + v, make_model(G, 7u + (unsigned)v), 0.0, 0.1);
+    }
+    graph.add_edge(2, 0, commuters(G, 0.02), sets);
+    graph.add_edge(0, 1, commuters(G, 0.03), sets);
+    graph.add_edge(1, 0, commuters(G, 0.01), sets);
+    graph.add_edge(0, 2, commuters(G, 0.02), sets);
+    auto a   = arrays_of(graph);
+    auto sim = make_mobility_sim(0.0, 0.5, std::move(graph));
+    sim.set_record_boundaries(false);
+    sim.advance(2.5);
+    sim.advance(6.0);
+    std::printf("{");
+    print_graph_arrays(a);
+    std::vector<double> t, v, counts;
+    for (auto& e : sim.get_graph().edges()) {
+        const auto& r = e.property.get_mobility_results();
+        counts.push_back((double)r.get_num_time_points());
+        for (size_t k = 0; k < r.get_num_time_points(); ++k) {
+            t.push_back(r.get_time(k));
+            const auto x = r.get_value(k);
+            v.insert(v.end(), x.begin(), x.end());
+        }
+    }
+    print_vec("counts", counts);
+    print_vec("times", t);
+    print_vec("values", v, false);
+    std::printf("}\n");
     return 0;
 }
 
@@ -643,6 +689,9 @@ int main(int argc, char** argv)
         }
         if (!std::strcmp(mode, "study")) {
             return mode_study();
+        }
+        if (!std::strcmp(mode, "commuters")) {
+            return mode_commuters();
         }
         if (!std::strcmp(mode, "npi_logic")) {
             return mode_npi_logic();

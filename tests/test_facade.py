@@ -165,3 +165,21 @@ def test_interpolate_simulation_result_matches_reference_tests(programs):
     near(d["given_tol"]["t"], [1, 2])
     near(d["chosen"]["t"], [0.2, 0.6, 1.0, 1.3, 2.4])
     near(d["chosen"]["v"], [1 / 8, 5 / 8, 1.2, 1.8, 2 + 10 / 11])
+
+
+@pytest.mark.gpu
+def test_mobility_results_match_oracle(programs):
+    # MobilityEdge::get_mobility_results with save indices through the facade
+    # (the reference's cpp/examples/ode_secir_graph.cpp sets), against the oracle
+    d = run(programs, "commuters")
+    g = graph_of(d)
+    G = g.num_groups
+    sets = [[gr * 10 + c for gr in range(G) for c in (L.INS, L.INSC)],
+            [gr * 10 + c for gr in range(G) for c in (L.ISY, L.ISYC)]]
+    _, counts, times, values, _ = O.graph_run_commuters(g, 0.0, 6.0, sets, capacity=16)
+    np.testing.assert_array_equal(np.array(d["counts"], int), counts)
+    got_t = np.array(d["times"]).reshape(g.num_edges, -1)
+    got_v = np.array(d["values"]).reshape(g.num_edges, -1, len(sets) + 1)
+    np.testing.assert_allclose(got_t, times[:, :counts[0]], rtol=0, atol=1e-12)
+    ref = values[:, :counts[0]]
+    assert np.max(np.abs(got_v - ref) / np.maximum(np.abs(ref), 1e-9 * ref[..., -1:])) < 1e-10
