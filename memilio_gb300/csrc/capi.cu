@@ -824,6 +824,64 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         dg[i].mob_mask = mob_mask[i];
         B.mob_union |= mob_mask[i];
     }
+    // One commuter fraction per (edge, age group): when every compartment the
+    // exchange moves has the same coefficient on every edge of every graph with
+    // static coefficients, the FP32 passes read that one float per (edge, group)
+    // instead of the two coefficient vectors (the products are the same).
+    std::vector<float> h_ecu;
+    if (is_mixed(b->opts.precision) && ecf > 0) {
+        const int mask = (B.mob_union & ~kMaskSEIYRBits) == 0 ? kMaskSEIYRBits : (1 << kC) - 1;
+        std::vector<char> uniform(num_graphs, 1);
+        parallel_for(num_graphs, [&](int64_t gi) {
+            const DevGraph& d = dg[gi];
+            if (!own_coeff[gi] || d.Ke != 0 || d.E == 0) {
+                return;
+            }
+            const int G = d.G;
+            for (int e = 0; e < d.E && uniform[gi]; ++e) {
+                for (int gr = 0; gr < G && uniform[gi]; ++gr) {
+                    const int64_t r0 = d.ecoef_f_off / kC + (int64_t)e * G;
+                    float u          = 0.0f;
+                    bool first       = true;
+                    for (int c = 0; c < kC; ++c) {
+                        if (!((mask >> c) & 1)) {
+                            continue;
+                        }
+                        const float v = h_ecr[rec_elem(r0, G, gr, rec_pos(c))];
+                        if (first) {
+                            u     = v;
+                            first = false;
+                        }
+                        else if (v != u) {
+                            uniform[gi] = 0;
+                        }
+                    }
+                }
+            }
+        });
+        bool all = true;
+        for (int i = 0; i < num_graphs; ++i) {
+            all = all && uniform[i];
+        }
+        if (all) {
+            int first_c = 0; // the first moved compartment (all carry the same value)
+            while (!((mask >> first_c) & 1)) {
+                ++first_c;
+            }
+            h_ecu.resize((size_t)(ecf / kC));
+            for (int i = 0; i < num_graphs; ++i) {
+                const DevGraph& d = dg[i];
+                if (!own_coeff[i] || d.Ke != 0) {
+                    continue;
+                }
+                for (int64_t r = 0; r < (int64_t)d.E * d.G; ++r) {
+                    const int64_t row = d.ecoef_f_off / kC + r;
+                    const int64_t r0  = d.ecoef_f_off / kC + (r / d.G) * d.G;
+                    h_ecu[(size_t)row] = h_ecr[rec_elem(r0, d.G, (int)(r % d.G), rec_pos(first_c))];
+                }
+            }
+        }
+    }
     trace.mark("packing");
     b->host_graphs = dg;
     b->damping_shared.assign(num_graphs, 0);
@@ -913,6 +971,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.risk       = (plain || b->pairs) ? nullptr : (void*)b->pool.alloc<double>(2 * nodes * MGPU_MAX_GROUPS * 2);
     B.aux        = plain ? nullptr : (void*)b->pool.alloc<double>(nodes * MGPU_MAX_GROUPS * 12);
     B.ecoef_r    = b->pairs ? b->pool.upload(h_ecr) : nullptr;
+    B.ecoef_u    = h_ecu.empty() ? nullptr : b->pool.upload(h_ecu);
     B.tab_f      = nullptr;
     B.contact_f  = nullptr;
     B.dvals_f    = nullptr;

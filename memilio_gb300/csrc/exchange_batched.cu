@@ -929,20 +929,30 @@ struct RecCtx {
     }
 };
 
-// the coefficients of edge e for age group gr (its record)
-template <int MASK>
+// the coefficients of edge e for age group gr: its record, or (UNI) the one
+// value every moved compartment has
+template <int MASK, bool UNI>
 __device__ __forceinline__ void ld_coef_m(const BatchDev& B, const RecCtx& x, int64_t e, int gr, float (&cf)[kC])
 {
-    float unused0, unused1;
-    ld_rec_m<MASK, false>(B.ecoef_r, x.crow0 + e * x.G, x.G, gr, cf, unused0, unused1);
+    if constexpr (UNI) {
+        const float u = __ldg(B.ecoef_u + x.crow0 + e * x.G + gr);
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            cf[c] = in_mask(MASK, c) ? u : 0.0f;
+        }
+    }
+    else {
+        float unused0, unused1;
+        ld_rec_m<MASK, false>(B.ecoef_r, x.crow0 + e * x.G, x.G, gr, cf, unused0, unused1);
+    }
 }
 
-template <int MASK = kMaskAll>
+template <int MASK, bool UNI>
 __device__ __forceinline__ void travelers_f(const BatchDev& B, const RecCtx& x, int64_t e, int gr,
                                             const GroupSnap& s, float (&m)[kC])
 {
     float cf[kC];
-    ld_coef_m<MASK>(B, x, e, gr, cf);
+    ld_coef_m<MASK, UNI>(B, x, e, gr, cf);
     travelers_cf<MASK>(s, s.nd, cf, m);
 }
 
@@ -998,7 +1008,7 @@ constexpr int kXfUnroll = MGPU_XF_UNROLL;
 #define MGPU_XF_DEPART_MIN_BLOCKS_ALL 4
 #endif
 // Dense (node, group) mapping as k_xf_return.
-template <int MASK>
+template <int MASK, bool UNI>
 __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_DEPART_MIN_BLOCKS_ALL : MGPU_XF_DEPART_MIN_BLOCKS)
     k_xf_depart(BatchDev B, const int32_t* inst, int64_t count, int G)
 {
@@ -1040,7 +1050,7 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_DEPART_MIN_BLO
         float m[kC];
         const int2 se = B.in_se[k];
         load_group_snap_m<MASK>(x, se.x, gr, src);
-        travelers_f<MASK>(B, x, se.y, gr, src, m);
+        travelers_f<MASK, UNI>(B, x, se.y, gr, src, m);
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
             if (in_mask(MASK, c)) {
@@ -1056,7 +1066,7 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_DEPART_MIN_BLO
 #pragma unroll kXfUnroll
     for (int64_t e = r.o0; e < r.o1; ++e) {
         float cf[kC], m[kC];
-        ld_coef_m<MASK>(B, x, e, gr, cf);
+        ld_coef_m<MASK, UNI>(B, x, e, gr, cf);
         if (detect) {
             // test_commuters: detected commuters move to the confirmed compartments first
             float mo[kC];
@@ -1095,7 +1105,7 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_DEPART_MIN_BLO
 
 // One thread per (node, group) of the nodes with G age groups (dense: node
 // = inst[tid / G], group = tid % G, so no lane idles on unused groups).
-template <int MASK>
+template <int MASK, bool UNI>
 __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_RETURN_MIN_BLOCKS_ALL : MGPU_XF_RETURN_MIN_BLOCKS)
     k_xf_return(BatchDev B, const int32_t* inst, int64_t count, int G)
 {
@@ -1189,7 +1199,7 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_RETURN_MIN_BLO
         float m[kC];
         const int2 se = B.in_se[k];
         load_group_snap_m<MASK>(x, se.x, gr, src);
-        travelers_f<MASK>(B, x, se.y, gr, src, m);
+        travelers_f<MASK, UNI>(B, x, se.y, gr, src, m);
         apply(a_own, m, -1.0f);
     };
     const EdgeRanges r(B, node);
@@ -1205,7 +1215,7 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_RETURN_MIN_BLO
     for (int64_t e = r.o0; e < r.o1; ++e) {
         float ax[kAux], m[kC];
         ld_aux_m<MASK>(aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux, ax);
-        travelers_f<MASK>(B, x, e, gr, own, m);
+        travelers_f<MASK, UNI>(B, x, e, gr, own, m);
         apply(ax, m, 1.0f);
     }
 #pragma unroll kXfUnroll
@@ -1934,11 +1944,22 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
     if (mixed) {
         for (int G = 1; G <= MGPU_MAX_GROUPS; ++G) {
             if (B.gcount[G] > 0) {
+                const unsigned nb = blocks_of(B.gcount[G] * G, T);
                 if ((B.mob_union & ~kMaskSEIYR) == 0) {
-                    k_xf_return<kMaskSEIYR><<<blocks_of(B.gcount[G] * G, T), T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                    if (B.ecoef_u) {
+                        k_xf_return<kMaskSEIYR, true><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                    }
+                    else {
+                        k_xf_return<kMaskSEIYR, false><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                    }
                 }
                 else {
-                    k_xf_return<kMaskAll><<<blocks_of(B.gcount[G] * G, T), T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                    if (B.ecoef_u) {
+                        k_xf_return<kMaskAll, true><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                    }
+                    else {
+                        k_xf_return<kMaskAll, false><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                    }
                 }
                 *launches += 1;
             }
@@ -1978,11 +1999,22 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
     if (mixed) {
         for (int G = 1; G <= MGPU_MAX_GROUPS; ++G) {
             if (B.gcount[G] > 0) {
+                const unsigned nb = blocks_of(B.gcount[G] * G, T);
                 if ((B.mob_union & ~kMaskSEIYR) == 0) {
-                    k_xf_depart<kMaskSEIYR><<<blocks_of(B.gcount[G] * G, T), T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                    if (B.ecoef_u) {
+                        k_xf_depart<kMaskSEIYR, true><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                    }
+                    else {
+                        k_xf_depart<kMaskSEIYR, false><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                    }
                 }
                 else {
-                    k_xf_depart<kMaskAll><<<blocks_of(B.gcount[G] * G, T), T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                    if (B.ecoef_u) {
+                        k_xf_depart<kMaskAll, true><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                    }
+                    else {
+                        k_xf_depart<kMaskAll, false><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
+                    }
                 }
                 *launches += 1;
             }

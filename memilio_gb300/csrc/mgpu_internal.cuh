@@ -142,6 +142,8 @@ struct BatchDev {
     void* risk;                  // [2][num_nodes][MAX_GROUPS] ISy mobility factor at departure (R)
     void* aux;                   // [num_nodes][MAX_GROUPS][12] return-time force of infection and rates (R)
     const float* ecoef_r;        // FP32 coefficient records of edges without dampings (mixed), see rec_vec
+    const float* ecoef_u;        // the same as one value per (edge, group) row when every moved
+                                 // compartment has the same coefficient everywhere (else null)
     const float* tab_f;          // [num_nodes][MAX_GROUPS][kTabF] FP32 node constants (mixed solver)
     const float* contact_f;      // FP32 copy of the contact pool
     const float* dvals_f;        // FP32 copy of the damping-value pool
@@ -176,6 +178,8 @@ enum {
 // (node, group) or (edge, group) ordinals: a node's first row is its state
 // offset / 10, an edge's is ecoef_f_off / 10 + (local edge) * G.
 constexpr int kRec = 12;
+// the usual commuter compartments S, E, INS, ISy, R as a bit mask
+constexpr int kMaskSEIYRBits = (1 << MGPU_S) | (1 << MGPU_E) | (1 << MGPU_INS) | (1 << MGPU_ISY) | (1 << MGPU_R);
 enum { REC_RISK = 5, REC_ND = 6 };
 __host__ __device__ constexpr int rec_pos(int c)
 {
