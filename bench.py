@@ -169,6 +169,32 @@ def workload_config(args):
             "l2": "inputs larger than L2 (node parameters and states of the ensemble exceed 129 MB)"}
 
 
+def schedule_leg(N, ctx, args, ms_step, prec):
+    """Cost of the per-interval launch schedule itself: a two-node graph with one
+    edge each way runs the same kernels per 0.5-day interval (phase bookkeeping,
+    instance order, node solve, return, four exact-scan passes, fallback,
+    cleanup, departure) with almost no work, so its time per interval is the
+    launch and bookkeeping overhead that one persistent kernel could at most save."""
+    from memilio_gb300 import workloads as W
+    g = W.mobility_graph(seed=9, N=2, G=6, out_degree=1)
+    b = N.Batch(ctx, [g], 0.0, N.solver_opts(precision=prec))
+    b.advance(args.days)  # warm-up (captures the interval's CUDA graph)
+    st0 = b.stats()
+    ms = []
+    for _ in range(3):
+        b.reset(0.0)
+        b.advance(args.days)
+        ms.append(b.timing()["advance_ms"])
+    st1 = b.stats()
+    b.close()
+    intervals = int(round(args.days / 0.5))
+    launches = (st1["kernel_launches"] - st0["kernel_launches"]) / 3 / intervals
+    per = min(ms) / intervals
+    return {"us_per_interval": per * 1e3, "launches_per_interval": launches, "intervals_per_step": intervals,
+            "ms_per_step": min(ms), "share_of_step": min(ms) / ms_step,
+            "workload": "2-node graph, one edge each way, 6 age groups: the interval schedule without work"}
+
+
 def uneven_leg(N, ctx, args):
     """Uneven batch: graphs with log-uniform node counts in [1, 2000], 1-6 age
     groups, horizons U[30, 180] days, out-degree U{0..50}, mixed precision, all
@@ -504,6 +530,7 @@ def main():
         plain = {"value": p_val, "unit": UNIT, "sample": f"{k} samples x {args.nodes} nodes x {args.days:g} days",
                  "speedup_of_value": value / world / p_val}
 
+    schedule = schedule_leg(N, ctx, args, ms_step, prec) if rank == 0 and prec != N.PRECISION_FP64_PLAIN else None
     uneven = uneven_leg(N, ctx, args) if rank == 0 and args.uneven > 0 else None
     serving = serving_leg(N, ctx, args) if rank == 0 and args.serve_seconds > 0 else None
 
@@ -533,6 +560,7 @@ def main():
             "attempts_per_node_day": attempts_step / nd_step, "wall_s_timed": t_wall,
             "exchange_per_step": exchange_stats, "plain_fp64": plain, "device_bytes": dev_bytes,
             "uneven_batch": uneven, "serving": serving, "oracle_error": oracle_error, "precision_legs": legs,
+            "schedule_overhead": schedule,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -260,6 +260,26 @@ int mgpu_batch_set_commuter_stats(mgpu_batch* batch, int32_t graph, int32_t num_
  * counts holds the true numbers). */
 int mgpu_batch_get_commuter_stats(mgpu_batch* batch, int32_t graph, int32_t* counts, double* times, double* values);
 
+/*
+ * Flow results of every node: FlowSimulation::get_flows()
+ * (cpp/memilio/compartments/flow_simulation.h:36-121, flow_simulation_base.h:
+ * 64-82) of each SimulationNode of the batch's graphs. With recording on, the
+ * node solves also sum, per node, age group and flow, the persons their own
+ * model moved along the flow (the 5th-order flow increments of every applied
+ * step); mobility moves persons without flows. So between two times, a node's
+ * population changes by its flows scattered to their compartments plus what
+ * the exchanges moved. The integrator's state stays the population (its error
+ * control is over compartments, where FlowSimulation's is over the flows), so
+ * the values agree with a FlowSimulation within the integrator's tolerance.
+ * mgpu_batch_set_flow_recording(batch, 1) starts from zero (and costs one sum
+ * per flow and step); mgpu_batch_reset sets them to zero again.
+ * mgpu_batch_get_flows: [sum_b N_b][15 G_b], flat index g * 15 + k in the
+ * order of the Flows typelist (models/ode_secir/model.h:45-59).
+ * Batched precisions only.
+ */
+int mgpu_batch_set_flow_recording(mgpu_batch* batch, int32_t on);
+int mgpu_batch_get_flows(mgpu_batch* batch, double* out);
+
 /* Failure flags of the node solves since creation or the last reset, per graph
  * [num_graphs]: 0, or MGPU_FAILED_STEP_CAP | MGPU_FAILED_NONFINITE; and the
  * number of failed graphs (either output may be NULL, not both). During an

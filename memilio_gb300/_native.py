@@ -36,7 +36,8 @@ EXPORTED = ["mgpu_default_solver_opts", "mgpu_create", "mgpu_destroy", "mgpu_las
             "mgpu_batch_step_nodes", "mgpu_batch_step_exchange", "mgpu_batch_get_compartment_sums", "mgpu_batch_get_stats", "mgpu_batch_get_timing",
             "mgpu_batch_device_bytes", "mgpu_batch_reset", "mgpu_batch_destroy", "mgpu_simulate_final_noalloc",
             "mgpu_batch_launch", "mgpu_batch_query", "mgpu_batch_get_failed", "mgpu_batch_set_commuter_stats",
-            "mgpu_batch_get_commuter_stats", "mgpu_batch_autotune", "mgpu_simulate_dt", "mgpu_simulate_flows", "mgpu_batch_ensemble_stats", "mgpu_batch_get_graph_state", "mgpu_batch_estimate_bytes",
+            "mgpu_batch_get_commuter_stats",
+            "mgpu_batch_set_flow_recording", "mgpu_batch_get_flows", "mgpu_batch_autotune", "mgpu_simulate_dt", "mgpu_simulate_flows", "mgpu_batch_ensemble_stats", "mgpu_batch_get_graph_state", "mgpu_batch_estimate_bytes",
             "mgpu_default_server_opts", "mgpu_server_create", "mgpu_server_destroy", "mgpu_server_submit",
             "mgpu_server_step", "mgpu_server_take", "mgpu_server_memory_in_use", "mgpu_server_num_batches"]
 
@@ -155,6 +156,8 @@ def lib():
     L.mgpu_batch_query.argtypes = [vp, P(i32)]
     L.mgpu_batch_get_failed.argtypes = [vp, P(i32), P(i32)]
     L.mgpu_batch_set_commuter_stats.argtypes = [vp, i32, i32, P(i32), P(i32), i32]
+    L.mgpu_batch_set_flow_recording.argtypes = [vp, i32]
+    L.mgpu_batch_get_flows.argtypes = [vp, P(d)]
     L.mgpu_batch_get_commuter_stats.argtypes = [vp, i32, P(i32), P(d), P(d)]
     L.mgpu_batch_autotune.argtypes = [vp, P(i32), P(i32)]
     L.mgpu_batch_ensemble_stats.argtypes = [vp, P(d), i32, P(d), P(d)]
@@ -348,6 +351,21 @@ class Batch:
                                                            _dp(times), _dp(values)))
         E = self.graphs[graph].num_edges
         return counts[:E], times[:E], values[:E]
+
+    def set_flow_recording(self, on: bool = True):
+        """mgpu_batch_set_flow_recording: sum every node's flows from now on (from zero)."""
+        self.ctx.check(lib().mgpu_batch_set_flow_recording(self._h, 1 if on else 0))
+
+    def flows(self):
+        """mgpu_batch_get_flows: per graph, the accumulated flows [N, 15 G]."""
+        nf = [g.num_nodes * 15 * g.num_groups for g in self.graphs]
+        out = np.empty(max(sum(nf), 1))
+        self.ctx.check(lib().mgpu_batch_get_flows(self._h, _dp(out)))
+        res, off = [], 0
+        for g, k in zip(self.graphs, nf):
+            res.append(out[off:off + k].reshape(g.num_nodes, 15 * g.num_groups))
+            off += k
+        return res
 
     def failed(self) -> np.ndarray:
         """mgpu_batch_get_failed: per graph 0, or FAILED_STEP_CAP | FAILED_NONFINITE."""

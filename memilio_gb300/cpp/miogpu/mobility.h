@@ -17,7 +17,9 @@
 
 #include "osecir.h"
 
+#include <algorithm>
 #include <functional>
+#include <stdexcept>
 
 namespace miogpu
 {
@@ -57,6 +59,15 @@ public:
     using NodeProperty = NodePropertyT;
     using EdgeProperty = EdgePropertyT;
 
+    Graph() = default;
+    /* Takes nodes and edges as they are (graph.h:154-160); the edges must be
+     * sorted by (start, end), as GraphBuilder::build leaves them. */
+    Graph(std::vector<Node<NodePropertyT>>&& nodes, std::vector<Edge<EdgePropertyT>>&& edges)
+        : m_nodes(std::move(nodes))
+        , m_edges(std::move(edges))
+    {
+    }
+
     template <class... Args>
     Node<NodePropertyT>& add_node(int id, Args&&... args)
     {
@@ -94,6 +105,65 @@ public:
     const std::vector<Edge<EdgePropertyT>>& edges() const
     {
         return m_edges;
+    }
+
+private:
+    std::vector<Node<NodePropertyT>> m_nodes;
+    std::vector<Edge<EdgePropertyT>> m_edges;
+};
+
+/* mio::GraphBuilder (mobility/graph_builder.h): collects nodes and edges in any
+ * order and builds the Graph in one go, sorting the edges by (start, end) once
+ * (stable, so equal pairs keep their insertion order) instead of inserting each
+ * edge in place. With make_unique, of several edges between the same nodes the
+ * one added last is kept. (A graph with duplicate edges is refused by the
+ * device batches, which need one edge per (start, end).) */
+template <class NodePropertyT, class EdgePropertyT>
+class GraphBuilder
+{
+public:
+    using NodeProperty = NodePropertyT;
+    using EdgeProperty = EdgePropertyT;
+
+    GraphBuilder() = default;
+    GraphBuilder(size_t num_nodes, size_t num_edges)
+    {
+        m_nodes.reserve(num_nodes);
+        m_edges.reserve(num_edges);
+    }
+    template <class... Args>
+    void add_node(int id, Args&&... args)
+    {
+        m_nodes.emplace_back(id, std::forward<Args>(args)...);
+    }
+    template <class... Args>
+    void add_edge(size_t start_node_idx, size_t end_node_idx, Args&&... args)
+    {
+        if (start_node_idx >= m_nodes.size() || end_node_idx >= m_nodes.size()) {
+            throw std::out_of_range("edge node index out of range");
+        }
+        m_edges.emplace_back(start_node_idx, end_node_idx, std::forward<Args>(args)...);
+    }
+    Graph<NodePropertyT, EdgePropertyT> build(bool make_unique = false) &&
+    {
+        std::stable_sort(m_edges.begin(), m_edges.end(), [](const auto& a, const auto& b) {
+            return a.start_node_idx == b.start_node_idx ? a.end_node_idx < b.end_node_idx
+                                                        : a.start_node_idx < b.start_node_idx;
+        });
+        if (make_unique && !m_edges.empty()) {
+            std::vector<Edge<EdgePropertyT>> unique;
+            unique.reserve(m_edges.size());
+            for (size_t i = 0; i < m_edges.size(); ++i) {
+                const bool last_of_pair = i + 1 == m_edges.size() ||
+                                          m_edges[i + 1].start_node_idx != m_edges[i].start_node_idx ||
+                                          m_edges[i + 1].end_node_idx != m_edges[i].end_node_idx;
+                if (last_of_pair) {
+                    unique.push_back(std::move(m_edges[i]));
+                }
+            }
+            m_edges = std::move(unique);
+        }
+        return Graph<NodePropertyT, EdgePropertyT>(std::move(m_nodes), std::move(m_edges));
     }
 
 private:

@@ -2,6 +2,7 @@
 //
 //   facade_check dampings   host only: damping caches of several damping lists
 //   facade_check pack       host only: the node/edge arrays of a small graph
+//   facade_check builder    host only: GraphBuilder against Graph::add_edge
 //   facade_check simulate   GPU: Simulation::advance in two pieces and in one
 //   facade_check flows      GPU: simulate_flows (FlowSimulation)
 //   facade_check graph      GPU: make_mobility_sim(...).advance, every boundary
@@ -192,6 +193,37 @@ int mode_pack()
     std::printf("{");
     print_graph_arrays(a);
     std::printf("\"ok\": 1}\n");
+    return 0;
+}
+
+// GraphBuilder (graph_builder.h): edges added out of order and twice between
+// nodes 0 and 1; build(true) keeps the one added last, like Graph::add_edge.
+int mode_builder()
+{
+    const int G = 2;
+    GraphBuilder<SimulationNode<Simulation<double>>, MobilityEdge<double>> builder(3, 5);
+    MobilitySimGraph<Simulation<double>> direct;
+    for (int v = 0; v < 3; ++v) {
+        builder.add_node(100 + v, make_model(G, 7u + (unsigned)v), 0.0, 0.1);
+        direct.add_node(100 + v, make_model(G, 7u + (unsigned)v), 0.0, 0.1);
+    }
+    const std::vector<std::tuple<int, int, double>> adds = {
+        {2, 0, 0.02}, {0, 1, 0.05}, {1, 0, 0.01}, {0, 2, 0.02}, {0, 1, 0.03}};
+    for (auto& a : adds) {
+        builder.add_edge(std::get<0>(a), std::get<1>(a), commuters(G, std::get<2>(a)));
+        direct.add_edge(std::get<0>(a), std::get<1>(a), commuters(G, std::get<2>(a)));
+    }
+    auto built = std::move(builder).build(true);
+    auto a     = arrays_of(built);
+    auto b     = arrays_of(direct);
+    std::printf("{\"same\": %d, \"E\": %d,\n", (int)(a.src == b.src && a.dst == b.dst &&
+                                                      a.coeff_baseline == b.coeff_baseline && a.params == b.params),
+                a.E);
+    std::vector<double> s(a.src.begin(), a.src.end()), d(a.dst.begin(), a.dst.end());
+    print_vec("src", s);
+    print_vec("dst", d);
+    print_vec("coeff_baseline", a.coeff_baseline, false);
+    std::printf("}\n");
     return 0;
 }
 
@@ -677,6 +709,9 @@ int main(int argc, char** argv)
         }
         if (!std::strcmp(mode, "pack")) {
             return mode_pack();
+        }
+        if (!std::strcmp(mode, "builder")) {
+            return mode_builder();
         }
         if (!std::strcmp(mode, "simulate")) {
             return mode_simulate();

@@ -338,6 +338,8 @@ struct mgpu_batch {
     // uploaded to dev.estats, and the device buffers of all graphs that record
     std::vector<EdgeStatsDev> stats_host;
     DevPool stats_pool;
+    // accumulated flows per (node, group) (mgpu_batch_set_flow_recording), kept once allocated
+    double* flows_buf = nullptr;
     // CUDA graph of one batched interval
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_failed          = false;
@@ -2015,6 +2017,9 @@ int mgpu_batch_autotune(mgpu_batch* b, int32_t* instances_per_block, int32_t* gr
             keep(B.counters, sizeof(unsigned long long) * CNT_NUM);
             keep(B.err, sizeof(int32_t));
             keep(B.graph_err, sizeof(int32_t) * (size_t)b->num_graphs);
+            if (B.flows) {
+                keep(B.flows, sizeof(double) * (size_t)(b->state_total / kC) * kF);
+            }
             for (int i = 0; i < b->num_graphs && !b->stats_host.empty(); ++i) {
                 if (b->stats_host[(size_t)i].num_sets) {
                     keep(b->stats_host[(size_t)i].count, sizeof(int32_t) * (size_t)b->host_graphs[(size_t)i].E);
@@ -2245,6 +2250,10 @@ int mgpu_batch_reset(mgpu_batch* b, double t0)
                                                                           b->dt0);
         ++b->launches;
         ck(cudaGetLastError(), "k_reset");
+        if (b->dev.flows) {
+            ck(cudaMemsetAsync(b->dev.flows, 0, sizeof(double) * (size_t)(b->state_total / kC) * kF, b->ctx->stream),
+               "memset");
+        }
         for (int i = 0; i < b->num_graphs && !b->stats_host.empty(); ++i) {
             const EdgeStatsDev& S = b->stats_host[(size_t)i];
             if (S.num_sets) {
@@ -2720,6 +2729,64 @@ int mgpu_batch_get_commuter_stats(mgpu_batch* b, int32_t graph, int32_t* counts,
                                             "); the first capacity points were kept");
             }
         }
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_set_flow_recording(mgpu_batch* b, int32_t on)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (b->async_active || b->half_step) {
+            fail(MGPU_INVALID_VALUE, "an advance is in progress");
+        }
+        if (b->opts.precision == MGPU_PRECISION_FP64_PLAIN) {
+            fail(MGPU_UNSUPPORTED, "flow recording needs a batched precision");
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        const size_t count = (size_t)(b->state_total / kC) * kF;
+        if (on && !b->dev.flows) {
+            if (!b->flows_buf) {
+                b->flows_buf = b->pool.alloc<double>((int64_t)count);
+            }
+            ck(cudaMemsetAsync(b->flows_buf, 0, sizeof(double) * std::max<size_t>(count, 1), b->ctx->stream),
+               "memset");
+            ck(cudaStreamSynchronize(b->ctx->stream), "sync");
+            b->dev.flows = b->flows_buf;
+            b->drop_graph();
+        }
+        else if (!on && b->dev.flows) {
+            b->dev.flows = nullptr;
+            b->drop_graph();
+        }
+        return MGPU_OK;
+    });
+}
+
+int mgpu_batch_get_flows(mgpu_batch* b, double* out)
+{
+    if (!b) {
+        return MGPU_INVALID_VALUE;
+    }
+    return guarded(b->ctx, [&]() -> int {
+        if (!out) {
+            fail(MGPU_INVALID_VALUE, "null output");
+        }
+        if (b->async_active) {
+            fail(MGPU_INVALID_VALUE, "an asynchronous advance is in progress");
+        }
+        if (!b->dev.flows) {
+            fail(MGPU_INVALID_VALUE, "flow recording is off (mgpu_batch_set_flow_recording)");
+        }
+        ck(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+        const size_t count = (size_t)(b->state_total / kC) * kF;
+        if (count > 0) {
+            ck(cudaMemcpyAsync(out, b->dev.flows, sizeof(double) * count, cudaMemcpyDeviceToHost, b->ctx->stream),
+               "d2h flows");
+        }
+        ck(cudaStreamSynchronize(b->ctx->stream), "sync");
         return MGPU_OK;
     });
 }

@@ -152,6 +152,7 @@ struct BatchDev {
     int32_t scratch_nmax;        // components per scratch vector
     DevOpts opts;
     const EdgeStatsDev* estats;  // [num_graphs] commuter statistics, or null (none recorded)
+    double* flows;               // [state_total / 10][15] accumulated flows per (node, group), or null
     int32_t* err;                // device error word (ERR_* bits of the whole batch)
     int32_t* graph_err;          // [num_graphs] ERR_STEP_CAP / ERR_NONFINITE of each graph's own instances
     unsigned long long* counters; // [8]: accepted, rejected, failed, underflow, sequential

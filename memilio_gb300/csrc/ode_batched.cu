@@ -11,17 +11,19 @@
 // independently.
 //
 // Kernels:
-//   k_ode_batched<G>         FP64 throughout, the reference's evaluation order
+//   k_ode_batched<G, FLOWS>  FP64 throughout, the reference's evaluation order
 //                            (MGPU_PRECISION_FP64).
-//   k_ode_mixed<G, false>    FP32 flows, stage combinations, error norm and
+//   k_ode_mixed<G, false, FLOWS>  FP32 flows, stage combinations, error norm and
 //                            step-size controller on an FP32 interval clock; the
 //                            node state as float-float pairs updated in flow
 //                            space with exact TwoSum (MGPU_PRECISION_MIXED).
-//   k_ode_mixed<G, true>     FP32 flows and stage combinations; the state
+//   k_ode_mixed<G, true, FLOWS>   FP32 flows and stage combinations; the state
 //                            update, the error norm, the controller and the
 //                            clock in FP64 (MGPU_PRECISION_MIXED_FP64_CONTROL).
 // In both mixed kernels every flow increment leaves its source and enters its
 // target with the same value, so every node conserves its population.
+// FLOWS: the flow increments of every applied step are also summed per (node,
+// age group, flow) into B.flows (FlowSimulation's flow result, FP64).
 //
 // Integrator: ControlledStepperWrapper<cash_karp54> inside
 // SystemIntegrator::advance (memilio/math/stepper_wrapper.h:112-163,
@@ -221,7 +223,7 @@ __device__ __forceinline__ double seg_max(const Seg<G>& X, double v)
     return m;
 }
 
-template <int G>
+template <int G, bool FLOWS>
 __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* inst, int64_t count)
 {
     constexpr int IPW = 32 / G;
@@ -279,6 +281,7 @@ __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* 
             bool success     = false;
             bool is_dt_valid = true;
             double yn[kC]; // 5th-order result
+            double phi[FLOWS ? kF : 1]; // (FLOWS) its flow increments
             while (!success && is_dt_valid) {
                 if (dt < dt_min) {
                     is_dt_valid = false;
@@ -299,6 +302,12 @@ __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* 
                     xe[c]   = (bk_db[0] * dt) * kc[c];
                     yn[c]   = y[c] + (bk_b5[0] * dt) * kc[c];
                 }
+                if constexpr (FLOWS) {
+#pragma unroll
+                    for (int f = 0; f < kF; ++f) {
+                        phi[f] = (bk_b5[0] * dt) * fl[f];
+                    }
+                }
 #pragma unroll
                 for (int s = 1; s < 6; ++s) {
                     double u[kC];
@@ -318,6 +327,14 @@ __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* 
                         yn[c] = yn[c] + (bk_b5[s] * dt) * kc[c];
                         if (s < 5) {
                             k[s][c] = kc[c];
+                        }
+                    }
+                    if constexpr (FLOWS) {
+                        if (bk_b5[s] != 0.0) {
+#pragma unroll
+                            for (int f = 0; f < kF; ++f) {
+                                phi[f] = phi[f] + (bk_b5[s] * dt) * fl[f];
+                            }
                         }
                     }
                 }
@@ -360,6 +377,13 @@ __global__ void __launch_bounds__(128) k_ode_batched(BatchDev B, const int32_t* 
 #pragma unroll
             for (int c = 0; c < kC; ++c) {
                 y[c] = yn[c];
+            }
+            if constexpr (FLOWS) {
+                double* F = B.flows + ((g.state_off + local * g.n) / kC + X.gi) * kF;
+#pragma unroll
+                for (int f = 0; f < kF; ++f) {
+                    F[f] += phi[f];
+                }
             }
         }
         dt = fmax(dt, dt_restore);
@@ -507,8 +531,9 @@ __device__ void segf_load(SegF<G>& X, const BatchDev& B, const DevGraph& g, int6
     X.t_base       = t_base;
     X.t_base_f     = (float)t_base;
 #pragma unroll
-    for (int q = 0; q < kTabF; ++q) {
-        X.tabv[q] = T[q];
+    for (int q = 0; q < kTabF / 4; ++q) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(T) + q);
+        X.tabv[4 * q] = v.x; X.tabv[4 * q + 1] = v.y; X.tabv[4 * q + 2] = v.z; X.tabv[4 * q + 3] = v.w;
     }
     X.season_s0    = (float)((nm.scalar(MGPU_P_START_DAY) + t_base) * (1.0 / 182.5) + 0.5);
     X.fast         = nm.M == 1;
@@ -634,7 +659,7 @@ __device__ __forceinline__ double err_ratio(float xe, double x, float dxdt, doub
 // error estimate), the controller and the interval clock in FP64.
 // In both, the right-hand side and the stage combinations run in FP32 from the
 // FP32 rounding of the state.
-template <int G, bool CTL64>
+template <int G, bool CTL64, bool FLOWS>
 __global__ void __launch_bounds__(kMixedThreads, CTL64 ? kMixedMinBlocks64 : kMixedMinBlocks)
     k_ode_mixed(BatchDev B, const int32_t* inst, int64_t count)
 {
@@ -657,10 +682,12 @@ __global__ void __launch_bounds__(kMixedThreads, CTL64 ? kMixedMinBlocks64 : kMi
     const Clk o_dt_max = (Clk)o.dt_max; // FP32: DBL_MAX becomes +inf
     // stage derivatives k_0..k_4: [warp][stage*10 + c][lane] (conflict-free columns)
     extern __shared__ float ode_smem[];
-    float* skw = ode_smem + (threadIdx.x >> 5) * (kOdeSmemPerLane * 32);
+    float* skw = ode_smem + (threadIdx.x >> 5) * ((kOdeSmemPerLane + (FLOWS ? kF : 0)) * 32);
 #define SK(s, c) skw[((s) * kC + (c)) * 32 + lane]
     // the 5th-order flow increments of the attempt, after the stage derivatives
 #define SP(f) skw[(5 * kC + (f)) * 32 + lane]
+    // (FLOWS) the increments of the interval's applied steps, summed per flow
+#define SF(f) skw[(kOdeSmemPerLane + (f)) * 32 + lane]
     unsigned long long n_acc = 0, n_rej = 0, n_fail = 0;
 
     for (int64_t slot = wid * IPW + seg; slot < count; slot += nw * IPW) {
@@ -679,9 +706,13 @@ __global__ void __launch_bounds__(kMixedThreads, CTL64 ? kMixedMinBlocks64 : kMi
         float hi[kC], lo[kC];
         double y64[CTL64 ? kC : 1];
 #pragma unroll
+        for (int c = 0; c < kC; c += 2) {
+            const float2 h2 = *reinterpret_cast<const float2*>(yhi + c);
+            const float2 l2 = *reinterpret_cast<const float2*>(ylo + c);
+            hi[c] = h2.x; hi[c + 1] = h2.y; lo[c] = l2.x; lo[c + 1] = l2.y;
+        }
+#pragma unroll
         for (int c = 0; c < kC; ++c) {
-            hi[c] = yhi[c];
-            lo[c] = ylo[c];
             if constexpr (CTL64) {
                 y64[c] = (double)hi[c] + (double)lo[c];
             }
@@ -689,6 +720,12 @@ __global__ void __launch_bounds__(kMixedThreads, CTL64 ? kMixedMinBlocks64 : kMi
         const double t_start = B.node_t[node];
         const double tmax    = rt.t_next;
         segf_load(X, B, g, local, t_start);
+        if constexpr (FLOWS) {
+#pragma unroll
+            for (int f = 0; f < kF; ++f) {
+                SF(f) = 0.0f;
+            }
+        }
         // Return-side values of the pending departure (the exchange's node pass,
         // done here): lambda and the transition rates at the state the travelers
         // left, i.e. at t_dep. That state is this interval's start state unless a
@@ -891,6 +928,12 @@ __global__ void __launch_bounds__(kMixedThreads, CTL64 ? kMixedMinBlocks64 : kMi
             }
             // flow-space update of the (last) attempt: each increment leaves its
             // source and enters its target with the same value
+            if constexpr (FLOWS) {
+#pragma unroll
+                for (int f = 0; f < kF; ++f) {
+                    SF(f) = SF(f) + SP(f);
+                }
+            }
             if constexpr (CTL64) {
 #pragma unroll
                 for (int f = 0; f < kF; ++f) {
@@ -931,6 +974,13 @@ __global__ void __launch_bounds__(kMixedThreads, CTL64 ? kMixedMinBlocks64 : kMi
             B.node_t[node]  = (tr >= span) ? tmax : t_start + (double)tr;
             B.node_dt[node] = (double)dt;
         }
+        if constexpr (FLOWS) {
+            double* F = B.flows + (so / kC) * kF;
+#pragma unroll
+            for (int f = 0; f < kF; ++f) {
+                F[f] += (double)SF(f);
+            }
+        }
         report_instance_failure(B, gidx, cap_hit, nonfinite);
         // Departure at the interval's end (the exchange's node pass, done here):
         // the snapshot record, i.e. the FP32 rounding of the state, the ISy mobility
@@ -961,6 +1011,7 @@ __global__ void __launch_bounds__(kMixedThreads, CTL64 ? kMixedMinBlocks64 : kMi
     }
 #undef SK
 #undef SP
+#undef SF
     if (X.gi == 0) {
         if (n_acc) {
             atomicAdd(&B.counters[CNT_ACCEPTED], n_acc);
@@ -1025,21 +1076,32 @@ int launch_g(const BatchDev& B, int precision, const int32_t* inst, int64_t coun
     if (blocks < 1) {
         blocks = 1;
     }
+    const bool flows = B.flows != nullptr;
     if (is_mixed(precision)) {
-        const size_t smem = (size_t)(threads / 32) * kOdeSmemPerLane * 32 * sizeof(float);
+        const size_t smem = (size_t)(threads / 32) * (kOdeSmemPerLane + (flows ? kF : 0)) * 32 * sizeof(float);
         if (B.gorder[G] && inst == B.glist[G] && count == B.gcount[G]) {
             k_ode_order<<<(unsigned)((count + 127) / 128), 128, 0, s>>>(B, G);
             inst = B.gorder[G];
         }
-        if (precision == MGPU_PRECISION_MIXED_FP64_CONTROL) {
-            k_ode_mixed<G, true><<<(unsigned)blocks, threads, smem, s>>>(B, inst, count);
+        const bool ctl64 = precision == MGPU_PRECISION_MIXED_FP64_CONTROL;
+        if (ctl64 && flows) {
+            k_ode_mixed<G, true, true><<<(unsigned)blocks, threads, smem, s>>>(B, inst, count);
+        }
+        else if (ctl64) {
+            k_ode_mixed<G, true, false><<<(unsigned)blocks, threads, smem, s>>>(B, inst, count);
+        }
+        else if (flows) {
+            k_ode_mixed<G, false, true><<<(unsigned)blocks, threads, smem, s>>>(B, inst, count);
         }
         else {
-            k_ode_mixed<G, false><<<(unsigned)blocks, threads, smem, s>>>(B, inst, count);
+            k_ode_mixed<G, false, false><<<(unsigned)blocks, threads, smem, s>>>(B, inst, count);
         }
     }
+    else if (flows) {
+        k_ode_batched<G, true><<<(unsigned)blocks, threads, 0, s>>>(B, inst, count);
+    }
     else {
-        k_ode_batched<G><<<(unsigned)blocks, threads, 0, s>>>(B, inst, count);
+        k_ode_batched<G, false><<<(unsigned)blocks, threads, 0, s>>>(B, inst, count);
     }
     return 0;
 }

@@ -183,3 +183,13 @@ def test_mobility_results_match_oracle(programs):
     np.testing.assert_allclose(got_t, times[:, :counts[0]], rtol=0, atol=1e-12)
     ref = values[:, :counts[0]]
     assert np.max(np.abs(got_v - ref) / np.maximum(np.abs(ref), 1e-9 * ref[..., -1:])) < 1e-10
+
+
+def test_graph_builder_sorts_and_deduplicates(programs):
+    # GraphBuilder::build(make_unique=true) (cpp/memilio/mobility/graph_builder.h):
+    # edges sorted by (start, end); of the two 0 -> 1 edges the one added last
+    # (coefficients 0.03) stays, as Graph::add_edge's replacement leaves it
+    d = run(programs, "builder")
+    assert d["same"] == 1 and d["E"] == 4
+    assert list(zip(d["src"], d["dst"])) == [(0, 1), (0, 2), (1, 0), (2, 0)]
+    assert abs(d["coeff_baseline"][0] - 0.03) < 1e-15
