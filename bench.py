@@ -235,11 +235,12 @@ def serving_leg(N, ctx, args):
         p_ms += pb.timing()["advance_ms"]
         p_nd += pool[i].num_nodes * horizons[i]
         pb.close()
-    out = {"window_s": args.serve_seconds, "plain_fp64_per_request": {"value": p_nd / (p_ms / 1e3), "unit": UNIT,
+    out = {"window_s": args.serve_seconds, "rebatch_max_graphs": args.serve_rebatch, "plain_fp64_per_request": {"value": p_nd / (p_ms / 1e3), "unit": UNIT,
                                                                        "sample": f"{len(pk)} requests"},
            "rates": []}
     for lam in args.serve_rates:
-        srv = N.Server(ctx_device(ctx), N.server_opts(max_batches=16, phases_per_launch=2))
+        srv = N.Server(ctx_device(ctx), N.server_opts(max_batches=16, phases_per_launch=2,
+                                                      rebatch_max_graphs=args.serve_rebatch))
         t_start = time.perf_counter()
         next_t = t_start + rng.exponential(1.0 / lam)
         submitted, nd_done, lat, k = {}, 0.0, [], 0
@@ -264,12 +265,13 @@ def serving_leg(N, ctx, args):
             if now - t_start > args.serve_seconds + 120.0:
                 break  # drain limit
         wall = time.perf_counter() - t_start
+        merges = srv.num_merges()
         srv.close()
         lat_ms = np.array(lat) * 1e3
         out["rates"].append({"lambda_per_s": lam, "completed": len(lat), "unfinished": len(submitted),
                              "p50_ms": float(np.percentile(lat_ms, 50)) if len(lat) else None,
                              "p99_ms": float(np.percentile(lat_ms, 99)) if len(lat) else None,
-                             "node_days_per_s": nd_done / wall, "wall_s": wall})
+                             "node_days_per_s": nd_done / wall, "wall_s": wall, "merges": merges})
     return out
 
 
@@ -374,6 +376,8 @@ def main():
     ap.add_argument("--uneven", type=int, default=4096, help="graphs of the uneven-batch leg (0 = skip)")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="arrival window per rate (0 = skip)")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 200.0, 800.0])
+    ap.add_argument("--serve-rebatch", type=int, default=0,
+                    help="re-batching: merge running batches of at most this many requests (0 = off)")
     ap.add_argument("--legs-samples", type=int, default=256,
                     help="samples of the ensemble the other batched precisions run once each (0 = skip)")
     args = ap.parse_args()

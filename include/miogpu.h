@@ -289,6 +289,24 @@ int mgpu_batch_get_flows(mgpu_batch* batch, double* out);
 #define MGPU_FAILED_NONFINITE 2
 int mgpu_batch_get_failed(mgpu_batch* batch, int32_t* flags, int32_t* num_failed);
 
+/*
+ * Regroup running graphs into one new batch on `ctx` (no counterpart in the
+ * reference; used by request loops to merge small batches): graph i of the new
+ * batch is graph src_graph[i] of batch src[i], described again by graphs[i]
+ * (the same arrays it was created from), and continues where it stands: node
+ * states, node times and step sizes, the graph's exchange clock and failure
+ * flag are copied, so it goes on exactly as in its source batch. Every source
+ * graph must be between exchange intervals with no travelers away (after a
+ * return, or before the first departure), its batch idle (an asynchronous
+ * advance may be open if the intervals it launched have finished); the
+ * sources must share the device,
+ * the precision and the exchange interval, and record no flows or commuter
+ * statistics. The sources are left unchanged (destroy them when done); the new
+ * batch's next mgpu_batch_launch / mgpu_batch_advance sets the horizons.
+ */
+int mgpu_batch_regroup(mgpu_context* ctx, const mgpu_graph* graphs, int32_t num_graphs, mgpu_batch* const* src,
+                       const int32_t* src_graph, mgpu_batch** out);
+
 /* Restart every graph at time t0 from the initial states given at creation,
  * with the inputs still resident on the device: the equivalent of building
  * a fresh make_mobility_sim(t0, dt, graph) from the same graph
@@ -416,6 +434,15 @@ typedef struct mgpu_server_opts {
     int32_t min_batch_graphs;      /* while batches run, admit once this many requests wait ... */
     double max_wait_ms;            /* ... or the oldest has waited this long (default 1 and 0:
                                       at once); with nothing running, requests are admitted at once */
+    int32_t rebatch_max_graphs;    /* re-batching: while the batch limit holds back admission,
+                                      running batches of at most this many unfinished requests that
+                                      stand between intervals with no travelers away are merged
+                                      into one (mgpu_batch_regroup), which frees batch slots and
+                                      runs their intervals as one launch sequence; 0 = off
+                                      (default: a merge rebuilds the merged graphs' batch on the
+                                      host, which on uneven request streams cost more latency
+                                      than the launches it saved) */
+    int32_t pad;
 } mgpu_server_opts;
 
 void mgpu_default_server_opts(mgpu_server_opts* opts);
@@ -428,6 +455,8 @@ int mgpu_server_take(mgpu_server* server, int64_t* request_id, double* final_sta
 /* Device bytes held by running batches, and their number. */
 int64_t mgpu_server_memory_in_use(const mgpu_server* server);
 int32_t mgpu_server_num_batches(const mgpu_server* server);
+/* Re-batching merges the server has made (rebatch_max_graphs). */
+int64_t mgpu_server_num_merges(const mgpu_server* server);
 
 #ifdef __cplusplus
 }

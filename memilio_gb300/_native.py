@@ -37,9 +37,9 @@ EXPORTED = ["mgpu_default_solver_opts", "mgpu_create", "mgpu_destroy", "mgpu_las
             "mgpu_batch_device_bytes", "mgpu_batch_reset", "mgpu_batch_destroy", "mgpu_simulate_final_noalloc",
             "mgpu_batch_launch", "mgpu_batch_query", "mgpu_batch_get_failed", "mgpu_batch_set_commuter_stats",
             "mgpu_batch_get_commuter_stats",
-            "mgpu_batch_set_flow_recording", "mgpu_batch_get_flows", "mgpu_batch_autotune", "mgpu_simulate_dt", "mgpu_simulate_flows", "mgpu_batch_ensemble_stats", "mgpu_batch_get_graph_state", "mgpu_batch_estimate_bytes",
+            "mgpu_batch_set_flow_recording", "mgpu_batch_get_flows", "mgpu_batch_regroup", "mgpu_batch_autotune", "mgpu_simulate_dt", "mgpu_simulate_flows", "mgpu_batch_ensemble_stats", "mgpu_batch_get_graph_state", "mgpu_batch_estimate_bytes",
             "mgpu_default_server_opts", "mgpu_server_create", "mgpu_server_destroy", "mgpu_server_submit",
-            "mgpu_server_step", "mgpu_server_take", "mgpu_server_memory_in_use", "mgpu_server_num_batches"]
+            "mgpu_server_step", "mgpu_server_take", "mgpu_server_memory_in_use", "mgpu_server_num_batches", "mgpu_server_num_merges"]
 
 
 class MgpuSolverOpts(ctypes.Structure):
@@ -64,6 +64,8 @@ class MgpuServerOpts(ctypes.Structure):
         ("max_graphs_per_batch", ctypes.c_int32),
         ("min_batch_graphs", ctypes.c_int32),
         ("max_wait_ms", ctypes.c_double),
+        ("rebatch_max_graphs", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
     ]
 
 
@@ -157,6 +159,7 @@ def lib():
     L.mgpu_batch_get_failed.argtypes = [vp, P(i32), P(i32)]
     L.mgpu_batch_set_commuter_stats.argtypes = [vp, i32, i32, P(i32), P(i32), i32]
     L.mgpu_batch_set_flow_recording.argtypes = [vp, i32]
+    L.mgpu_batch_regroup.argtypes = [vp, P(MgpuGraph), i32, P(vp), P(i32), P(vp)]
     L.mgpu_batch_get_flows.argtypes = [vp, P(d)]
     L.mgpu_batch_get_commuter_stats.argtypes = [vp, i32, P(i32), P(d), P(d)]
     L.mgpu_batch_autotune.argtypes = [vp, P(i32), P(i32)]
@@ -176,6 +179,8 @@ def lib():
     L.mgpu_server_memory_in_use.restype = ctypes.c_int64
     L.mgpu_server_num_batches.argtypes = [vp]
     L.mgpu_server_num_batches.restype = ctypes.c_int32
+    L.mgpu_server_num_merges.argtypes = [vp]
+    L.mgpu_server_num_merges.restype = ctypes.c_int64
     L.mgpu_batch_device_bytes.argtypes = [vp]
     L.mgpu_batch_device_bytes.restype = ctypes.c_int64
     L.mgpu_batch_destroy.argtypes = [vp]
@@ -472,7 +477,8 @@ class Batch:
 
 
 def server_opts(precision=PRECISION_MIXED, memory_budget=0, max_batches=16, phases_per_launch=2,
-                max_graphs_per_batch=4096, min_batch_graphs=1, max_wait_ms=0.0, **solver_kw) -> MgpuServerOpts:
+                max_graphs_per_batch=4096, min_batch_graphs=1, max_wait_ms=0.0, rebatch_max_graphs=0,
+                **solver_kw) -> MgpuServerOpts:
     o = MgpuServerOpts()
     lib().mgpu_default_server_opts(ctypes.byref(o))
     o.solver = solver_opts(precision=precision, **solver_kw)
@@ -482,6 +488,7 @@ def server_opts(precision=PRECISION_MIXED, memory_budget=0, max_batches=16, phas
     o.max_graphs_per_batch = int(max_graphs_per_batch)
     o.min_batch_graphs = int(min_batch_graphs)
     o.max_wait_ms = float(max_wait_ms)
+    o.rebatch_max_graphs = int(rebatch_max_graphs)
     return o
 
 
@@ -532,6 +539,9 @@ class Server:
 
     def num_batches(self) -> int:
         return int(lib().mgpu_server_num_batches(self._h))
+
+    def num_merges(self) -> int:
+        return int(lib().mgpu_server_num_merges(self._h))
 
     def close(self):
         if self._h:

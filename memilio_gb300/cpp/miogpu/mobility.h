@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <functional>
 #include <stdexcept>
+#include <type_traits>
 
 namespace miogpu
 {
@@ -363,6 +364,14 @@ private:
 
 namespace detail
 {
+
+/* Does a node simulation keep flow results (FlowSimulation::get_flows)? */
+template <class S, class = void>
+struct has_flows : std::false_type {
+};
+template <class S>
+struct has_flows<S, std::void_t<decltype(std::declval<S&>().get_flows())>> : std::true_type {
+};
 
 /* The arrays of one graph in the layout of include/miogpu_layout.h. */
 struct GraphArrays {
@@ -797,6 +806,15 @@ private:
         }
         mgpu_context* ctx = Device::context();
         check(mgpu_batch_create(ctx, &g, 1, m_t, &o, &m_batch), ctx, "mgpu_batch_create");
+        using SimT = std::decay_t<decltype(m_graph.nodes()[0].property.get_simulation())>;
+        if constexpr (detail::has_flows<SimT>::value) {
+            // FlowSimulation nodes: the device sums their flows from here on
+            check(mgpu_batch_set_flow_recording(m_batch, 1), ctx, "mgpu_batch_set_flow_recording");
+            m_flow_offsets.clear();
+            for (auto& nd : m_graph.nodes()) {
+                m_flow_offsets.push_back(nd.property.get_simulation().get_flows().get_last_value());
+            }
+        }
     }
     void record()
     {
@@ -809,6 +827,20 @@ private:
             nd.get_result().add_time_point(m_t, st.data() + v * n);
             nd.set_last_state(st.data() + v * n);
         }
+        using SimT = std::decay_t<decltype(m_graph.nodes()[0].property.get_simulation())>;
+        if constexpr (detail::has_flows<SimT>::value) {
+            // the flows of the nodes' own models at the same time (mobility moves people without flows)
+            const size_t nf = (size_t)m_arrays.G * MGPU_NUM_FLOWS;
+            std::vector<double> fl((size_t)m_arrays.N * nf);
+            check(mgpu_batch_get_flows(m_batch, fl.data()), ctx, "mgpu_batch_get_flows");
+            for (size_t v = 0; v < m_graph.nodes().size(); ++v) {
+                std::vector<double> acc(m_flow_offsets[v]);
+                for (size_t q = 0; q < nf; ++q) {
+                    acc[q] += fl[v * nf + q];
+                }
+                m_graph.nodes()[v].property.get_simulation().get_flows().add_time_point(m_t, acc);
+            }
+        }
     }
 
     double m_t, m_dt;
@@ -820,6 +852,7 @@ private:
     mgpu_batch* m_batch = nullptr;
     detail::GraphArrays m_arrays;
     SaveIndices m_save_sets; // the edges' save indices (all equal)
+    std::vector<std::vector<double>> m_flow_offsets; // FlowSimulation nodes: their flows when the batch began
     int32_t m_stats_capacity = 0;
 };
 

@@ -571,8 +571,8 @@ private:
 
 /* get_infections_relative (model.h:413-423): the symptomatic infections of the
  * value vector y relative to the model's total population. */
-template <typename FP>
-FP get_infections_relative(const Simulation<FP>& sim, FP /*t*/, const std::vector<FP>& y)
+template <typename FP, class Sim>
+FP get_infections_relative(const Sim& sim, FP /*t*/, const std::vector<FP>& y)
 {
     const auto& model = sim.get_model();
     FP sum_inf        = 0;
@@ -582,8 +582,8 @@ FP get_infections_relative(const Simulation<FP>& sim, FP /*t*/, const std::vecto
     return sum_inf / model.populations.get_total();
 }
 /* The same from the symptomatic infections summed over the age groups. */
-template <typename FP>
-FP get_infections_relative_of_sum(const Simulation<FP>& sim, FP sum_inf)
+template <typename FP, class Sim>
+FP get_infections_relative_of_sum(const Sim& sim, FP sum_inf)
 {
     return sum_inf / sim.get_model().populations.get_total();
 }
@@ -665,7 +665,15 @@ public:
     {
         return m_model;
     }
+    const Model& get_model() const
+    {
+        return m_model;
+    }
     FP& get_dt()
+    {
+        return m_dt;
+    }
+    const FP& get_dt() const
     {
         return m_dt;
     }
@@ -673,12 +681,26 @@ public:
     {
         m_core = core;
     }
+    const IntegratorCore& get_integrator_core() const
+    {
+        return m_core;
+    }
+    /* The node's dynamic-NPI state when it runs in a graph simulation. */
+    DynamicNPIState& get_dynamic_npi_state()
+    {
+        return m_npi;
+    }
+    const DynamicNPIState& get_dynamic_npi_state() const
+    {
+        return m_npi;
+    }
 
 private:
     Model m_model;
     TimeSeries<FP> m_result, m_flows;
     FP m_dt;
     IntegratorCore m_core;
+    DynamicNPIState m_npi;
 };
 
 /* mio::simulate_flows (flow_simulation.h:104-121): {populations, flows}. */

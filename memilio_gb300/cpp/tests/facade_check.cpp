@@ -8,6 +8,7 @@
 //   facade_check graph      GPU: make_mobility_sim(...).advance, every boundary
 //   facade_check study      GPU: ParameterStudy over 4 sampled graphs
 //   facade_check commuters  GPU: the edges' mobility results (commuter statistics)
+//   facade_check flows_graph  GPU: a graph of FlowSimulation nodes next to Simulation nodes
 //   facade_check npi_logic  host only: implement_dynamic_npis and the NPI check
 //                           of Simulation::advance with the state held fixed
 //   facade_check npi_graph  GPU: a graph simulation with dynamic NPIs (FP64 and mixed)
@@ -351,6 +352,55 @@ int mode_commuters()
     print_vec("counts", counts);
     print_vec("times", t);
     print_vec("values", v, false);
+    std::printf("}\n");
+    return 0;
+}
+
+// A graph of FlowSimulation nodes (the reference's graph of FlowSimulation
+// nodes, cpp/tests/test_graph_simulation.cpp:276-340) next to the same graph of
+// Simulation nodes: the states at every boundary and the flows of the nodes.
+int mode_flows_graph()
+{
+    const int G = 2;
+    MobilitySimGraph<Simulation<double>> plain;
+    Graph<SimulationNode<FlowSimulation<double>>, MobilityEdge<double>> flows;
+    for (int v = 0; v < 3; ++v) {
+        plain.add_node(100 + v, make_model(G, 7u + (unsigned)v), 0.0, 0.1);
+        flows.add_node(100 + v, make_model(G, 7u + (unsigned)v), 0.0, 0.1);
+    }
+    const std::vector<std::tuple<int, int, double>> edges = {{2, 0, 0.02}, {0, 1, 0.03}, {1, 0, 0.01}, {0, 2, 0.02}};
+    for (auto& e : edges) {
+        plain.add_edge(std::get<0>(e), std::get<1>(e), commuters(G, std::get<2>(e)));
+        flows.add_edge(std::get<0>(e), std::get<1>(e), commuters(G, std::get<2>(e)));
+    }
+    auto a    = arrays_of(plain);
+    auto sim0 = make_mobility_sim(0.0, 0.5, std::move(plain));
+    GraphSimulation<decltype(flows)> sim1(0.0, 0.5, std::move(flows));
+    sim0.advance(3.0);
+    sim1.advance(3.0);
+    sim1.advance(6.0);
+    sim0.advance(6.0);
+    std::printf("{");
+    print_graph_arrays(a);
+    std::vector<double> s0, s1, f, t;
+    for (size_t v = 0; v < 3; ++v) {
+        const auto& r0 = sim0.get_graph().nodes()[v].property.get_result();
+        const auto& r1 = sim1.get_graph().nodes()[v].property.get_result();
+        const auto& fl = sim1.get_graph().nodes()[v].property.get_simulation().get_flows();
+        for (size_t k = 0; k < r1.get_num_time_points(); ++k) {
+            const auto x0 = r0.get_value(k), x1 = r1.get_value(k), y = fl.get_value(k);
+            s0.insert(s0.end(), x0.begin(), x0.end());
+            s1.insert(s1.end(), x1.begin(), x1.end());
+            f.insert(f.end(), y.begin(), y.end());
+            if (v == 0) {
+                t.push_back(fl.get_time(k));
+            }
+        }
+    }
+    print_vec("t", t);
+    print_vec("states_plain", s0);
+    print_vec("states_flows", s1);
+    print_vec("flows", f, false);
     std::printf("}\n");
     return 0;
 }
@@ -727,6 +777,9 @@ int main(int argc, char** argv)
         }
         if (!std::strcmp(mode, "commuters")) {
             return mode_commuters();
+        }
+        if (!std::strcmp(mode, "flows_graph")) {
+            return mode_flows_graph();
         }
         if (!std::strcmp(mode, "npi_logic")) {
             return mode_npi_logic();

@@ -1599,6 +1599,119 @@ int mgpu_batch_create(mgpu_context* ctx, const mgpu_graph* graphs, int32_t num_g
     });
 }
 
+int mgpu_batch_regroup(mgpu_context* ctx, const mgpu_graph* graphs, int32_t num_graphs, mgpu_batch* const* src,
+                       const int32_t* src_graph, mgpu_batch** out)
+{
+    return guarded(ctx, [&]() -> int {
+        if (!graphs || num_graphs < 1 || !src || !src_graph || !out) {
+            fail(MGPU_INVALID_VALUE, "null argument or no graphs");
+        }
+        *out = nullptr;
+        {
+            std::lock_guard<std::mutex> lock(g_batches_mutex);
+            for (int i = 0; i < num_graphs; ++i) {
+                if (!src[i] || !g_batches.count(src[i])) {
+                    fail(MGPU_INVALID_VALUE, "source " + std::to_string(i) + " is not a live batch");
+                }
+            }
+        }
+        const mgpu_solver_opts o = src[0]->opts;
+        if (o.precision == MGPU_PRECISION_FP64_PLAIN) {
+            fail(MGPU_UNSUPPORTED, "regrouping needs a batched precision");
+        }
+        std::vector<GraphRt> rts((size_t)num_graphs);
+        for (int i = 0; i < num_graphs; ++i) {
+            mgpu_batch* sb = src[i];
+            const int j    = src_graph[i];
+            if (j < 0 || j >= sb->num_graphs) {
+                fail(MGPU_OUT_OF_RANGE, "source graph index out of range");
+            }
+            if (sb->ctx->device != ctx->device || sb->opts.precision != o.precision ||
+                sb->opts.dt_exchange != o.dt_exchange || sb->dev.flows || !sb->stats_host.empty()) {
+                fail(MGPU_UNSUPPORTED, "sources differ in device, precision or exchange interval, or record "
+                                       "flows or commuter statistics");
+            }
+            if (sb->half_step) {
+                fail(MGPU_INVALID_VALUE, "a source batch awaits mgpu_batch_step_exchange");
+            }
+            if (sb->async_active && cudaEventQuery(sb->ev_async) != cudaSuccess) {
+                cudaGetLastError(); // (not-ready is no error of this call)
+                fail(MGPU_INVALID_VALUE, "a source batch's launched intervals are still running");
+            }
+            const DevGraph& d = sb->host_graphs[(size_t)j];
+            if (graphs[i].num_nodes != d.N || graphs[i].num_groups != d.G || graphs[i].num_edges != d.E) {
+                fail(MGPU_INVALID_VALUE, "graph " + std::to_string(i) + " is not the source graph's shape");
+            }
+            ck(cudaSetDevice(sb->ctx->device), "cudaSetDevice");
+            ck(cudaMemcpyAsync(&rts[(size_t)i], sb->dev.rt + j, sizeof(GraphRt), cudaMemcpyDeviceToHost,
+                               sb->ctx->stream),
+               "d2h graph record");
+            ck(cudaStreamSynchronize(sb->ctx->stream), "sync");
+            if (rts[(size_t)i].has_pending) {
+                fail(MGPU_INVALID_VALUE, "graph " + std::to_string(i) + " has travelers away");
+            }
+        }
+        mgpu_batch* b = nullptr;
+        const int rc  = mgpu_batch_create(ctx, graphs, num_graphs, 0.0, &o, &b);
+        if (rc != MGPU_OK) {
+            return rc;
+        }
+        try {
+            cudaStream_t s = ctx->stream;
+            for (int i = 0; i < num_graphs; ++i) {
+                const mgpu_batch* sb = src[i];
+                const int j          = src_graph[i];
+                const int64_t cnt    = (int64_t)b->N[(size_t)i] * b->n[(size_t)i];
+                const int64_t so     = sb->state_off[(size_t)j], dn = b->state_off[(size_t)i];
+                if (b->pairs) {
+                    ck(cudaMemcpyAsync(b->dev.st_hi + dn, sb->dev.st_hi + so, sizeof(float) * cnt,
+                                       cudaMemcpyDeviceToDevice, s),
+                       "d2d state");
+                    ck(cudaMemcpyAsync(b->dev.st_lo + dn, sb->dev.st_lo + so, sizeof(float) * cnt,
+                                       cudaMemcpyDeviceToDevice, s),
+                       "d2d state");
+                }
+                else {
+                    ck(cudaMemcpyAsync(b->dev.state + dn, sb->dev.state + so, sizeof(double) * cnt,
+                                       cudaMemcpyDeviceToDevice, s),
+                       "d2d state");
+                }
+                const int64_t N = b->N[(size_t)i];
+                ck(cudaMemcpyAsync(b->dev.node_t + b->node0[(size_t)i], sb->dev.node_t + sb->node0[(size_t)j],
+                                   sizeof(double) * N, cudaMemcpyDeviceToDevice, s),
+                   "d2d node times");
+                ck(cudaMemcpyAsync(b->dev.node_dt + b->node0[(size_t)i], sb->dev.node_dt + sb->node0[(size_t)j],
+                                   sizeof(double) * N, cudaMemcpyDeviceToDevice, s),
+                   "d2d node steps");
+                ck(cudaMemcpyAsync(b->dev.rt + i, &rts[(size_t)i], sizeof(GraphRt), cudaMemcpyHostToDevice, s),
+                   "h2d graph record");
+                ck(cudaMemcpyAsync(b->dev.graph_err + i, sb->dev.graph_err + j, sizeof(int32_t),
+                                   cudaMemcpyDeviceToDevice, s),
+                   "d2d failure word");
+                // (the source's host mirror of the time lags during an asynchronous advance)
+                b->t_host[(size_t)i]    = rts[(size_t)i].t;
+                b->tmax_host[(size_t)i] = rts[(size_t)i].tmax;
+            }
+            // a graph that failed before keeps failing the advances of the new batch
+            const std::vector<int32_t> f = read_graph_errors(b);
+            int32_t any = 0;
+            for (int32_t x : f) {
+                any |= x;
+            }
+            if (any) {
+                ck(cudaMemcpyAsync(b->dev.err, &any, sizeof(int32_t), cudaMemcpyHostToDevice, s), "h2d error word");
+            }
+            ck(cudaStreamSynchronize(s), "sync");
+        }
+        catch (...) {
+            mgpu_batch_destroy(b);
+            throw;
+        }
+        *out = b;
+        return MGPU_OK;
+    });
+}
+
 int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
 {
     if (!b) {

@@ -53,11 +53,13 @@ struct Running {
     mgpu_batch* batch = nullptr;
     std::vector<Request> reqs;
     std::vector<char> delivered;
+    std::vector<int64_t> base; // intervals each request had completed before it joined this batch
     int64_t bytes     = 0;
     int64_t launched  = 0; // intervals enqueued so far
     int64_t finished  = 0; // intervals known to have finished
     int32_t remaining = 0;
     bool in_flight    = false;
+    bool started      = false; // the batch's advance has been launched (its horizons are set)
 };
 
 } // namespace
@@ -72,6 +74,7 @@ struct mgpu_server {
     std::deque<Done> done;
     std::vector<mgpu_context*> idle_ctx;
     int64_t completed_total = 0;
+    int64_t merges          = 0; // re-batching merges so far
 };
 
 namespace
@@ -112,7 +115,7 @@ int deliver(mgpu_server* s, Running& r, bool all_done, int32_t batch_status)
     int n = 0;
     std::vector<int32_t> failed;
     for (size_t i = 0; i < r.reqs.size(); ++i) {
-        if (r.delivered[i] || (!all_done && r.reqs[i].phases > r.finished)) {
+        if (r.delivered[i] || (!all_done && r.reqs[i].phases > r.base[i] + r.finished)) {
             continue;
         }
         Done d;
@@ -138,6 +141,78 @@ int deliver(mgpu_server* s, Running& r, bool all_done, int32_t batch_status)
     return n;
 }
 
+// Merges the running batches that are between intervals (not in flight, not
+// finished) and hold at most rebatch_max_graphs unfinished requests into one
+// new batch (mgpu_batch_regroup). Batches whose graphs have travelers away, or
+// a merge that would not fit the memory budget, are left as they are.
+void rebatch(mgpu_server* s)
+{
+    // only when the batch limit holds back admission: a merge rebuilds the
+    // merged graphs' batch on the host, which costs more than the launches it
+    // saves while there is room for more batches
+    if ((int32_t)s->running.size() < s->opts.max_batches || s->queue.empty()) {
+        return;
+    }
+    std::vector<size_t> cand;
+    int64_t graphs = 0;
+    for (size_t k = 0; k < s->running.size(); ++k) {
+        const Running& r = s->running[k];
+        int64_t open     = 0;
+        for (char d : r.delivered) {
+            open += d ? 0 : 1;
+        }
+        if (!r.in_flight && r.started && open > 0 && open <= s->opts.rebatch_max_graphs &&
+            graphs + open <= s->opts.max_graphs_per_batch) {
+            cand.push_back(k);
+            graphs += open;
+        }
+    }
+    if (cand.size() < 2) {
+        return;
+    }
+    Running m;
+    std::vector<mgpu_graph> gs;
+    std::vector<mgpu_batch*> src;
+    std::vector<int32_t> src_graph;
+    for (size_t k : cand) {
+        const Running& r = s->running[k];
+        for (size_t i = 0; i < r.reqs.size(); ++i) {
+            if (r.delivered[i]) {
+                continue;
+            }
+            m.reqs.push_back(r.reqs[i]);
+            m.base.push_back(r.base[i] + r.finished);
+            gs.push_back(r.reqs[i].graph);
+            src.push_back(r.batch);
+            src_graph.push_back((int32_t)i);
+        }
+    }
+    const int64_t est = mgpu_batch_estimate_bytes(gs.data(), (int32_t)gs.size(), &s->opts.solver);
+    if (est < 0 || s->in_use + est > s->budget) {
+        return;
+    }
+    m.ctx = take_ctx(s);
+    if (!m.ctx) {
+        return;
+    }
+    if (mgpu_batch_regroup(m.ctx, gs.data(), (int32_t)gs.size(), src.data(), src_graph.data(), &m.batch) != MGPU_OK) {
+        s->idle_ctx.push_back(m.ctx); // e.g. travelers away: try again at a later step
+        return;
+    }
+    m.delivered.assign(m.reqs.size(), 0);
+    m.bytes = std::max<int64_t>(est, mgpu_batch_device_bytes(m.batch));
+    for (auto it = cand.rbegin(); it != cand.rend(); ++it) {
+        Running& r = s->running[*it];
+        mgpu_batch_destroy(r.batch);
+        s->idle_ctx.push_back(r.ctx);
+        s->in_use -= r.bytes;
+        s->running.erase(s->running.begin() + (long)*it);
+    }
+    s->in_use += m.bytes;
+    ++s->merges;
+    s->running.push_back(std::move(m));
+}
+
 } // namespace
 
 extern "C" {
@@ -155,6 +230,8 @@ void mgpu_default_server_opts(mgpu_server_opts* o)
     o->max_graphs_per_batch = 4096;
     o->min_batch_graphs     = 1; // admit at once (measured: waiting to batch did not raise throughput)
     o->max_wait_ms          = 0.0;
+    o->rebatch_max_graphs   = 0; // off: measured slower on the uneven request stream (a merge rebuilds on the host)
+    o->pad                  = 0;
 }
 
 int mgpu_server_create(int device, const mgpu_server_opts* opts, mgpu_server** out)
@@ -174,7 +251,7 @@ int mgpu_server_create(int device, const mgpu_server_opts* opts, mgpu_server** o
         return MGPU_UNSUPPORTED;
     }
     if (o.max_batches < 1 || o.phases_per_launch < 1 || o.max_graphs_per_batch < 1 || o.memory_budget < 0 ||
-        o.min_batch_graphs < 1 || !(o.max_wait_ms >= 0.0)) {
+        o.min_batch_graphs < 1 || !(o.max_wait_ms >= 0.0) || o.rebatch_max_graphs < 0) {
         return MGPU_INVALID_VALUE;
     }
     if (cudaSetDevice(device) != cudaSuccess) {
@@ -244,35 +321,73 @@ int mgpu_server_step(mgpu_server* s, int32_t* completed, int32_t* running, int32
         return MGPU_CUDA_ERROR;
     }
     int n_completed = 0;
-    // 1. progress of the running batches
+    // 1. progress of the running batches: deliver what their finished intervals completed
     for (size_t k = 0; k < s->running.size();) {
         Running& r = s->running[k];
-        bool finished_all = false;
-        int32_t st        = MGPU_OK;
         if (r.in_flight) {
-            int32_t done = 0;
-            st           = mgpu_batch_query(r.batch, &done);
+            int32_t done   = 0;
+            const int32_t st = mgpu_batch_query(r.batch, &done);
             if (st == MGPU_OK && !done) {
                 ++k;
                 continue;
             }
-            r.in_flight = false;
-            r.finished  = r.launched;
-            finished_all = st != MGPU_OK || r.remaining == 0;
+            r.in_flight             = false;
+            r.finished              = r.launched;
+            const bool finished_all = st != MGPU_OK || r.remaining == 0;
             n_completed += deliver(s, r, finished_all, st);
+            if (finished_all) {
+                mgpu_batch_destroy(r.batch);
+                s->idle_ctx.push_back(r.ctx);
+                s->in_use -= r.bytes;
+                s->running.erase(s->running.begin() + (long)k);
+                continue;
+            }
         }
-        if (!finished_all) {
-            int32_t rem = 0;
-            st          = mgpu_batch_launch(r.batch, 0.0, nullptr, s->opts.phases_per_launch, &rem);
+        ++k;
+    }
+    // 1b. re-batching: small batches that stand between intervals with no
+    // travelers away merge into one, so that their next intervals run as one
+    // launch sequence (every graph goes on exactly as before)
+    if (s->opts.rebatch_max_graphs > 0) {
+        rebatch(s);
+    }
+    // 1c. the next intervals of every running batch that is not in flight
+    for (size_t k = 0; k < s->running.size();) {
+        Running& r = s->running[k];
+        if (r.in_flight) {
+            ++k;
+            continue;
+        }
+        int32_t rem = 0;
+        int32_t st  = MGPU_OK;
+        if (!r.started) {
+            // a merged batch: its requests' horizons, from where each stands
+            std::vector<double> tmax(r.reqs.size());
+            int64_t total = 0;
+            for (size_t i = 0; i < r.reqs.size(); ++i) {
+                tmax[i] = r.reqs[i].tmax;
+                total   = std::max<int64_t>(total, r.reqs[i].phases - r.base[i]);
+            }
+            st = mgpu_batch_launch(r.batch, 0.0, tmax.data(), s->opts.phases_per_launch, &rem);
+            if (st == MGPU_OK) {
+                r.started   = true;
+                r.launched  = total - rem;
+                r.remaining = rem;
+            }
+        }
+        else {
+            st = mgpu_batch_launch(r.batch, 0.0, nullptr, s->opts.phases_per_launch, &rem);
             if (st == MGPU_OK) {
                 r.launched += r.remaining - rem;
                 r.remaining = rem;
-                r.in_flight = true;
-                ++k;
-                continue;
             }
-            n_completed += deliver(s, r, true, st);
         }
+        if (st == MGPU_OK) {
+            r.in_flight = true;
+            ++k;
+            continue;
+        }
+        n_completed += deliver(s, r, true, st);
         mgpu_batch_destroy(r.batch);
         s->idle_ctx.push_back(r.ctx);
         s->in_use -= r.bytes;
@@ -350,9 +465,11 @@ int mgpu_server_step(mgpu_server* s, int32_t* completed, int32_t* running, int32
         st = mgpu_batch_launch(r.batch, 0.0, tmax.data(), s->opts.phases_per_launch, &rem);
         r.reqs      = std::move(take);
         r.delivered.assign(r.reqs.size(), 0);
+        r.base.assign(r.reqs.size(), 0);
         r.remaining = rem;
         r.launched  = total - rem;
         r.in_flight = st == MGPU_OK;
+        r.started   = true;
         s->in_use += r.bytes;
         if (st != MGPU_OK) {
             n_completed += deliver(s, r, true, st);
@@ -419,6 +536,11 @@ int64_t mgpu_server_memory_in_use(const mgpu_server* s)
 int32_t mgpu_server_num_batches(const mgpu_server* s)
 {
     return s ? (int32_t)s->running.size() : -1;
+}
+
+int64_t mgpu_server_num_merges(const mgpu_server* s)
+{
+    return s ? s->merges : -1;
 }
 
 } // extern "C"

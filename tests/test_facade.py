@@ -193,3 +193,19 @@ def test_graph_builder_sorts_and_deduplicates(programs):
     assert d["same"] == 1 and d["E"] == 4
     assert list(zip(d["src"], d["dst"])) == [(0, 1), (0, 2), (1, 0), (2, 0)]
     assert abs(d["coeff_baseline"][0] - 0.03) < 1e-15
+
+
+@pytest.mark.gpu
+def test_graph_of_flow_simulations(programs):
+    # the reference's consistency test of a graph of FlowSimulation nodes
+    # (cpp/tests/test_graph_simulation.cpp:276-340): the same states as a graph
+    # of Simulation nodes (to rounding: the FP64 kernel that also sums the flows
+    # contracts a few multiply-adds differently), the flows start at zero and
+    # only grow
+    d = run(programs, "flows_graph")
+    G = d["G"]
+    P = len(d["t"])
+    assert P == 13 and abs(d["t"][-1] - 6.0) < 1e-12
+    np.testing.assert_allclose(d["states_flows"], d["states_plain"], rtol=1e-12, atol=1e-12)
+    f = np.array(d["flows"]).reshape(3, P, 15 * G)
+    assert (f[:, 0] == 0).all() and (np.diff(f, axis=1) >= 0).all() and f[:, -1].max() > 0

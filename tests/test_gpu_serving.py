@@ -175,3 +175,45 @@ def test_server_waits_to_batch_requests_while_busy(ctx):
             break
     assert done == 5
     srv.close()
+
+
+@pytest.mark.parametrize("rebatch", [16, 0])
+def test_rebatching_merges_running_batches(ctx, rebatch):
+    # two waves fill the server's two batch slots while a third waits; once both
+    # batches stand between intervals (no travelers away after each pair of
+    # intervals) the server merges them into one (mgpu_batch_regroup), which
+    # frees a slot for the third wave, and every request still ends exactly as
+    # when solved alone
+    import time
+    graphs, horizons = requests(10, seed=61)
+    horizons = np.maximum(horizons, 6.0)
+    srv = N.Server(0, N.server_opts(max_batches=2, rebatch_max_graphs=rebatch))
+    ids, results = {}, {}
+    for i in range(4):
+        ids[srv.submit(graphs[i], 0.0, horizons[i])] = i
+    srv.step()
+    for i in range(4, 8):
+        ids[srv.submit(graphs[i], 0.0, horizons[i])] = i
+    srv.step()
+    assert srv.num_batches() == 2
+    for i in range(8, 10):
+        ids[srv.submit(graphs[i], 0.0, horizons[i])] = i
+    time.sleep(0.3)  # both batches finish the intervals they were given
+    _, _, queued = srv.step()
+    if rebatch:
+        assert srv.num_merges() == 1 and queued == 0 and srv.num_batches() == 2
+    else:
+        assert srv.num_merges() == 0 and queued == 2
+    for _ in range(200000):
+        srv.step()
+        while True:
+            t = srv.take()
+            if t is None:
+                break
+            results[ids[t[0]]] = t[1]
+        if len(results) == len(graphs):
+            break
+    assert srv.memory_in_use() == 0
+    srv.close()
+    for i, g in enumerate(graphs):
+        np.testing.assert_array_equal(results[i], alone(ctx, g, horizons[i]))
