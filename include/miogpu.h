@@ -62,6 +62,10 @@ typedef struct mgpu_solver_opts {
     int32_t use_cuda_graph;          /* capture the fixed exchange schedule as a CUDA graph */
     int32_t profile;                 /* time node solves and exchanges separately with CUDA events
                                         (launches stream by stream; no CUDA graph) */
+    int32_t staged_exchange;         /* mixed solvers: graphs whose exchange tables fit in shared
+                                        memory return and depart one CTA per graph from a copy
+                                        there (1, default); 0 = every graph in the node-list passes.
+                                        Both give identical results. */
 } mgpu_solver_opts;
 
 /* Device times of the last mgpu_batch_advance, from CUDA events on the context's stream. */
@@ -255,7 +259,8 @@ int mgpu_batch_set_commuter_stats(mgpu_batch* batch, int32_t graph, int32_t num_
                                   const int32_t* set_indices, int32_t capacity);
 /* The recorded time points of every edge of the graph (edges in the graph's
  * (start, end) order): counts [E], times [E][capacity], values
- * [E][capacity][num_sets + 1] (times and values may be NULL). MGPU_OUT_OF_RANGE
+ * [E][capacity][num_sets + 1] (times and values may be NULL; the slots after an
+ * edge's counts[e] points are zero). MGPU_OUT_OF_RANGE
  * if an edge recorded more points than the capacity (the first ones are kept;
  * counts holds the true numbers). */
 int mgpu_batch_get_commuter_stats(mgpu_batch* batch, int32_t graph, int32_t* counts, double* times, double* values);

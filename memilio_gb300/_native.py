@@ -52,6 +52,7 @@ class MgpuSolverOpts(ctypes.Structure):
         ("max_steps_per_interval", ctypes.c_int32),
         ("use_cuda_graph", ctypes.c_int32),
         ("profile", ctypes.c_int32),
+        ("staged_exchange", ctypes.c_int32),
     ]
 
 
@@ -199,7 +200,7 @@ def _ip(a: np.ndarray):
 
 def solver_opts(precision=PRECISION_MIXED, dt0=0.1, dt_exchange=0.5, integrator: Optional[MgpuIntegratorOpts] = None,
                 instances_per_block=0, max_steps_per_interval=0, use_cuda_graph=True,
-                profile=False) -> MgpuSolverOpts:
+                profile=False, staged_exchange=True) -> MgpuSolverOpts:
     o = MgpuSolverOpts()
     lib().mgpu_default_solver_opts(ctypes.byref(o))
     if integrator is not None:
@@ -211,6 +212,7 @@ def solver_opts(precision=PRECISION_MIXED, dt0=0.1, dt_exchange=0.5, integrator:
     o.max_steps_per_interval = max_steps_per_interval
     o.use_cuda_graph = 1 if use_cuda_graph else 0
     o.profile = 1 if profile else 0
+    o.staged_exchange = 1 if staged_exchange else 0
     return o
 
 

@@ -824,7 +824,14 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.mob_union = 0;
     for (int i = 0; i < num_graphs; ++i) {
         dg[i].mob_mask = mob_mask[i];
+        dg[i].staged   = 0;
         B.mob_union |= mob_mask[i];
+    }
+    // graphs whose FP32 exchange passes run one CTA per graph from shared memory
+    XsPlan xs;
+    if (is_mixed(b->opts.precision) && b->opts.staged_exchange) {
+        xs = plan_staged_exchange(dg, B.mob_union, ctx->device);
+        ck(xs.err, "staged exchange setup");
     }
     // One commuter fraction per (edge, age group): when every compartment the
     // exchange moves has the same coefficient on every edge of every graph with
@@ -1076,6 +1083,39 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
                           ? b->pool.alloc<int32_t>(B.gcount[G])
                           : nullptr;
     }
+    // the exchange passes: the staged graphs, and per G the nodes of the others
+    B.xs_count    = (int32_t)xs.graphs.size();
+    B.xs_graphs   = xs.graphs.empty() ? nullptr : b->pool.upload(xs.graphs);
+    B.xs_smem_ret = xs.smem_ret;
+    B.xs_smem_dep = xs.smem_dep;
+    B.xs_aux      = xs.aux;
+    // (graphs without edges or with edge dampings take no part in the FP32 node-list passes)
+    for (int G = 0; G <= MGPU_MAX_GROUPS; ++G) {
+        B.xlist[G]  = nullptr;
+        B.xcount[G] = 0;
+    }
+    if (is_mixed(b->opts.precision)) {
+        std::map<int, std::vector<int32_t>> xl;
+        for (int i = 0; i < num_graphs; ++i) {
+            if (!dg[i].staged && dg[i].E > 0 && dg[i].Ke == 0) {
+                auto& l = xl[b->G[i]];
+                for (int v = 0; v < b->N[i]; ++v) {
+                    l.push_back((int32_t)(b->node0[i] + v));
+                }
+            }
+        }
+        for (int G = 0; G <= MGPU_MAX_GROUPS; ++G) {
+            auto it = xl.find(G);
+            if (it == xl.end()) {
+                continue;
+            }
+            auto ig = b->inst_by_G.find(G);
+            // the same list as the node solves' when it holds every node with G groups
+            const bool all = ig != b->inst_by_G.end() && ig->second.second == (int64_t)it->second.size();
+            B.xlist[G]     = all ? ig->second.first : b->pool.upload(it->second);
+            B.xcount[G]    = (int64_t)it->second.size();
+        }
+    }
     B.order_cnt = b->pool.alloc<int32_t>(2 * (MGPU_MAX_GROUPS + 1));
     ck(cudaMemsetAsync(B.order_cnt, 0, sizeof(int32_t) * 2 * (MGPU_MAX_GROUPS + 1), ctx->stream), "memset");
     ck(cudaStreamSynchronize(ctx->stream), "upload sync");
@@ -1226,6 +1266,7 @@ void mgpu_default_solver_opts(mgpu_solver_opts* o)
     o->dt_exchange        = 0.5;
     o->precision          = MGPU_PRECISION_MIXED;
     o->use_cuda_graph     = 1;
+    o->staged_exchange    = 1;
 }
 
 int mgpu_create(int device, mgpu_context** out)
@@ -1811,7 +1852,7 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
                 ode_launches += (int64_t)b->inst_by_G.size(); // node-solve kernels (their ordering passes excluded)
             }
             b->launches +=
-                P * (2 + node_kernel_launches(b) + exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size(), b->dev.estats != nullptr));
+                P * (2 + node_kernel_launches(b) + exchange_batched_launches(b->dev, b->opts.precision, b->any_edge_dampings));
             b->phases += P;
         }
         else {
@@ -1832,7 +1873,7 @@ int mgpu_batch_advance(mgpu_batch* b, double tmax, const double* tmax_per_graph)
                 }
             }
             const int64_t per_phase = 2 + node_kernel_launches(b) +
-                                      exchange_batched_launches(b->opts.precision, B.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size(), b->dev.estats != nullptr);
+                                      exchange_batched_launches(b->dev, b->opts.precision, b->any_edge_dampings);
             for (int64_t p = 0; p < P; ++p) {
                 if (b->graph_exec) {
                     ck(cudaGraphLaunch(b->graph_exec, s), "cudaGraphLaunch");
@@ -1943,7 +1984,7 @@ int mgpu_batch_launch(mgpu_batch* b, double tmax, const double* tmax_per_graph, 
         }
         ck(cudaGetLastError(), "launch");
         b->launches += n * (2 + node_kernel_launches(b) +
-                            exchange_batched_launches(b->opts.precision, b->dev.num_edges > 0, b->any_edge_dampings, (int)b->inst_by_G.size(), b->dev.estats != nullptr));
+                            exchange_batched_launches(b->dev, b->opts.precision, b->any_edge_dampings));
         b->phases += n;
         b->async_left -= n;
         ck(cudaEventRecord(b->ev_async, s), "cudaEventRecord");
@@ -2835,6 +2876,17 @@ int mgpu_batch_get_commuter_stats(mgpu_batch* b, int32_t graph, int32_t* counts,
             }
         }
         ck(cudaStreamSynchronize(s), "sync");
+        // the slots after an edge's recorded points read as zero
+        const int64_t w = x.num_sets + 1;
+        for (int64_t e = 0; e < E; ++e) {
+            const int64_t k = std::min<int64_t>(std::max(counts[e], 0), x.capacity);
+            if (times) {
+                std::fill(times + e * x.capacity + k, times + (e + 1) * x.capacity, 0.0);
+            }
+            if (values) {
+                std::fill(values + (e * x.capacity + k) * w, values + (e + 1) * x.capacity * w, 0.0);
+            }
+        }
         for (int64_t e = 0; e < E; ++e) {
             if (counts[e] > x.capacity) {
                 fail(MGPU_OUT_OF_RANGE, "an edge recorded more time points than the capacity (" +

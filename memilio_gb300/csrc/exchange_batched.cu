@@ -30,7 +30,9 @@
 // handles what the scan passes leave unresolved.
 #include "mgpu_internal.cuh"
 
+#include <algorithm>
 #include <type_traits>
+#include <utility>
 
 namespace mgpu
 {
@@ -1007,25 +1009,166 @@ constexpr int kXfUnroll = MGPU_XF_UNROLL;
 #ifndef MGPU_XF_DEPART_MIN_BLOCKS_ALL
 #define MGPU_XF_DEPART_MIN_BLOCKS_ALL 4
 #endif
-// Dense (node, group) mapping as k_xf_return.
-template <int MASK, bool UNI>
-__global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_DEPART_MIN_BLOCKS_ALL : MGPU_XF_DEPART_MIN_BLOCKS)
-    k_xf_depart(BatchDev B, const int32_t* inst, int64_t count, int G)
+// Where the FP32 passes read the snapshot records and the return-time rates:
+// TabG gathers them from the global tables (L2), TabS from the copy of one
+// graph's rows in shared memory (rates from shared memory when AUXS). Both
+// produce the same values, so the two kinds of pass give identical results.
+template <int MASK>
+struct TabG {
+    RecCtx x;
+    const float* aux;
+    __device__ __forceinline__ void snap(int64_t node, int gr, GroupSnap& s) const
+    {
+        load_group_snap_m<MASK>(x, node, gr, s);
+    }
+    __device__ __forceinline__ void rates(int64_t node, int gr, float (&a)[kAux]) const
+    {
+        ld_aux_m<MASK>(aux + (node * MGPU_MAX_GROUPS + gr) * kAux, a);
+    }
+};
+
+// record vectors (float4) of the snapshot records, and of the return-time
+// rates, that MASK needs: their count and the slot of vector v among them
+__host__ __device__ constexpr int aux_need(int mask, int v)
 {
-    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= count * G) {
-        return;
+    bool need = false;
+    for (int k = 0; k < kF; ++k) {
+        const int a = aux_of_flow(k);
+        need        = need || (in_mask(mask, kFlowSrcI(k)) && a >= 4 * v && a < 4 * v + 4);
     }
-    const int64_t qi   = tid / G;
-    const int64_t node = inst[qi];
-    const int gr       = (int)(tid - qi * G);
-    const int gi       = B.node_graph[node];
-    const DevGraph& g  = B.graphs[gi];
-    const GraphRt& rt  = B.rt[gi];
-    if (!xb_departing(rt) || g.Ke != 0) {
-        return;
+    return need;
+}
+__host__ __device__ constexpr int snap_nvec(int mask)
+{
+    return (int)rec_need(mask, 0, true) + (int)rec_need(mask, 1, true) + (int)rec_need(mask, 2, true);
+}
+__host__ __device__ constexpr int aux_nvec(int mask)
+{
+    return (int)aux_need(mask, 0) + (int)aux_need(mask, 1) + (int)aux_need(mask, 2);
+}
+__host__ __device__ constexpr int snap_slot_of(int mask, int v)
+{
+    return v == 0 ? 0 : (int)rec_need(mask, 0, true) + (v == 2 ? (int)rec_need(mask, 1, true) : 0);
+}
+__host__ __device__ constexpr int aux_slot_of(int mask, int v)
+{
+    return v == 0 ? 0 : (int)aux_need(mask, 0) + (v == 2 ? (int)aux_need(mask, 1) : 0);
+}
+
+// Shared-memory copy of one graph: snapshot vector slot j of (local node v,
+// group gr) at float4 (v * NS + j) * G + gr (the groups of a node side by
+// side, as in the global records); rate vector slot j at (v * G + gr) * NA + j.
+template <int MASK, bool AUXS>
+struct TabS {
+    static constexpr int NS = snap_nvec(MASK);
+    static constexpr int NA = aux_nvec(MASK);
+    RecCtx x;
+    const float* aux;
+    const float4* ss;
+    const float4* sa;
+    int64_t node0;
+    __device__ __forceinline__ void snap(int64_t node, int gr, GroupSnap& s) const
+    {
+        const int64_t v = node - node0;
+        float r[kRec];
+#pragma unroll
+        for (int q = 0; q < kRec / 4; ++q) {
+            if (rec_need(MASK, q, true)) {
+                const float4 a = ss[(v * NS + snap_slot_of(MASK, q)) * x.G + gr];
+                r[4 * q]       = a.x;
+                r[4 * q + 1]   = a.y;
+                r[4 * q + 2]   = a.z;
+                r[4 * q + 3]   = a.w;
+            }
+            else {
+                r[4 * q] = r[4 * q + 1] = r[4 * q + 2] = r[4 * q + 3] = 0.0f;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            s.y[c] = in_mask(MASK, c) ? r[rec_pos(c)] : 0.0f;
+        }
+        s.risk = r[REC_RISK];
+        s.nd   = r[REC_ND];
     }
-    const int ws     = rt.snap_slot ^ 1;
+    __device__ __forceinline__ void rates(int64_t node, int gr, float (&a)[kAux]) const
+    {
+        if constexpr (AUXS) {
+            const int64_t i = ((node - node0) * x.G + gr) * NA;
+#pragma unroll
+            for (int q = 0; q < kAux / 4; ++q) {
+                if (aux_need(MASK, q)) {
+                    const float4 w = sa[i + aux_slot_of(MASK, q)];
+                    a[4 * q]       = w.x;
+                    a[4 * q + 1]   = w.y;
+                    a[4 * q + 2]   = w.z;
+                    a[4 * q + 3]   = w.w;
+                }
+                else {
+                    a[4 * q] = a[4 * q + 1] = a[4 * q + 2] = a[4 * q + 3] = 0.0f;
+                }
+            }
+        }
+        else {
+            ld_aux_m<MASK>(aux + (node * MGPU_MAX_GROUPS + gr) * kAux, a);
+        }
+    }
+};
+
+// Copies graph g's snapshot records of slot `slot` (and, when AUXS, its
+// return-time rates) to shared memory: coalesced float4 loads of the vectors
+// MASK needs, by the whole block.
+template <int MASK, bool AUXS>
+__device__ __forceinline__ void stage_graph(const BatchDev& B, const DevGraph& g, int slot, float4* ss, float4* sa)
+{
+    constexpr int NS = snap_nvec(MASK);
+    constexpr int NA = aux_nvec(MASK);
+    const int G      = g.G;
+    const float4* gs = reinterpret_cast<const float4*>(B.gsnap + (int64_t)slot * (B.state_total / kC) * kRec) +
+                       (g.state_off / kC) * (kRec / 4);
+    const int ns = g.N * NS * G;
+    for (int u = threadIdx.x; u < ns; u += blockDim.x) {
+        const int v   = u / (NS * G);
+        const int rem = u - v * NS * G;
+        const int j   = rem / G;
+        const int gr  = rem - j * G;
+        // the record vector of slot j
+        int vec = 0;
+#pragma unroll
+        for (int q = 0; q < kRec / 4; ++q) {
+            if (rec_need(MASK, q, true) && snap_slot_of(MASK, q) == j) {
+                vec = q;
+            }
+        }
+        ss[u] = __ldg(gs + (int64_t)v * G * (kRec / 4) + vec * G + gr);
+    }
+    if constexpr (AUXS) {
+        const float4* ga = reinterpret_cast<const float4*>(B.aux) + g.node0 * MGPU_MAX_GROUPS * (kAux / 4);
+        const int na     = g.N * G * NA;
+        for (int u = threadIdx.x; u < na; u += blockDim.x) {
+            const int item = u / NA;
+            const int j    = u - item * NA;
+            const int v    = item / G;
+            const int gr   = item - v * G;
+            int vec        = 0;
+#pragma unroll
+            for (int q = 0; q < kAux / 4; ++q) {
+                if (aux_need(MASK, q) && aux_slot_of(MASK, q) == j) {
+                    vec = q;
+                }
+            }
+            sa[u] = __ldg(ga + ((int64_t)v * MGPU_MAX_GROUPS + gr) * (kAux / 4) + vec);
+        }
+    }
+    __syncthreads();
+}
+
+// Departure of one (node, age group): the travelers of its out-edges leave, the
+// travelers of its in-edges arrive, summed in the serial order of the edges.
+template <int MASK, bool UNI, class Tab>
+__device__ __forceinline__ void xf_depart_item(const BatchDev& B, const DevGraph& g, const GraphRt& rt,
+                                               const Tab& tab, int64_t node, int gr)
+{
     const int64_t lv = node - g.node0;
     const int64_t so = g.state_off + lv * g.n + gr * kC;
     Acc<float> acc[kC];
@@ -1038,9 +1181,9 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_DEPART_MIN_BLO
             acc[c].init_pair(h[c], l[c]);
         }
     }
-    const RecCtx x(B, g, ws);
+    const RecCtx& x = tab.x;
     GroupSnap own;
-    load_group_snap_m<MASK>(x, node, gr, own);
+    tab.snap(node, gr, own);
     const bool detect = own.nd != 1.0f;
     const float q     = 1.0f - own.nd;
     // travelers arriving from the source of in-edge k
@@ -1049,7 +1192,7 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_DEPART_MIN_BLO
         GroupSnap src;
         float m[kC];
         const int2 se = B.in_se[k];
-        load_group_snap_m<MASK>(x, se.x, gr, src);
+        tab.snap(se.x, gr, src);
         travelers_f<MASK, UNI>(B, x, se.y, gr, src, m);
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
@@ -1103,26 +1246,70 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_DEPART_MIN_BLO
     st_state(B.v0_lo + so, l);
 }
 
-// One thread per (node, group) of the nodes with G age groups (dense: node
-// = inst[tid / G], group = tid % G, so no lane idles on unused groups).
+// Dense (node, group) mapping as k_xf_return.
 template <int MASK, bool UNI>
-__global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_RETURN_MIN_BLOCKS_ALL : MGPU_XF_RETURN_MIN_BLOCKS)
-    k_xf_return(BatchDev B, const int32_t* inst, int64_t count, int G)
+__global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_DEPART_MIN_BLOCKS_ALL : MGPU_XF_DEPART_MIN_BLOCKS)
+    k_xf_depart(BatchDev B, const int32_t* inst, int64_t count, int G)
 {
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= count * G) {
         return;
     }
-    const int64_t q    = tid / G;
-    const int64_t node = inst[q];
-    const int gr       = (int)(tid - q * G);
+    const int64_t qi   = tid / G;
+    const int64_t node = inst[qi];
+    const int gr       = (int)(tid - qi * G);
     const int gi       = B.node_graph[node];
     const DevGraph& g  = B.graphs[gi];
     const GraphRt& rt  = B.rt[gi];
-    if (!xb_returning(rt) || g.Ke != 0) {
+    if (!xb_departing(rt) || g.Ke != 0 || g.staged) {
         return;
     }
-    const int slot   = rt.snap_slot;
+    const TabG<MASK> tab{RecCtx(B, g, rt.snap_slot ^ 1), reinterpret_cast<const float*>(B.aux)};
+    xf_depart_item<MASK, UNI>(B, g, rt, tab, node, gr);
+}
+
+#ifndef MGPU_XS_THREADS
+#define MGPU_XS_THREADS 512 // threads of the per-graph passes
+#endif
+#ifndef MGPU_XS_DEPART_MIN_BLOCKS
+#define MGPU_XS_DEPART_MIN_BLOCKS 2
+#endif
+#ifndef MGPU_XS_RETURN_MIN_BLOCKS
+#define MGPU_XS_RETURN_MIN_BLOCKS 1
+#endif
+constexpr int kXsThreads = MGPU_XS_THREADS;
+
+// One CTA per staged graph (B.xs_graphs): the departure snapshot of the graph
+// in shared memory, then the graph's (node, group) items in the dense order.
+template <int MASK, bool UNI>
+__global__ void __launch_bounds__(kXsThreads, MGPU_XS_DEPART_MIN_BLOCKS) k_xs_depart(BatchDev B)
+{
+    extern __shared__ float4 xs_smem[];
+    const int gi      = B.xs_graphs[blockIdx.x];
+    const DevGraph& g = B.graphs[gi];
+    const GraphRt& rt = B.rt[gi];
+    if (!xb_departing(rt)) {
+        return;
+    }
+    const int ws = rt.snap_slot ^ 1;
+    stage_graph<MASK, false>(B, g, ws, xs_smem, nullptr);
+    const TabS<MASK, false> tab{RecCtx(B, g, ws), reinterpret_cast<const float*>(B.aux), xs_smem, nullptr, g.node0};
+    const int G     = g.G;
+    const int items = g.N * G;
+    for (int i = threadIdx.x; i < items; i += blockDim.x) {
+        const int v = i / G;
+        xf_depart_item<MASK, UNI>(B, g, rt, tab, g.node0 + v, i - v * G);
+    }
+}
+
+// Return of one (node, age group): the travelers of its in-edges go home, the
+// travelers of its out-edges come home, each with its Euler flows; the state
+// is updated in place, the state before it kept for the exact path, and the
+// item queued for that path when the no-underflow bound fails.
+template <int MASK, bool UNI, class Tab>
+__device__ __forceinline__ void xf_return_item(const BatchDev& B, const DevGraph& g, const GraphRt& rt,
+                                               const Tab& tab, int64_t node, int gr)
+{
     const float dt   = (float)rt.dt;
     const int64_t lv = node - g.node0;
     const int64_t s0 = g.state_off + lv * g.n + gr * kC;
@@ -1148,12 +1335,11 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_RETURN_MIN_BLO
     for (int f = 0; f < kF; ++f) {
         phi_net[f] = 0.0f;
     }
-    const float* aux = reinterpret_cast<const float*>(B.aux);
     float a_own[kAux];
-    ld_aux_m<MASK>(aux + (node * MGPU_MAX_GROUPS + gr) * kAux, a_own);
-    const RecCtx x(B, g, slot);
+    tab.rates(node, gr, a_own);
+    const RecCtx& x = tab.x;
     GroupSnap own;
-    load_group_snap_m<MASK>(x, node, gr, own);
+    tab.snap(node, gr, own);
     // run[c] is a lower bound of the exact running state of the serial order:
     // in-edges take max(t, 0) away, out-edges add t (negative amounts included),
     // so within each run of in-edges it only decreases, and the underflow test of
@@ -1198,7 +1384,7 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_RETURN_MIN_BLO
         GroupSnap src;
         float m[kC];
         const int2 se = B.in_se[k];
-        load_group_snap_m<MASK>(x, se.x, gr, src);
+        tab.snap(se.x, gr, src);
         travelers_f<MASK, UNI>(B, x, se.y, gr, src, m);
         apply(a_own, m, -1.0f);
     };
@@ -1214,7 +1400,7 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_RETURN_MIN_BLO
 #pragma unroll kXfUnroll
     for (int64_t e = r.o0; e < r.o1; ++e) {
         float ax[kAux], m[kC];
-        ld_aux_m<MASK>(aux + (B.edge_dst[e] * MGPU_MAX_GROUPS + gr) * kAux, ax);
+        tab.rates(B.edge_dst[e], gr, ax);
         travelers_f<MASK, UNI>(B, x, e, gr, own, m);
         apply(ax, m, 1.0f);
     }
@@ -1241,6 +1427,54 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_RETURN_MIN_BLO
     st_state(B.st_hi + so, h);
     st_state(B.st_lo + so, l);
     list0_push(B, node * MGPU_MAX_GROUPS + gr, flag);
+}
+
+// One thread per (node, group) of the nodes with G age groups (dense: node
+// = inst[tid / G], group = tid % G, so no lane idles on unused groups).
+template <int MASK, bool UNI>
+__global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_RETURN_MIN_BLOCKS_ALL : MGPU_XF_RETURN_MIN_BLOCKS)
+    k_xf_return(BatchDev B, const int32_t* inst, int64_t count, int G)
+{
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= count * G) {
+        return;
+    }
+    const int64_t q    = tid / G;
+    const int64_t node = inst[q];
+    const int gr       = (int)(tid - q * G);
+    const int gi       = B.node_graph[node];
+    const DevGraph& g  = B.graphs[gi];
+    const GraphRt& rt  = B.rt[gi];
+    if (!xb_returning(rt) || g.Ke != 0 || g.staged) {
+        return;
+    }
+    const TabG<MASK> tab{RecCtx(B, g, rt.snap_slot), reinterpret_cast<const float*>(B.aux)};
+    xf_return_item<MASK, UNI>(B, g, rt, tab, node, gr);
+}
+
+// One CTA per staged graph: the graph's departure snapshot (and, when AUXS, its
+// return-time rates) in shared memory, then its (node, group) items.
+template <int MASK, bool UNI, bool AUXS>
+__global__ void __launch_bounds__(kXsThreads, MGPU_XS_RETURN_MIN_BLOCKS) k_xs_return(BatchDev B)
+{
+    extern __shared__ float4 xs_smem[];
+    const int gi      = B.xs_graphs[blockIdx.x];
+    const DevGraph& g = B.graphs[gi];
+    const GraphRt& rt = B.rt[gi];
+    if (!xb_returning(rt)) {
+        return;
+    }
+    constexpr int NS = snap_nvec(MASK);
+    float4* sa       = xs_smem + g.N * g.G * NS;
+    stage_graph<MASK, AUXS>(B, g, rt.snap_slot, xs_smem, sa);
+    const TabS<MASK, AUXS> tab{RecCtx(B, g, rt.snap_slot), reinterpret_cast<const float*>(B.aux), xs_smem, sa,
+                               g.node0};
+    const int G     = g.G;
+    const int items = g.N * G;
+    for (int i = threadIdx.x; i < items; i += blockDim.x) {
+        const int v = i / G;
+        xf_return_item<MASK, UNI>(B, g, rt, tab, g.node0 + v, i - v * G);
+    }
 }
 
 // ---- exact underflow path ------------------------------------------------------
@@ -1914,6 +2148,62 @@ constexpr int kXbScanPasses = 4;
 
 // ev (profiling, may be null): recorded after the node pass, after the return
 // pass, and after the exact path with the commit.
+// The FP32 return (RET) or departure pass of a mixed batch: one launch over the
+// staged graphs (one CTA each) and one per age-group count over the nodes of
+// the other graphs, each instantiated for the batch's compartment mask and
+// coefficient form.
+template <int MASK, bool UNI, bool RET>
+void launch_xf_pass_m(const BatchDev& B, cudaStream_t s, int64_t* launches)
+{
+    if (B.xs_count > 0) {
+        if constexpr (RET) {
+            if (B.xs_aux) {
+                k_xs_return<MASK, UNI, true><<<(unsigned)B.xs_count, kXsThreads, B.xs_smem_ret, s>>>(B);
+            }
+            else {
+                k_xs_return<MASK, UNI, false><<<(unsigned)B.xs_count, kXsThreads, B.xs_smem_ret, s>>>(B);
+            }
+        }
+        else {
+            k_xs_depart<MASK, UNI><<<(unsigned)B.xs_count, kXsThreads, B.xs_smem_dep, s>>>(B);
+        }
+        *launches += 1;
+    }
+    const int T = 128;
+    for (int G = 1; G <= MGPU_MAX_GROUPS; ++G) {
+        if (B.xcount[G] > 0) {
+            const unsigned nb = blocks_of(B.xcount[G] * G, T);
+            if constexpr (RET) {
+                k_xf_return<MASK, UNI><<<nb, T, 0, s>>>(B, B.xlist[G], B.xcount[G], G);
+            }
+            else {
+                k_xf_depart<MASK, UNI><<<nb, T, 0, s>>>(B, B.xlist[G], B.xcount[G], G);
+            }
+            *launches += 1;
+        }
+    }
+}
+template <bool RET>
+void launch_xf_pass(const BatchDev& B, cudaStream_t s, int64_t* launches)
+{
+    if ((B.mob_union & ~kMaskSEIYR) == 0) {
+        if (B.ecoef_u) {
+            launch_xf_pass_m<kMaskSEIYR, true, RET>(B, s, launches);
+        }
+        else {
+            launch_xf_pass_m<kMaskSEIYR, false, RET>(B, s, launches);
+        }
+    }
+    else {
+        if (B.ecoef_u) {
+            launch_xf_pass_m<kMaskAll, true, RET>(B, s, launches);
+        }
+        else {
+            launch_xf_pass_m<kMaskAll, false, RET>(B, s, launches);
+        }
+    }
+}
+
 template <class R>
 void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStream_t s, int64_t* launches,
                cudaEvent_t* ev)
@@ -1942,28 +2232,7 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
     const int64_t ng  = nn * MGPU_MAX_GROUPS;
     const bool mixed  = std::is_same<R, float>::value;
     if (mixed) {
-        for (int G = 1; G <= MGPU_MAX_GROUPS; ++G) {
-            if (B.gcount[G] > 0) {
-                const unsigned nb = blocks_of(B.gcount[G] * G, T);
-                if ((B.mob_union & ~kMaskSEIYR) == 0) {
-                    if (B.ecoef_u) {
-                        k_xf_return<kMaskSEIYR, true><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
-                    }
-                    else {
-                        k_xf_return<kMaskSEIYR, false><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
-                    }
-                }
-                else {
-                    if (B.ecoef_u) {
-                        k_xf_return<kMaskAll, true><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
-                    }
-                    else {
-                        k_xf_return<kMaskAll, false><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
-                    }
-                }
-                *launches += 1;
-            }
-        }
+        launch_xf_pass<true>(B, s, launches);
     }
     if (!mixed || any_edge_dampings) {
         k_xb_return<R><<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
@@ -1997,28 +2266,7 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
         *launches += 1;
     }
     if (mixed) {
-        for (int G = 1; G <= MGPU_MAX_GROUPS; ++G) {
-            if (B.gcount[G] > 0) {
-                const unsigned nb = blocks_of(B.gcount[G] * G, T);
-                if ((B.mob_union & ~kMaskSEIYR) == 0) {
-                    if (B.ecoef_u) {
-                        k_xf_depart<kMaskSEIYR, true><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
-                    }
-                    else {
-                        k_xf_depart<kMaskSEIYR, false><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
-                    }
-                }
-                else {
-                    if (B.ecoef_u) {
-                        k_xf_depart<kMaskAll, true><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
-                    }
-                    else {
-                        k_xf_depart<kMaskAll, false><<<nb, T, 0, s>>>(B, B.glist[G], B.gcount[G], G);
-                    }
-                }
-                *launches += 1;
-            }
-        }
+        launch_xf_pass<false>(B, s, launches);
     }
     if (!mixed || any_edge_dampings) {
         k_xb_depart<R><<<blocks_of(ng, T), T, 0, s>>>(B, 0, nn);
@@ -2033,18 +2281,92 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
 
 } // namespace
 
-int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings, int group_lists, bool stats)
+int exchange_batched_launches(const BatchDev& B, int precision, bool any_edge_dampings)
 {
     const bool mixed = is_mixed(precision);
     const int prep   = mixed ? 0 : 1; // the node pass (inside the node kernel when mixed)
-    if (!has_edges) {
+    if (B.num_edges == 0) {
         return prep;
     }
     const int extra  = !any_edge_dampings ? 0 : (mixed ? 3 : 1);
     const int commit = (!mixed || any_edge_dampings) ? 1 : 0;
-    // return and departure passes (one per age-group count when mixed); the exact
-    // path: scan passes, done, sequential, cleanup
-    return prep + 3 + (mixed ? 2 * group_lists : 2) + kXbScanPasses + commit + extra + (stats ? 2 : 0);
+    // return and departure passes (when mixed: one over the staged graphs and
+    // one per age-group count of the other nodes); the exact path: scan passes,
+    // done, sequential, cleanup
+    int passes = 2;
+    if (mixed) {
+        passes = B.xs_count > 0 ? 2 : 0;
+        for (int G = 1; G <= MGPU_MAX_GROUPS; ++G) {
+            passes += B.xcount[G] > 0 ? 2 : 0;
+        }
+    }
+    return prep + 3 + passes + kXbScanPasses + commit + extra + (B.estats ? 2 : 0);
+}
+
+#ifndef MGPU_XS_MIN_ITEMS
+#define MGPU_XS_MIN_ITEMS 256 // smaller graphs stay in the node-list passes, which pack them densely
+#endif
+#ifndef MGPU_XS_AUX
+#define MGPU_XS_AUX 1 // the staged return also copies the return-time rates when they fit
+#endif
+
+namespace
+{
+template <int MASK, bool UNI>
+void set_xs_smem(int bytes, cudaError_t& err)
+{
+    const cudaError_t e[3] = {
+        cudaFuncSetAttribute(k_xs_depart<MASK, UNI>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
+        cudaFuncSetAttribute(k_xs_return<MASK, UNI, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
+        cudaFuncSetAttribute(k_xs_return<MASK, UNI, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)};
+    for (const cudaError_t x : e) {
+        err = err == cudaSuccess ? x : err;
+    }
+}
+} // namespace
+
+XsPlan plan_staged_exchange(std::vector<DevGraph>& dg, int mob_union, int device)
+{
+    XsPlan p;
+    const bool seiyr  = (mob_union & ~kMaskSEIYR) == 0;
+    const int64_t ns  = 16 * (seiyr ? snap_nvec(kMaskSEIYR) : snap_nvec(kMaskAll)); // bytes per (node, group)
+    const int64_t na  = 16 * (seiyr ? aux_nvec(kMaskSEIYR) : aux_nvec(kMaskAll));
+    int limit         = 0;
+    p.err             = cudaDeviceGetAttribute(&limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (p.err != cudaSuccess) {
+        limit = 0; // nothing staged
+    }
+    std::vector<std::pair<int64_t, int32_t>> by_size;
+    for (size_t i = 0; i < dg.size(); ++i) {
+        DevGraph& d         = dg[i];
+        const int64_t items = (int64_t)d.N * d.G;
+        d.staged            = d.E > 0 && d.Ke == 0 && items >= MGPU_XS_MIN_ITEMS && items * ns <= limit;
+        if (d.staged) {
+            by_size.push_back({items, (int32_t)i});
+        }
+    }
+    // largest graphs first: the CTAs that run longest start first
+    std::stable_sort(by_size.begin(), by_size.end(),
+                     [](const std::pair<int64_t, int32_t>& a, const std::pair<int64_t, int32_t>& b) {
+                         return a.first > b.first;
+                     });
+    int64_t max_items = 0;
+    for (const auto& it : by_size) {
+        p.graphs.push_back(it.second);
+        max_items = std::max(max_items, it.first);
+    }
+    p.aux      = MGPU_XS_AUX && max_items * (ns + na) <= limit;
+    p.smem_dep = (int32_t)(max_items * ns);
+    p.smem_ret = (int32_t)(max_items * (ns + (p.aux ? na : 0)));
+    if (!p.graphs.empty()) {
+        // the largest allowed size: the attribute is per kernel, and batches of
+        // different sizes share the kernels
+        set_xs_smem<kMaskSEIYR, true>(limit, p.err);
+        set_xs_smem<kMaskSEIYR, false>(limit, p.err);
+        set_xs_smem<kMaskAll, true>(limit, p.err);
+        set_xs_smem<kMaskAll, false>(limit, p.err);
+    }
+    return p;
 }
 
 void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "../../include/miogpu.h"
 
 namespace mgpu
@@ -40,6 +42,7 @@ struct DevGraph {
     int64_t edv_off;     // doubles, [E][Ke][n]
     int64_t ecoef_f_off; // [E][n] floats before the records: the edges' first row * 10 (Ke == 0, mixed)
     int32_t mob_mask;    // compartments c with a nonzero coefficient on some edge and age group
+    int32_t staged;      // the FP32 return and departure run one CTA per graph from shared memory
 };
 
 // Mutable per-graph state (GraphSimulation::m_t and the edges' shared return flag).
@@ -144,6 +147,17 @@ struct BatchDev {
     const float* ecoef_r;        // FP32 coefficient records of edges without dampings (mixed), see rec_vec
     const float* ecoef_u;        // the same as one value per (edge, group) row when every moved
                                  // compartment has the same coefficient everywhere (else null)
+    // graphs whose FP32 return and departure run one CTA per graph with the
+    // graph's snapshot records (and return-time rates) copied to shared memory,
+    // and the dynamic shared memory of those launches
+    const int32_t* xs_graphs;
+    // the node instances of the other graphs, per age-group count, for the
+    // FP32 passes over node lists
+    const int32_t* xlist[MGPU_MAX_GROUPS + 1];
+    int64_t xcount[MGPU_MAX_GROUPS + 1];
+    int32_t xs_count;
+    int32_t xs_smem_ret, xs_smem_dep;
+    int32_t xs_aux; // the staged return also copies the return-time rates
     const float* tab_f;          // [num_nodes][MAX_GROUPS][kTabF] FP32 node constants (mixed solver)
     const float* contact_f;      // FP32 copy of the contact pool
     const float* dvals_f;        // FP32 copy of the damping-value pool
@@ -584,8 +598,18 @@ int exchange_launches(bool has_edges);
 void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bool any_edge_dampings,
                              cudaStream_t s, int64_t* launches,
                              cudaEvent_t* ev = nullptr);
-int exchange_batched_launches(int precision, bool has_edges, bool any_edge_dampings, int group_lists,
-                              bool stats);
+int exchange_batched_launches(const BatchDev& B, int precision, bool any_edge_dampings);
+// Marks the graphs of a mixed batch whose FP32 return and departure run one CTA
+// per graph from shared memory (static coefficients, edges, enough (node, group)
+// items, tables within the device's shared memory per block), largest first;
+// gives the dynamic shared memory of the return and departure launches and
+// whether the return copies the rates. err: the first failed CUDA call.
+struct XsPlan {
+    std::vector<int32_t> graphs;
+    int32_t smem_ret = 0, smem_dep = 0, aux = 0;
+    cudaError_t err = cudaSuccess;
+};
+XsPlan plan_staged_exchange(std::vector<DevGraph>& dg, int mob_union, int device);
 
 // Device and stream of a context (for entry points defined outside capi.cu).
 int context_device_stream(const mgpu_context* ctx, int* device, cudaStream_t* stream);
