@@ -1084,8 +1084,8 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
                           : nullptr;
     }
     // the exchange passes: the staged graphs, and per G the nodes of the others
-    B.xs_count    = (int32_t)xs.graphs.size();
-    B.xs_graphs   = xs.graphs.empty() ? nullptr : b->pool.upload(xs.graphs);
+    B.xs_count    = (int32_t)xs.work.size();
+    B.xs_work     = xs.work.empty() ? nullptr : b->pool.upload(xs.work);
     B.xs_smem_ret = xs.smem_ret;
     B.xs_smem_dep = xs.smem_dep;
     B.xs_aux      = xs.aux;

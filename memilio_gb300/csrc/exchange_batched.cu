@@ -1115,9 +1115,21 @@ struct TabS {
     }
 };
 
+// 16-byte asynchronous copy global -> shared (L2 only), and the wait for all of
+// this thread's copies (the hardware wait of cp.async, no spin loop)
+__device__ __forceinline__ void cp_async16(float4* smem, const float4* gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 // Copies graph g's snapshot records of slot `slot` (and, when AUXS, its
-// return-time rates) to shared memory: coalesced float4 loads of the vectors
-// MASK needs, by the whole block.
+// return-time rates) to shared memory: the float4 vectors MASK needs, as
+// coalesced asynchronous copies by the whole block, all in flight at once.
 template <int MASK, bool AUXS>
 __device__ __forceinline__ void stage_graph(const BatchDev& B, const DevGraph& g, int slot, float4* ss, float4* sa)
 {
@@ -1140,7 +1152,7 @@ __device__ __forceinline__ void stage_graph(const BatchDev& B, const DevGraph& g
                 vec = q;
             }
         }
-        ss[u] = __ldg(gs + (int64_t)v * G * (kRec / 4) + vec * G + gr);
+        cp_async16(ss + u, gs + (int64_t)v * G * (kRec / 4) + vec * G + gr);
     }
     if constexpr (AUXS) {
         const float4* ga = reinterpret_cast<const float4*>(B.aux) + g.node0 * MGPU_MAX_GROUPS * (kAux / 4);
@@ -1157,15 +1169,16 @@ __device__ __forceinline__ void stage_graph(const BatchDev& B, const DevGraph& g
                     vec = q;
                 }
             }
-            sa[u] = __ldg(ga + ((int64_t)v * MGPU_MAX_GROUPS + gr) * (kAux / 4) + vec);
+            cp_async16(sa + u, ga + ((int64_t)v * MGPU_MAX_GROUPS + gr) * (kAux / 4) + vec);
         }
     }
+    cp_async_wait_all();
     __syncthreads();
 }
 
 // Departure of one (node, age group): the travelers of its out-edges leave, the
 // travelers of its in-edges arrive, summed in the serial order of the edges.
-template <int MASK, bool UNI, class Tab>
+template <int MASK, bool UNI, int UNR, class Tab>
 __device__ __forceinline__ void xf_depart_item(const BatchDev& B, const DevGraph& g, const GraphRt& rt,
                                                const Tab& tab, int64_t node, int gr)
 {
@@ -1202,11 +1215,11 @@ __device__ __forceinline__ void xf_depart_item(const BatchDev& B, const DevGraph
         }
     };
     const EdgeRanges r(B, node);
-#pragma unroll kXfUnroll
+#pragma unroll UNR
     for (int64_t k = r.k0; k < r.km; ++k) {
         arrive(k);
     }
-#pragma unroll kXfUnroll
+#pragma unroll UNR
     for (int64_t e = r.o0; e < r.o1; ++e) {
         float cf[kC], m[kC];
         ld_coef_m<MASK, UNI>(B, x, e, gr, cf);
@@ -1231,7 +1244,7 @@ __device__ __forceinline__ void xf_depart_item(const BatchDev& B, const DevGraph
             }
         }
     }
-#pragma unroll kXfUnroll
+#pragma unroll UNR
     for (int64_t k = r.km; k < r.k1; ++k) {
         arrive(k);
     }
@@ -1265,7 +1278,7 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_DEPART_MIN_BLO
         return;
     }
     const TabG<MASK> tab{RecCtx(B, g, rt.snap_slot ^ 1), reinterpret_cast<const float*>(B.aux)};
-    xf_depart_item<MASK, UNI>(B, g, rt, tab, node, gr);
+    xf_depart_item<MASK, UNI, kXfUnroll>(B, g, rt, tab, node, gr);
 }
 
 #ifndef MGPU_XS_THREADS
@@ -1277,28 +1290,50 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_DEPART_MIN_BLO
 #ifndef MGPU_XS_RETURN_MIN_BLOCKS
 #define MGPU_XS_RETURN_MIN_BLOCKS 1
 #endif
+#ifndef MGPU_XS_UNROLL
+#define MGPU_XS_UNROLL 4 // edges per iteration of the per-graph passes' edge loops
+#endif
 constexpr int kXsThreads = MGPU_XS_THREADS;
 
-// One CTA per staged graph (B.xs_graphs): the departure snapshot of the graph
-// in shared memory, then the graph's (node, group) items in the dense order.
+// The (node, group) items [i0, i1) of the work item's chunk of its graph: a
+// graph of I items split into n chunks has chunks of R items, R = I / n rounded
+// up to whole rounds of the block's threads, so that only its last chunk
+// leaves threads idle in its last round.
+struct XsChunk {
+    int gi, i0, i1;
+    __device__ XsChunk(const BatchDev& B, const DevGraph* graphs)
+    {
+        const int2 w = B.xs_work[blockIdx.x];
+        gi           = w.x;
+        const int k  = w.y >> 16;
+        const int n  = w.y & 0xffff;
+        const int I  = graphs[gi].N * graphs[gi].G;
+        const int T  = (int)blockDim.x;
+        const int R  = ((I + n - 1) / n + T - 1) / T * T;
+        i0           = min(k * R, I);
+        i1           = min(i0 + R, I);
+    }
+};
+
+// One CTA per chunk of a staged graph (B.xs_work): the departure snapshot of
+// the whole graph in shared memory, then the chunk's (node, group) items.
 template <int MASK, bool UNI>
 __global__ void __launch_bounds__(kXsThreads, MGPU_XS_DEPART_MIN_BLOCKS) k_xs_depart(BatchDev B)
 {
     extern __shared__ float4 xs_smem[];
-    const int gi      = B.xs_graphs[blockIdx.x];
-    const DevGraph& g = B.graphs[gi];
-    const GraphRt& rt = B.rt[gi];
+    const XsChunk c(B, B.graphs);
+    const DevGraph& g = B.graphs[c.gi];
+    const GraphRt& rt = B.rt[c.gi];
     if (!xb_departing(rt)) {
         return;
     }
     const int ws = rt.snap_slot ^ 1;
     stage_graph<MASK, false>(B, g, ws, xs_smem, nullptr);
     const TabS<MASK, false> tab{RecCtx(B, g, ws), reinterpret_cast<const float*>(B.aux), xs_smem, nullptr, g.node0};
-    const int G     = g.G;
-    const int items = g.N * G;
-    for (int i = threadIdx.x; i < items; i += blockDim.x) {
+    const int G = g.G;
+    for (int i = c.i0 + threadIdx.x; i < c.i1; i += blockDim.x) {
         const int v = i / G;
-        xf_depart_item<MASK, UNI>(B, g, rt, tab, g.node0 + v, i - v * G);
+        xf_depart_item<MASK, UNI, MGPU_XS_UNROLL>(B, g, rt, tab, g.node0 + v, i - v * G);
     }
 }
 
@@ -1306,7 +1341,7 @@ __global__ void __launch_bounds__(kXsThreads, MGPU_XS_DEPART_MIN_BLOCKS) k_xs_de
 // travelers of its out-edges come home, each with its Euler flows; the state
 // is updated in place, the state before it kept for the exact path, and the
 // item queued for that path when the no-underflow bound fails.
-template <int MASK, bool UNI, class Tab>
+template <int MASK, bool UNI, int UNR, class Tab>
 __device__ __forceinline__ void xf_return_item(const BatchDev& B, const DevGraph& g, const GraphRt& rt,
                                                const Tab& tab, int64_t node, int gr)
 {
@@ -1389,7 +1424,7 @@ __device__ __forceinline__ void xf_return_item(const BatchDev& B, const DevGraph
         apply(a_own, m, -1.0f);
     };
     const EdgeRanges r(B, node);
-#pragma unroll kXfUnroll
+#pragma unroll UNR
     for (int64_t k = r.k0; k < r.km; ++k) {
         leave(k);
     }
@@ -1397,14 +1432,14 @@ __device__ __forceinline__ void xf_return_item(const BatchDev& B, const DevGraph
     for (int c = 0; c < kC; ++c) {
         flag = flag || run[c] < 1e-5f * mag[c];
     }
-#pragma unroll kXfUnroll
+#pragma unroll UNR
     for (int64_t e = r.o0; e < r.o1; ++e) {
         float ax[kAux], m[kC];
         tab.rates(B.edge_dst[e], gr, ax);
         travelers_f<MASK, UNI>(B, x, e, gr, own, m);
         apply(ax, m, 1.0f);
     }
-#pragma unroll kXfUnroll
+#pragma unroll UNR
     for (int64_t k = r.km; k < r.k1; ++k) {
         leave(k);
     }
@@ -1449,18 +1484,19 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_RETURN_MIN_BLO
         return;
     }
     const TabG<MASK> tab{RecCtx(B, g, rt.snap_slot), reinterpret_cast<const float*>(B.aux)};
-    xf_return_item<MASK, UNI>(B, g, rt, tab, node, gr);
+    xf_return_item<MASK, UNI, kXfUnroll>(B, g, rt, tab, node, gr);
 }
 
-// One CTA per staged graph: the graph's departure snapshot (and, when AUXS, its
-// return-time rates) in shared memory, then its (node, group) items.
+// One CTA per chunk of a staged graph: the whole graph's departure snapshot
+// (and, when AUXS, its return-time rates) in shared memory, then the chunk's
+// (node, group) items.
 template <int MASK, bool UNI, bool AUXS>
 __global__ void __launch_bounds__(kXsThreads, MGPU_XS_RETURN_MIN_BLOCKS) k_xs_return(BatchDev B)
 {
     extern __shared__ float4 xs_smem[];
-    const int gi      = B.xs_graphs[blockIdx.x];
-    const DevGraph& g = B.graphs[gi];
-    const GraphRt& rt = B.rt[gi];
+    const XsChunk c(B, B.graphs);
+    const DevGraph& g = B.graphs[c.gi];
+    const GraphRt& rt = B.rt[c.gi];
     if (!xb_returning(rt)) {
         return;
     }
@@ -1469,11 +1505,10 @@ __global__ void __launch_bounds__(kXsThreads, MGPU_XS_RETURN_MIN_BLOCKS) k_xs_re
     stage_graph<MASK, AUXS>(B, g, rt.snap_slot, xs_smem, sa);
     const TabS<MASK, AUXS> tab{RecCtx(B, g, rt.snap_slot), reinterpret_cast<const float*>(B.aux), xs_smem, sa,
                                g.node0};
-    const int G     = g.G;
-    const int items = g.N * G;
-    for (int i = threadIdx.x; i < items; i += blockDim.x) {
+    const int G = g.G;
+    for (int i = c.i0 + threadIdx.x; i < c.i1; i += blockDim.x) {
         const int v = i / G;
-        xf_return_item<MASK, UNI>(B, g, rt, tab, g.node0 + v, i - v * G);
+        xf_return_item<MASK, UNI, MGPU_XS_UNROLL>(B, g, rt, tab, g.node0 + v, i - v * G);
     }
 }
 
@@ -2309,6 +2344,9 @@ int exchange_batched_launches(const BatchDev& B, int precision, bool any_edge_da
 #ifndef MGPU_XS_AUX
 #define MGPU_XS_AUX 1 // the staged return also copies the return-time rates when they fit
 #endif
+#ifndef MGPU_XS_CHUNK
+#define MGPU_XS_CHUNK 2560 // (node, group) items per CTA of the per-graph passes, at most
+#endif
 
 namespace
 {
@@ -2331,16 +2369,27 @@ XsPlan plan_staged_exchange(std::vector<DevGraph>& dg, int mob_union, int device
     const bool seiyr  = (mob_union & ~kMaskSEIYR) == 0;
     const int64_t ns  = 16 * (seiyr ? snap_nvec(kMaskSEIYR) : snap_nvec(kMaskAll)); // bytes per (node, group)
     const int64_t na  = 16 * (seiyr ? aux_nvec(kMaskSEIYR) : aux_nvec(kMaskAll));
-    int limit         = 0;
-    p.err             = cudaDeviceGetAttribute(&limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
-    if (p.err != cudaSuccess) {
-        limit = 0; // nothing staged
+    int limit = 0, per_sm = 0, reserved = 0;
+    p.err = cudaDeviceGetAttribute(&limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (p.err == cudaSuccess) {
+        p.err = cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
     }
+    if (p.err == cudaSuccess) {
+        p.err = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, device);
+    }
+    if (p.err != cudaSuccess) {
+        limit = per_sm = 0; // nothing staged
+    }
+    // a staged graph's snapshot leaves room for two departure CTAs per SM: one
+    // larger graph would raise every CTA's shared memory and halve the
+    // departure's residency (measured: a batch with graphs up to the per-block
+    // limit lost more on the departure than staging gained)
+    const int64_t cap = std::min<int64_t>(limit, per_sm / 2 - reserved);
     std::vector<std::pair<int64_t, int32_t>> by_size;
     for (size_t i = 0; i < dg.size(); ++i) {
         DevGraph& d         = dg[i];
         const int64_t items = (int64_t)d.N * d.G;
-        d.staged            = d.E > 0 && d.Ke == 0 && items >= MGPU_XS_MIN_ITEMS && items * ns <= limit;
+        d.staged            = d.E > 0 && d.Ke == 0 && items >= MGPU_XS_MIN_ITEMS && items * ns <= cap;
         if (d.staged) {
             by_size.push_back({items, (int32_t)i});
         }
@@ -2350,15 +2399,20 @@ XsPlan plan_staged_exchange(std::vector<DevGraph>& dg, int mob_union, int device
                      [](const std::pair<int64_t, int32_t>& a, const std::pair<int64_t, int32_t>& b) {
                          return a.first > b.first;
                      });
+    // each graph in near-equal chunks of at most MGPU_XS_CHUNK items, one CTA
+    // each, so that a few large graphs do not leave the last wave of CTAs short
     int64_t max_items = 0;
     for (const auto& it : by_size) {
-        p.graphs.push_back(it.second);
+        const int n = (int)std::min<int64_t>((it.first + MGPU_XS_CHUNK - 1) / MGPU_XS_CHUNK, 0xffff);
+        for (int k = 0; k < n; ++k) {
+            p.work.push_back(make_int2(it.second, (k << 16) | n));
+        }
         max_items = std::max(max_items, it.first);
     }
     p.aux      = MGPU_XS_AUX && max_items * (ns + na) <= limit;
     p.smem_dep = (int32_t)(max_items * ns);
     p.smem_ret = (int32_t)(max_items * (ns + (p.aux ? na : 0)));
-    if (!p.graphs.empty()) {
+    if (!p.work.empty()) {
         // the largest allowed size: the attribute is per kernel, and batches of
         // different sizes share the kernels
         set_xs_smem<kMaskSEIYR, true>(limit, p.err);

@@ -147,10 +147,11 @@ struct BatchDev {
     const float* ecoef_r;        // FP32 coefficient records of edges without dampings (mixed), see rec_vec
     const float* ecoef_u;        // the same as one value per (edge, group) row when every moved
                                  // compartment has the same coefficient everywhere (else null)
-    // graphs whose FP32 return and departure run one CTA per graph with the
-    // graph's snapshot records (and return-time rates) copied to shared memory,
-    // and the dynamic shared memory of those launches
-    const int32_t* xs_graphs;
+    // chunks of the graphs whose FP32 return and departure run with the graph's
+    // snapshot records (and return-time rates) copied to shared memory, one CTA
+    // per chunk: (graph, chunk << 16 | chunks of the graph); their count and
+    // the dynamic shared memory of those launches
+    const int2* xs_work;
     // the node instances of the other graphs, per age-group count, for the
     // FP32 passes over node lists
     const int32_t* xlist[MGPU_MAX_GROUPS + 1];
@@ -599,13 +600,14 @@ void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bo
                              cudaStream_t s, int64_t* launches,
                              cudaEvent_t* ev = nullptr);
 int exchange_batched_launches(const BatchDev& B, int precision, bool any_edge_dampings);
-// Marks the graphs of a mixed batch whose FP32 return and departure run one CTA
-// per graph from shared memory (static coefficients, edges, enough (node, group)
-// items, tables within the device's shared memory per block), largest first;
-// gives the dynamic shared memory of the return and departure launches and
-// whether the return copies the rates. err: the first failed CUDA call.
+// Marks the graphs of a mixed batch whose FP32 return and departure run from
+// shared memory (static coefficients, edges, enough (node, group) items, tables
+// within the device's shared memory per block) and lists their chunks, one CTA
+// each, largest graphs first; gives the dynamic shared memory of the return and
+// departure launches and whether the return copies the rates. err: the first
+// failed CUDA call.
 struct XsPlan {
-    std::vector<int32_t> graphs;
+    std::vector<int2> work;
     int32_t smem_ret = 0, smem_dep = 0, aux = 0;
     cudaError_t err = cudaSuccess;
 };
