@@ -1794,9 +1794,9 @@ __device__ __forceinline__ int fix_group_ff(const FF (&y)[kC], FF (&t)[kC])
 }
 
 // One warp per item: the lanes compute the returning travelers of 32 incident
-// edges at a time in parallel (the gathers), then replay the serial order over
-// them together: every lane holds the same running state, the travelers of
-// edge j come from lane j by shuffles, and lane j publishes edge j's fix.
+// edges at a time in parallel (the gathers), then follow the serial order with
+// prefix sums over the lanes, stopping only at the edges that need the fix:
+// every lane holds the same running state, and lane j publishes edge j's fix.
 __global__ void k_xf_scan(BatchDev B, int pass)
 {
     constexpr unsigned kFull = 0xffffffffu;
@@ -1894,55 +1894,103 @@ __global__ void k_xf_scan(BatchDev B, int pass)
                 }
             }
             const int nchunk = deg - base < 32 ? deg - base : 32;
-            for (int j = 0; j < nchunk; ++j) {
-                const int kj = __shfl_sync(kFull, kind, j);
+            // publication of this lane's in-edge after the serial step decided
+            // it: the fixed travelers and fix count (nfix > 0) or the reset of
+            // an earlier fix; a change sends the source's item to a rescan
+            auto publish = [&](int nfix, const FF (&tf)[kC]) {
+                uint8_t* fc  = B.fix_cnt + e * MGPU_MAX_GROUPS + gr;
+                float2* mf   = reinterpret_cast<float2*>(B.mfix + B.trav_off[e] + gr * kC);
+                bool changed = false;
+                if (nfix) {
+                    changed = prev == 0;
+                    if (prev == 0) {
+                        fix_edge_push(B, e);
+                    }
+#pragma unroll
+                    for (int c = 0; c < kC; ++c) {
+                        const float2 old = __ldcg(mf + c);
+                        changed          = changed || old.x != tf[c].h || old.y != tf[c].l;
+                        __stcg(mf + c, make_float2(tf[c].h, tf[c].l));
+                    }
+                    __threadfence();
+                    *(volatile uint8_t*)fc = (uint8_t)nfix;
+                }
+                else if (prev) {
+                    *(volatile uint8_t*)fc = 0;
+                    changed                = true;
+                }
+                if (changed) {
+                    list_push(B, lout, u * MGPU_MAX_GROUPS + gr);
+                }
+            };
+            // The serial order in parallel: the running state after edge k is
+            // y + P_k, P the inclusive prefix sum of the signed travelers (out-edges
+            // add theirs, in-edges take theirs away) over the lanes not yet
+            // applied; an in-edge needs the underflow fix when y + P_k has a
+            // negative compartment. The first such edge j is fixed against the
+            // exact running state (y advanced to just before it), as in the serial
+            // loop, and the scan restarts after it with the fixed travelers applied.
+            int start = 0;
+            while (start < nchunk) {
+                FF p[kC];
+                const bool live = lane >= start && lane < nchunk && kind != 0;
+#pragma unroll
+                for (int c = 0; c < kC; ++c) {
+                    p[c] = !live ? FF{0.0f, 0.0f} : (kind == 2 ? t[c] : ff_neg(t[c]));
+                }
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+#pragma unroll
+                    for (int c = 0; c < kC; ++c) {
+                        FF q;
+                        q.h = __shfl_up_sync(kFull, p[c].h, d);
+                        q.l = __shfl_up_sync(kFull, p[c].l, d);
+                        if (lane >= d) {
+                            p[c] = ff_add(q, p[c]);
+                        }
+                    }
+                }
+                bool need = false;
+                if (live && kind == 1) {
+#pragma unroll
+                    for (int c = 0; c < kC; ++c) {
+                        need = need || ff_neg_p(ff_add(y[c], p[c]));
+                    }
+                }
+                const unsigned m = __ballot_sync(kFull, need);
+                const int j      = m ? __ffs(m) - 1 : nchunk;
+                // in-edges before j keep their travelers: only an earlier fix is reset
+                if (live && kind == 1 && lane < j && prev != 0) {
+                    const FF none[kC] = {};
+                    publish(0, none);
+                }
+                if (j > start) {
+#pragma unroll
+                    for (int c = 0; c < kC; ++c) {
+                        FF q;
+                        q.h  = __shfl_sync(kFull, p[c].h, j - 1);
+                        q.l  = __shfl_sync(kFull, p[c].l, j - 1);
+                        y[c] = ff_add(y[c], q);
+                    }
+                }
+                if (j >= nchunk) {
+                    break;
+                }
                 FF tj[kC];
 #pragma unroll
                 for (int c = 0; c < kC; ++c) {
                     tj[c].h = __shfl_sync(kFull, t[c].h, j);
                     tj[c].l = __shfl_sync(kFull, t[c].l, j);
                 }
-                if (kj == 0) {
-                    continue;
-                }
-                if (kj == 2) {
-#pragma unroll
-                    for (int c = 0; c < kC; ++c) {
-                        y[c] = ff_add(y[c], tj[c]);
-                    }
-                    continue;
-                }
                 const int nfix = fix_group_ff(y, tj);
                 if (lane == j) {
-                    uint8_t* fc  = B.fix_cnt + e * MGPU_MAX_GROUPS + gr;
-                    float2* mf   = reinterpret_cast<float2*>(B.mfix + B.trav_off[e] + gr * kC);
-                    bool changed = false;
-                    if (nfix) {
-                        changed = prev == 0;
-                        if (prev == 0) {
-                            fix_edge_push(B, e);
-                        }
-#pragma unroll
-                        for (int c = 0; c < kC; ++c) {
-                            const float2 old = __ldcg(mf + c);
-                            changed          = changed || old.x != tj[c].h || old.y != tj[c].l;
-                            __stcg(mf + c, make_float2(tj[c].h, tj[c].l));
-                        }
-                        __threadfence();
-                        *(volatile uint8_t*)fc = (uint8_t)nfix;
-                    }
-                    else if (prev) {
-                        *(volatile uint8_t*)fc = 0;
-                        changed                = true;
-                    }
-                    if (changed) {
-                        list_push(B, lout, u * MGPU_MAX_GROUPS + gr);
-                    }
+                    publish(nfix, tj);
                 }
 #pragma unroll
                 for (int c = 0; c < kC; ++c) {
                     y[c] = ff_add(y[c], ff_neg(tj[c]));
                 }
+                start = j + 1;
             }
         }
         if (lane == 0) {
