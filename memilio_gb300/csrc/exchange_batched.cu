@@ -1349,8 +1349,7 @@ __device__ __forceinline__ void xf_return_item(const BatchDev& B, const DevGraph
     const int64_t lv = node - g.node0;
     const int64_t s0 = g.state_off + lv * g.n + gr * kC;
     Acc<float> acc[kC];
-    // lower bound of the running state along the serial order, and its magnitude
-    float run[kC], mag[kC], phi_net[kF];
+    float y0[kC];
     {
         // the return is applied in place; the state before it goes to yn for the
         // exact path (rescans and the sequential fallback start from it)
@@ -1362,94 +1361,164 @@ __device__ __forceinline__ void xf_return_item(const BatchDev& B, const DevGraph
 #pragma unroll
         for (int c = 0; c < kC; ++c) {
             acc[c].init_pair(h[c], l[c]);
-            run[c] = h[c];
-            mag[c] = fabsf(h[c]);
+            y0[c] = h[c];
         }
-    }
-#pragma unroll
-    for (int f = 0; f < kF; ++f) {
-        phi_net[f] = 0.0f;
     }
     float a_own[kAux];
     tab.rates(node, gr, a_own);
     const RecCtx& x = tab.x;
     GroupSnap own;
     tab.snap(node, gr, own);
-    // run[c] is a lower bound of the exact running state of the serial order:
-    // in-edges take max(t, 0) away, out-edges add t (negative amounts included),
-    // so within each run of in-edges it only decreases, and the underflow test of
-    // the reference (rem = running - t < 0 at in-edges) can only fail if run
-    // drops below zero at the end of a run of in-edges. Those two points are
-    // checked with a margin of 1e-5 of the magnitudes, above the FP32 rounding of
-    // the running sums.
-    bool flag = false;
-    // one returning edge: travelers m, their Euler flows phi at the destination's
-    // rates a; sgn = -1 for in-edges (travelers leave), +1 for out-edges
-    // (an edge without travelers has zero coefficients and adds exact zeros)
-    auto apply = [&](const float (&a)[kAux], const float (&m)[kC], float sgn) {
-        float phi[kF];
-        flows_f<MASK>(a, dt, m, phi);
-        // returning amounts t_c = m_c + inflows - outflows (for the bound only)
-        float t[kC];
+    // Sums of the travelers of the in-edges (all of them, and of the lower run)
+    // and of the out-edges, the out-edges' Euler flows at their destinations'
+    // rates, and the sum of the in-edge travelers' negative parts (for the bound).
+    float m_in[kC], m_out[kC], phi_out[kF];
 #pragma unroll
-        for (int c = 0; c < kC; ++c) {
-            if (in_mask(MASK, c)) {
-                acc[c].add(sgn * m[c]);
-            }
-            t[c] = m[c];
-        }
+    for (int c = 0; c < kC; ++c) {
+        m_in[c] = m_out[c] = 0.0f;
+    }
 #pragma unroll
-        for (int f = 0; f < kF; ++f) {
-            if (in_mask(MASK, kFlowSrcI(f))) {
-                phi_net[f] += sgn * phi[f];
-                t[kFlowSrcI(f)] -= phi[f];
-                t[kFlowDstI(f)] += phi[f];
-            }
-        }
-#pragma unroll
-        for (int c = 0; c < kC; ++c) {
-            // in-edges take max(t, 0) away; out-edges bring t home (a negative t counts against)
-            if (in_mask(touched_mask(MASK), c)) {
-                run[c] += sgn < 0.0f ? -fmaxf(t[c], 0.0f) : t[c];
-                mag[c] += fabsf(t[c]);
-            }
-        }
-    };
+    for (int f = 0; f < kF; ++f) {
+        phi_out[f] = 0.0f;
+    }
+    float neg_in = 0.0f;
+    // in-edge k: its travelers leave this node (an edge without travelers has
+    // zero coefficients and adds exact zeros)
     auto leave = [&](int64_t k) {
         GroupSnap src;
         float m[kC];
         const int2 se = B.in_se[k];
         tab.snap(se.x, gr, src);
         travelers_f<MASK, UNI>(B, x, se.y, gr, src, m);
-        apply(a_own, m, -1.0f);
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            if (in_mask(MASK, c)) {
+                acc[c].add(-m[c]);
+                m_in[c] += m[c];
+                neg_in += fminf(m[c], 0.0f);
+            }
+        }
     };
     const EdgeRanges r(B, node);
 #pragma unroll UNR
     for (int64_t k = r.k0; k < r.km; ++k) {
         leave(k);
     }
+    float m_low[kC];
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
-        flag = flag || run[c] < 1e-5f * mag[c];
+        m_low[c] = m_in[c];
     }
+    const float neg_low = neg_in;
+    // out-edge e: this node's travelers come home with their Euler flows at the
+    // destination's rates
 #pragma unroll UNR
     for (int64_t e = r.o0; e < r.o1; ++e) {
-        float ax[kAux], m[kC];
+        float ax[kAux], m[kC], phi[kF];
         tab.rates(B.edge_dst[e], gr, ax);
         travelers_f<MASK, UNI>(B, x, e, gr, own, m);
-        apply(ax, m, 1.0f);
+        flows_f<MASK>(ax, dt, m, phi);
+#pragma unroll
+        for (int c = 0; c < kC; ++c) {
+            if (in_mask(MASK, c)) {
+                acc[c].add(m[c]);
+                m_out[c] += m[c];
+            }
+        }
+#pragma unroll
+        for (int f = 0; f < kF; ++f) {
+            if (in_mask(MASK, kFlowSrcI(f))) {
+                phi_out[f] += phi[f];
+            }
+        }
     }
 #pragma unroll UNR
     for (int64_t k = r.km; k < r.k1; ++k) {
         leave(k);
     }
-    // flow increments: in-edges take travelers away (their increments count with
-    // the opposite sign), out-edges bring them home
+    // The in-edges' travelers all take this node's own rates, so their Euler
+    // flows are those of their sum. Flow increments: in-edges take their
+    // travelers' increments away, out-edges bring theirs home.
+    float phi_in[kF], phi_low[kF];
+    flows_f<MASK>(a_own, dt, m_in, phi_in);
+    flows_f<MASK>(a_own, dt, m_low, phi_low);
 #pragma unroll
     for (int f = 0; f < kF; ++f) {
         if (in_mask(MASK, kFlowSrcI(f))) {
-            acc[kFlowSrcI(f)].add(-phi_net[f]);
-            acc[kFlowDstI(f)].add(phi_net[f]);
+            const float net = phi_out[f] - phi_in[f];
+            acc[kFlowSrcI(f)].add(-net);
+            acc[kFlowDstI(f)].add(net);
+        }
+    }
+    // The no-underflow bound. In the reference's serial order (lower in-edges,
+    // out-edges, higher in-edges) an in-edge's returning amount
+    // t = m + inflows - outflows is taken away and fails when the running state
+    // minus t has a negative compartment. At this node's own rates t is linear in
+    // the edge's travelers: t_c = d_c m_c + sum over flows f into c of dt a_f m_src(f),
+    // d_c = 1 - dt (total outflow rate of c). Per compartment:
+    //  * d_c >= 0: every coefficient is >= 0, so t_c >= 0 up to K_c times the
+    //    negative parts of the travelers (states slightly below zero),
+    //    K_c = |d_c| + the inflow coefficients; the running state only decreases
+    //    within a run of in-edges and is smallest at the run's end, where it is
+    //    y0 - T(lower) after the lower run and y0 - T(all in) + T(out) after the
+    //    higher one, T the summed returning amounts (from the traveler and flow sums);
+    //  * d_c < 0 and no inflow into c: t_c <= 0 up to the same correction, so the
+    //    in-edges take nothing from c (the serial loop's max(t, 0));
+    //  * d_c < 0 with inflows: signs can differ between edges; the item takes the
+    //    exact path.
+    // The ends are checked less the correction and with a margin of 1e-5 of y0
+    // plus the summed magnitudes (above the FP32 rounding of the sums).
+    bool flag = false;
+    float t_low[kC], t_in[kC], t_out[kC], mag[kC];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        t_low[c] = m_low[c];
+        t_in[c]  = m_in[c];
+        t_out[c] = m_out[c];
+        mag[c]   = fabsf(y0[c]) + m_in[c] + m_out[c];
+    }
+#pragma unroll
+    for (int f = 0; f < kF; ++f) {
+        if (in_mask(MASK, kFlowSrcI(f))) {
+            t_low[kFlowSrcI(f)] -= phi_low[f];
+            t_low[kFlowDstI(f)] += phi_low[f];
+            t_in[kFlowSrcI(f)] -= phi_in[f];
+            t_in[kFlowDstI(f)] += phi_in[f];
+            t_out[kFlowSrcI(f)] -= phi_out[f];
+            t_out[kFlowDstI(f)] += phi_out[f];
+            mag[kFlowSrcI(f)] += phi_in[f] + phi_out[f];
+            mag[kFlowDstI(f)] += phi_in[f] + phi_out[f];
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        if (in_mask(touched_mask(MASK), c)) {
+            float rate = 0.0f, inflow = 0.0f;
+            bool has_inflow = false;
+#pragma unroll
+            for (int f = 0; f < kF; ++f) {
+                if (in_mask(MASK, kFlowSrcI(f))) {
+                    if (kFlowSrcI(f) == c) {
+                        rate += a_own[aux_of_flow(f)];
+                    }
+                    if (kFlowDstI(f) == c) {
+                        inflow += dt * a_own[aux_of_flow(f)];
+                        has_inflow = true;
+                    }
+                }
+            }
+            const float d = 1.0f - dt * rate;
+            if (d < 0.0f) {
+                if (has_inflow) {
+                    flag = true;
+                }
+                t_low[c] = 0.0f;
+                t_in[c]  = 0.0f;
+            }
+            const float k      = fabsf(d) + inflow;
+            const float margin = 1e-5f * mag[c];
+            flag = flag || (y0[c] - t_low[c]) + k * neg_low < margin ||
+                   ((y0[c] - t_in[c]) + t_out[c]) + k * neg_in < margin;
         }
     }
     const int64_t so = g.state_off + lv * g.n + gr * kC;
@@ -1457,7 +1526,6 @@ __device__ __forceinline__ void xf_return_item(const BatchDev& B, const DevGraph
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
         acc[c].store(&h[c], &l[c]);
-        flag = flag || run[c] < 1e-5f * mag[c];
     }
     st_state(B.st_hi + so, h);
     st_state(B.st_lo + so, l);
