@@ -1176,12 +1176,359 @@ __device__ __forceinline__ void stage_graph(const BatchDev& B, const DevGraph& g
     __syncthreads();
 }
 
+// The end of an item's return: the in-edges' Euler flows from their sum, the
+// flow increments of both directions, the no-underflow bound, the store and the
+// exact path's work list.
+template <int MASK>
+__device__ __forceinline__ void xf_return_finish(const BatchDev& B, const DevGraph& g, int64_t node, int gr,
+                                                 float dt, const float (&y0)[kC], const float (&a_own)[kAux],
+                                                 Acc<float> (&acc)[kC], const float (&m_in)[kC],
+                                                 const float (&m_low)[kC], const float (&m_out)[kC],
+                                                 const float (&phi_out)[kF], float neg_in, float neg_low)
+{
+    // The in-edges' travelers all take this node's own rates, so their Euler
+    // flows are those of their sum. Flow increments: in-edges take their
+    // travelers' increments away, out-edges bring theirs home.
+    float phi_in[kF], phi_low[kF];
+    flows_f<MASK>(a_own, dt, m_in, phi_in);
+    flows_f<MASK>(a_own, dt, m_low, phi_low);
+#pragma unroll
+    for (int f = 0; f < kF; ++f) {
+        if (in_mask(MASK, kFlowSrcI(f))) {
+            const float net = phi_out[f] - phi_in[f];
+            acc[kFlowSrcI(f)].add(-net);
+            acc[kFlowDstI(f)].add(net);
+        }
+    }
+    // The no-underflow bound. In the reference's serial order (lower in-edges,
+    // out-edges, higher in-edges) an in-edge's returning amount
+    // t = m + inflows - outflows is taken away and fails when the running state
+    // minus t has a negative compartment. At this node's own rates t is linear in
+    // the edge's travelers: t_c = d_c m_c + sum over flows f into c of dt a_f m_src(f),
+    // d_c = 1 - dt (total outflow rate of c). Per compartment:
+    //  * d_c >= 0: every coefficient is >= 0, so t_c >= 0 up to K_c times the
+    //    negative parts of the travelers (states slightly below zero),
+    //    K_c = |d_c| + the inflow coefficients; the running state only decreases
+    //    within a run of in-edges and is smallest at the run's end, where it is
+    //    y0 - T(lower) after the lower run and y0 - T(all in) + T(out) after the
+    //    higher one, T the summed returning amounts (from the traveler and flow sums);
+    //  * d_c < 0 and no inflow into c: t_c <= 0 up to the same correction, so the
+    //    in-edges take nothing from c (the serial loop's max(t, 0));
+    //  * d_c < 0 with inflows: signs can differ between edges; the item takes the
+    //    exact path.
+    // The ends are checked less the correction and with a margin of 1e-5 of y0
+    // plus the summed magnitudes (above the FP32 rounding of the sums).
+    bool flag = false;
+    float t_low[kC], t_in[kC], t_out[kC], mag[kC];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        t_low[c] = m_low[c];
+        t_in[c]  = m_in[c];
+        t_out[c] = m_out[c];
+        mag[c]   = fabsf(y0[c]) + m_in[c] + m_out[c];
+    }
+#pragma unroll
+    for (int f = 0; f < kF; ++f) {
+        if (in_mask(MASK, kFlowSrcI(f))) {
+            t_low[kFlowSrcI(f)] -= phi_low[f];
+            t_low[kFlowDstI(f)] += phi_low[f];
+            t_in[kFlowSrcI(f)] -= phi_in[f];
+            t_in[kFlowDstI(f)] += phi_in[f];
+            t_out[kFlowSrcI(f)] -= phi_out[f];
+            t_out[kFlowDstI(f)] += phi_out[f];
+            mag[kFlowSrcI(f)] += phi_in[f] + phi_out[f];
+            mag[kFlowDstI(f)] += phi_in[f] + phi_out[f];
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        if (in_mask(touched_mask(MASK), c)) {
+            float rate = 0.0f, inflow = 0.0f;
+            bool has_inflow = false;
+#pragma unroll
+            for (int f = 0; f < kF; ++f) {
+                if (in_mask(MASK, kFlowSrcI(f))) {
+                    if (kFlowSrcI(f) == c) {
+                        rate += a_own[aux_of_flow(f)];
+                    }
+                    if (kFlowDstI(f) == c) {
+                        inflow += dt * a_own[aux_of_flow(f)];
+                        has_inflow = true;
+                    }
+                }
+            }
+            const float d = 1.0f - dt * rate;
+            if (d < 0.0f) {
+                if (has_inflow) {
+                    flag = true;
+                }
+                t_low[c] = 0.0f;
+                t_in[c]  = 0.0f;
+            }
+            const float k      = fabsf(d) + inflow;
+            const float margin = 1e-5f * mag[c];
+            flag = flag || (y0[c] - t_low[c]) + k * neg_low < margin ||
+                   ((y0[c] - t_in[c]) + t_out[c]) + k * neg_in < margin;
+        }
+    }
+    const int64_t so = g.state_off + (node - g.node0) * g.n + gr * kC;
+    float h[kC], l[kC];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        acc[c].store(&h[c], &l[c]);
+    }
+    st_state(B.st_hi + so, h);
+    st_state(B.st_lo + so, l);
+    list0_push(B, node * MGPU_MAX_GROUPS + gr, flag);
+}
+
+// Packed forms for the commuter compartments S, E, INS, ISy, R with one
+// coefficient per (edge, group): S and E, INS and ISy as FP32x2 pairs
+// (__fadd2_rn / __fmul2_rn / __ffma2_rn, each lane rounded as the scalar
+// intrinsic), so the pairs take one instruction where the scalar form takes two,
+// with the same roundings in the same order as the general form.
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b)
+{
+    return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); // a - b, rounded once
+}
+struct AccP {
+    float2 hi, lo;
+    // TwoSum of hi and t, the error into lo (Acc<float>::add, lane by lane)
+    __device__ __forceinline__ void add(float2 t)
+    {
+        const float2 s  = __fadd2_rn(hi, t);
+        const float2 bb = f2sub(s, hi);
+        const float2 e  = __fadd2_rn(f2sub(hi, f2sub(s, bb)), f2sub(t, bb));
+        hi              = s;
+        lo              = __fadd2_rn(lo, e);
+    }
+    // add(-m) with the same roundings
+    __device__ __forceinline__ void sub(float2 m)
+    {
+        const float2 s  = f2sub(hi, m);
+        const float2 bb = f2sub(s, hi);
+        const float2 e  = f2sub(f2sub(hi, f2sub(s, bb)), __fadd2_rn(m, bb));
+        hi              = s;
+        lo              = __fadd2_rn(lo, e);
+    }
+};
+// travelers of a group snapshot s with coefficient u and nondetection factor
+// nd: (S, E), (INS, ISy) and R as in travelers_cf
+struct TravP {
+    float2 se, iy;
+    float r;
+};
+__device__ __forceinline__ TravP trav_p(const GroupSnap& s, float u, float nd)
+{
+    const float2 uu = make_float2(u, u);
+    TravP m;
+    m.se   = __fmul2_rn(make_float2(s.y[MGPU_S], s.y[MGPU_E]), uu);
+    m.iy   = __fmul2_rn(make_float2(s.y[MGPU_INS], s.y[MGPU_ISY]), uu);
+    m.iy.y = __fmul_rn(m.iy.y, s.risk);
+    m.iy   = __fmul2_rn(m.iy, make_float2(nd, nd));
+    m.r    = __fmul_rn(s.y[MGPU_R], u);
+    return m;
+}
+__device__ __forceinline__ float coef_u(const BatchDev& B, const RecCtx& x, int64_t e, int gr)
+{
+    return __ldg(B.ecoef_u + x.crow0 + e * x.G + gr);
+}
+__device__ __forceinline__ void acc_to_array(const AccP& se, const AccP& iy, const Acc<float>& r,
+                                             Acc<float> (&acc)[kC])
+{
+    acc[MGPU_S].init_pair(se.hi.x, se.lo.x);
+    acc[MGPU_E].init_pair(se.hi.y, se.lo.y);
+    acc[MGPU_INS].init_pair(iy.hi.x, iy.lo.x);
+    acc[MGPU_ISY].init_pair(iy.hi.y, iy.lo.y);
+    acc[MGPU_R] = r;
+}
+
+// xf_return_item for the commuter compartments with one coefficient per (edge, group)
+template <int UNR, class Tab>
+__device__ __forceinline__ void xf_return_item_p(const BatchDev& B, const DevGraph& g, const GraphRt& rt,
+                                                 const Tab& tab, int64_t node, int gr)
+{
+    constexpr int MASK = kMaskSEIYR;
+    const float dt     = (float)rt.dt;
+    const int64_t s0   = g.state_off + (node - g.node0) * g.n + gr * kC;
+    float y0[kC], l0[kC];
+    ld_state(B.st_hi + s0, y0);
+    ld_state(B.st_lo + s0, l0);
+    st_state(B.yn_hi + s0, y0);
+    st_state(B.yn_lo + s0, l0);
+    AccP a_se{make_float2(y0[MGPU_S], y0[MGPU_E]), make_float2(l0[MGPU_S], l0[MGPU_E])};
+    AccP a_iy{make_float2(y0[MGPU_INS], y0[MGPU_ISY]), make_float2(l0[MGPU_INS], l0[MGPU_ISY])};
+    Acc<float> a_r;
+    a_r.init_pair(y0[MGPU_R], l0[MGPU_R]);
+    float a_own[kAux];
+    tab.rates(node, gr, a_own);
+    const RecCtx& x = tab.x;
+    GroupSnap own;
+    tab.snap(node, gr, own);
+    float2 in_se = make_float2(0.0f, 0.0f), in_iy = in_se, out_se = in_se, out_iy = in_se;
+    float2 po01 = in_se, po23 = in_se, po67 = in_se;
+    float in_r = 0.0f, out_r = 0.0f, neg_in = 0.0f;
+    auto leave = [&](int64_t k) {
+        GroupSnap src;
+        const int2 se = B.in_se[k];
+        tab.snap(se.x, gr, src);
+        const TravP m = trav_p(src, coef_u(B, x, se.y, gr), src.nd);
+        a_se.sub(m.se);
+        a_iy.sub(m.iy);
+        a_r.add(-m.r);
+        in_se = __fadd2_rn(in_se, m.se);
+        in_iy = __fadd2_rn(in_iy, m.iy);
+        in_r += m.r;
+        neg_in += fminf(m.se.x, 0.0f);
+        neg_in += fminf(m.se.y, 0.0f);
+        neg_in += fminf(m.iy.x, 0.0f);
+        neg_in += fminf(m.iy.y, 0.0f);
+        neg_in += fminf(m.r, 0.0f);
+    };
+    const EdgeRanges r(B, node);
+#pragma unroll UNR
+    for (int64_t k = r.k0; k < r.km; ++k) {
+        leave(k);
+    }
+    const float2 low_se = in_se, low_iy = in_iy;
+    const float low_r = in_r, neg_low = neg_in;
+    const float2 dt2  = make_float2(dt, dt);
+#pragma unroll UNR
+    for (int64_t e = r.o0; e < r.o1; ++e) {
+        float ax[kAux];
+        tab.rates(B.edge_dst[e], gr, ax);
+        const TravP m = trav_p(own, coef_u(B, x, e, gr), own.nd);
+        // Euler flows at the destination's rates: S->E, E->INS; INS->ISy, INS->R; ISy->ISev, ISy->R
+        const float2 p01 = __fmul2_rn(dt2, __fmul2_rn(make_float2(ax[0], ax[1]), m.se));
+        const float2 p23 = __fmul2_rn(dt2, __fmul2_rn(make_float2(ax[2], ax[3]), make_float2(m.iy.x, m.iy.x)));
+        const float2 p67 = __fmul2_rn(dt2, __fmul2_rn(make_float2(ax[4], ax[5]), make_float2(m.iy.y, m.iy.y)));
+        a_se.add(m.se);
+        a_iy.add(m.iy);
+        a_r.add(m.r);
+        out_se = __fadd2_rn(out_se, m.se);
+        out_iy = __fadd2_rn(out_iy, m.iy);
+        out_r += m.r;
+        po01 = __fadd2_rn(po01, p01);
+        po23 = __fadd2_rn(po23, p23);
+        po67 = __fadd2_rn(po67, p67);
+    }
+#pragma unroll UNR
+    for (int64_t k = r.km; k < r.k1; ++k) {
+        leave(k);
+    }
+    Acc<float> acc[kC];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        acc[c].init_pair(y0[c], l0[c]);
+    }
+    acc_to_array(a_se, a_iy, a_r, acc);
+    float m_in[kC] = {}, m_low[kC] = {}, m_out[kC] = {}, phi_out[kF] = {};
+    m_in[MGPU_S]   = in_se.x;
+    m_in[MGPU_E]   = in_se.y;
+    m_in[MGPU_INS] = in_iy.x;
+    m_in[MGPU_ISY] = in_iy.y;
+    m_in[MGPU_R]   = in_r;
+    m_low[MGPU_S]   = low_se.x;
+    m_low[MGPU_E]   = low_se.y;
+    m_low[MGPU_INS] = low_iy.x;
+    m_low[MGPU_ISY] = low_iy.y;
+    m_low[MGPU_R]   = low_r;
+    m_out[MGPU_S]   = out_se.x;
+    m_out[MGPU_E]   = out_se.y;
+    m_out[MGPU_INS] = out_iy.x;
+    m_out[MGPU_ISY] = out_iy.y;
+    m_out[MGPU_R]   = out_r;
+    phi_out[0] = po01.x;
+    phi_out[1] = po01.y;
+    phi_out[2] = po23.x;
+    phi_out[3] = po23.y;
+    phi_out[6] = po67.x;
+    phi_out[7] = po67.y;
+    xf_return_finish<MASK>(B, g, node, gr, dt, y0, a_own, acc, m_in, m_low, m_out, phi_out, neg_in, neg_low);
+}
+
+// xf_depart_item for the commuter compartments with one coefficient per (edge, group)
+template <int UNR, class Tab>
+__device__ __forceinline__ void xf_depart_item_p(const BatchDev& B, const DevGraph& g, const Tab& tab, int64_t node,
+                                                 int gr)
+{
+    const int64_t so = g.state_off + (node - g.node0) * g.n + gr * kC;
+    float h[kC], l[kC];
+    ld_state(B.st_hi + so, h);
+    ld_state(B.st_lo + so, l);
+    AccP a_se{make_float2(h[MGPU_S], h[MGPU_E]), make_float2(l[MGPU_S], l[MGPU_E])};
+    AccP a_iy{make_float2(h[MGPU_INS], h[MGPU_ISY]), make_float2(l[MGPU_INS], l[MGPU_ISY])};
+    Acc<float> a_r, a_insc, a_isyc;
+    a_r.init_pair(h[MGPU_R], l[MGPU_R]);
+    a_insc.init_pair(h[MGPU_INSC], l[MGPU_INSC]);
+    a_isyc.init_pair(h[MGPU_ISYC], l[MGPU_ISYC]);
+    const RecCtx& x = tab.x;
+    GroupSnap own;
+    tab.snap(node, gr, own);
+    const bool detect = own.nd != 1.0f;
+    const float q     = 1.0f - own.nd;
+    auto arrive       = [&](int64_t k) {
+        GroupSnap src;
+        const int2 se = B.in_se[k];
+        tab.snap(se.x, gr, src);
+        const TravP m = trav_p(src, coef_u(B, x, se.y, gr), src.nd);
+        a_se.add(m.se);
+        a_iy.add(m.iy);
+        a_r.add(m.r);
+    };
+    const EdgeRanges r(B, node);
+#pragma unroll UNR
+    for (int64_t k = r.k0; k < r.km; ++k) {
+        arrive(k);
+    }
+#pragma unroll UNR
+    for (int64_t e = r.o0; e < r.o1; ++e) {
+        const float u = coef_u(B, x, e, gr);
+        if (detect) {
+            // test_commuters: detected commuters move to the confirmed compartments first
+            const TravP mo = trav_p(own, u, 1.0f);
+            const float2 d = __fmul2_rn(mo.iy, make_float2(q, q));
+            a_iy.sub(d);
+            a_insc.add(d.x);
+            a_isyc.add(d.y);
+        }
+        const TravP m = trav_p(own, u, own.nd);
+        a_se.sub(m.se);
+        a_iy.sub(m.iy);
+        a_r.add(-m.r);
+    }
+#pragma unroll UNR
+    for (int64_t k = r.km; k < r.k1; ++k) {
+        arrive(k);
+    }
+    Acc<float> acc[kC];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        acc[c].init_pair(h[c], l[c]);
+    }
+    acc_to_array(a_se, a_iy, a_r, acc);
+    acc[MGPU_INSC] = a_insc;
+    acc[MGPU_ISYC] = a_isyc;
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+        acc[c].store(&h[c], &l[c]);
+    }
+    st_state(B.st_hi + so, h);
+    st_state(B.st_lo + so, l);
+    st_state(B.v0_hi + so, h);
+    st_state(B.v0_lo + so, l);
+}
+
 // Departure of one (node, age group): the travelers of its out-edges leave, the
 // travelers of its in-edges arrive, summed in the serial order of the edges.
 template <int MASK, bool UNI, int UNR, class Tab>
 __device__ __forceinline__ void xf_depart_item(const BatchDev& B, const DevGraph& g, const GraphRt& rt,
                                                const Tab& tab, int64_t node, int gr)
 {
+    if constexpr (MASK == kMaskSEIYR && UNI) {
+        xf_depart_item_p<UNR>(B, g, tab, node, gr);
+        return;
+    }
     const int64_t lv = node - g.node0;
     const int64_t so = g.state_off + lv * g.n + gr * kC;
     Acc<float> acc[kC];
@@ -1345,6 +1692,10 @@ template <int MASK, bool UNI, int UNR, class Tab>
 __device__ __forceinline__ void xf_return_item(const BatchDev& B, const DevGraph& g, const GraphRt& rt,
                                                const Tab& tab, int64_t node, int gr)
 {
+    if constexpr (MASK == kMaskSEIYR && UNI) {
+        xf_return_item_p<UNR>(B, g, rt, tab, node, gr);
+        return;
+    }
     const float dt   = (float)rt.dt;
     const int64_t lv = node - g.node0;
     const int64_t s0 = g.state_off + lv * g.n + gr * kC;
@@ -1436,100 +1787,7 @@ __device__ __forceinline__ void xf_return_item(const BatchDev& B, const DevGraph
     for (int64_t k = r.km; k < r.k1; ++k) {
         leave(k);
     }
-    // The in-edges' travelers all take this node's own rates, so their Euler
-    // flows are those of their sum. Flow increments: in-edges take their
-    // travelers' increments away, out-edges bring theirs home.
-    float phi_in[kF], phi_low[kF];
-    flows_f<MASK>(a_own, dt, m_in, phi_in);
-    flows_f<MASK>(a_own, dt, m_low, phi_low);
-#pragma unroll
-    for (int f = 0; f < kF; ++f) {
-        if (in_mask(MASK, kFlowSrcI(f))) {
-            const float net = phi_out[f] - phi_in[f];
-            acc[kFlowSrcI(f)].add(-net);
-            acc[kFlowDstI(f)].add(net);
-        }
-    }
-    // The no-underflow bound. In the reference's serial order (lower in-edges,
-    // out-edges, higher in-edges) an in-edge's returning amount
-    // t = m + inflows - outflows is taken away and fails when the running state
-    // minus t has a negative compartment. At this node's own rates t is linear in
-    // the edge's travelers: t_c = d_c m_c + sum over flows f into c of dt a_f m_src(f),
-    // d_c = 1 - dt (total outflow rate of c). Per compartment:
-    //  * d_c >= 0: every coefficient is >= 0, so t_c >= 0 up to K_c times the
-    //    negative parts of the travelers (states slightly below zero),
-    //    K_c = |d_c| + the inflow coefficients; the running state only decreases
-    //    within a run of in-edges and is smallest at the run's end, where it is
-    //    y0 - T(lower) after the lower run and y0 - T(all in) + T(out) after the
-    //    higher one, T the summed returning amounts (from the traveler and flow sums);
-    //  * d_c < 0 and no inflow into c: t_c <= 0 up to the same correction, so the
-    //    in-edges take nothing from c (the serial loop's max(t, 0));
-    //  * d_c < 0 with inflows: signs can differ between edges; the item takes the
-    //    exact path.
-    // The ends are checked less the correction and with a margin of 1e-5 of y0
-    // plus the summed magnitudes (above the FP32 rounding of the sums).
-    bool flag = false;
-    float t_low[kC], t_in[kC], t_out[kC], mag[kC];
-#pragma unroll
-    for (int c = 0; c < kC; ++c) {
-        t_low[c] = m_low[c];
-        t_in[c]  = m_in[c];
-        t_out[c] = m_out[c];
-        mag[c]   = fabsf(y0[c]) + m_in[c] + m_out[c];
-    }
-#pragma unroll
-    for (int f = 0; f < kF; ++f) {
-        if (in_mask(MASK, kFlowSrcI(f))) {
-            t_low[kFlowSrcI(f)] -= phi_low[f];
-            t_low[kFlowDstI(f)] += phi_low[f];
-            t_in[kFlowSrcI(f)] -= phi_in[f];
-            t_in[kFlowDstI(f)] += phi_in[f];
-            t_out[kFlowSrcI(f)] -= phi_out[f];
-            t_out[kFlowDstI(f)] += phi_out[f];
-            mag[kFlowSrcI(f)] += phi_in[f] + phi_out[f];
-            mag[kFlowDstI(f)] += phi_in[f] + phi_out[f];
-        }
-    }
-#pragma unroll
-    for (int c = 0; c < kC; ++c) {
-        if (in_mask(touched_mask(MASK), c)) {
-            float rate = 0.0f, inflow = 0.0f;
-            bool has_inflow = false;
-#pragma unroll
-            for (int f = 0; f < kF; ++f) {
-                if (in_mask(MASK, kFlowSrcI(f))) {
-                    if (kFlowSrcI(f) == c) {
-                        rate += a_own[aux_of_flow(f)];
-                    }
-                    if (kFlowDstI(f) == c) {
-                        inflow += dt * a_own[aux_of_flow(f)];
-                        has_inflow = true;
-                    }
-                }
-            }
-            const float d = 1.0f - dt * rate;
-            if (d < 0.0f) {
-                if (has_inflow) {
-                    flag = true;
-                }
-                t_low[c] = 0.0f;
-                t_in[c]  = 0.0f;
-            }
-            const float k      = fabsf(d) + inflow;
-            const float margin = 1e-5f * mag[c];
-            flag = flag || (y0[c] - t_low[c]) + k * neg_low < margin ||
-                   ((y0[c] - t_in[c]) + t_out[c]) + k * neg_in < margin;
-        }
-    }
-    const int64_t so = g.state_off + lv * g.n + gr * kC;
-    float h[kC], l[kC];
-#pragma unroll
-    for (int c = 0; c < kC; ++c) {
-        acc[c].store(&h[c], &l[c]);
-    }
-    st_state(B.st_hi + so, h);
-    st_state(B.st_lo + so, l);
-    list0_push(B, node * MGPU_MAX_GROUPS + gr, flag);
+    xf_return_finish<MASK>(B, g, node, gr, dt, y0, a_own, acc, m_in, m_low, m_out, phi_out, neg_in, neg_low);
 }
 
 // One thread per (node, group) of the nodes with G age groups (dense: node
