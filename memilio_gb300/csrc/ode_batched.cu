@@ -632,8 +632,10 @@ __device__ __forceinline__ void segf_rhs(SegF<G>& X, const float (&u)[kC], float
     kc[D_]    = fl[12] + fl[13];
 }
 
-// shared memory per lane of the mixed solver: 5 stage derivative vectors and the flow increments
-constexpr int kOdeSmemPerLane = 5 * kC + kF;
+// shared memory per lane of the mixed solver: 5 stage derivative vectors and the
+// flow increments (15, padded to 16 for the float2 pairs)
+constexpr int kOdeSmemPerLane = 5 * kC + 16;
+static_assert(kC % 2 == 0 && kF == 15, "pair layout of the stage storage");
 constexpr int kMixedThreads   = 128; // largest block of the mixed node kernels
 // resident blocks per SM the register budget must allow (measured best for the
 // FP32 step; the FP64 step holds its state and clock in FP64 registers)
@@ -680,12 +682,16 @@ __global__ void __launch_bounds__(kMixedThreads, CTL64 ? kMixedMinBlocks64 : kMi
     const Clk abs_tol  = (Clk)o.abs_tol, rel_tol = (Clk)o.rel_tol;
     const Clk o_dt_min = (Clk)o.dt_min; // FP32: DBL_MIN becomes 0, no lower bound, as in FP64
     const Clk o_dt_max = (Clk)o.dt_max; // FP32: DBL_MAX becomes +inf
-    // stage derivatives k_0..k_4: [warp][stage*10 + c][lane] (conflict-free columns)
+    // stage derivatives k_0..k_4 as compartment pairs: [warp][stage*5 + pair][lane]
+    // float2 (conflict-free 64-bit columns), so that the stage combinations run
+    // as FP32x2 multiply-adds (__ffma2_rn: each lane the FFMA of the scalar form)
     extern __shared__ float ode_smem[];
     float* skw = ode_smem + (threadIdx.x >> 5) * ((kOdeSmemPerLane + (FLOWS ? kF : 0)) * 32);
-#define SK(s, c) skw[((s) * kC + (c)) * 32 + lane]
-    // the 5th-order flow increments of the attempt, after the stage derivatives
-#define SP(f) skw[(5 * kC + (f)) * 32 + lane]
+#define SK2(s, p) reinterpret_cast<float2*>(skw)[((s) * (kC / 2) + (p)) * 32 + lane]
+#define SK(s, c) skw[(((s) * (kC / 2) + (c) / 2) * 32 + lane) * 2 + ((c) & 1)]
+    // the 5th-order flow increments of the attempt as flow pairs, after the stage derivatives
+#define SP2(p) reinterpret_cast<float2*>(skw + 5 * kC * 32)[(p) * 32 + lane]
+#define SP(f) skw[5 * kC * 32 + (((f) / 2) * 32 + lane) * 2 + ((f) & 1)]
     // (FLOWS) the increments of the interval's applied steps, summed per flow
 #define SF(f) skw[(kOdeSmemPerLane + (f)) * 32 + lane]
     unsigned long long n_acc = 0, n_rej = 0, n_fail = 0;
@@ -817,61 +823,80 @@ __global__ void __launch_bounds__(kMixedThreads, CTL64 ? kMixedMinBlocks64 : kMi
                 // stage derivatives in this lane's shared-memory column
 #pragma unroll 1
                 for (int s = 0; s < 6; ++s) {
-                    float u[kC];
+                    float2 u2[kC / 2];
 #pragma unroll
-                    for (int c = 0; c < kC; ++c) {
-                        u[c] = hi[c];
+                    for (int q = 0; q < kC / 2; ++q) {
+                        u2[q] = make_float2(hi[2 * q], hi[2 * q + 1]);
                     }
 #pragma unroll 1
                     for (int j = 0; j < s; ++j) {
-                        const float a = fk_a[s][j] * dtf;
+                        const float a   = fk_a[s][j] * dtf;
+                        const float2 a2 = make_float2(a, a);
 #pragma unroll
-                        for (int c = 0; c < kC; ++c) {
-                            u[c] = u[c] + a * SK(j, c);
+                        for (int q = 0; q < kC / 2; ++q) {
+                            u2[q] = __ffma2_rn(a2, SK2(j, q), u2[q]);
                         }
+                    }
+                    float u[kC];
+#pragma unroll
+                    for (int q = 0; q < kC / 2; ++q) {
+                        u[2 * q]     = u2[q].x;
+                        u[2 * q + 1] = u2[q].y;
                     }
                     segf_rhs(X, u, trel + fk_c[s] * dtf, fl, kc);
                     if (s < 5) {
 #pragma unroll
-                        for (int c = 0; c < kC; ++c) {
-                            SK(s, c) = kc[c];
+                        for (int q = 0; q < kC / 2; ++q) {
+                            SK2(s, q) = make_float2(kc[2 * q], kc[2 * q + 1]);
                         }
                     }
-                    const float b5 = fk_b5[s] * dtf;
+                    const float b5   = fk_b5[s] * dtf;
+                    const float2 b52 = make_float2(b5, b5);
                     if (s == 0) {
 #pragma unroll
-                        for (int f = 0; f < kF; ++f) {
-                            SP(f) = b5 * fl[f];
+                        for (int q = 0; q < kF / 2; ++q) {
+                            SP2(q) = __fmul2_rn(b52, make_float2(fl[2 * q], fl[2 * q + 1]));
                         }
+                        SP(kF - 1) = b5 * fl[kF - 1];
                     }
                     else if (b5 != 0.0f) {
 #pragma unroll
-                        for (int f = 0; f < kF; ++f) {
-                            SP(f) = SP(f) + b5 * fl[f];
+                        for (int q = 0; q < kF / 2; ++q) {
+                            SP2(q) = __ffma2_rn(b52, make_float2(fl[2 * q], fl[2 * q + 1]), SP2(q));
                         }
+                        SP(kF - 1) = SP(kF - 1) + b5 * fl[kF - 1];
                     }
                 }
                 // embedded error: the stage derivatives weighted in stage order
                 // (k_0..k_4 from shared memory, k_5 still in registers)
-                float xe[kC];
+                float2 xe2[kC / 2];
+                {
+                    const float d0 = fk_db[0] * dtf;
 #pragma unroll
-                for (int c = 0; c < kC; ++c) {
-                    xe[c] = (fk_db[0] * dtf) * SK(0, c);
+                    for (int q = 0; q < kC / 2; ++q) {
+                        xe2[q] = __fmul2_rn(make_float2(d0, d0), SK2(0, q));
+                    }
                 }
 #pragma unroll 1
                 for (int s = 1; s < 5; ++s) {
                     const float db = fk_db[s] * dtf;
 #pragma unroll
-                    for (int c = 0; c < kC; ++c) {
-                        xe[c] = xe[c] + db * SK(s, c);
+                    for (int q = 0; q < kC / 2; ++q) {
+                        xe2[q] = __ffma2_rn(make_float2(db, db), SK2(s, q), xe2[q]);
                     }
                 }
                 {
                     const float db = fk_db[5] * dtf;
 #pragma unroll
-                    for (int c = 0; c < kC; ++c) {
-                        xe[c] = xe[c] + db * kc[c];
+                    for (int q = 0; q < kC / 2; ++q) {
+                        xe2[q] = __ffma2_rn(make_float2(db, db), make_float2(kc[2 * q], kc[2 * q + 1]), xe2[q]);
                     }
+                }
+                float xe[kC];
+#pragma unroll
+                for (int q = 0; q < kC / 2; ++q) {
+                    xe[2 * q]     = xe2[q].x;
+                    xe[2 * q + 1] = xe2[q].y;
                 }
                 // Odeint error measure, max over the instance
                 Clk el = 0;
