@@ -2063,7 +2063,10 @@ __device__ __forceinline__ bool ff_gt(FF a, FF b)
 }
 
 // Returning travelers of group gr on edge e as float-float values: the FP32
-// travelers plus the Euler flow increments (return_travelers in pairs).
+// travelers plus the Euler flow increments (return_travelers in pairs). Only
+// the compartments of MASK move (every coefficient of the others is zero, so
+// their travelers and the flows out of them are exact zeros and are skipped).
+template <int MASK>
 __device__ __forceinline__ void return_travelers_ff(const BatchDev& B, const DevGraph& g, const GraphRt& rt,
                                                     int64_t e, int gr, FF (&t)[kC])
 {
@@ -2071,12 +2074,14 @@ __device__ __forceinline__ void return_travelers_ff(const BatchDev& B, const Dev
     return_flows<float>(B, g, rt, e, gr, m, phi);
 #pragma unroll
     for (int c = 0; c < kC; ++c) {
-        t[c] = {m[c], 0.0f};
+        t[c] = {in_mask(MASK, c) ? m[c] : 0.0f, 0.0f};
     }
 #pragma unroll
     for (int k = 0; k < kF; ++k) {
-        t[kFlowSrcI(k)] = ff_add_f(t[kFlowSrcI(k)], -phi[k]);
-        t[kFlowDstI(k)] = ff_add_f(t[kFlowDstI(k)], phi[k]);
+        if (in_mask(MASK, kFlowSrcI(k))) {
+            t[kFlowSrcI(k)] = ff_add_f(t[kFlowSrcI(k)], -phi[k]);
+            t[kFlowDstI(k)] = ff_add_f(t[kFlowDstI(k)], phi[k]);
+        }
     }
 }
 
@@ -2123,6 +2128,7 @@ __device__ __forceinline__ int fix_group_ff(const FF (&y)[kC], FF (&t)[kC])
 // edges at a time in parallel (the gathers), then follow the serial order with
 // prefix sums over the lanes, stopping only at the edges that need the fix:
 // every lane holds the same running state, and lane j publishes edge j's fix.
+template <int MASK>
 __global__ void k_xf_scan(BatchDev B, int pass)
 {
     constexpr unsigned kFull = 0xffffffffu;
@@ -2210,7 +2216,7 @@ __global__ void k_xf_scan(BatchDev B, int pass)
                     }
                 }
                 else {
-                    return_travelers_ff(B, g, rt, e, gr, t);
+                    return_travelers_ff<MASK>(B, g, rt, e, gr, t);
                 }
             }
             else {
@@ -2256,23 +2262,31 @@ __global__ void k_xf_scan(BatchDev B, int pass)
             // negative compartment. The first such edge j is fixed against the
             // exact running state (y advanced to just before it), as in the serial
             // loop, and the scan restarts after it with the fixed travelers applied.
+            // The travelers of unfixed edges are zero outside touched_mask(MASK);
+            // a published fix can carry any compartment, so a chunk holding one
+            // sums all ten.
+            const bool any_fixed = __any_sync(kFull, kind == 2 && prev != 0);
+            auto scan_chunk = [&](auto tm) {
+                constexpr int TM = decltype(tm)::value;
             int start = 0;
             while (start < nchunk) {
                 FF p[kC];
                 const bool live = lane >= start && lane < nchunk && kind != 0;
 #pragma unroll
                 for (int c = 0; c < kC; ++c) {
-                    p[c] = !live ? FF{0.0f, 0.0f} : (kind == 2 ? t[c] : ff_neg(t[c]));
+                    p[c] = (!live || !in_mask(TM, c)) ? FF{0.0f, 0.0f} : (kind == 2 ? t[c] : ff_neg(t[c]));
                 }
 #pragma unroll
                 for (int d = 1; d < 32; d <<= 1) {
 #pragma unroll
                     for (int c = 0; c < kC; ++c) {
-                        FF q;
-                        q.h = __shfl_up_sync(kFull, p[c].h, d);
-                        q.l = __shfl_up_sync(kFull, p[c].l, d);
-                        if (lane >= d) {
-                            p[c] = ff_add(q, p[c]);
+                        if (in_mask(TM, c)) {
+                            FF q;
+                            q.h = __shfl_up_sync(kFull, p[c].h, d);
+                            q.l = __shfl_up_sync(kFull, p[c].l, d);
+                            if (lane >= d) {
+                                p[c] = ff_add(q, p[c]);
+                            }
                         }
                     }
                 }
@@ -2280,7 +2294,7 @@ __global__ void k_xf_scan(BatchDev B, int pass)
                 if (live && kind == 1) {
 #pragma unroll
                     for (int c = 0; c < kC; ++c) {
-                        need = need || ff_neg_p(ff_add(y[c], p[c]));
+                        need = need || ff_neg_p(in_mask(TM, c) ? ff_add(y[c], p[c]) : y[c]);
                     }
                 }
                 const unsigned m = __ballot_sync(kFull, need);
@@ -2293,10 +2307,12 @@ __global__ void k_xf_scan(BatchDev B, int pass)
                 if (j > start) {
 #pragma unroll
                     for (int c = 0; c < kC; ++c) {
-                        FF q;
-                        q.h  = __shfl_sync(kFull, p[c].h, j - 1);
-                        q.l  = __shfl_sync(kFull, p[c].l, j - 1);
-                        y[c] = ff_add(y[c], q);
+                        if (in_mask(TM, c)) {
+                            FF q;
+                            q.h  = __shfl_sync(kFull, p[c].h, j - 1);
+                            q.l  = __shfl_sync(kFull, p[c].l, j - 1);
+                            y[c] = ff_add(y[c], q);
+                        }
                     }
                 }
                 if (j >= nchunk) {
@@ -2317,6 +2333,13 @@ __global__ void k_xf_scan(BatchDev B, int pass)
                     y[c] = ff_add(y[c], ff_neg(tj[c]));
                 }
                 start = j + 1;
+            }
+            };
+            if (any_fixed) {
+                scan_chunk(std::integral_constant<int, kMaskAll>());
+            }
+            else {
+                scan_chunk(std::integral_constant<int, touched_mask(MASK)>());
             }
         }
         if (lane == 0) {
@@ -2652,7 +2675,12 @@ void launch_xb(const BatchDev& B, int64_t n_max, bool any_edge_dampings, cudaStr
     const unsigned scan_blocks = 152 * 8;
     for (int pass = 0; pass < kXbScanPasses; ++pass) {
         if (std::is_same<R, float>::value) {
-            k_xf_scan<<<scan_blocks, 128, 0, s>>>(B, pass);
+            if ((B.mob_union & ~kMaskSEIYR) == 0) {
+                k_xf_scan<kMaskSEIYR><<<scan_blocks, 128, 0, s>>>(B, pass);
+            }
+            else {
+                k_xf_scan<kMaskAll><<<scan_blocks, 128, 0, s>>>(B, pass);
+            }
         }
         else {
             k_xg_scan<R><<<scan_blocks, 128, 0, s>>>(B, pass);
