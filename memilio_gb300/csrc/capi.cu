@@ -891,6 +891,45 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
             }
         }
     }
+    // the one-value coefficients also in each graph's in-edge order (graphs with
+    // the same coefficient and edge arrays share one copy, as they share ecoef_u)
+    std::vector<float> h_ecu_in;
+    for (int i = 0; i < num_graphs; ++i) {
+        dg[i].ecoef_in_off = -1;
+    }
+    if (!h_ecu.empty()) {
+        std::map<Key, int> ein_first;
+        std::vector<int> ein_own;
+        int64_t pos = 0;
+        for (int i = 0; i < num_graphs; ++i) {
+            DevGraph& d = dg[i];
+            if (d.E == 0 || d.Ke != 0) {
+                continue;
+            }
+            const Key k{graphs[i].edge_coeff_baseline, graphs[i].edge_src, graphs[i].edge_dst, nullptr, d.E, d.G, 0};
+            auto it = ein_first.find(k);
+            if (it != ein_first.end()) {
+                d.ecoef_in_off = dg[it->second].ecoef_in_off;
+            }
+            else {
+                ein_first[k]   = i;
+                d.ecoef_in_off = pos;
+                pos += (int64_t)d.E * d.G;
+                ein_own.push_back(i);
+            }
+        }
+        h_ecu_in.resize((size_t)pos);
+        parallel_for((int64_t)ein_own.size(), [&](int64_t q) {
+            const DevGraph& d = dg[ein_own[(size_t)q]];
+            for (int64_t k = 0; k < d.E; ++k) {
+                const int64_t el = h_in_edges[d.edge0 + k] - d.edge0;
+                for (int gr = 0; gr < d.G; ++gr) {
+                    h_ecu_in[(size_t)(d.ecoef_in_off + k * d.G + gr)] =
+                        h_ecu[(size_t)(d.ecoef_f_off / kC + el * d.G + gr)];
+                }
+            }
+        });
+    }
     trace.mark("packing");
     b->host_graphs = dg;
     b->damping_shared.assign(num_graphs, 0);
@@ -981,6 +1020,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.aux        = plain ? nullptr : (void*)b->pool.alloc<double>(nodes * MGPU_MAX_GROUPS * 12);
     B.ecoef_r    = b->pairs ? b->pool.upload(h_ecr) : nullptr;
     B.ecoef_u    = h_ecu.empty() ? nullptr : b->pool.upload(h_ecu);
+    B.ecoef_in   = h_ecu_in.empty() ? nullptr : b->pool.upload(h_ecu_in);
     B.tab_f      = nullptr;
     B.contact_f  = nullptr;
     B.dvals_f    = nullptr;

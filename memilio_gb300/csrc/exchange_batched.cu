@@ -1333,6 +1333,11 @@ __device__ __forceinline__ float coef_u(const BatchDev& B, const RecCtx& x, int6
 {
     return __ldg(B.ecoef_u + x.crow0 + e * x.G + gr);
 }
+// the coefficient of in-edge k (CSC position) of graph g, from the in-edge-ordered copy
+__device__ __forceinline__ float coef_in(const BatchDev& B, const DevGraph& g, int64_t k, int gr)
+{
+    return __ldg(B.ecoef_in + g.ecoef_in_off + (k - g.edge0) * g.G + gr);
+}
 __device__ __forceinline__ void acc_to_array(const AccP& se, const AccP& iy, const Acc<float>& r,
                                              Acc<float> (&acc)[kC])
 {
@@ -1372,7 +1377,7 @@ __device__ __forceinline__ void xf_return_item_p(const BatchDev& B, const DevGra
         GroupSnap src;
         const int2 se = B.in_se[k];
         tab.snap(se.x, gr, src);
-        const TravP m = trav_p(src, coef_u(B, x, se.y, gr), src.nd);
+        const TravP m = trav_p(src, coef_in(B, g, k, gr), src.nd);
         a_se.sub(m.se);
         a_iy.sub(m.iy);
         a_r.add(-m.r);
@@ -1471,7 +1476,7 @@ __device__ __forceinline__ void xf_depart_item_p(const BatchDev& B, const DevGra
         GroupSnap src;
         const int2 se = B.in_se[k];
         tab.snap(se.x, gr, src);
-        const TravP m = trav_p(src, coef_u(B, x, se.y, gr), src.nd);
+        const TravP m = trav_p(src, coef_in(B, g, k, gr), src.nd);
         a_se.add(m.se);
         a_iy.add(m.iy);
         a_r.add(m.r);

@@ -43,6 +43,7 @@ struct DevGraph {
     int64_t ecoef_f_off; // [E][n] floats before the records: the edges' first row * 10 (Ke == 0, mixed)
     int32_t mob_mask;    // compartments c with a nonzero coefficient on some edge and age group
     int32_t staged;      // the FP32 return and departure run one CTA per graph from shared memory
+    int64_t ecoef_in_off; // ecoef_in row of the graph's first in-edge (its in-edges in CSC order), or -1
 };
 
 // Mutable per-graph state (GraphSimulation::m_t and the edges' shared return flag).
@@ -147,6 +148,8 @@ struct BatchDev {
     const float* ecoef_r;        // FP32 coefficient records of edges without dampings (mixed), see rec_vec
     const float* ecoef_u;        // the same as one value per (edge, group) row when every moved
                                  // compartment has the same coefficient everywhere (else null)
+    const float* ecoef_in;       // ecoef_u in each graph's in-edge (CSC) order, [in-edge][group], so
+                                 // that an in-edge's coefficient is read without its edge id first
     // chunks of the graphs whose FP32 return and departure run with the graph's
     // snapshot records (and return-time rates) copied to shared memory, one CTA
     // per chunk: (graph, chunk << 16 | chunks of the graph); their count and
