@@ -609,6 +609,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         par += (int64_t)g.num_nodes * param_stride(G);
         st += (int64_t)g.num_nodes * n;
         trav0[i] = tr;
+        d.trav0  = tr;
         tr += (int64_t)E * n;
         const Key kc{g.contact_baseline, g.contact_minimum, nullptr, nullptr, g.num_nodes, d.M, G};
         auto itc = contact_first.find(kc);
@@ -683,8 +684,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     HostSpan<double> h_par, h_con, h_dtt, h_dtv, h_state, h_ec, h_edt, h_edv;
     HostSpan<int32_t> h_node_graph, h_edge_graph, h_src, h_dst;
     HostSpan<uint8_t> h_any;
-    HostSpan<int64_t> h_trav_off, h_in_ptr, h_in_edges, h_in_mid;
-    HostSpan<int2> h_in_se;
+    HostSpan<int64_t> h_in_ptr, h_in_edges;
     StagingArena arena{ctx};
     arena.take(h_par, par);
     arena.take(h_con, con);
@@ -699,11 +699,8 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     arena.take(h_src, edges);
     arena.take(h_dst, edges);
     arena.take(h_any, edges);
-    arena.take(h_trav_off, edges);
     arena.take(h_in_ptr, nodes + 1);
     arena.take(h_in_edges, edges);
-    arena.take(h_in_mid, nodes);
-    arena.take(h_in_se, edges);
     ck(cudaStreamSynchronize(ctx->stream), "staging sync"); // an earlier upload may still read the buffer
     arena.place();
     trace.mark("page-locked staging");
@@ -745,7 +742,6 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         }
         // edges: CSR by source (already sorted), CSC by destination (sorted by source within)
         std::vector<int64_t> indeg(g.num_nodes + 1, 0);
-        int64_t trav_pos = trav0[i];
         for (int e = 0; e < d.E; ++e) {
             const int64_t ge = d.edge0 + e;
             h_edge_graph[ge] = i;
@@ -787,8 +783,6 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
                                 g.edge_damping_values + (int64_t)e * d.Ke * n, sizeof(double) * d.Ke * n);
                 }
             }
-            h_trav_off[ge] = trav_pos;
-            trav_pos += n;
         }
         for (int v = 0; v < g.num_nodes; ++v) {
             indeg[v + 1] += indeg[v];
@@ -1063,27 +1057,20 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     ck(cudaMemsetAsync(B.edge_fixed, 0, sizeof(int32_t) * std::max<int64_t>(edges, 1), ctx->stream), "memset");
     ck(cudaMemsetAsync(B.node_flag, 0, std::max<int64_t>(nodes, 1), ctx->stream), "memset");
     ck(cudaMemsetAsync(B.node_dirty, 0, std::max<int64_t>(2 * nodes, 1), ctx->stream), "memset");
-    B.trav_off = b->pool.upload(h_trav_off);
     B.out_ptr  = b->pool.upload(h_out_ptr);
     B.in_ptr   = b->pool.upload(h_in_ptr);
     B.in_edges = b->pool.upload(h_in_edges);
     {
-        parallel_for(num_graphs, [&](int64_t i) {
-            const DevGraph& d = dg[i];
-            for (int64_t k = d.edge0; k < d.edge0 + d.E; ++k) {
-                h_in_se[k] = make_int2(h_src[h_in_edges[k]], (int32_t)h_in_edges[k]);
-            }
-            // the serial return order splits each node's in-edges at the node itself
-            for (int64_t v = d.node0; v < d.node0 + d.N; ++v) {
-                int64_t k = h_in_ptr[v];
-                while (k < h_in_ptr[v + 1] && h_in_se[k].x < v) {
-                    ++k;
-                }
-                h_in_mid[v] = k;
-            }
-        });
-        B.in_se  = b->pool.upload(h_in_se);
-        B.in_mid = b->pool.upload(h_in_mid);
+        // derived on the device from the uploaded edge arrays: the (source, edge)
+        // pairs of the in-edges, each node's first in-edge from a higher source,
+        // and the offsets of the edges' traveler records
+        int64_t* trav_off = b->pool.alloc<int64_t>(edges);
+        int2* in_se       = b->pool.alloc<int2>(edges);
+        int64_t* in_mid   = b->pool.alloc<int64_t>(nodes);
+        B.trav_off        = trav_off;
+        B.in_se           = in_se;
+        B.in_mid          = in_mid;
+        ck(launch_edge_indices(B, trav_off, in_se, in_mid, ctx->stream), "edge index kernel");
         trace.mark("uploads, in-edge indices");
     }
     B.scratch_stride = std::max<int64_t>(scratch_slots, 1);

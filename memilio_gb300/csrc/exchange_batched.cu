@@ -2745,6 +2745,51 @@ int exchange_batched_launches(const BatchDev& B, int precision, bool any_edge_da
     return prep + 3 + passes + kXbScanPasses + commit + extra + (B.estats ? 2 : 0);
 }
 
+namespace
+{
+// Per-edge and per-node indices of a batch (one grid-stride pass each): the
+// traveler offset of every edge, the (source, edge) pair of every in-edge in
+// CSC order, and for every node the first of its in-edges whose source is not
+// lower than the node (sources ascend within a node's in-edges, so a binary
+// search finds it): the split of the serial return order.
+__global__ void k_edge_indices(BatchDev B, int64_t* trav_off, int2* in_se, int64_t* in_mid)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t0     = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (int64_t e = t0; e < B.num_edges; e += stride) {
+        const DevGraph& g = B.graphs[B.edge_graph[e]];
+        trav_off[e]       = g.trav0 + (e - g.edge0) * g.n;
+        const int64_t ie  = B.in_edges[e];
+        in_se[e]          = make_int2(B.edge_src[ie], (int32_t)ie);
+    }
+    for (int64_t v = t0; v < B.num_nodes; v += stride) {
+        int64_t lo = B.in_ptr[v], hi = B.in_ptr[v + 1];
+        while (lo < hi) {
+            const int64_t mid = lo + (hi - lo) / 2;
+            if (B.edge_src[B.in_edges[mid]] < v) {
+                lo = mid + 1;
+            }
+            else {
+                hi = mid;
+            }
+        }
+        in_mid[v] = lo;
+    }
+}
+} // namespace
+
+cudaError_t launch_edge_indices(const BatchDev& B, int64_t* trav_off, int2* in_se, int64_t* in_mid,
+                                cudaStream_t s)
+{
+    const int64_t n = std::max<int64_t>(B.num_edges, B.num_nodes);
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16);
+    k_edge_indices<<<blocks, 256, 0, s>>>(B, trav_off, in_se, in_mid);
+    return cudaGetLastError();
+}
+
 #ifndef MGPU_XS_MIN_ITEMS
 #define MGPU_XS_MIN_ITEMS 256 // smaller graphs stay in the node-list passes, which pack them densely
 #endif

@@ -44,6 +44,7 @@ struct DevGraph {
     int32_t mob_mask;    // compartments c with a nonzero coefficient on some edge and age group
     int32_t staged;      // the FP32 return and departure run one CTA per graph from shared memory
     int64_t ecoef_in_off; // ecoef_in row of the graph's first in-edge (its in-edges in CSC order), or -1
+    int64_t trav0;       // traveler-record offset of the graph's first edge ([E][n] doubles)
 };
 
 // Mutable per-graph state (GraphSimulation::m_t and the edges' shared return flag).
@@ -603,6 +604,11 @@ void launch_exchange_batched(const BatchDev& B, int precision, int64_t n_max, bo
                              cudaStream_t s, int64_t* launches,
                              cudaEvent_t* ev = nullptr);
 int exchange_batched_launches(const BatchDev& B, int precision, bool any_edge_dampings);
+// Fills the per-edge traveler offsets, the in-edges' (source, edge) pairs and
+// every node's first in-edge from a higher source, from B.graphs, B.edge_graph,
+// B.edge_src, B.in_ptr and B.in_edges (already on the device).
+cudaError_t launch_edge_indices(const BatchDev& B, int64_t* trav_off, int2* in_se, int64_t* in_mid,
+                                cudaStream_t s);
 // Marks the graphs of a mixed batch whose FP32 return and departure run from
 // shared memory (static coefficients, edges, enough (node, group) items, tables
 // within the device's shared memory per block) and lists their chunks, one CTA

@@ -9,6 +9,7 @@ osecir::InfectionState and the osecir Flows typelist
 from __future__ import annotations
 
 import ctypes
+import operator
 from dataclasses import dataclass, field
 from typing import Optional
 
@@ -131,6 +132,7 @@ class GraphArrays:
     edge_damping_times: Optional[np.ndarray] = None
     edge_damping_values: Optional[np.ndarray] = None
     _c: Optional[MgpuGraph] = field(default=None, repr=False)
+    _c_src: Optional[tuple] = field(default=None, repr=False, compare=False)
 
     def __post_init__(self):
         G = self.num_groups
@@ -184,7 +186,14 @@ class GraphArrays:
         return NUM_COMPARTMENTS * self.num_groups
 
     def as_ctypes(self) -> MgpuGraph:
-        """The mgpu_graph view of the arrays (they must outlive its use)."""
+        """The mgpu_graph view of the arrays (they must outlive its use); kept
+        while the arrays are the same objects (changes in place need no rebuild,
+        an attribute set to another array rebuilds it)."""
+        src = (self.params, self.contact_baseline, self.contact_minimum, self.damping_times, self.damping_values,
+               self.init_state, self.edge_src, self.edge_dst, self.edge_coeff_baseline, self.edge_coeff_minimum,
+               self.edge_damping_times, self.edge_damping_values)
+        if self._c is not None and self._c_src is not None and all(map(operator.is_, src, self._c_src)):
+            return self._c
         f8, i4 = np.float64, np.int32
         a = _addr
         g = MgpuGraph(self.num_nodes, self.num_groups, self.num_edges, self.num_contact_matrices,
@@ -195,6 +204,7 @@ class GraphArrays:
                       a(self.edge_coeff_minimum, f8), a(self.edge_damping_times, f8),
                       a(self.edge_damping_values, f8))
         self._c = g
+        self._c_src = src
         return g
 
     def subgraph_nodes(self, nodes) -> "GraphArrays":
