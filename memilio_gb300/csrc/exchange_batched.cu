@@ -1645,7 +1645,11 @@ __global__ void __launch_bounds__(128, MASK == kMaskAll ? MGPU_XF_DEPART_MIN_BLO
 #ifndef MGPU_XS_UNROLL
 #define MGPU_XS_UNROLL 4 // edges per iteration of the per-graph passes' edge loops
 #endif
-constexpr int kXsThreads = MGPU_XS_THREADS;
+#ifndef MGPU_XS_DEPART_THREADS
+#define MGPU_XS_DEPART_THREADS MGPU_XS_THREADS
+#endif
+constexpr int kXsThreads    = MGPU_XS_THREADS;
+constexpr int kXsDepThreads = MGPU_XS_DEPART_THREADS;
 
 // The (node, group) items [i0, i1) of the work item's chunk of its graph: a
 // graph of I items split into n chunks has chunks of R items, R = I / n rounded
@@ -1670,7 +1674,7 @@ struct XsChunk {
 // One CTA per chunk of a staged graph (B.xs_work): the departure snapshot of
 // the whole graph in shared memory, then the chunk's (node, group) items.
 template <int MASK, bool UNI>
-__global__ void __launch_bounds__(kXsThreads, MGPU_XS_DEPART_MIN_BLOCKS) k_xs_depart(BatchDev B)
+__global__ void __launch_bounds__(kXsDepThreads, MGPU_XS_DEPART_MIN_BLOCKS) k_xs_depart(BatchDev B)
 {
     extern __shared__ float4 xs_smem[];
     const XsChunk c(B, B.graphs);
@@ -2602,7 +2606,7 @@ void launch_xf_pass_m(const BatchDev& B, cudaStream_t s, int64_t* launches)
             }
         }
         else {
-            k_xs_depart<MASK, UNI><<<(unsigned)B.xs_count, kXsThreads, B.xs_smem_dep, s>>>(B);
+            k_xs_depart<MASK, UNI><<<(unsigned)B.xs_count, kXsDepThreads, B.xs_smem_dep, s>>>(B);
         }
         *launches += 1;
     }

@@ -13,9 +13,12 @@ without.
 
 Cases: the benchmark's 400-node, 6-group graph (commuter compartments S, E,
 INS, ISy, R; one fraction per (edge, group)); every compartment mobile with
-per-compartment coefficients; staged, small and edge-damped graphs in one
-batch; a stressed graph whose returns take the exact underflow path; flow
-recording and commuter statistics; the FP64-control variant.
+per-compartment coefficients; the commuter compartments with per-compartment
+coefficients; staged, small and edge-damped graphs in one batch; a stressed
+graph whose returns take the exact underflow path; flow recording and
+commuter statistics; the FP64-control variant. And two graphs that pass the
+same coefficient array with different edges run as they do alone (the
+in-edge-ordered copy of the coefficients is shared only with the same edges).
 """
 import numpy as np
 import pytest
@@ -138,3 +141,33 @@ def test_flows_and_commuter_statistics(ctx):
     a = run(ctx, graphs, N.PRECISION_MIXED, True, 6.0, flows=True, stats_graph=0)
     b = run(ctx, graphs, N.PRECISION_MIXED, False, 6.0, flows=True, stats_graph=0)
     assert_same(a, b)
+
+
+def test_commuter_mask_with_per_compartment_coefficients(ctx):
+    # S, E, INS, ISy, R mobile with a different fraction per compartment: the
+    # commuter mask without one value per (edge, group)
+    g0 = W.mobility_graph(seed=95, N=100, G=6, out_degree=10)
+    rng = np.random.default_rng(96)
+    coeff = g0.edge_coeff_baseline * rng.uniform(0.5, 1.5, g0.edge_coeff_baseline.shape)
+    g = L.GraphArrays(g0.num_groups, g0.params, g0.contact_baseline, g0.contact_minimum, g0.damping_times,
+                      g0.damping_values, g0.init_state, g0.edge_src, g0.edge_dst, coeff)
+    assert_same(run(ctx, [g], N.PRECISION_MIXED, True, 8.0), run(ctx, [g], N.PRECISION_MIXED, False, 8.0))
+
+
+def test_shared_coefficients_with_other_edges(ctx):
+    # two graphs pass the same coefficient array with different edges: each keeps
+    # its own in-edge order of the coefficients, so each runs as it does alone
+    a = W.mobility_graph(seed=97, N=60, G=6, out_degree=8)
+    rng = np.random.default_rng(98)
+    dst = a.edge_dst.copy()
+    for v in range(a.num_nodes):  # other targets, the same number of out-edges per node
+        sel = np.nonzero(a.edge_src == v)[0]
+        pool = np.setdiff1d(np.arange(a.num_nodes), [v])
+        dst[sel] = np.sort(rng.choice(pool, size=sel.size, replace=False))
+    b = L.GraphArrays(a.num_groups, a.params, a.contact_baseline, a.contact_minimum, a.damping_times,
+                      a.damping_values, a.init_state, a.edge_src, dst, a.edge_coeff_baseline)
+    both = run(ctx, [a, b], N.PRECISION_MIXED, True, 6.0)
+    alone_a = run(ctx, [a], N.PRECISION_MIXED, True, 6.0)
+    alone_b = run(ctx, [b], N.PRECISION_MIXED, True, 6.0)
+    np.testing.assert_array_equal(both["states"][0], alone_a["states"][0])
+    np.testing.assert_array_equal(both["states"][1], alone_b["states"][0])
