@@ -710,7 +710,26 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     std::vector<int32_t> mob_mask(num_graphs, 0);
     // Graphs pack into disjoint ranges of the staging buffers, on the host's
     // cores; a graph that shares the coefficient arrays of an earlier one copies
-    // that graph's flags afterwards.
+    // that graph's flags afterwards, and a graph that passes the same edge
+    // arrays as an earlier one (the samples of an ensemble) copies that graph's
+    // edge indices with its own node and edge offsets.
+    std::vector<int> edge_owner(num_graphs);
+    {
+        std::map<Key, int> first;
+        for (int i = 0; i < num_graphs; ++i) {
+            edge_owner[i] = i;
+            if (dg[i].E > 0) {
+                const Key k{graphs[i].edge_src, graphs[i].edge_dst, nullptr, nullptr, dg[i].N, dg[i].E, 0};
+                auto it = first.find(k);
+                if (it != first.end()) {
+                    edge_owner[i] = it->second;
+                }
+                else {
+                    first[k] = i;
+                }
+            }
+        }
+    }
     parallel_for(num_graphs, [&](int64_t gi) {
         const int i         = (int)gi;
         const mgpu_graph& g = graphs[i];
@@ -741,14 +760,17 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
             h_node_graph[d.node0 + v] = i;
         }
         // edges: CSR by source (already sorted), CSC by destination (sorted by source within)
-        std::vector<int64_t> indeg(g.num_nodes + 1, 0);
+        const bool own_edges = edge_owner[i] == i;
+        std::vector<int64_t> indeg(own_edges ? g.num_nodes + 1 : 0, 0);
         for (int e = 0; e < d.E; ++e) {
             const int64_t ge = d.edge0 + e;
             h_edge_graph[ge] = i;
-            h_src[ge]        = (int32_t)(d.node0 + g.edge_src[e]);
-            h_dst[ge]        = (int32_t)(d.node0 + g.edge_dst[e]);
-            h_out_ptr[d.node0 + g.edge_src[e] + 1]++;
-            indeg[g.edge_dst[e] + 1]++;
+            if (own_edges) {
+                h_src[ge] = (int32_t)(d.node0 + g.edge_src[e]);
+                h_dst[ge] = (int32_t)(d.node0 + g.edge_dst[e]);
+                h_out_ptr[d.node0 + g.edge_src[e] + 1]++;
+                indeg[g.edge_dst[e] + 1]++;
+            }
             const double* cb = g.edge_coeff_baseline + (int64_t)e * n;
             if (own_coeff[i]) {
                 double* dc = h_ec.data() + d.ecoef_off + (int64_t)e * 2 * n;
@@ -784,6 +806,9 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
                 }
             }
         }
+        if (!own_edges) {
+            return;
+        }
         for (int v = 0; v < g.num_nodes; ++v) {
             indeg[v + 1] += indeg[v];
         }
@@ -794,6 +819,26 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         }
         for (int v = 0; v < g.num_nodes; ++v) {
             h_in_ptr[d.node0 + v] = d.edge0 + indeg[v];
+        }
+    });
+    parallel_for(num_graphs, [&](int64_t gi) {
+        const int i = (int)gi;
+        const int o = edge_owner[i];
+        if (o == i) {
+            return;
+        }
+        const DevGraph& d  = dg[i];
+        const DevGraph& s  = dg[o];
+        const int32_t dn   = (int32_t)(d.node0 - s.node0);
+        const int64_t de   = d.edge0 - s.edge0;
+        for (int64_t e = 0; e < d.E; ++e) {
+            h_src[d.edge0 + e]      = h_src[s.edge0 + e] + dn;
+            h_dst[d.edge0 + e]      = h_dst[s.edge0 + e] + dn;
+            h_in_edges[d.edge0 + e] = h_in_edges[s.edge0 + e] + de;
+        }
+        for (int64_t v = 0; v < d.N; ++v) {
+            h_out_ptr[d.node0 + v + 1] = h_out_ptr[s.node0 + v + 1];
+            h_in_ptr[d.node0 + v]      = h_in_ptr[s.node0 + v] + de;
         }
     });
     h_in_ptr[nodes] = edges;
