@@ -63,9 +63,10 @@ typedef struct mgpu_solver_opts {
     int32_t profile;                 /* time node solves and exchanges separately with CUDA events
                                         (launches stream by stream; no CUDA graph) */
     int32_t staged_exchange;         /* mixed solvers: graphs whose exchange tables fit in shared
-                                        memory return and depart one CTA per graph from a copy
-                                        there (1, default); 0 = every graph in the node-list passes.
-                                        Both give identical results. */
+                                        memory return and depart in one CTA per chunk of the graph
+                                        from a copy there: 1 (default) when those CTAs fill the GPU
+                                        (two per SM), 2 always, 0 never (every graph in the
+                                        node-list passes). All give identical results. */
 } mgpu_solver_opts;
 
 /* Device times of the last mgpu_batch_advance, from CUDA events on the context's stream. */

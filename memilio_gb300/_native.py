@@ -212,7 +212,7 @@ def solver_opts(precision=PRECISION_MIXED, dt0=0.1, dt_exchange=0.5, integrator:
     o.max_steps_per_interval = max_steps_per_interval
     o.use_cuda_graph = 1 if use_cuda_graph else 0
     o.profile = 1 if profile else 0
-    o.staged_exchange = 1 if staged_exchange else 0
+    o.staged_exchange = int(staged_exchange)  # True/1: when the per-graph CTAs fill the GPU, 2: always
     return o
 
 

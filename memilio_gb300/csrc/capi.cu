@@ -869,7 +869,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     // graphs whose FP32 exchange passes run one CTA per graph from shared memory
     XsPlan xs;
     if (is_mixed(b->opts.precision) && b->opts.staged_exchange) {
-        xs = plan_staged_exchange(dg, B.mob_union, ctx->device);
+        xs = plan_staged_exchange(dg, B.mob_union, ctx->device, b->opts.staged_exchange);
         ck(xs.err, "staged exchange setup");
     }
     // One commuter fraction per (edge, age group): when every compartment the

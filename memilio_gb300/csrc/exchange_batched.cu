@@ -2819,7 +2819,7 @@ void set_xs_smem(int bytes, cudaError_t& err)
 }
 } // namespace
 
-XsPlan plan_staged_exchange(std::vector<DevGraph>& dg, int mob_union, int device)
+XsPlan plan_staged_exchange(std::vector<DevGraph>& dg, int mob_union, int device, int mode)
 {
     XsPlan p;
     const bool seiyr  = (mob_union & ~kMaskSEIYR) == 0;
@@ -2864,6 +2864,18 @@ XsPlan plan_staged_exchange(std::vector<DevGraph>& dg, int mob_union, int device
             p.work.push_back(make_int2(it.second, (k << 16) | n));
         }
         max_items = std::max(max_items, it.first);
+    }
+    // automatic mode: per-graph passes only when their CTAs fill the GPU (two
+    // per SM); a batch of a few graphs spreads better over the node lists
+    int sms = 0;
+    if (mode == 1 && (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+                      (int64_t)p.work.size() < 2 * (int64_t)sms)) {
+        p.work.clear();
+        max_items = 0;
+        for (DevGraph& d : dg) {
+            d.staged = 0;
+        }
+        return p;
     }
     p.aux      = MGPU_XS_AUX && max_items * (ns + na) <= limit;
     p.smem_dep = (int32_t)(max_items * ns);

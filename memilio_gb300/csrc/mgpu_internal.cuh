@@ -620,7 +620,8 @@ struct XsPlan {
     int32_t smem_ret = 0, smem_dep = 0, aux = 0;
     cudaError_t err = cudaSuccess;
 };
-XsPlan plan_staged_exchange(std::vector<DevGraph>& dg, int mob_union, int device);
+// mode 1: only when the chunks give at least two CTAs per SM; 2: always.
+XsPlan plan_staged_exchange(std::vector<DevGraph>& dg, int mob_union, int device, int mode);
 
 // Device and stream of a context (for entry points defined outside capi.cu).
 int context_device_stream(const mgpu_context* ctx, int* device, cudaStream_t* stream);

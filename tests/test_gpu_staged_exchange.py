@@ -8,8 +8,8 @@ TwoSum updates over each (node, age group)'s incident edges in the serial
 order of MobilityEdge::apply_mobility
 (memilio/mobility/metapopulation_mobility_instant.h:544-623), so states,
 flows, commuter statistics and counters are bitwise equal between a batch
-with staging (mgpu_solver_opts.staged_exchange = 1, the default) and one
-without.
+with every eligible graph staged (mgpu_solver_opts.staged_exchange = 2) and
+one without (0); the default (1) stages when the per-graph CTAs fill the GPU.
 
 Cases: the benchmark's 400-node, 6-group graph (commuter compartments S, E,
 INS, ISy, R; one fraction per (edge, group)); every compartment mobile with
@@ -42,7 +42,8 @@ def ctx():
 
 
 def run(ctx, graphs, precision, staged, days, horizons=None, flows=False, stats_graph=None):
-    b = N.Batch(ctx, graphs, 0.0, N.solver_opts(precision=precision, staged_exchange=staged))
+    # staged: every eligible graph staged (2), else the node-list passes only (0)
+    b = N.Batch(ctx, graphs, 0.0, N.solver_opts(precision=precision, staged_exchange=2 if staged else 0))
     if flows:
         b.set_flow_recording(True)
     if stats_graph is not None:
