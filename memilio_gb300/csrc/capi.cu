@@ -1039,6 +1039,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     }
     B.ypre = b->opts.precision == MGPU_PRECISION_FP64_PLAIN ? b->pool.alloc<double>(st) : nullptr;
     std::vector<double> h_t(nodes, t0), h_dt(nodes, dt0);
+    trace.mark("uploads: node and state pools");
     B.node_t          = b->pool.upload(h_t);
     B.node_dt         = b->pool.upload(h_dt);
     B.edge_src        = b->pool.upload(h_src);
@@ -1057,6 +1058,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     B.gsnap      = b->pairs ? b->pool.alloc<float>(2 * (st / kC) * kRec) : nullptr;
     B.risk       = (plain || b->pairs) ? nullptr : (void*)b->pool.alloc<double>(2 * nodes * MGPU_MAX_GROUPS * 2);
     B.aux        = plain ? nullptr : (void*)b->pool.alloc<double>(nodes * MGPU_MAX_GROUPS * 12);
+    trace.mark("uploads: edge arrays, snapshots");
     B.ecoef_r    = b->pairs ? b->pool.upload(h_ecr) : nullptr;
     B.ecoef_u    = h_ecu.empty() ? nullptr : b->pool.upload(h_ecu);
     B.ecoef_in   = h_ecu_in.empty() ? nullptr : b->pool.upload(h_ecu_in);
@@ -1084,6 +1086,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     for (int i = 0; i < num_graphs; ++i) {
         b->any_edge_dampings = b->any_edge_dampings || (dg[i].Ke > 0 && dg[i].E > 0);
     }
+    trace.mark("FP32 coefficients and tables");
     B.edge_fixed = b->pool.alloc<int32_t>(edges);
     B.scan_mark  = b->pool.alloc<int32_t>(3 * nodes * MGPU_MAX_GROUPS);
     B.scan_list  = b->pool.alloc<int32_t>(3 * nodes * MGPU_MAX_GROUPS);
@@ -1102,6 +1105,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
     ck(cudaMemsetAsync(B.edge_fixed, 0, sizeof(int32_t) * std::max<int64_t>(edges, 1), ctx->stream), "memset");
     ck(cudaMemsetAsync(B.node_flag, 0, std::max<int64_t>(nodes, 1), ctx->stream), "memset");
     ck(cudaMemsetAsync(B.node_dirty, 0, std::max<int64_t>(2 * nodes, 1), ctx->stream), "memset");
+    trace.mark("exchange work space");
     B.out_ptr  = b->pool.upload(h_out_ptr);
     B.in_ptr   = b->pool.upload(h_in_ptr);
     B.in_edges = b->pool.upload(h_in_edges);
@@ -1116,7 +1120,7 @@ void build_batch(mgpu_batch* b, const mgpu_graph* graphs, int32_t num_graphs, do
         B.in_se           = in_se;
         B.in_mid          = in_mid;
         ck(launch_edge_indices(B, trav_off, in_se, in_mid, ctx->stream), "edge index kernel");
-        trace.mark("uploads, in-edge indices");
+        trace.mark("edge indices");
     }
     B.scratch_stride = std::max<int64_t>(scratch_slots, 1);
     B.scratch_nmax   = (int32_t)b->n_max;
