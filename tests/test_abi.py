@@ -1,5 +1,6 @@
 """The C ABI library: it builds for sm_103a, loads, exports every entry point
-declared in include/miogpu.h, and reports a missing GPU as a status code."""
+declared in include/miogpu.h, reports a missing GPU as a status code, and the
+Python mirror lays out the ABI's structs as a C compiler does from the headers."""
 import ctypes
 import os
 import re
@@ -61,3 +62,30 @@ def test_status_codes_mirror_reference_statuscode():
              "MGPU_KEY_NOT_FOUND", "MGPU_INVALID_TYPE", "MGPU_FILE_NOT_FOUND"]
     for i, name in enumerate(order):
         assert re.search(rf"{name}\s*=\s*{i}\b", src), name
+
+
+def test_struct_layouts_match_the_python_mirror(tmp_path):
+    # sizes and field offsets of the ABI's structs, as a C compiler lays them
+    # out from the headers, against the ctypes mirror the Python entry uses
+    import subprocess
+    from memilio_gb300 import _native as N
+    from memilio_gb300 import layout as L
+    mirrors = {"mgpu_solver_opts": N.MgpuSolverOpts, "mgpu_server_opts": N.MgpuServerOpts,
+               "mgpu_timing": N.MgpuTiming, "mgpu_stats": N.MgpuStats, "mgpu_graph": L.MgpuGraph,
+               "mgpu_integrator_opts": L.MgpuIntegratorOpts}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "miogpu.h"', 'int main(void) {']
+    for cname, py in mirrors.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append('return 0; }')
+    src = tmp_path / "layout.c"
+    exe = tmp_path / "layout"
+    src.write_text("\n".join(lines))
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    c = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in mirrors.items():
+        assert c[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert c[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
