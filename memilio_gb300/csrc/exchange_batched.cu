@@ -15,19 +15,26 @@
 //    time, computed once per destination node (not once per edge).
 //  * Node updates are (node, age group) threads walking the node's incident
 //    edges in serial order, so no atomics and a deterministic result.
+//  * Graphs whose snapshot records fit in shared memory run those threads in
+//    one CTA per chunk of the graph, reading every edge's source record from a
+//    copy in shared memory (k_xs_*); the others gather them from L2 (k_xf_*).
+//    Both share the per-item code and give bitwise identical results.
 //
 // Precision (template R): R = double reproduces the FP64 arithmetic of the
 // reference (up to the association of the force-of-infection sum). R = float
 // computes travelers and Euler increments in FP32 with correctly rounded
 // intrinsics only (no contraction), so both endpoints of an edge obtain the
-// bit-identical value; the node states accumulate them in float-float
-// (TwoSum) pairs and are stored as FP64, which conserves every population.
+// bit-identical travelers; the destination forms its in-edges' Euler
+// increments from their sum (one rounding instead of one per edge). The node
+// states accumulate them in float-float (TwoSum) pairs, which conserves every
+// population to the FP32 rounding of the Euler increments.
 //
 // Underflow fixes: a conservative per-node bound flags the nodes whose serial
 // return order might meet a negative remainder; those run the exact
 // (node, age group) scan of exchange.cu semantics (k_xg_scan in FP64, k_xf_scan
-// in float-float for the mixed solver), then the per-graph sequential pass
-// handles what the scan passes leave unresolved.
+// in float-float for the mixed solver, which follows the serial order with
+// prefix sums over a warp's lanes and stops only at the edges to fix), then the
+// per-graph sequential pass handles what the scan passes leave unresolved.
 #include "mgpu_internal.cuh"
 
 #include <algorithm>
