@@ -27,7 +27,9 @@
 // bit-identical travelers; the destination forms its in-edges' Euler
 // increments from their sum (one rounding instead of one per edge). The node
 // states accumulate them in float-float (TwoSum) pairs, which conserves every
-// population to the FP32 rounding of the Euler increments.
+// node's and the whole population to float-float rounding (an Euler increment
+// moves an amount between two compartments of one node; its FP32 rounding only
+// shifts the split between compartments).
 //
 // Underflow fixes: a conservative per-node bound flags the nodes whose serial
 // return order might meet a negative remainder; those run the exact
