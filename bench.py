@@ -308,12 +308,13 @@ def h2d_bytes(graphs) -> int:
 BYTES_PER_ITEM = {"return": 256, "depart": 288, "exact": 256}
 # DRAM bytes (read + write) per (node, group) item of one launch, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum) of a 256-sample x
-# 400-node ensemble: 236.4 MB (return) and 156.6 MB (departure) for 614,400 items.
-# The traffic grows in proportion to the items, so it scales to the full launch.
-NCU_BYTES_PER_ITEM = {"return": (162.609408e6 + 73.811456e6) / 614400, "depart": (110.047488e6 + 46.544896e6) / 614400}
+# 400-node ensemble (per-graph passes): 209.7 MB (return, with the pre-return
+# copy for the exact path) and 154.9 MB (departure) for 614,400 items. The
+# traffic grows in proportion to the items, so it scales to the full launch.
+NCU_BYTES_PER_ITEM = {"return": (158.565376e6 + 51.165696e6) / 614400, "depart": (106.436608e6 + 48.486144e6) / 614400}
 # the same for the mixed node kernel, per node instance of one interval
-# (223.8 MB for 102,400 instances)
-NCU_ODE_BYTES_PER_INSTANCE = (178.190080e6 + 45.599744e6) / 102400
+# (225.3 MB for 102,400 instances)
+NCU_ODE_BYTES_PER_INSTANCE = (178.253824e6 + 47.016960e6) / 102400
 
 
 # --precision names, the ABI's precision constants and the arithmetic each computes in
@@ -486,7 +487,8 @@ def main():
         bytes_launch = items * BYTES_PER_ITEM[dominant]
         ms_launch = parts[dominant] / launches_active
         ach = bytes_launch / (ms_launch / 1e3) / 1e9
-        roofline = dict(roofline, bound="hbm", kernel={"return": "k_xf_return", "depart": "k_xf_depart",
+        roofline = dict(roofline, bound="hbm", kernel={"return": "k_xs_return / k_xf_return",
+                                                      "depart": "k_xs_depart / k_xf_depart",
                                                       "exact": "k_xf_scan"}[dominant],
                         achieved=ach, unit="GB/s", peak=peaks["hbm_gbs"], peak_source=peaks["source"],
                         frac=ach / peaks["hbm_gbs"], algorithmic_bytes_per_launch=bytes_launch,
