@@ -1,4 +1,4 @@
-"""Synthetic workload generators: shapes, ranges, edge order."""
+"""Synthetic workload generators: shapes, ranges, edge order; the graph view of the arrays."""
 import numpy as np
 
 from memilio_gb300 import layout as L
@@ -49,3 +49,17 @@ def test_uneven_batch_distribution():
     assert all(1 <= g.num_nodes <= 2000 for g in graphs)
     assert all(1 <= g.num_groups <= 6 for g in graphs)
     assert np.all((h >= 30) & (h <= 180))
+
+
+def test_graph_view_follows_its_arrays():
+    # the mgpu_graph view is kept while the arrays are the same objects (their
+    # contents may change in place) and rebuilt when an array is replaced
+    g = W.mobility_graph(seed=7, N=12, G=2, out_degree=3)
+    v1 = g.as_ctypes()
+    g.init_state[0, 0] += 1.0
+    assert g.as_ctypes() is v1
+    g.init_state = g.init_state.copy()
+    v2 = g.as_ctypes()
+    assert v2 is not v1
+    assert v2.init_state == g.init_state.ctypes.data
+    assert v2.edge_src == v1.edge_src and v2.params == v1.params
